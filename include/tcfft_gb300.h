@@ -1,0 +1,141 @@
+/*
+ * tcfft_gb300.h -- C ABI of the GB300 (sm_103a) half-precision FFT library.
+ *
+ * This is the drop-in boundary for the reference's plan API (rox906/tcFFT):
+ *
+ *   reference (C++ linkage, tcfft_half.h:20-21, tcfft_half_2d.h:20-21)
+ *     void tcfftCreate(tcfftHandle *plan, int n, int n_batch);
+ *     void tcfftCreate(tcfftHandle *plan, int nx, int ny, int n_batch);
+ *     void tcfftExec(tcfftHandle plan, half *data);
+ *     (no destroy function; errors are undefined behaviour)
+ *
+ *   this library (extern "C", plain pointers and sizes, status codes)
+ *     tcfftPlan1d / tcfftPlan2d / tcfftPlanMany   <- tcfftCreate
+ *     tcfftExecute                                <- tcfftExec
+ *     tcfftDestroy                                (new: the reference leaks)
+ *
+ * Semantics kept from the reference (tcfft_doit_half.cpp:31-67):
+ *   - `data` is a device pointer owned by the caller, interleaved complex
+ *     (re, im), batch-major contiguous: [batch][n] (1D), [batch][nx][ny] (2D,
+ *     row-major, ny contiguous);
+ *   - the transform is in place, unnormalised, forward sign -1 (the reference
+ *     builds F = exp(-2 pi i jk/16), tcfft_half.cu:1339);
+ *   - execution is asynchronous on the given stream (the reference uses the
+ *     default stream; pass 0 for the same behaviour).
+ * Additions: status codes, stream argument, natural input order by default
+ * (the reference expects digit-reversed input, tcfft_doit_half.cpp:38-46;
+ * TCFFT_ORDER_REFERENCE_DIGIT_REVERSED reproduces that contract), split
+ * precision, the adjoint transform, and uneven batches.
+ */
+#ifndef TCFFT_GB300_H
+#define TCFFT_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum tcfftStatus {
+  TCFFT_SUCCESS = 0,
+  TCFFT_INVALID_VALUE = 1,  /* null pointer, bad option value */
+  TCFFT_INVALID_SIZE = 2,   /* unsupported n / nx / ny / batch */
+  TCFFT_MISALIGNED = 3,     /* data pointer not 128-byte aligned */
+  TCFFT_ALLOC_FAILED = 4,   /* device or host allocation failed */
+  TCFFT_CUDA_ERROR = 5,     /* a CUDA runtime/driver call failed */
+  TCFFT_TIMEOUT = 6,        /* a bounded device-side wait expired */
+  TCFFT_NOT_SUPPORTED = 7,  /* valid request this build does not implement */
+  TCFFT_INVALID_PLAN = 8    /* null or already destroyed plan */
+} tcfftStatus;
+
+typedef enum tcfftPrecision {
+  /* fp16 complex in/out (4 bytes per element), fp16 tensor-core operands with
+   * fp32 accumulation, fp16 between passes. Same data type as the reference. */
+  TCFFT_PRECISION_PLAIN = 0,
+  /* fp32 complex in/out (8 bytes per element); every tensor-core product is
+   * split into hi+lo fp16 pairs (hi*hi + hi*lo + lo*hi, fp32 accumulation),
+   * fp32 twiddles and fp32 storage between passes. */
+  TCFFT_PRECISION_SPLIT = 1
+} tcfftPrecision;
+
+typedef enum tcfftInputOrder {
+  TCFFT_ORDER_NATURAL = 0,
+  /* input permuted by the reference's digit-reversal (gen_rev with the
+   * reference's radix chain, tcfft_doit_half.cpp:6-29); output natural. Only
+   * for sizes the reference supports. */
+  TCFFT_ORDER_REFERENCE_DIGIT_REVERSED = 1
+} tcfftInputOrder;
+
+typedef struct tcfftOptions {
+  int32_t precision;   /* tcfftPrecision */
+  int32_t input_order; /* tcfftInputOrder */
+  int32_t autotune;    /* 0: built-in schedule; 1: time candidates at plan time */
+  int32_t reserved;
+  const char* tune_cache_path; /* optional file for autotune results (NULL: none) */
+} tcfftOptions;
+
+typedef struct tcfftPlanImpl* tcfftPlan;
+
+/* Fill `opts` with defaults (plain, natural order, no autotune). */
+tcfftStatus tcfftOptionsDefault(tcfftOptions* opts);
+
+/* 1D batched plan: `batch` transforms of length n (power of two, 256 <= n <= 2^27). */
+tcfftStatus tcfftPlan1d(tcfftPlan* plan, int64_t n, int64_t batch, const tcfftOptions* opts);
+
+/* 2D batched plan: `batch` transforms of nx x ny (powers of two, 128 <= nx, ny). */
+tcfftStatus tcfftPlan2d(tcfftPlan* plan, int64_t nx, int64_t ny, int64_t batch, const tcfftOptions* opts);
+
+/* Uneven batch in one launch: `count` independent transforms, transform i has
+ * rank ranks[i] (1 or 2), shape (nx[i]) for 1D or (nx[i], ny[i]) for 2D, and
+ * starts at element offset offsets[i] of the single device buffer passed to
+ * tcfftExecute (in elements; must keep 128-byte alignment). */
+tcfftStatus tcfftPlanMany(tcfftPlan* plan, int64_t count, const int32_t* ranks, const int64_t* nx,
+                          const int64_t* ny, const int64_t* offsets, const tcfftOptions* opts);
+
+/* Forward transform in place on device memory `data` on `stream`
+ * (a cudaStream_t; NULL = legacy default stream). */
+tcfftStatus tcfftExecute(tcfftPlan plan, void* data, void* stream);
+
+/* Adjoint transform (conjugate direction, unnormalised: the exact adjoint of
+ * tcfftExecute, i.e. n * inverse DFT), same layout and schedule. */
+tcfftStatus tcfftExecuteAdjoint(tcfftPlan plan, void* data, void* stream);
+
+/* Synchronise `stream` and report device-side errors (TCFFT_TIMEOUT) raised
+ * by bounded waits since the last check; clears the flag. */
+tcfftStatus tcfftCheckDevice(tcfftPlan plan, void* stream);
+
+tcfftStatus tcfftDestroy(tcfftPlan plan);
+
+const char* tcfftGetErrorString(tcfftStatus status);
+
+/* Plan introspection: element count per transform set (sum over the batch),
+ * bytes per element (4 plain / 8 split), scratch bytes, number of kernel
+ * launches per execute, and the reference-compatible radix chain (up to
+ * `max_radices` entries; 2D: x then y) used for
+ * TCFFT_ORDER_REFERENCE_DIGIT_REVERSED. */
+typedef struct tcfftPlanInfo {
+  int64_t total_elements;
+  int32_t element_bytes;
+  int32_t launches_per_exec;
+  int64_t scratch_bytes;
+  int32_t n_radices;
+  int32_t radices[16];
+  int32_t n_radices_y;
+  int32_t radices_y[16];
+  char schedule[128];
+} tcfftPlanInfo;
+tcfftStatus tcfftGetPlanInfo(tcfftPlan plan, tcfftPlanInfo* info);
+
+/* Describe the schedule for a 1D size without touching the GPU (host-only
+ * planner; used by CPU tests). Writes a short text into buf. */
+tcfftStatus tcfftDescribe1d(int64_t n, int64_t batch, int32_t precision, char* buf, size_t buf_len);
+
+/* Library version string. */
+const char* tcfftVersion(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TCFFT_GB300_H */

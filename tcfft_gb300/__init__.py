@@ -1,0 +1,289 @@
+"""tcfft_gb300 -- GB300-native (sm_103a) half-precision FFT library, host side.
+
+The compute path is the CUDA library ``libtcfft_gb300.so`` built from
+``tcfft_gb300/csrc`` (see ``tcfft_gb300/build.py``); this module binds its
+C ABI (``include/tcfft_gb300.h``) with ctypes and mirrors the reference's plan
+API (rox906/tcFFT, tcfft_half.h:20-21 / tcfft_half_2d.h:20-21):
+
+    plan = tcfftCreate(n, n_batch)            # 1D   (tcfft_half.h:21)
+    plan = tcfftCreate(nx, ny, n_batch)       # 2D   (tcfft_half_2d.h:21)
+    tcfftExec(plan, data)                     # in place, forward (tcfft_half.h:20)
+    tcfftDestroy(plan)                        # new: the reference never frees
+
+``data`` is a CUDA torch tensor holding interleaved complex values: fp16
+``[..., 2]`` / ``torch.complex32`` for the plain path (the reference's
+``half*``), fp32 ``[..., 2]`` / ``torch.complex64`` for split precision.
+Unlike the reference, input is in natural order by default, errors raise
+:class:`TcfftError`, and execution goes on the current torch stream.
+
+There is no CPU fallback: if the CUDA library is missing, importing works but
+every plan/execute call raises.
+"""
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libtcfft_gb300.so")
+
+PRECISION_PLAIN = 0
+PRECISION_SPLIT = 1
+ORDER_NATURAL = 0
+ORDER_REFERENCE_DIGIT_REVERSED = 1
+
+_STATUS = {
+    0: "TCFFT_SUCCESS", 1: "TCFFT_INVALID_VALUE", 2: "TCFFT_INVALID_SIZE", 3: "TCFFT_MISALIGNED",
+    4: "TCFFT_ALLOC_FAILED", 5: "TCFFT_CUDA_ERROR", 6: "TCFFT_TIMEOUT", 7: "TCFFT_NOT_SUPPORTED",
+    8: "TCFFT_INVALID_PLAN",
+}
+
+
+class TcfftError(RuntimeError):
+    """A tcfft C-ABI call returned a non-success status."""
+
+    def __init__(self, status, what=""):
+        self.status = int(status)
+        name = _STATUS.get(self.status, "status %d" % self.status)
+        msg = "%s: %s" % (what, name) if what else name
+        try:
+            msg += " (%s)" % lib().tcfftGetErrorString(self.status).decode()
+        except Exception:  # noqa: BLE001 - message decoration only
+            pass
+        super().__init__(msg)
+
+
+class Options(ctypes.Structure):
+    """struct tcfftOptions (include/tcfft_gb300.h)."""
+    _fields_ = [("precision", ctypes.c_int32), ("input_order", ctypes.c_int32),
+                ("autotune", ctypes.c_int32), ("reserved", ctypes.c_int32),
+                ("tune_cache_path", ctypes.c_char_p)]
+
+
+class PlanInfo(ctypes.Structure):
+    """struct tcfftPlanInfo (include/tcfft_gb300.h)."""
+    _fields_ = [("total_elements", ctypes.c_int64), ("element_bytes", ctypes.c_int32),
+                ("launches_per_exec", ctypes.c_int32), ("scratch_bytes", ctypes.c_int64),
+                ("n_radices", ctypes.c_int32), ("radices", ctypes.c_int32 * 16),
+                ("n_radices_y", ctypes.c_int32), ("radices_y", ctypes.c_int32 * 16),
+                ("schedule", ctypes.c_char * 128)]
+
+
+_LIB = None
+
+# Every entry point declared in include/tcfft_gb300.h, with its ctypes signature.
+_SIGNATURES = {
+    "tcfftOptionsDefault": ([ctypes.POINTER(Options)], ctypes.c_int),
+    "tcfftPlan1d": ([ctypes.POINTER(ctypes.c_void_p), ctypes.c_int64, ctypes.c_int64, ctypes.POINTER(Options)],
+                    ctypes.c_int),
+    "tcfftPlan2d": ([ctypes.POINTER(ctypes.c_void_p), ctypes.c_int64, ctypes.c_int64, ctypes.c_int64,
+                     ctypes.POINTER(Options)], ctypes.c_int),
+    "tcfftPlanMany": ([ctypes.POINTER(ctypes.c_void_p), ctypes.c_int64, ctypes.POINTER(ctypes.c_int32),
+                       ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64),
+                       ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(Options)], ctypes.c_int),
+    "tcfftExecute": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
+    "tcfftExecuteAdjoint": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
+    "tcfftCheckDevice": ([ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
+    "tcfftDestroy": ([ctypes.c_void_p], ctypes.c_int),
+    "tcfftGetErrorString": ([ctypes.c_int], ctypes.c_char_p),
+    "tcfftGetPlanInfo": ([ctypes.c_void_p, ctypes.POINTER(PlanInfo)], ctypes.c_int),
+    "tcfftDescribe1d": ([ctypes.c_int64, ctypes.c_int64, ctypes.c_int32, ctypes.c_char_p, ctypes.c_size_t],
+                        ctypes.c_int),
+    "tcfftVersion": ([], ctypes.c_char_p),
+}
+
+
+def exported_symbols():
+    """Names of the C-ABI entry points this module binds."""
+    return sorted(_SIGNATURES)
+
+
+def lib():
+    """Load (once) and return the CUDA library; raises if it was not built."""
+    global _LIB
+    if _LIB is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError("tcfft_gb300: %s is missing; build it with "
+                              "`python -c 'import __graft_entry__ as g; g.build()'`" % LIB_PATH)
+        handle = ctypes.CDLL(LIB_PATH)
+        for name, (args, res) in _SIGNATURES.items():
+            fn = getattr(handle, name)
+            fn.argtypes = args
+            fn.restype = res
+        _LIB = handle
+    return _LIB
+
+
+def _check(status, what):
+    if status != 0:
+        raise TcfftError(status, what)
+
+
+def describe_1d(n, batch=1, precision=PRECISION_PLAIN):
+    """Host-only schedule description for a 1D size (no GPU needed)."""
+    buf = ctypes.create_string_buffer(256)
+    _check(lib().tcfftDescribe1d(int(n), int(batch), int(precision), buf, 256), "tcfftDescribe1d")
+    return buf.value.decode()
+
+
+def _precision_of(p):
+    if p in (PRECISION_PLAIN, "plain", "fp16", None):
+        return PRECISION_PLAIN
+    if p in (PRECISION_SPLIT, "split"):
+        return PRECISION_SPLIT
+    raise ValueError("precision must be 'plain' or 'split', got %r" % (p,))
+
+
+def _stream_handle(stream):
+    if stream is None:
+        import torch
+        return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    if isinstance(stream, int):
+        return ctypes.c_void_p(stream)
+    return ctypes.c_void_p(stream.cuda_stream)
+
+
+class Plan:
+    """An FFT plan (owns its device tables; call :meth:`destroy` or use ``with``).
+
+    1D: ``Plan(n=N, batch=B)``; 2D: ``Plan(nx=NX, ny=NY, batch=B)``;
+    uneven batch: ``Plan.many([...shapes...])``.
+    """
+
+    def __init__(self, n=None, batch=1, nx=None, ny=None, precision="plain", input_order=ORDER_NATURAL,
+                 autotune=False, tune_cache_path=None, _handle=None, _shapes=None):
+        self._handle = ctypes.c_void_p(None)
+        self.precision = _precision_of(precision)
+        self.input_order = int(input_order)
+        if _handle is not None:
+            self._handle = _handle
+            self.shapes = _shapes
+            self.n = self.nx = self.ny = None
+            self.batch = None
+            return
+        opts = Options()
+        lib().tcfftOptionsDefault(ctypes.byref(opts))
+        opts.precision = self.precision
+        opts.input_order = self.input_order
+        opts.autotune = 1 if autotune else 0
+        opts.tune_cache_path = tune_cache_path.encode() if tune_cache_path else None
+        self._opts = opts
+        if n is not None:
+            self.n, self.nx, self.ny, self.batch = int(n), None, None, int(batch)
+            _check(lib().tcfftPlan1d(ctypes.byref(self._handle), self.n, self.batch, ctypes.byref(opts)),
+                   "tcfftPlan1d(n=%d, batch=%d)" % (self.n, self.batch))
+        elif nx is not None and ny is not None:
+            self.n, self.nx, self.ny, self.batch = None, int(nx), int(ny), int(batch)
+            _check(lib().tcfftPlan2d(ctypes.byref(self._handle), self.nx, self.ny, self.batch, ctypes.byref(opts)),
+                   "tcfftPlan2d(nx=%d, ny=%d, batch=%d)" % (self.nx, self.ny, self.batch))
+        else:
+            raise ValueError("give n (1D) or nx and ny (2D)")
+
+    @classmethod
+    def many(cls, shapes, offsets=None, precision="plain", autotune=False):
+        """Uneven batch: ``shapes`` is a list of ``(n,)`` or ``(nx, ny)`` tuples,
+        transforms packed back to back (or at ``offsets``, in elements)."""
+        count = len(shapes)
+        ranks = (ctypes.c_int32 * count)(*[len(s) for s in shapes])
+        nxs = (ctypes.c_int64 * count)(*[int(s[0]) for s in shapes])
+        nys = (ctypes.c_int64 * count)(*[int(s[1]) if len(s) > 1 else 1 for s in shapes])
+        if offsets is None:
+            offs, acc = [], 0
+            for s in shapes:
+                offs.append(acc)
+                acc += int(s[0]) * (int(s[1]) if len(s) > 1 else 1)
+            offsets = offs
+        offa = (ctypes.c_int64 * count)(*[int(o) for o in offsets])
+        opts = Options()
+        lib().tcfftOptionsDefault(ctypes.byref(opts))
+        opts.precision = _precision_of(precision)
+        opts.autotune = 1 if autotune else 0
+        h = ctypes.c_void_p(None)
+        _check(lib().tcfftPlanMany(ctypes.byref(h), count, ranks, nxs, nys, offa, ctypes.byref(opts)),
+               "tcfftPlanMany(count=%d)" % count)
+        p = cls(precision=precision, _handle=h, _shapes=[tuple(s) for s in shapes])
+        p.offsets = list(offsets)
+        return p
+
+    # -- execution -------------------------------------------------------
+    def _ptr(self, data):
+        if isinstance(data, int):
+            return data
+        import torch
+        if not isinstance(data, torch.Tensor):
+            raise TypeError("data must be a CUDA torch tensor or a device pointer (int)")
+        if not data.is_cuda:
+            raise ValueError("tcfft executes on device memory; got a CPU tensor")
+        if not data.is_contiguous():
+            raise ValueError("data must be contiguous")
+        want = (torch.float16, torch.complex32) if self.precision == PRECISION_PLAIN else (torch.float32,
+                                                                                             torch.complex64)
+        if data.dtype not in want:
+            raise TypeError("precision %s expects %s, got %s" % (
+                "plain" if self.precision == PRECISION_PLAIN else "split", want, data.dtype))
+        return data.data_ptr()
+
+    def exec(self, data, stream=None, adjoint=False):
+        """Transform ``data`` in place (forward, or the adjoint)."""
+        if not self._handle:
+            raise TcfftError(8, "exec on destroyed plan")
+        fn = lib().tcfftExecuteAdjoint if adjoint else lib().tcfftExecute
+        _check(fn(self._handle, ctypes.c_void_p(self._ptr(data)), _stream_handle(stream)),
+               "tcfftExecute%s" % ("Adjoint" if adjoint else ""))
+        return data
+
+    def check_device(self, stream=None):
+        """Synchronise and raise TcfftError(TCFFT_TIMEOUT) if a bounded wait expired."""
+        _check(lib().tcfftCheckDevice(self._handle, _stream_handle(stream)), "tcfftCheckDevice")
+
+    @property
+    def info(self):
+        inf = PlanInfo()
+        _check(lib().tcfftGetPlanInfo(self._handle, ctypes.byref(inf)), "tcfftGetPlanInfo")
+        return {
+            "total_elements": inf.total_elements, "element_bytes": inf.element_bytes,
+            "launches_per_exec": inf.launches_per_exec, "scratch_bytes": inf.scratch_bytes,
+            "radices": list(inf.radices[:inf.n_radices]), "radices_y": list(inf.radices_y[:inf.n_radices_y]),
+            "schedule": inf.schedule.decode(),
+        }
+
+    def destroy(self):
+        if self._handle:
+            _check(lib().tcfftDestroy(self._handle), "tcfftDestroy")
+            self._handle = ctypes.c_void_p(None)
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.destroy()
+
+    def __del__(self):
+        try:
+            if self._handle and _LIB is not None:
+                _LIB.tcfftDestroy(self._handle)
+                self._handle = ctypes.c_void_p(None)
+        except Exception:  # noqa: BLE001 - interpreter shutdown
+            pass
+
+
+# ---------------------------------------------------------------- reference-named API
+def tcfftCreate(*args, precision="plain", input_order=ORDER_NATURAL):
+    """Mirror of the reference's ``tcfftCreate`` (tcfft_half.h:21 / tcfft_half_2d.h:21):
+    ``tcfftCreate(n, n_batch)`` or ``tcfftCreate(nx, ny, n_batch)``; returns a :class:`Plan`."""
+    if len(args) == 2:
+        return Plan(n=args[0], batch=args[1], precision=precision, input_order=input_order)
+    if len(args) == 3:
+        return Plan(nx=args[0], ny=args[1], batch=args[2], precision=precision, input_order=input_order)
+    raise TypeError("tcfftCreate(n, n_batch) or tcfftCreate(nx, ny, n_batch)")
+
+
+def tcfftExec(plan, data, stream=None):
+    """Mirror of ``tcfftExec(tcfftHandle, half*)`` (tcfft_half.h:20): forward, in place."""
+    return plan.exec(data, stream=stream)
+
+
+def tcfftDestroy(plan):
+    plan.destroy()
+
+
+def version():
+    return lib().tcfftVersion().decode()

@@ -1,0 +1,259 @@
+// fft_small.cuh -- single-pass kernels for transforms of N = 256*R points
+// (R in {1,2,4,8}: N = 256 ... 2048), one HBM round trip per element.
+//
+// Replaces the reference's layer_{256,512,1024}_0 kernels
+// (tcfft_half.cu:69-161, 586-699, 1011-1095), which compute the same
+// contiguous sub-FFTs with WMMA and fp16 accumulation on digit-reversed input.
+// Here the input is in natural order and the algorithm is decimation in
+// frequency:  n = m + 256 a,  k = q + R k',
+//   X[q + R k'] = sum_m W256^(m k') [ W_N^(m q) sum_a x[m + 256 a] W_R^(a q) ]
+// i.e. a radix-R butterfly over a (fp32, registers), a twiddle, then a
+// 256-point FFT per q done as two radix-16 tensor-core stages
+// (m = 16 m1 + m0:  sum over m1 -> k0, twiddle W256^(m0 k0), sum over m0 -> k1,
+// k' = k0 + 16 k1).  Everything between the TMA load and the TMA store stays
+// in registers.
+//
+// CTA structure: persistent CTAs, 8 warps, a ring of NSTAGE shared-memory
+// tiles filled by 2D TMA loads (128B swizzle) and drained by TMA stores; the
+// transform is in place (each tile is loaded, transformed and stored back to
+// the same global rows).
+#pragma once
+#include "fft_common.cuh"
+
+namespace tcfft {
+
+template <int R, bool SPLIT>
+struct SmallCfg {
+  static constexpr int kN = 256 * R;
+  static constexpr int kES = SPLIT ? 8 : 4;              // bytes per complex element
+  static constexpr int kER = 128 / kES;                  // elements per 128-byte row
+  static constexpr int kBoxElems = kER * 256;            // one TMA box: 256 rows
+  static constexpr int kJPW = SPLIT ? (R >= 2 ? 1 : 2) : (R >= 4 ? 1 : 4 / R);  // jobs per warp
+  static constexpr int kTE = 8 * kJPW * kN;              // elements per tile
+  static constexpr int kBoxes = kTE / kBoxElems;
+  static constexpr int kTileBytes = kTE * kES;
+  static constexpr int kStages = 3;
+  static constexpr int kSmem = kStages * kTileBytes + 1024 + 64;
+  static constexpr int kMinBlocks = (kStages * kTileBytes <= 100 * 1024) ? 2 : 1;
+  static_assert(kTE % kBoxElems == 0, "tile must be whole TMA boxes");
+  // bank-conflict-free slot permutations (see fft_common.cuh)
+  using PI = typename std::conditional<SPLIT, BitPerm<0, 1, 2, 3>, BitPerm<0, 1, 3, 2>>::type;
+  using RHO = typename std::conditional<
+      SPLIT,
+      typename std::conditional<R == 1, BitPerm<1, 0, 3, 2>, BitPerm<0, 2, 3, 1>>::type,
+      typename std::conditional<R == 1, BitPerm<2, 0, 1, 3>,
+                                typename std::conditional<R == 2, BitPerm<1, 0, 3, 2>, BitPerm<0, 2, 3, 1>>::type>::type>::type;
+};
+
+struct SmallParams {
+  const float2* tw;  // W_2048^j, j < 2048, direction-specific (fp32 from fp64)
+  int num_tiles;
+  float dsign;       // +1 forward, -1 adjoint (conjugate direction)
+  int* err;
+};
+
+template <int R, bool SPLIT>
+__global__ void __launch_bounds__(256, SmallCfg<R, SPLIT>::kMinBlocks)
+    fft_small_kernel(const __grid_constant__ CUtensorMap tmap, const SmallParams p) {
+  using C = SmallCfg<R, SPLIT>;
+  using PI = typename C::PI;
+  using RHO = typename C::RHO;
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  unsigned char* smem = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + C::kStages * C::kTileBytes);
+
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, g = lane >> 2, t = lane & 3;
+  const int ntile_cta = (p.num_tiles - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x;
+
+  if (tid == 0) {
+    prefetch_tmap(&tmap);
+    for (int s = 0; s < C::kStages; ++s) mbar_init(&full[s], 1);
+    fence_barrier_init();
+  }
+  __syncthreads();
+
+  auto issue_load = [&](int i) {  // thread 0 only: tile #i of this CTA into stage i % kStages
+    const int tile = blockIdx.x + i * gridDim.x;
+    const int s = i % C::kStages;
+    mbar_arrive_expect_tx(&full[s], C::kTileBytes);
+#pragma unroll
+    for (int b = 0; b < C::kBoxes; ++b)
+      tma_load_2d(smem + s * C::kTileBytes + b * C::kBoxElems * C::kES, &tmap, 0,
+                  tile * (C::kTE / C::kER) + b * 256, &full[s]);
+  };
+  if (tid == 0)
+    for (int i = 0; i < C::kStages && i < ntile_cta; ++i) issue_load(i);
+
+  // ---- per-thread constants
+  uint32_t afr[2][2][4], afr_lo[2][2][4];
+  build_dft_frags<PI, RHO>(p.tw, 128, afr, afr_lo, SPLIT);
+  float2 tw1[2][2][2];  // W256^(m0 k0) for stage-1 output (j, h, e)
+#pragma unroll
+  for (int j = 0; j < 2; ++j)
+#pragma unroll
+    for (int h = 0; h < 2; ++h)
+#pragma unroll
+      for (int e = 0; e < 2; ++e) {
+        const int m0 = PI::apply(2 * t + e + 8 * j), k0 = RHO::apply(g + 8 * h);
+        tw1[j][h][e] = p.tw[((m0 * k0) & 255) * 8];
+      }
+  uint32_t in_off[2][2][2];   // physical element offset of load slot (kt, r, j) in tile a = 0
+  int mval[2][2][2];          // m = 16 m1 + m0 of that slot
+#pragma unroll
+  for (int kt = 0; kt < 2; ++kt)
+#pragma unroll
+    for (int r = 0; r < 2; ++r)
+#pragma unroll
+      for (int j = 0; j < 2; ++j) {
+        const int m = 16 * PI::apply(2 * t + r + 8 * kt) + PI::apply(g + 8 * j);
+        mval[kt][r][j] = m;
+        in_off[kt][r][j] = swz_w<C::kES>(m);
+      }
+  uint32_t out_off[2][2][2];  // physical offset of output slot (h, e, hh) for q = 0 (k = R k')
+#pragma unroll
+  for (int h = 0; h < 2; ++h)
+#pragma unroll
+    for (int e = 0; e < 2; ++e)
+#pragma unroll
+      for (int hh = 0; hh < 2; ++hh) {
+        const int kp = RHO::apply(2 * t + e + 8 * h) + 16 * RHO::apply(g + 8 * hh);
+        out_off[h][e][hh] = swz_w<C::kES>(R * kp);
+      }
+
+  int issued = 0;  // thread 0: loads issued so far (tiles [0, issued) of this CTA)
+  if (tid == 0) issued = ntile_cta < C::kStages ? ntile_cta : C::kStages;
+  bool failed = false;
+  for (int i = 0; i < ntile_cta; ++i) {
+    const int s = i % C::kStages;
+    const bool ok = mbar_wait(&full[s], (i / C::kStages) & 1, p.err);
+    unsigned char* tile_base = smem + s * C::kTileBytes;
+
+#pragma unroll 1
+    for (int jj = 0; jj < (ok ? C::kJPW : 0); ++jj) {
+      const uint32_t job = smem_addr(tile_base) + (uint32_t)((warp * C::kJPW + jj) * C::kN * C::kES);
+      // ---------------- load + radix-R (DIF) + twiddle -> B operands per tile q
+      uint32_t bhi[R][2][2][2], blo[SPLIT ? R : 1][2][2][2];
+#pragma unroll
+      for (int kt = 0; kt < 2; ++kt)
+#pragma unroll
+        for (int r = 0; r < 2; ++r)
+#pragma unroll
+          for (int j = 0; j < 2; ++j) {
+            if constexpr (!SPLIT && R == 1) {
+              bhi[0][kt][r][j] = lds32(job + in_off[kt][r][j] * 4);
+            } else {
+              float2 x[R];
+#pragma unroll
+              for (int a = 0; a < R; ++a) {
+                const uint32_t addr = job + (uint32_t)(a * 256 + in_off[kt][r][j]) * C::kES;
+                if constexpr (SPLIT) x[a] = lds64f(addr);
+                else x[a] = unpack_h2(lds32(addr));
+              }
+              if constexpr (R > 1) {
+                dft_small<R>(x, p.dsign);
+#pragma unroll
+                for (int q = 1; q < R; ++q)
+                  x[q] = cmul(x[q], p.tw[((2048 / C::kN) * mval[kt][r][j] * q) & 2047]);
+              }
+#pragma unroll
+              for (int q = 0; q < R; ++q) {
+                if constexpr (SPLIT) split_h2(x[q], bhi[q][kt][r][j], blo[q][kt][r][j]);
+                else bhi[q][kt][r][j] = pack_h2(x[q].x, x[q].y);
+              }
+            }
+          }
+      __syncwarp();  // all lanes finished reading this job's region (in-place)
+
+      // ---------------- two radix-16 tensor-core stages per tile q
+      float2 res[R][2][2][2];  // SPLIT: fp32 results; PLAIN: packed half2 in .x bits
+#pragma unroll
+      for (int q = 0; q < R; ++q) {
+        float acc[2][2][4];
+        if constexpr (SPLIT) dft16_mma_split(afr, afr_lo, bhi[q], blo[q], acc);
+        else dft16_mma(afr, bhi[q], acc);
+        uint32_t b2[2][2][2], b2lo[2][2][2];
+#pragma unroll
+        for (int kt = 0; kt < 2; ++kt)
+#pragma unroll
+          for (int r = 0; r < 2; ++r)
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+              const float2 v = cmul(acc_get(acc, kt, h, r), tw1[kt][h][r]);
+              if constexpr (SPLIT) split_h2(v, b2[kt][r][h], b2lo[kt][r][h]);
+              else b2[kt][r][h] = pack_h2(v.x, v.y);
+            }
+        if constexpr (SPLIT) dft16_mma_split(afr, afr_lo, b2, b2lo, acc);
+        else dft16_mma(afr, b2, acc);
+#pragma unroll
+        for (int h = 0; h < 2; ++h)
+#pragma unroll
+          for (int e = 0; e < 2; ++e)
+#pragma unroll
+            for (int hh = 0; hh < 2; ++hh) {
+              const float2 v = acc_get(acc, h, hh, e);
+              if constexpr (SPLIT) res[q][h][e][hh] = v;
+              else res[q][h][e][hh].x = __uint_as_float(pack_h2(v.x, v.y));
+            }
+      }
+      // ---------------- store natural order: k = q + R k'
+#pragma unroll
+      for (int h = 0; h < 2; ++h)
+#pragma unroll
+        for (int e = 0; e < 2; ++e)
+#pragma unroll
+          for (int hh = 0; hh < 2; ++hh) {
+            const uint32_t base = job + out_off[h][e][hh] * C::kES;
+            if constexpr (!SPLIT) {
+              if constexpr (R == 1) sts32(base, __float_as_uint(res[0][h][e][hh].x));
+              else if constexpr (R == 2)
+                sts64(base, __float_as_uint(res[0][h][e][hh].x), __float_as_uint(res[1][h][e][hh].x));
+              else {
+#pragma unroll
+                for (int q4 = 0; q4 < R; q4 += 4) {
+                  // consecutive 16-byte chunks of the same row: chunk index differs by one
+                  const uint32_t addr = job + swz_w<4>(swz_w<4>(out_off[h][e][hh]) + q4) * 4;
+                  sts128(addr, __float_as_uint(res[q4][h][e][hh].x), __float_as_uint(res[q4 + 1][h][e][hh].x),
+                         __float_as_uint(res[q4 + 2][h][e][hh].x), __float_as_uint(res[q4 + 3][h][e][hh].x));
+                }
+              }
+            } else {
+              if constexpr (R == 1) sts64f(base, res[0][h][e][hh]);
+              else {
+#pragma unroll
+                for (int q2 = 0; q2 < R; q2 += 2) {
+                  const uint32_t addr = job + swz_w<8>(swz_w<8>(out_off[h][e][hh]) + q2) * 8;
+                  sts128f(addr, res[q2][h][e][hh], res[q2 + 1][h][e][hh]);
+                }
+              }
+            }
+          }
+    }
+    // ---------------- hand the tile to the TMA store, refill the ring
+    fence_proxy_async_smem();
+    if (__syncthreads_or(!ok)) {  // a bounded wait expired somewhere: stop consistently
+      failed = true;
+      break;
+    }
+    if (tid == 0) {
+      const int tile = blockIdx.x + i * gridDim.x;
+#pragma unroll
+      for (int b = 0; b < C::kBoxes; ++b)
+        tma_store_2d(&tmap, 0, tile * (C::kTE / C::kER) + b * 256, tile_base + b * C::kBoxElems * C::kES);
+      bulk_commit();
+      // the store issued in iteration i-1 has finished reading its stage -> reuse it
+      if (i >= 1 && i - 1 + C::kStages < ntile_cta) {
+        bulk_wait_read<1>();
+        issue_load(i - 1 + C::kStages);
+        ++issued;
+      }
+    }
+  }
+  if (tid == 0) {
+    if (failed) {  // let loads still in flight land before the CTA exits (bounded)
+      for (int i = 0; i < issued; ++i) mbar_wait(&full[i % C::kStages], (i / C::kStages) & 1, nullptr);
+    }
+    bulk_wait<0>();
+  }
+}
+
+}  // namespace tcfft

@@ -1,0 +1,34 @@
+// tcfft_host.h -- internal host-side declarations shared by the C-ABI
+// implementation (tcfft_api.cu) and the per-kernel launch translation units.
+#pragma once
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/tcfft_gb300.h"
+
+namespace tcfft {
+
+// cuTensorMapEncodeTiled, fetched through the runtime's driver entry point
+// (no link-time dependency on libcuda).
+CUresult encode_tmap(CUtensorMap* map, CUtensorMapDataType dtype, int rank, void* addr, const uint64_t* dims,
+                     const uint64_t* strides_bytes /* rank-1 entries */, const uint32_t* box,
+                     CUtensorMapSwizzle swizzle);
+
+struct DeviceTables {
+  int device = -1;
+  float2* tw2048[2] = {nullptr, nullptr};  // W_2048^j: [0] forward, [1] adjoint
+  int* err = nullptr;                      // device error word
+};
+
+// Launch entry points implemented in the kernel translation units. Each
+// returns cudaSuccess or the launch error.
+cudaError_t launch_small(int R, bool split, const CUtensorMap& tmap, int64_t total_elems, const float2* tw,
+                         float dsign, int* err, int num_sms, cudaStream_t stream, int* launches);
+int small_tile_elems(int R, bool split);
+int small_smem_bytes(int R, bool split);
+
+}  // namespace tcfft
