@@ -27,8 +27,14 @@
 namespace tcfft {
 
 // ---------------------------------------------------------------- constants
-constexpr int kTimeoutIters = 1 << 26;  // bounded mbarrier/flag spins (~1-2 s)
+constexpr unsigned long long kTimeoutNs = 2000000000ull;  // every device-side wait gives up after 2 s
 enum DeviceError : int { kDevOk = 0, kDevTimeout = 1 };
+
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
 
 // 4-bit index permutation: bit i of x moves to bit P_i.
 template <int P0, int P1, int P2, int P3>
@@ -69,12 +75,18 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
       : "memory");
   return ok != 0;
 }
-// Bounded wait; on expiry records kDevTimeout in *err and returns false.
+// Bounded wait (wall clock, kTimeoutNs); on expiry records kDevTimeout in
+// *err and returns false.
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* err) {
-  for (int i = 0; i < kTimeoutIters; ++i)
-    if (mbar_try_wait(bar, parity)) return true;
-  if (err) atomicExch(err, kDevTimeout);
-  return false;
+  if (mbar_try_wait(bar, parity)) return true;
+  const unsigned long long t0 = global_ns();
+  while (!mbar_try_wait(bar, parity)) {
+    if (global_ns() - t0 > kTimeoutNs) {
+      if (err) atomicExch(err, kDevTimeout);
+      return false;
+    }
+  }
+  return true;
 }
 __device__ __forceinline__ void fence_barrier_init() {
   asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -111,6 +123,13 @@ __device__ __forceinline__ void tma_store_3d(const CUtensorMap* map, int x, int 
   asm volatile("cp.async.bulk.tensor.3d.global.shared::cta.tile.bulk_group [%0, {%1, %2, %3}], [%4];" ::"l"(map),
                "r"(x), "r"(y), "r"(z), "r"(smem_addr(src))
                : "memory");
+}
+__device__ __forceinline__ void tma_store_5d(const CUtensorMap* map, int c0, int c1, int c2, int c3, int c4,
+                                             const void* src) {
+  asm volatile(
+      "cp.async.bulk.tensor.5d.global.shared::cta.tile.bulk_group [%0, {%1, %2, %3, %4, %5}], [%6];" ::"l"(map),
+      "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(c4), "r"(smem_addr(src))
+      : "memory");
 }
 __device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
 template <int N>

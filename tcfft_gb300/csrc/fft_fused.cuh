@@ -1,0 +1,445 @@
+// fft_fused.cuh -- persistent two-phase FFT executor (large 1D sizes and 2D).
+//
+// A transform is processed in two phases with TMA-fed shared-memory tiles:
+//
+//   1D, N = N1*N2 (four-step, replaces the reference's chain of layer_*_0 +
+//   layer_*_1 launches, tcfft_half.cu:1205-1232, which make one full HBM
+//   round trip per launch):
+//     phase 0  (COL):   data[n1][n2] -> FFT over n1 (length N1, stride N2)
+//                       -> twiddle W_N^(n2 k1) -> scratch[k1][n2]
+//     phase 1  (ROW_T): scratch row k1 -> FFT over n2 (length N2)
+//                       -> data[k1 + N1 k2]  (transposed write)
+//   2D, [NX][NY] row-major (replaces tcfft_half_2d.cu:1128-1149's two
+//   launches):
+//     phase 0  (ROW):   FFT of each contiguous row (length NY), in place
+//     phase 1  (COL):   FFT of each column (length NX, stride NY), in place
+//
+// One launch processes every transform of the batch.  Work items (tiles) are
+// ordered in blocks: block s holds the phase-0 tiles of transform s followed by
+// the phase-1 tiles of transform s - D, so the intermediate of a transform is
+// consumed D blocks after it was produced, while it is still in L2.  The 1D
+// intermediate lives in a ring of S >= D + 1 scratch slots.  Cross-CTA
+// ordering uses per-slot completion counters (release/acquire, bounded spins
+// that raise kDevTimeout instead of hanging).
+//
+// CTA = 8 compute warps + 1 TMA-load warp + 1 TMA-store warp, a ring of
+// kStages shared-memory tiles (full / computed / empty mbarriers).
+#pragma once
+#include "fft_job.cuh"
+
+namespace tcfft {
+
+enum Role : int { kRoleCol = 0, kRoleRowT = 1, kRoleRow = 2 };
+
+struct FusedMaps {
+  CUtensorMap load0, store0, load1, store1;
+};
+
+struct FusedParams {
+  const float2* tw2048;
+  const float2* twlo;  // W_N^j, j < 2^tw_shift        (1D phase-0 twiddle)
+  const float2* twhi;  // W_N^(j << tw_shift)
+  int tw_shift;
+  long long n_mask;    // N - 1 (1D)
+  int batch;           // transforms
+  int D;               // lag in blocks between phase 0 and phase 1 of a transform
+  int S;               // counter / scratch slots
+  int T0, T1;          // tiles per transform in each phase
+  int rows0, rows1;    // rows per transform in the phase's load geometry (see launcher)
+  int cols0, cols1;    // column groups per transform (COL tiles) / row groups (ROW tiles)
+  int* cnt0;           // [S] completed phase-0 tiles per slot (monotonic within an execute)
+  int* cnt1;           // [S] completed phase-1 tiles per slot
+  int* err;
+  float dsign;
+};
+
+template <int C, int ES>
+__device__ __forceinline__ uint32_t col_tile_off(int row, int col) {
+  // tile of C columns; one row = C*ES bytes (32, 64 or 128) with the matching
+  // TMA swizzle (16-byte chunk index XOR address bits [7:9] / [7:8] / [7])
+  constexpr int RB = C * ES;
+  static_assert(RB == 32 || RB == 64 || RB == 128, "column tiles are 32-, 64- or 128-byte rows");
+  const int chunk = (col * ES) >> 4;
+  const int within = (col * ES) & 15;
+  const int sw = RB == 128 ? (row & 7) : (RB == 64 ? ((row >> 1) & 3) : ((row >> 2) & 1));
+  return (uint32_t)(row * RB + ((chunk ^ sw) << 4) + within);
+}
+
+// Row of output k = q + R (k0 + 16 k1) inside a column/transposed output tile:
+// rows are stored in (k1, k0, q) order so that the 32 lanes of a warp, whose
+// k1 digits are 8 consecutive values, touch rows with 8 distinct low bits; a
+// 5D TMA store box puts them back in natural order.
+__device__ __forceinline__ int out_row(int kp, int q) { return (kp >> 4) + 16 * (kp & 15) + 256 * q; }
+
+template <bool SPLIT>
+__device__ __forceinline__ float2 lds_elem(uint32_t addr) {
+  if constexpr (SPLIT) return lds64f(addr);
+  else return unpack_h2(lds32(addr));
+}
+template <bool SPLIT>
+__device__ __forceinline__ void sts_elem(uint32_t addr, float2 v) {
+  if constexpr (SPLIT) sts64f(addr, v);
+  else sts32(addr, pack_h2(v.x, v.y));
+}
+
+__device__ __forceinline__ int ld_acquire(const int* p) {
+  int v;
+  asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void red_release_add(int* p, int v) {
+  asm volatile("red.release.gpu.global.add.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+// Bounded spin until *p >= target.
+__device__ __forceinline__ bool wait_counter(const int* p, int target, int* err) {
+  if (ld_acquire(p) >= target) return true;
+  const unsigned long long t0 = global_ns();
+  while (ld_acquire(p) < target) {
+    if (global_ns() - t0 > kTimeoutNs) {
+      if (err) atomicExch(err, kDevTimeout);
+      return false;
+    }
+    __nanosleep(64);
+  }
+  return true;
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
+__device__ __forceinline__ void named_bar_sync(int id, int n) {
+  asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n) : "memory");
+}
+// Barrier over `n` threads that also returns the AND of `pred` across them.
+__device__ __forceinline__ bool named_bar_and(int id, int n, bool pred) {
+  uint32_t r;
+  asm volatile(
+      "{\n .reg .pred p, q;\n setp.ne.u32 p, %1, 0;\n bar.red.and.pred q, %2, %3, p;\n selp.u32 %0, 1, 0, q;\n}\n"
+      : "=r"(r)
+      : "r"((uint32_t)pred), "r"(id), "r"(n)
+      : "memory");
+  return r != 0;
+}
+
+template <int ROLE0, int R0, int C0, int ROLE1, int R1, int C1, bool SPLIT>
+struct FusedCfg {
+  static constexpr int kES = SPLIT ? 8 : 4;
+  static constexpr int kER = 128 / kES;
+  static constexpr int kTile0 = C0 * 256 * R0;  // elements per tile
+  static constexpr int kTile1 = C1 * 256 * R1;
+  static constexpr int kTileMax = kTile0 > kTile1 ? kTile0 : kTile1;
+  static constexpr int kStageBytes = kTileMax * kES;
+  // shared-memory twiddle tables: W_{256 Rmax}^j and the two halves of W_N^j (1D)
+  static constexpr int kRmax = R0 > R1 ? R0 : R1;
+  static constexpr int kLog2R01 = (R0 >= 8 ? 3 : R0 >= 4 ? 2 : R0 >= 2 ? 1 : 0) + (R1 >= 8 ? 3 : R1 >= 4 ? 2 : R1 >= 2 ? 1 : 0);
+  static constexpr int kTwShift = 8 + (kLog2R01 + 1) / 2;                  // log2 of the low table length
+  static constexpr int kTwHi = 1 << (16 + kLog2R01 - kTwShift);            // N >> shift
+  static constexpr int kTabBytes = (256 * kRmax + (1 << kTwShift) + kTwHi) * 8;
+  // contiguous-row tiles move as boxes of [kER elements][kBH rows] (kBH <= 256)
+  static constexpr int kBH0 = kTile0 / kER < 256 ? kTile0 / kER : 256;
+  static constexpr int kBH1 = kTile1 / kER < 256 ? kTile1 / kER : 256;
+  static constexpr int kBudget = 225 * 1024 - kTabBytes - 1024 - 256;
+  static constexpr int kStages = kBudget / kStageBytes >= 4 ? 4 : kBudget / kStageBytes;
+  static constexpr int kSmem = kStages * kStageBytes + kTabBytes + 1024 + 256;
+  static_assert(kStages >= 2, "at least two tile stages");
+  static constexpr int kThreads = 320;  // 8 compute warps + producer + storer
+  using PI = typename std::conditional<SPLIT, BitPerm<0, 1, 2, 3>, BitPerm<0, 1, 3, 2>>::type;
+  using RHO = BitPerm<0, 2, 3, 1>;
+};
+
+// Item decode: block s = idx / (T0+T1); phase-0 tiles of transform s, then
+// phase-1 tiles of transform s - D.
+struct Item {
+  int phase, b, tile;
+  bool valid;
+};
+__device__ __forceinline__ Item decode_item(long long idx, const FusedParams& p) {
+  const int per = p.T0 + p.T1;
+  const long long blk = idx / per;
+  const int r = (int)(idx - blk * per);
+  Item it;
+  if (r < p.T0) {
+    it.phase = 0;
+    it.b = (int)blk;
+    it.tile = r;
+  } else {
+    it.phase = 1;
+    it.b = (int)(blk - p.D);
+    it.tile = r - p.T0;
+  }
+  it.valid = it.b >= 0 && it.b < p.batch;
+  return it;
+}
+
+template <int ROLE0, int R0, int C0, int ROLE1, int R1, int C1, bool SPLIT>
+__global__ void __launch_bounds__(320, 1)  // 10 warps: <= 168 registers (3 warps on one SM sub-partition)
+    fft_fused_kernel(const __grid_constant__ FusedMaps maps, const FusedParams p) {
+  using Cfg = FusedCfg<ROLE0, R0, C0, ROLE1, R1, C1, SPLIT>;
+  constexpr int ES = Cfg::kES, ER = Cfg::kER, NST = Cfg::kStages;
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  unsigned char* smem =
+      reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  float2* s_twR = reinterpret_cast<float2*>(smem + NST * Cfg::kStageBytes);  // W_{256 Rmax}^j
+  float2* s_twlo = s_twR + 256 * Cfg::kRmax;                                 // W_N^j, j < 2^shift
+  float2* s_twhi = s_twlo + (1 << Cfg::kTwShift);                            // W_N^(j << shift)
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + NST * Cfg::kStageBytes + Cfg::kTabBytes);
+  uint64_t* computed = full + NST;
+  uint64_t* empty = computed + NST;
+
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const long long total = (long long)(p.batch + p.D) * (p.T0 + p.T1);
+
+  if (tid == 0) {
+    for (int s = 0; s < NST; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&computed[s], 8);
+      mbar_init(&empty[s], 1);
+    }
+    fence_barrier_init();
+  }
+  // twiddle tables into shared memory (the inner loops never touch global tables)
+  for (int j = tid; j < 256 * Cfg::kRmax; j += blockDim.x) s_twR[j] = p.tw2048[j * (8 / Cfg::kRmax)];
+  if (ROLE1 == kRoleRowT) {
+    for (int j = tid; j < (1 << Cfg::kTwShift); j += blockDim.x) s_twlo[j] = p.twlo[j];
+    for (int j = tid; j < Cfg::kTwHi; j += blockDim.x) s_twhi[j] = p.twhi[j];
+  }
+  __syncthreads();
+
+  if (warp == 8) {
+    // ------------------------------------------------------------ TMA producer
+    if (lane == 0) {
+      prefetch_tmap(&maps.load0);
+      prefetch_tmap(&maps.load1);
+      int cnt = 0;
+      for (long long idx = blockIdx.x; idx < total; idx += gridDim.x) {
+        const Item it = decode_item(idx, p);
+        if (!it.valid) continue;
+        const int s = cnt % NST;
+        if (!mbar_wait(&empty[s], ((cnt / NST) + 1) & 1, p.err)) break;
+        const int slot = it.b % p.S, epoch = it.b / p.S;
+        if (it.phase == 0) {
+          // the previous occupant of this slot (transform b - S) must be finished, so that
+          // the slot's scratch (1D) and completion counters (1D and 2D) are free
+          if (epoch > 0 && !wait_counter(&p.cnt1[slot], epoch * p.T1, p.err)) break;
+        } else {
+          if (!wait_counter(&p.cnt0[slot], (epoch + 1) * p.T0, p.err)) break;
+          fence_proxy_async_global();
+        }
+        unsigned char* dst = smem + s * Cfg::kStageBytes;
+        if (it.phase == 0) {
+          mbar_arrive_expect_tx(&full[s], Cfg::kTile0 * ES);
+          if constexpr (ROLE0 == kRoleCol) {
+            const int cg = it.tile % p.cols0;
+#pragma unroll 1
+            for (int i = 0; i < R0; ++i)
+              tma_load_2d(dst + i * (256 * C0 * ES), &maps.load0, cg * C0, it.b * p.rows0 + 256 * i, &full[s]);
+          } else {  // contiguous rows
+            const int y0 = (int)(((long long)it.b * p.rows0 + (long long)it.tile * C0) * (256 * R0) / ER);
+#pragma unroll 1
+            for (int i = 0; i < Cfg::kTile0 / (ER * Cfg::kBH0); ++i)
+              tma_load_2d(dst + i * (ER * Cfg::kBH0 * ES), &maps.load0, 0, y0 + Cfg::kBH0 * i, &full[s]);
+          }
+        } else {
+          mbar_arrive_expect_tx(&full[s], Cfg::kTile1 * ES);
+          if constexpr (ROLE1 == kRoleCol) {
+            const int cg = it.tile % p.cols1;
+#pragma unroll 1
+            for (int i = 0; i < R1; ++i)
+              tma_load_2d(dst + i * (256 * C1 * ES), &maps.load1, cg * C1, it.b * p.rows1 + 256 * i, &full[s]);
+          } else {
+            // 1D: source is the scratch slot; 2D never has a contiguous phase 1
+            const long long row0 = (long long)slot * p.rows1 + (long long)it.tile * C1;
+            const int y0 = (int)(row0 * (256 * R1) / ER);
+#pragma unroll 1
+            for (int i = 0; i < Cfg::kTile1 / (ER * Cfg::kBH1); ++i)
+              tma_load_2d(dst + i * (ER * Cfg::kBH1 * ES), &maps.load1, 0, y0 + Cfg::kBH1 * i, &full[s]);
+          }
+        }
+        ++cnt;
+      }
+      // on an early exit let loads still in flight land before the CTA ends (bounded)
+      for (int i = (cnt > NST ? cnt - NST : 0); i < cnt; ++i) mbar_wait(&full[i % NST], (i / NST) & 1, nullptr);
+    }
+    return;
+  }
+  if (warp == 9) {
+    // ------------------------------------------------------------ TMA storer
+    // Up to kMaxPending stores stay in flight; their completion counters are
+    // released in order once the bulk group reports them written.  Before the
+    // storer blocks on the next computed tile it drains and releases every
+    // pending store, so a consumer waiting on this CTA's output never waits
+    // behind this CTA's own pipeline.
+    if (lane == 0) {
+      prefetch_tmap(&maps.store0);
+      prefetch_tmap(&maps.store1);
+      constexpr int kMaxPending = 2;
+      int* pend[kMaxPending + 1];
+      int npend = 0;
+      auto release_all = [&]() {
+        if (npend == 0) return;
+        bulk_wait<0>();
+        fence_proxy_async_global();
+        __threadfence();
+        for (int i = 0; i < npend; ++i) red_release_add(pend[i], 1);
+        npend = 0;
+      };
+      int cnt = 0;
+      bool failed = false;
+      for (long long idx = blockIdx.x; idx < total && !failed; idx += gridDim.x) {
+        const Item it = decode_item(idx, p);
+        if (!it.valid) continue;
+        const int s = cnt % NST;
+        const uint32_t par = (cnt / NST) & 1;
+        if (!mbar_try_wait(&computed[s], par)) {
+          release_all();
+          if (!mbar_wait(&computed[s], par, p.err)) {
+            failed = true;
+            break;
+          }
+        }
+        const unsigned char* src = smem + s * Cfg::kStageBytes;
+        const int slot = it.b % p.S;
+        if (it.phase == 0) {
+          if constexpr (ROLE0 == kRoleCol) {
+            // 5D box [C0][k1][k0][q][transform]: 1D -> scratch slot, 2D -> the data
+            const int cg = it.tile % p.cols0;
+            tma_store_5d(&maps.store0, cg * C0, 0, 0, 0, (ROLE1 == kRoleRowT) ? slot : it.b, src);
+          } else {
+            const int y0 = (int)(((long long)it.b * p.rows0 + (long long)it.tile * C0) * (256 * R0) / ER);
+#pragma unroll 1
+            for (int i = 0; i < Cfg::kTile0 / (ER * Cfg::kBH0); ++i)
+              tma_store_2d(&maps.store0, 0, y0 + Cfg::kBH0 * i, src + i * (ER * Cfg::kBH0 * ES));
+          }
+        } else {
+          if constexpr (ROLE1 == kRoleCol) {
+            const int cg = it.tile % p.cols1;
+            tma_store_5d(&maps.store1, cg * C1, 0, 0, 0, it.b, src);
+          } else {  // ROW_T: output columns k1 of data viewed [B][N2 rows k2][N1 cols]
+            tma_store_5d(&maps.store1, it.tile * C1, 0, 0, 0, it.b, src);
+          }
+        }
+        bulk_commit();
+        pend[npend++] = it.phase == 0 ? &p.cnt0[slot] : &p.cnt1[slot];
+        bulk_wait_read<0>();
+        mbar_arrive(&empty[s]);
+        if (npend > kMaxPending) {
+          // the oldest group is complete once at most kMaxPending remain
+          bulk_wait<kMaxPending>();
+          fence_proxy_async_global();
+          __threadfence();
+          red_release_add(pend[0], 1);
+          for (int i = 1; i < npend; ++i) pend[i - 1] = pend[i];
+          --npend;
+        }
+        ++cnt;
+      }
+      release_all();
+    }
+    return;
+  }
+
+  // -------------------------------------------------------------- compute warps
+  using PI = typename Cfg::PI;
+  using RHO = typename Cfg::RHO;
+  JobConsts<SPLIT> jc;
+  init_job_consts<SPLIT, PI, RHO>(jc, p.tw2048);
+  int cnt = 0;
+  for (long long idx = blockIdx.x; idx < total; idx += gridDim.x) {
+    const Item it = decode_item(idx, p);
+    if (!it.valid) continue;
+    const int s = cnt % NST;
+    // all compute warps agree on success before any of them enters a named barrier
+    const bool ok = named_bar_and(2, 256, mbar_wait(&full[s], (cnt / NST) & 1, p.err));
+    const uint32_t base = smem_addr(smem + s * Cfg::kStageBytes);
+    if (ok) {
+      if (it.phase == 0) {
+        if constexpr (ROLE0 == kRoleCol) {
+          // columns in place; 1D adds the four-step twiddle W_N^(n2 k1)
+          const int cg = it.tile % p.cols0;
+#pragma unroll 1
+          for (int j = warp; j < C0; j += 8) {
+            const int n2 = cg * C0 + j;
+            auto ld = [&](int n) { return lds_elem<SPLIT>(base + col_tile_off<C0, ES>(n, j)); };
+            if constexpr (ROLE1 == kRoleRowT) {
+              // four-step twiddle W_N^(n2 k), k = q + R0 k':  W^(n2 q) * W^(n2 R0 k'), factors per job
+              const int nmask = (int)p.n_mask;
+              auto wn = [&](int e) {
+                e &= nmask;
+                return cmul(s_twhi[e >> Cfg::kTwShift], s_twlo[e & ((1 << Cfg::kTwShift) - 1)]);
+              };
+              float2 fk[8], fq[R0];
+#pragma unroll
+              for (int sl = 0; sl < 8; ++sl) fk[sl] = wn(n2 * R0 * jc.kval[sl >> 2][(sl >> 1) & 1][sl & 1]);
+#pragma unroll
+              for (int q = 0; q < R0; ++q) fq[q] = wn(n2 * q);
+              auto st = [&](int k, int q, int sl, float2 v) {
+                v = cmul(v, cmul(fk[sl], fq[q]));
+                sts_elem<SPLIT>(base + col_tile_off<C0, ES>(out_row((k - q) / R0, q), j), v);
+              };
+              fft256r_job<R0, SPLIT, Cfg::kRmax / R0>(jc, s_twR, p.dsign, ld, st);
+            } else {
+              auto st = [&](int k, int q, int sl, float2 v) {
+                sts_elem<SPLIT>(base + col_tile_off<C0, ES>(out_row((k - q) / R0, q), j), v);
+              };
+              fft256r_job<R0, SPLIT, Cfg::kRmax / R0>(jc, s_twR, p.dsign, ld, st);
+            }
+          }
+        } else {  // kRoleRow: contiguous rows in place (2D phase 0)
+#pragma unroll 1
+          for (int j = warp; j < C0; j += 8) {
+            const uint32_t rb = base + (uint32_t)(j * 256 * R0 * ES);
+            auto ld = [&](int n) { return lds_elem<SPLIT>(rb + swz_w<ES>(n) * ES); };
+            auto st = [&](int k, int q, int sl, float2 v) { sts_elem<SPLIT>(rb + swz_w<ES>(k) * ES, v); };
+            fft256r_job<R0, SPLIT, Cfg::kRmax / R0>(jc, s_twR, p.dsign, ld, st);
+          }
+        }
+      } else {
+        if constexpr (ROLE1 == kRoleCol) {
+#pragma unroll 1
+          for (int j = warp; j < C1; j += 8) {
+            auto ld = [&](int n) { return lds_elem<SPLIT>(base + col_tile_off<C1, ES>(n, j)); };
+            auto st = [&](int k, int q, int sl, float2 v) {
+              sts_elem<SPLIT>(base + col_tile_off<C1, ES>(out_row((k - q) / R1, q), j), v);
+            };
+            fft256r_job<R1, SPLIT, Cfg::kRmax / R1>(jc, s_twR, p.dsign, ld, st);
+          }
+        } else {  // kRoleRowT: rows -> transposed output tile in the same stage
+          static_assert(C1 == 16 || C1 == 8, "row-transpose tiles hold 8 or 16 rows");
+          constexpr int JPW = C1 / 8;  // jobs per compute warp
+          using Hold = typename std::conditional<SPLIT, float2, uint32_t>::type;
+          Hold out[JPW][256 * R1 / 32];
+#pragma unroll
+          for (int jj = 0; jj < JPW; ++jj) {
+            const int j = warp + 8 * jj;
+            const uint32_t rb = base + (uint32_t)(j * 256 * R1 * ES);
+            auto ld = [&](int n) { return lds_elem<SPLIT>(rb + swz_w<ES>(n) * ES); };
+            auto st = [&](int k, int q, int sl, float2 v) {
+              if constexpr (SPLIT) out[jj][8 * q + sl] = v;
+              else out[jj][8 * q + sl] = pack_h2(v.x, v.y);
+            };
+            fft256r_job<R1, SPLIT, Cfg::kRmax / R1>(jc, s_twR, p.dsign, ld, st);
+          }
+          named_bar_sync(1, 256);  // every compute warp finished reading the stage
+#pragma unroll
+          for (int jj = 0; jj < JPW; ++jj) {
+            const int j = warp + 8 * jj;
+#pragma unroll
+            for (int q = 0; q < R1; ++q)
+#pragma unroll
+              for (int sl = 0; sl < 8; ++sl) {
+                const int row = out_row(jc.kval[sl >> 2][(sl >> 1) & 1][sl & 1], q);
+                if constexpr (SPLIT) sts64f(base + col_tile_off<C1, ES>(row, j), out[jj][8 * q + sl]);
+                else sts32(base + col_tile_off<C1, ES>(row, j), out[jj][8 * q + sl]);
+              }
+          }
+        }
+      }
+    }
+    fence_proxy_async_smem();
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&computed[s]);
+    if (!ok) break;
+    ++cnt;
+  }
+}
+
+}  // namespace tcfft

@@ -8,6 +8,7 @@
 // stream and returns a status.
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <new>
@@ -60,7 +61,21 @@ namespace {
 
 bool is_pow2(int64_t v) { return v > 0 && (v & (v - 1)) == 0; }
 
-tcfftStatus cuda_status(cudaError_t e) { return e == cudaSuccess ? TCFFT_SUCCESS : TCFFT_CUDA_ERROR; }
+// With TCFFT_DEBUG set, failing CUDA calls are reported on stderr.
+bool debug_on() {
+  static const bool on = getenv("TCFFT_DEBUG") != nullptr;
+  return on;
+}
+tcfftStatus cuda_status(cudaError_t e, const char* what = "launch") {
+  if (e == cudaSuccess) return TCFFT_SUCCESS;
+  if (debug_on()) fprintf(stderr, "tcfft: %s failed: %s\n", what, cudaGetErrorString(e));
+  return TCFFT_CUDA_ERROR;
+}
+tcfftStatus cu_status(CUresult r, const char* what) {
+  if (r == CUDA_SUCCESS) return TCFFT_SUCCESS;
+  if (debug_on()) fprintf(stderr, "tcfft: %s failed: CUresult %d\n", what, (int)r);
+  return TCFFT_CUDA_ERROR;
+}
 
 // W_2048^j in fp32, computed in fp64 with exact octant reduction.
 void host_twiddles(int n, int sign, std::vector<float2>& out) {
@@ -95,8 +110,35 @@ void free_tables(tcfftPlanImpl* p) {
     if (p->tables.tw2048[d]) cudaFree(p->tables.tw2048[d]);
   if (p->tables.err) cudaFree(p->tables.err);
   if (p->scratch) cudaFree(p->scratch);
+  for (int d = 0; d < 2; ++d) {
+    if (p->twlo[d]) cudaFree(p->twlo[d]);
+    if (p->twhi[d]) cudaFree(p->twhi[d]);
+    p->twlo[d] = p->twhi[d] = nullptr;
+  }
+  if (p->counters) cudaFree(p->counters);
+  p->counters = nullptr;
   p->tables = DeviceTables();
   p->scratch = nullptr;
+}
+
+int ilog2_exact(int64_t v) {
+  int r = 0;
+  while ((int64_t(1) << r) < v) ++r;
+  return r;
+}
+
+// Lag (in blocks) between the two phases of the fused executor and the number
+// of slots: enough tiles in flight across the GPU to cover, L2-sized ring.
+// Tiles in flight span about (CTAs x stages) items; a transform's phase 1 is
+// placed D blocks after its phase 0, and a slot is reused S blocks later, so
+// both D and S - D must exceed the blocks in flight.
+void fused_lag(int T0, int T1, int64_t batch, Schedule& s) {
+  const int in_flight = 152 * 4;  // CTAs x tiles per CTA
+  int D = (in_flight + (T0 + T1) - 1) / (T0 + T1) + 1;
+  if (D > batch) D = (int)batch;
+  if (D < 1) D = 1;
+  s.D = D;
+  s.S = 2 * D + 2;
 }
 
 // Host-only schedule selection for a 1D size (no CUDA calls).
@@ -105,12 +147,38 @@ tcfftStatus choose_1d(int64_t n, int64_t batch, int precision, Schedule& s) {
   if (batch < 1 || batch > (int64_t(1) << 40) / n) return TCFFT_INVALID_SIZE;
   const bool split = precision == TCFFT_PRECISION_SPLIT;
   s = Schedule();
+  char buf[160];
   if (n <= 2048 && !(split && n == 2048)) {
     s.kind = Schedule::kSmall;
     s.R = (int)(n / 256);
     s.launches = 1;
-    char buf[96];
     snprintf(buf, sizeof buf, "small(R=%d,%s): 1 pass, 2 mma stages + radix-%d", s.R, split ? "split" : "plain", s.R);
+    s.text = buf;
+    return TCFFT_SUCCESS;
+  }
+  const int lg = ilog2_exact(n);
+  if (lg >= 16 && lg <= 22) {
+    const int64_t n1 = int64_t(1) << ((lg + 1) / 2), n2 = n / n1;
+    FusedKey k;
+    k.role0 = kRoleCol;
+    k.R0 = (int)(n1 / 256);
+    k.C0 = fused_cols(k.R0, split);
+    k.role1 = kRoleRowT;
+    k.R1 = (int)(n2 / 256);
+    k.C1 = fused_cols(k.R1, split);
+    k.split = split;
+    if (k.C0 == 0 || k.C1 == 0) return TCFFT_NOT_SUPPORTED;
+    s.kind = Schedule::kFused1d;
+    s.N1 = n1;
+    s.N2 = n2;
+    s.key = k;
+    s.T0 = (int)(n2 / k.C0);
+    s.T1 = (int)(n1 / k.C1);
+    fused_lag(s.T0, s.T1, batch, s);
+    s.launches = 1;
+    snprintf(buf, sizeof buf,
+             "fused1d(%s): N=%lld x %lld, phase0 columns R=%d C=%d, phase1 rows R=%d C=%d, lag %d, %d slots",
+             split ? "split" : "plain", (long long)n1, (long long)n2, k.R0, k.C0, k.R1, k.C1, s.D, s.S);
     s.text = buf;
     return TCFFT_SUCCESS;
   }
@@ -138,21 +206,128 @@ tcfftStatus exec_plan(tcfftPlan plan, void* data, void* stream, int dir) {
     // 2D view of the whole batch: rows of 128 bytes
     const int es = split ? 8 : 4, er = 128 / es;
     const uint64_t rows = (uint64_t)plan->total_elems / er;
-    if (plan->tmap_ptr != data || plan->tmap_dir_kind != 0) {
+    if (plan->tmap_ptr != data) {
       uint64_t dims[2] = {(uint64_t)er, rows};
       uint64_t strides[1] = {128};
       uint32_t box[2] = {(uint32_t)er, 256};
       CUresult r = encode_tmap(&plan->tmap0, split ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_UINT32,
                                2, data, dims, strides, box, CU_TENSOR_MAP_SWIZZLE_128B);
-      if (r != CUDA_SUCCESS) return TCFFT_CUDA_ERROR;
+      if (cu_status(r, "tmap small")) return TCFFT_CUDA_ERROR;
       plan->tmap_ptr = data;
-      plan->tmap_dir_kind = 0;
     }
     int launches = 0;
     return cuda_status(launch_small(s.R, split, plan->tmap0, plan->total_elems, tw, dsign, plan->tables.err,
                                     plan->num_sms, st, &launches));
   }
+  if (s.kind == Schedule::kFused1d) {
+    const int es = split ? 8 : 4, er = 128 / es;
+    const CUtensorMapDataType dt = split ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_UINT32;
+    if (plan->tmap_ptr != data) {
+      const FusedKey& k = s.key;
+      auto sw = [&](int c) {
+        return c * es == 32 ? CU_TENSOR_MAP_SWIZZLE_32B
+                            : (c * es == 64 ? CU_TENSOR_MAP_SWIZZLE_64B : CU_TENSOR_MAP_SWIZZLE_128B);
+      };
+      {  // phase-0 load: data as [B*N1][N2]
+        uint64_t dims[2] = {(uint64_t)s.N2, (uint64_t)(plan->batch * s.N1)};
+        uint64_t str[1] = {(uint64_t)(s.N2 * es)};
+        uint32_t box[2] = {(uint32_t)k.C0, 256};
+        if (cu_status(encode_tmap(&plan->fmaps.load0, dt, 2, data, dims, str, box, sw(k.C0)), "tmap load0"))
+          return TCFFT_CUDA_ERROR;
+      }
+      {  // phase-1 store: X[k1 + N1 k2], k2 = q + R1 (k0 + 16 k1'): dims [N1][k1'][k0][q][B]
+        const uint64_t rowb = (uint64_t)s.N1 * es;
+        uint64_t dims[5] = {(uint64_t)s.N1, 16, 16, (uint64_t)k.R1, (uint64_t)plan->batch};
+        uint64_t str[4] = {rowb * 16 * k.R1, rowb * k.R1, rowb, rowb * s.N2};
+        uint32_t box[5] = {(uint32_t)k.C1, 16, 16, (uint32_t)k.R1, 1};
+        if (cu_status(encode_tmap(&plan->fmaps.store1, dt, 5, data, dims, str, box, sw(k.C1)), "tmap store1"))
+          return TCFFT_CUDA_ERROR;
+      }
+      {  // phase-0 store: scratch rows k1 = q + R0 (k0 + 16 k1'): dims [N2][k1'][k0][q][slot]
+        const uint64_t rowb = (uint64_t)s.N2 * es;
+        uint64_t dims[5] = {(uint64_t)s.N2, 16, 16, (uint64_t)k.R0, (uint64_t)s.S};
+        uint64_t str[4] = {rowb * 16 * k.R0, rowb * k.R0, rowb, rowb * s.N1};
+        uint32_t box[5] = {(uint32_t)k.C0, 16, 16, (uint32_t)k.R0, 1};
+        if (cu_status(encode_tmap(&plan->fmaps.store0, dt, 5, plan->scratch, dims, str, box, sw(k.C0)),
+                      "tmap store0"))
+          return TCFFT_CUDA_ERROR;
+      }
+      {  // phase-1 load: scratch as contiguous 128-byte rows, boxes of one tile (<= 256 rows)
+        const int64_t tile_rows = (int64_t)k.C1 * s.N2 / er;
+        uint64_t dims[2] = {(uint64_t)er, (uint64_t)(s.S * s.N1 * s.N2 / er)};
+        uint64_t str[1] = {128};
+        uint32_t box[2] = {(uint32_t)er, (uint32_t)(tile_rows < 256 ? tile_rows : 256)};
+        if (cu_status(encode_tmap(&plan->fmaps.load1, dt, 2, plan->scratch, dims, str, box,
+                                  CU_TENSOR_MAP_SWIZZLE_128B),
+                      "tmap load1"))
+          return TCFFT_CUDA_ERROR;
+      }
+      plan->tmap_ptr = data;
+    }
+    FusedParams fp;
+    fp.tw2048 = tw;
+    fp.twlo = plan->twlo[dir];
+    fp.twhi = plan->twhi[dir];
+    fp.tw_shift = plan->tw_shift;
+    fp.n_mask = (long long)(plan->n - 1);
+    fp.batch = (int)plan->batch;
+    fp.D = s.D;
+    fp.S = s.S;
+    fp.T0 = s.T0;
+    fp.T1 = s.T1;
+    fp.rows0 = (int)s.N1;
+    fp.rows1 = (int)s.N1;
+    fp.cols0 = s.T0;
+    fp.cols1 = s.T1;
+    fp.cnt0 = plan->counters;
+    fp.cnt1 = plan->counters + s.S;
+    fp.err = plan->tables.err;
+    fp.dsign = dsign;
+    if (cuda_status(cudaMemsetAsync(plan->counters, 0, sizeof(int) * 2 * s.S, st), "counter reset"))
+      return TCFFT_CUDA_ERROR;
+    int grid = 0;
+    return cuda_status(launch_fused(s.key, plan->fmaps, fp, plan->num_sms, st, &grid), "fused launch");
+  }
   return TCFFT_NOT_SUPPORTED;
+}
+
+// Two-level W_N table (fp32 from long double): W_N^j = hi[j >> shift] * lo[j & mask].
+tcfftStatus alloc_wn_tables(tcfftPlanImpl* p, int64_t n) {
+  const int lg = ilog2_exact(n);
+  p->tw_shift = (lg + 1) / 2;
+  const int64_t nlo = int64_t(1) << p->tw_shift, nhi = n >> p->tw_shift;
+  std::vector<float2> lo(nlo), hi(nhi);
+  for (int d = 0; d < 2; ++d) {
+    const long double sgn = d == 0 ? -1.0L : 1.0L;
+    const long double twopi = 2.0L * 3.141592653589793238462643383279502884L;
+    for (int64_t j = 0; j < nlo; ++j) {
+      const long double th = twopi * (long double)j / (long double)n;
+      lo[j] = make_float2((float)cosl(th), (float)(sgn * sinl(th)));
+    }
+    for (int64_t j = 0; j < nhi; ++j) {
+      const long double th = twopi * (long double)(j << p->tw_shift) / (long double)n;
+      hi[j] = make_float2((float)cosl(th), (float)(sgn * sinl(th)));
+    }
+    if (cudaMalloc(&p->twlo[d], nlo * sizeof(float2)) != cudaSuccess) return TCFFT_ALLOC_FAILED;
+    if (cudaMalloc(&p->twhi[d], nhi * sizeof(float2)) != cudaSuccess) return TCFFT_ALLOC_FAILED;
+    if (cudaMemcpy(p->twlo[d], lo.data(), nlo * sizeof(float2), cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(p->twhi[d], hi.data(), nhi * sizeof(float2), cudaMemcpyHostToDevice) != cudaSuccess)
+      return TCFFT_CUDA_ERROR;
+  }
+  return TCFFT_SUCCESS;
+}
+
+tcfftStatus alloc_fused(tcfftPlanImpl* p) {
+  const Schedule& s = p->sched;
+  const int es = p->precision == TCFFT_PRECISION_SPLIT ? 8 : 4;
+  if (cudaMalloc(&p->counters, sizeof(int) * 2 * s.S) != cudaSuccess) return TCFFT_ALLOC_FAILED;
+  if (s.kind == Schedule::kFused1d) {
+    tcfftStatus st = alloc_wn_tables(p, p->n);
+    if (st != TCFFT_SUCCESS) return st;
+    p->scratch_bytes = (int64_t)s.S * p->n * es;
+    if (cudaMalloc(&p->scratch, p->scratch_bytes) != cudaSuccess) return TCFFT_ALLOC_FAILED;
+  }
+  return TCFFT_SUCCESS;
 }
 
 }  // namespace
@@ -217,6 +392,7 @@ tcfftStatus tcfftPlan1d(tcfftPlan* out, int64_t n, int64_t batch, const tcfftOpt
   p->total_elems = n * batch;
   p->sched = s;
   st = alloc_tables(p);
+  if (st == TCFFT_SUCCESS && s.kind != Schedule::kSmall) st = alloc_fused(p);
   if (st != TCFFT_SUCCESS) {
     free_tables(p);
     delete p;

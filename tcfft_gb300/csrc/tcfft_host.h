@@ -24,6 +24,17 @@ struct DeviceTables {
   int* err = nullptr;                      // device error word
 };
 
+struct FusedMaps;
+struct FusedParams;
+// Identifies one instantiation of the two-phase executor (fft_fused.cuh).
+struct FusedKey {
+  int role0 = 0, R0 = 1, C0 = 16, role1 = 0, R1 = 1, C1 = 16;
+  bool split = false;
+};
+int fused_cols(int R, bool split);
+cudaError_t launch_fused(const FusedKey& k, const FusedMaps& maps, const FusedParams& p, int num_sms,
+                         cudaStream_t st, int* grid_out);
+
 // Launch entry points implemented in the kernel translation units. Each
 // returns cudaSuccess or the launch error.
 cudaError_t launch_small(int R, bool split, const CUtensorMap& tmap, int64_t total_elems, const float2* tw,

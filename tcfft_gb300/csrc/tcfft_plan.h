@@ -2,16 +2,20 @@
 #pragma once
 #include <string>
 
+#include "fft_fused.cuh"
 #include "tcfft_host.h"
 
 namespace tcfft {
 
-// Execution schedule chosen at plan time.
+// Execution schedule chosen at plan time (host-only, no CUDA calls).
 struct Schedule {
-  enum Kind { kNone = 0, kSmall = 1 } kind = kNone;
-  int R = 1;          // small: radix of the tail (N = 256 R)
-  int launches = 0;   // kernel launches per execute
-  std::string text;   // human-readable description
+  enum Kind { kNone = 0, kSmall = 1, kFused1d = 2, kFused2d = 3 } kind = kNone;
+  int R = 1;             // small: N = 256 R
+  int64_t N1 = 0, N2 = 0;  // fused 1D: N = N1 N2 (phase 0 columns of N1, phase 1 rows of N2)
+  FusedKey key;          // fused: kernel instantiation
+  int T0 = 0, T1 = 0, D = 0, S = 0;
+  int launches = 0;      // kernel launches per execute
+  std::string text;      // human-readable description
 };
 
 }  // namespace tcfft
@@ -26,10 +30,15 @@ struct tcfftPlanImpl {
   int64_t total_elems = 0;
   tcfft::Schedule sched;
   tcfft::DeviceTables tables;
+  // fused executor resources
+  float2* twlo[2] = {nullptr, nullptr};
+  float2* twhi[2] = {nullptr, nullptr};
+  int tw_shift = 0;
+  int* counters = nullptr;  // [2 * S]
   void* scratch = nullptr;
   int64_t scratch_bytes = 0;
   // tensor maps encoded for the last data pointer
   void* tmap_ptr = nullptr;
-  int tmap_dir_kind = -1;
   CUtensorMap tmap0;
+  tcfft::FusedMaps fmaps;
 };

@@ -85,3 +85,51 @@ def test_linearity_and_parseval(cuda_device):
     assert oracle.rel_l2(fab, fa + fb) < 1e-5
     ta = a[..., 0] + 1j * a[..., 1]
     assert abs(np.sum(np.abs(fa) ** 2) / (n * np.sum(np.abs(ta) ** 2)) - 1) < 1e-5
+
+
+LARGE = [1 << 16, 1 << 17, 1 << 18, 1 << 19, 1 << 20, 1 << 21, 1 << 22]
+
+
+@pytest.mark.parametrize("n", LARGE)
+@pytest.mark.parametrize("batch", [1, 3])
+def test_plain_large(cuda_device, n, batch):
+    x = uniform_input((batch, n), seed=n % 1000 + batch)
+    xq = quantize(x, "plain")
+    with tc.Plan(n=n, batch=batch) as p:
+        assert "fused1d" in p.info["schedule"]
+        y = run_gpu(p, xq, "plain")
+    ref = oracle_1d(xq)
+    assert np.isfinite(y).all()
+    err = oracle.rel_l2(y, ref)
+    assert err < TOL_PLAIN, "n=%d batch=%d rel-L2 %.3e" % (n, batch, err)
+
+
+@pytest.mark.parametrize("n", [1 << 16, 1 << 18, 1 << 20])
+def test_split_large(cuda_device, n):
+    batch = 2
+    x = uniform_input((batch, n), seed=n % 997)
+    xq = quantize(x, "split")
+    with tc.Plan(n=n, batch=batch, precision="split") as p:
+        y = run_gpu(p, xq, "split")
+    err = oracle.rel_l2(y, oracle_1d(xq))
+    assert err < TOL_SPLIT, "n=%d rel-L2 %.3e" % (n, err)
+
+
+@pytest.mark.parametrize("n", [1 << 16, 1 << 20])
+def test_adjoint_large(cuda_device, n):
+    batch = 2
+    xq = quantize(uniform_input((batch, n), seed=5), "plain")
+    with tc.Plan(n=n, batch=batch) as p:
+        y = run_gpu(p, xq, "plain", adjoint=True)
+    assert oracle.rel_l2(y, oracle_1d(xq, adjoint=True)) < TOL_PLAIN
+
+
+def test_large_batch_many_waves(cuda_device):
+    """More transforms than scratch slots: the slot ring is reused many times."""
+    n, batch = 1 << 16, 100
+    xq = quantize(uniform_input((batch, n), seed=77), "plain")
+    with tc.Plan(n=n, batch=batch) as p:
+        y = run_gpu(p, xq, "plain")
+    ref = oracle_1d(xq)
+    per = np.linalg.norm(y - ref, axis=-1) / np.linalg.norm(ref, axis=-1)
+    assert per.max() < TOL_PLAIN
