@@ -141,7 +141,13 @@ struct FusedCfg {
   static constexpr int kStages = kBudget / kStageBytes >= 4 ? 4 : kBudget / kStageBytes;
   static constexpr int kSmem = kStages * kStageBytes + kTabBytes + 1024 + 256;
   static_assert(kStages >= 2, "at least two tile stages");
-  static constexpr int kThreads = 320;  // 8 compute warps + producer + storer
+  // 3 warpgroups: two of compute warps, one holding the producer and storer warps.
+  // Launched at 168 registers/thread (384 x 168 = 64512); setmaxnreg moves
+  // registers to the compute warpgroups: 256 x kComputeRegs + 128 x kAuxRegs = 64512.
+  static constexpr int kThreads = 384;
+  static constexpr int kComputeRegs = 224;
+  static constexpr int kAuxRegs = 56;
+  static_assert(256 * kComputeRegs + 128 * kAuxRegs == 384 * 168, "register split must match the launch");
   using PI = typename std::conditional<SPLIT, BitPerm<0, 1, 2, 3>, BitPerm<0, 1, 3, 2>>::type;
   using RHO = BitPerm<0, 2, 3, 1>;
 };
@@ -171,7 +177,7 @@ __device__ __forceinline__ Item decode_item(long long idx, const FusedParams& p)
 }
 
 template <int ROLE0, int R0, int C0, int ROLE1, int R1, int C1, bool SPLIT>
-__global__ void __launch_bounds__(320, 1)  // 10 warps: <= 168 registers (3 warps on one SM sub-partition)
+__global__ void __launch_bounds__(384, 1)  // 12 warps at launch: 168 registers (3 warps per SM sub-partition)
     fft_fused_kernel(const __grid_constant__ FusedMaps maps, const FusedParams p) {
   using Cfg = FusedCfg<ROLE0, R0, C0, ROLE1, R1, C1, SPLIT>;
   constexpr int ES = Cfg::kES, ER = Cfg::kER, NST = Cfg::kStages;
@@ -203,6 +209,13 @@ __global__ void __launch_bounds__(320, 1)  // 10 warps: <= 168 registers (3 warp
     for (int j = tid; j < Cfg::kTwHi; j += blockDim.x) s_twhi[j] = p.twhi[j];
   }
   __syncthreads();
+
+  if (warp >= 8) {
+    // auxiliary warpgroup: give registers back; each path below ends in return,
+    // so the compute code is reached only through the setmaxnreg.inc further down
+    asm volatile("setmaxnreg.dec.sync.aligned.u32 %0;" ::"n"(Cfg::kAuxRegs));
+    if (warp >= 10) return;  // spare warps
+  }
 
   if (warp == 8) {
     // ------------------------------------------------------------ TMA producer
@@ -338,6 +351,7 @@ __global__ void __launch_bounds__(320, 1)  // 10 warps: <= 168 registers (3 warp
   }
 
   // -------------------------------------------------------------- compute warps
+  asm volatile("setmaxnreg.inc.sync.aligned.u32 %0;" ::"n"(Cfg::kComputeRegs));
   using PI = typename Cfg::PI;
   using RHO = typename Cfg::RHO;
   JobConsts<SPLIT> jc;
