@@ -1,5 +1,4 @@
-// fft_fused.cu -- instantiations and launcher of the persistent two-phase
-// executor (1D four-step N = N1*N2, 2D row+column).
+// fft_fused.cu -- instantiations of the persistent two-phase executor (1D four-step).
 #include <mutex>
 
 #include "fft_fused.cuh"
@@ -8,7 +7,6 @@
 namespace tcfft {
 
 namespace {
-
 template <int ROLE0, int R0, int C0, int ROLE1, int R1, int C1, bool SPLIT>
 cudaError_t launch_t(const FusedMaps& maps, const FusedParams& p, int num_sms, cudaStream_t st, int* grid_out) {
   using Cfg = FusedCfg<ROLE0, R0, C0, ROLE1, R1, C1, SPLIT>;
@@ -26,25 +24,17 @@ cudaError_t launch_t(const FusedMaps& maps, const FusedParams& p, int num_sms, c
   kern<<<(int)grid, Cfg::kThreads, Cfg::kSmem, st>>>(maps, p);
   return cudaGetLastError();
 }
-
-// key: role pair, R0, R1, split (C derived)
-#define TCFFT_FUSED_CASE(RO0, RR0, CC0, RO1, RR1, CC1, SP)                                                        \
-  if (k.role0 == RO0 && k.R0 == RR0 && k.C0 == CC0 && k.role1 == RO1 && k.R1 == RR1 && k.C1 == CC1 && k.split == SP) \
-    return launch_t<RO0, RR0, CC0, RO1, RR1, CC1, SP>(maps, p, num_sms, st, grid_out);
-
 }  // namespace
 
-int fused_cols(int R, bool split) {
-  // columns (or rows) per tile: keep a tile <= 64 KB and its rows at 64 or 128 bytes
-  const int es = split ? 8 : 4;
-  int c = 16;
-  while (c > 8 && c * 256 * R * es > 64 * 1024) c /= 2;
-  if (c * 256 * R * es > 64 * 1024) return 0;
-  return c;
-}
+#define TCFFT_FUSED_CASE(RO0, RR0, CC0, RO1, RR1, CC1, SP)                                                        \
+  if (k.role0 == RO0 && k.R0 == RR0 && k.C0 == CC0 && k.role1 == RO1 && k.R1 == RR1 && k.C1 == CC1 && k.split == SP) { \
+    *handled = true;                                                                                                \
+    return launch_t<RO0, RR0, CC0, RO1, RR1, CC1, SP>(maps, p, num_sms, st, grid_out);                             \
+  }
 
-cudaError_t launch_fused(const FusedKey& k, const FusedMaps& maps, const FusedParams& p, int num_sms,
-                         cudaStream_t st, int* grid_out) {
+cudaError_t launch_fused_1d(const FusedKey& k, const FusedMaps& maps, const FusedParams& p, int num_sms, cudaStream_t st,
+                int* grid_out, bool* handled) {
+  *handled = false;
   // 1D four-step: phase 0 = columns of N1 = 256*R0, phase 1 = rows of N2 = 256*R1 (N1 >= N2)
   TCFFT_FUSED_CASE(kRoleCol, 1, 16, kRoleRowT, 1, 16, false)
   TCFFT_FUSED_CASE(kRoleCol, 2, 16, kRoleRowT, 1, 16, false)
@@ -58,6 +48,14 @@ cudaError_t launch_fused(const FusedKey& k, const FusedMaps& maps, const FusedPa
   TCFFT_FUSED_CASE(kRoleCol, 2, 16, kRoleRowT, 2, 16, true)
   TCFFT_FUSED_CASE(kRoleCol, 4, 8, kRoleRowT, 2, 16, true)
   TCFFT_FUSED_CASE(kRoleCol, 4, 8, kRoleRowT, 4, 8, true)
+  // 1D N = 256 x (16..128): phase 1 = 16 short rows per warp
+  TCFFT_FUSED_CASE(kRoleCol, 1, 16, kRoleRow16T, 1, 128, false)
+  TCFFT_FUSED_CASE(kRoleCol, 1, 16, kRoleRow16T, 2, 128, false)
+  TCFFT_FUSED_CASE(kRoleCol, 1, 16, kRoleRow16T, 4, 128, false)
+  TCFFT_FUSED_CASE(kRoleCol, 1, 16, kRoleRow16T, 8, 128, false)
+  TCFFT_FUSED_CASE(kRoleCol, 1, 16, kRoleRow16T, 1, 128, true)
+  TCFFT_FUSED_CASE(kRoleCol, 1, 16, kRoleRow16T, 2, 128, true)
+  TCFFT_FUSED_CASE(kRoleCol, 1, 16, kRoleRow16T, 4, 128, true)
   return cudaErrorNotSupported;
 }
 

@@ -29,7 +29,13 @@
 
 namespace tcfft {
 
-enum Role : int { kRoleCol = 0, kRoleRowT = 1, kRoleRow = 2 };
+// kRoleCol:    FFT of length 256R down tile columns, in place (TMA 5D store, digit-ordered rows)
+// kRoleRowT:   FFT of length 256R along contiguous rows, written transposed (1D phase 1)
+// kRoleRow:    FFT of length 256R along contiguous rows, in place (2D phase 0)
+// kRoleRow16T: 16 rows at a time, FFT of length 16R along each, written transposed (1D phase 1, short rows)
+enum Role : int { kRoleCol = 0, kRoleRowT = 1, kRoleRow = 2, kRoleRow16T = 3 };
+__host__ __device__ constexpr int role_len(int role, int R) { return role == kRoleRow16T ? 16 * R : 256 * R; }
+__host__ __device__ constexpr int ilog2c(int v) { return v <= 1 ? 0 : 1 + ilog2c(v >> 1); }
 
 struct FusedMaps {
   CUtensorMap load0, store0, load1, store1;
@@ -124,16 +130,21 @@ template <int ROLE0, int R0, int C0, int ROLE1, int R1, int C1, bool SPLIT>
 struct FusedCfg {
   static constexpr int kES = SPLIT ? 8 : 4;
   static constexpr int kER = 128 / kES;
-  static constexpr int kTile0 = C0 * 256 * R0;  // elements per tile
-  static constexpr int kTile1 = C1 * 256 * R1;
+  static constexpr bool k1D = ROLE1 == kRoleRowT || ROLE1 == kRoleRow16T;
+  static constexpr int kLen0 = role_len(ROLE0, R0), kLen1 = role_len(ROLE1, R1);  // FFT lengths
+  static constexpr int kTile0 = C0 * kLen0;  // elements per tile
+  static constexpr int kTile1 = C1 * kLen1;
   static constexpr int kTileMax = kTile0 > kTile1 ? kTile0 : kTile1;
   static constexpr int kStageBytes = kTileMax * kES;
-  // shared-memory twiddle tables: W_{256 Rmax}^j and the two halves of W_N^j (1D)
-  static constexpr int kRmax = R0 > R1 ? R0 : R1;
-  static constexpr int kLog2R01 = (R0 >= 8 ? 3 : R0 >= 4 ? 2 : R0 >= 2 ? 1 : 0) + (R1 >= 8 ? 3 : R1 >= 4 ? 2 : R1 >= 2 ? 1 : 0);
-  static constexpr int kTwShift = 8 + (kLog2R01 + 1) / 2;                  // log2 of the low table length
-  static constexpr int kTwHi = 1 << (16 + kLog2R01 - kTwShift);            // N >> shift
-  static constexpr int kTabBytes = (256 * kRmax + (1 << kTwShift) + kTwHi) * 8;
+  // shared-memory twiddle tables: W_L^j (L = the longer job length) and the two
+  // halves of W_N^j (1D four-step, N = kLen0 * kLen1)
+  static constexpr int kLmax = kLen0 > kLen1 ? kLen0 : kLen1;
+  static constexpr int kLog2N = ilog2c(kLen0) + ilog2c(kLen1);
+  static constexpr int kTwShift = (kLog2N + 1) / 2;          // log2 of the low table length
+  static constexpr int kTwHi = 1 << (kLog2N - kTwShift);     // N >> shift
+  static constexpr int kTabBytes = (kLmax + (k1D ? (1 << kTwShift) + kTwHi : 0)) * 8;
+  // kRoleRow16T output boxes: kBW columns (128 bytes) each
+  static constexpr int kBW = 128 / kES;
   // contiguous-row tiles move as boxes of [kER elements][kBH rows] (kBH <= 256)
   static constexpr int kBH0 = kTile0 / kER < 256 ? kTile0 / kER : 256;
   static constexpr int kBH1 = kTile1 / kER < 256 ? kTile1 / kER : 256;
@@ -184,8 +195,8 @@ __global__ void __launch_bounds__(384, 1)  // 12 warps at launch: 168 registers 
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* smem =
       reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-  float2* s_twR = reinterpret_cast<float2*>(smem + NST * Cfg::kStageBytes);  // W_{256 Rmax}^j
-  float2* s_twlo = s_twR + 256 * Cfg::kRmax;                                 // W_N^j, j < 2^shift
+  float2* s_twR = reinterpret_cast<float2*>(smem + NST * Cfg::kStageBytes);  // W_Lmax^j
+  float2* s_twlo = s_twR + Cfg::kLmax;                                       // W_N^j, j < 2^shift
   float2* s_twhi = s_twlo + (1 << Cfg::kTwShift);                            // W_N^(j << shift)
   uint64_t* full = reinterpret_cast<uint64_t*>(smem + NST * Cfg::kStageBytes + Cfg::kTabBytes);
   uint64_t* computed = full + NST;
@@ -203,8 +214,8 @@ __global__ void __launch_bounds__(384, 1)  // 12 warps at launch: 168 registers 
     fence_barrier_init();
   }
   // twiddle tables into shared memory (the inner loops never touch global tables)
-  for (int j = tid; j < 256 * Cfg::kRmax; j += blockDim.x) s_twR[j] = p.tw2048[j * (8 / Cfg::kRmax)];
-  if (ROLE1 == kRoleRowT) {
+  for (int j = tid; j < Cfg::kLmax; j += blockDim.x) s_twR[j] = p.tw2048[j * (2048 / Cfg::kLmax)];
+  if (Cfg::k1D) {
     for (int j = tid; j < (1 << Cfg::kTwShift); j += blockDim.x) s_twlo[j] = p.twlo[j];
     for (int j = tid; j < Cfg::kTwHi; j += blockDim.x) s_twhi[j] = p.twhi[j];
   }
@@ -261,7 +272,7 @@ __global__ void __launch_bounds__(384, 1)  // 12 warps at launch: 168 registers 
           } else {
             // 1D: source is the scratch slot; 2D never has a contiguous phase 1
             const long long row0 = (long long)slot * p.rows1 + (long long)it.tile * C1;
-            const int y0 = (int)(row0 * (256 * R1) / ER);
+            const int y0 = (int)(row0 * Cfg::kLen1 / ER);
 #pragma unroll 1
             for (int i = 0; i < Cfg::kTile1 / (ER * Cfg::kBH1); ++i)
               tma_load_2d(dst + i * (ER * Cfg::kBH1 * ES), &maps.load1, 0, y0 + Cfg::kBH1 * i, &full[s]);
@@ -315,7 +326,7 @@ __global__ void __launch_bounds__(384, 1)  // 12 warps at launch: 168 registers 
           if constexpr (ROLE0 == kRoleCol) {
             // 5D box [C0][k1][k0][q][transform]: 1D -> scratch slot, 2D -> the data
             const int cg = it.tile % p.cols0;
-            tma_store_5d(&maps.store0, cg * C0, 0, 0, 0, (ROLE1 == kRoleRowT) ? slot : it.b, src);
+            tma_store_5d(&maps.store0, cg * C0, 0, 0, 0, Cfg::k1D ? slot : it.b, src);
           } else {
             const int y0 = (int)(((long long)it.b * p.rows0 + (long long)it.tile * C0) * (256 * R0) / ER);
 #pragma unroll 1
@@ -326,8 +337,13 @@ __global__ void __launch_bounds__(384, 1)  // 12 warps at launch: 168 registers 
           if constexpr (ROLE1 == kRoleCol) {
             const int cg = it.tile % p.cols1;
             tma_store_5d(&maps.store1, cg * C1, 0, 0, 0, it.b, src);
-          } else {  // ROW_T: output columns k1 of data viewed [B][N2 rows k2][N1 cols]
+          } else if constexpr (ROLE1 == kRoleRowT) {  // output columns k1 of data viewed [B][N2 rows k2][N1 cols]
             tma_store_5d(&maps.store1, it.tile * C1, 0, 0, 0, it.b, src);
+          } else {  // kRoleRow16T: C1 columns as boxes of kBW, 4D [cols][k0][q][B]
+#pragma unroll 1
+            for (int bx = 0; bx < C1 / Cfg::kBW; ++bx)
+              tma_store_4d(&maps.store1, it.tile * C1 + bx * Cfg::kBW, 0, 0, it.b,
+                           src + bx * (Cfg::kBW * Cfg::kLen1 * ES));
           }
         }
         bulk_commit();
@@ -373,7 +389,7 @@ __global__ void __launch_bounds__(384, 1)  // 12 warps at launch: 168 registers 
           for (int j = warp; j < C0; j += 8) {
             const int n2 = cg * C0 + j;
             auto ld = [&](int n) { return lds_elem<SPLIT>(base + col_tile_off<C0, ES>(n, j)); };
-            if constexpr (ROLE1 == kRoleRowT) {
+            if constexpr (Cfg::k1D) {
               // four-step twiddle W_N^(n2 k), k = q + R0 k':  W^(n2 q) * W^(n2 R0 k'), factors per job
               const int nmask = (int)p.n_mask;
               auto wn = [&](int e) {
@@ -389,12 +405,12 @@ __global__ void __launch_bounds__(384, 1)  // 12 warps at launch: 168 registers 
                 v = cmul(v, cmul(fk[sl], fq[q]));
                 sts_elem<SPLIT>(base + col_tile_off<C0, ES>(out_row((k - q) / R0, q), j), v);
               };
-              fft256r_job<R0, SPLIT, Cfg::kRmax / R0>(jc, s_twR, p.dsign, ld, st);
+              fft256r_job<R0, SPLIT, Cfg::kLmax / (256 * R0)>(jc, s_twR, p.dsign, ld, st);
             } else {
               auto st = [&](int k, int q, int sl, float2 v) {
                 sts_elem<SPLIT>(base + col_tile_off<C0, ES>(out_row((k - q) / R0, q), j), v);
               };
-              fft256r_job<R0, SPLIT, Cfg::kRmax / R0>(jc, s_twR, p.dsign, ld, st);
+              fft256r_job<R0, SPLIT, Cfg::kLmax / (256 * R0)>(jc, s_twR, p.dsign, ld, st);
             }
           }
         } else {  // kRoleRow: contiguous rows in place (2D phase 0)
@@ -402,8 +418,34 @@ __global__ void __launch_bounds__(384, 1)  // 12 warps at launch: 168 registers 
           for (int j = warp; j < C0; j += 8) {
             const uint32_t rb = base + (uint32_t)(j * 256 * R0 * ES);
             auto ld = [&](int n) { return lds_elem<SPLIT>(rb + swz_w<ES>(n) * ES); };
-            auto st = [&](int k, int q, int sl, float2 v) { sts_elem<SPLIT>(rb + swz_w<ES>(k) * ES, v); };
-            fft256r_job<R0, SPLIT, Cfg::kRmax / R0>(jc, s_twR, p.dsign, ld, st);
+            // outputs k = q + R0 k' of one slot are R0 consecutive elements: hold all q, then
+            // store each slot's run with vector stores (conflict-free, like the single-pass kernel)
+            using Hold = typename std::conditional<SPLIT, float2, uint32_t>::type;
+            Hold out[R0][8];
+            auto st = [&](int k, int q, int sl, float2 v) {
+              if constexpr (SPLIT) out[q][sl] = v;
+              else out[q][sl] = pack_h2(v.x, v.y);
+            };
+            fft256r_job<R0, SPLIT, Cfg::kLmax / (256 * R0)>(jc, s_twR, p.dsign, ld, st);
+#pragma unroll
+            for (int sl = 0; sl < 8; ++sl) {
+              const int k0 = R0 * jc.kval[sl >> 2][(sl >> 1) & 1][sl & 1];
+              if constexpr (!SPLIT) {
+                if constexpr (R0 == 1) sts32(rb + swz_w<4>(k0) * 4, out[0][sl]);
+                else if constexpr (R0 == 2) sts64(rb + swz_w<4>(k0) * 4, out[0][sl], out[1][sl]);
+                else {
+#pragma unroll
+                  for (int q4 = 0; q4 < R0; q4 += 4)
+                    sts128(rb + swz_w<4>(k0 + q4) * 4, out[q4][sl], out[q4 + 1][sl], out[q4 + 2][sl], out[q4 + 3][sl]);
+                }
+              } else {
+                if constexpr (R0 == 1) sts64f(rb + swz_w<8>(k0) * 8, out[0][sl]);
+                else {
+#pragma unroll
+                  for (int q2 = 0; q2 < R0; q2 += 2) sts128f(rb + swz_w<8>(k0 + q2) * 8, out[q2][sl], out[q2 + 1][sl]);
+                }
+              }
+            }
           }
         }
       } else {
@@ -414,7 +456,38 @@ __global__ void __launch_bounds__(384, 1)  // 12 warps at launch: 168 registers 
             auto st = [&](int k, int q, int sl, float2 v) {
               sts_elem<SPLIT>(base + col_tile_off<C1, ES>(out_row((k - q) / R1, q), j), v);
             };
-            fft256r_job<R1, SPLIT, Cfg::kRmax / R1>(jc, s_twR, p.dsign, ld, st);
+            fft256r_job<R1, SPLIT, Cfg::kLmax / (256 * R1)>(jc, s_twR, p.dsign, ld, st);
+          }
+        } else if constexpr (ROLE1 == kRoleRow16T) {
+          // 16 short rows per warp (one S1 job), held in registers, then written
+          // transposed as [k0 + 16 q rows][C1 cols] in boxes of kBW columns
+          static_assert(C1 == 128, "short-row tiles hold 8 warps x 16 rows");
+          using Hold = typename std::conditional<SPLIT, float2, uint32_t>::type;
+          Hold out[8 * R1];
+          {
+            const uint32_t rb = base + (uint32_t)(warp * 16 * Cfg::kLen1 * ES);
+            auto ld = [&](int v, int n) { return lds_elem<SPLIT>(rb + swz_w<ES>(v * Cfg::kLen1 + n) * ES); };
+            auto st = [&](int v, int k, int q, int sl, float2 val) {
+              if constexpr (SPLIT) out[8 * q + sl] = val;
+              else out[8 * q + sl] = pack_h2(val.x, val.y);
+            };
+            fft16r_job<R1, SPLIT, Cfg::kLmax / (16 * R1), PI, RHO>(jc, s_twR, p.dsign, ld, st);
+          }
+          named_bar_sync(1, 256);
+          {
+            const int lane_g = lane >> 2, lane_t = lane & 3;
+#pragma unroll
+            for (int q = 0; q < R1; ++q)
+#pragma unroll
+              for (int sl = 0; sl < 8; ++sl) {
+                const int jj = sl >> 2, h = (sl >> 1) & 1, e = sl & 1;
+                const int col = warp * 16 + 2 * lane_t + e + 8 * jj;
+                const int row = RHO::apply(lane_g + 8 * h) + 16 * q;
+                const uint32_t addr = base + (uint32_t)((col / Cfg::kBW) * (Cfg::kBW * Cfg::kLen1 * ES)) +
+                                      col_tile_off<Cfg::kBW, ES>(row, col % Cfg::kBW);
+                if constexpr (SPLIT) sts64f(addr, out[8 * q + sl]);
+                else sts32(addr, out[8 * q + sl]);
+              }
           }
         } else {  // kRoleRowT: rows -> transposed output tile in the same stage
           static_assert(C1 == 16 || C1 == 8, "row-transpose tiles hold 8 or 16 rows");
@@ -430,7 +503,7 @@ __global__ void __launch_bounds__(384, 1)  // 12 warps at launch: 168 registers 
               if constexpr (SPLIT) out[jj][8 * q + sl] = v;
               else out[jj][8 * q + sl] = pack_h2(v.x, v.y);
             };
-            fft256r_job<R1, SPLIT, Cfg::kRmax / R1>(jc, s_twR, p.dsign, ld, st);
+            fft256r_job<R1, SPLIT, Cfg::kLmax / (256 * R1)>(jc, s_twR, p.dsign, ld, st);
           }
           named_bar_sync(1, 256);  // every compute warp finished reading the stage
 #pragma unroll

@@ -114,3 +114,60 @@ __device__ __forceinline__ void fft256r_job(const JobConsts<SPLIT>& c, const flo
 }
 
 }  // namespace tcfft
+
+namespace tcfft {
+
+// ---------------------------------------------------------------------------
+// One warp computes 16 FFTs of length 16*R at once (one radix-16 tensor-core
+// stage plus a radix-R tail), the 16 transforms being the MMA's N dimension.
+//   n = m1 + 16 a, k = q + R k0:
+//   X_v[q + R k0] = sum_m1 W16^(m1 k0) [ W_{16R}^(m1 q) sum_a x_v[m1 + 16 a] W_R^(a q) ]
+// LOAD(v, n) -> float2 element n of transform v (0 <= v < 16).
+// STORE(v, k, q, slot, float2) receives output k = q + R k0 of transform v;
+// slot = 4j + 2h + e (compile-time after unrolling) with v = 2t + e + 8j,
+// k0 = RHO(g + 8h).
+// tw16R: table with W_{16R}^j at index j*TWS.
+template <int R, bool SPLIT, int TWS, class PI, class RHO, class LoadF, class StoreF>
+__device__ __forceinline__ void fft16r_job(const JobConsts<SPLIT>& c, const float2* __restrict__ tw16R, float dsign,
+                                           LoadF&& load, StoreF&& store) {
+  const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+  uint32_t bhi[R][2][2][2], blo[SPLIT ? R : 1][2][2][2];
+#pragma unroll
+  for (int kt = 0; kt < 2; ++kt)
+#pragma unroll
+    for (int r = 0; r < 2; ++r)
+#pragma unroll
+      for (int j = 0; j < 2; ++j) {
+        const int m1 = PI::apply(2 * t + r + 8 * kt);
+        const int v = g + 8 * j;
+        float2 x[R];
+#pragma unroll
+        for (int a = 0; a < R; ++a) x[a] = load(v, m1 + 16 * a);
+        if constexpr (R > 1) {
+          dft_small<R>(x, dsign);
+#pragma unroll
+          for (int q = 1; q < R; ++q) x[q] = cmul(x[q], tw16R[((m1 * q) & (16 * R - 1)) * TWS]);
+        }
+#pragma unroll
+        for (int q = 0; q < R; ++q) {
+          if constexpr (SPLIT) split_h2(x[q], bhi[q][kt][r][j], blo[q][kt][r][j]);
+          else bhi[q][kt][r][j] = pack_h2(x[q].x, x[q].y);
+        }
+      }
+  __syncwarp();
+#pragma unroll
+  for (int q = 0; q < R; ++q) {
+    float acc[2][2][4];
+    if constexpr (SPLIT) dft16_mma_split(c.afr, c.afr_lo, bhi[q], blo[q], acc);
+    else dft16_mma(c.afr, bhi[q], acc);
+#pragma unroll
+    for (int j = 0; j < 2; ++j)
+#pragma unroll
+      for (int h = 0; h < 2; ++h)
+#pragma unroll
+        for (int e = 0; e < 2; ++e)
+          store(2 * t + e + 8 * j, q + R * RHO::apply(g + 8 * h), q, 4 * j + 2 * h + e, acc_get(acc, j, h, e));
+  }
+}
+
+}  // namespace tcfft

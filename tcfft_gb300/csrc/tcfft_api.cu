@@ -157,6 +157,30 @@ tcfftStatus choose_1d(int64_t n, int64_t batch, int precision, Schedule& s) {
     return TCFFT_SUCCESS;
   }
   const int lg = ilog2_exact(n);
+  if (lg >= 12 && lg <= 15) {
+    // N = 256 x N2 with short rows N2 = 16 R1: phase 0 columns of 256, phase 1 16 rows per warp
+    FusedKey k;
+    k.role0 = kRoleCol;
+    k.R0 = 1;
+    k.C0 = 16;
+    k.role1 = kRoleRow16T;
+    k.R1 = (int)(n / 256 / 16);
+    k.C1 = 128;
+    k.split = split;
+    if (split && k.R1 > 4) return TCFFT_NOT_SUPPORTED;
+    s.kind = Schedule::kFused1d;
+    s.N1 = 256;
+    s.N2 = n / 256;
+    s.key = k;
+    s.T0 = (int)(s.N2 / k.C0 > 0 ? s.N2 / k.C0 : 1);
+    s.T1 = (int)(s.N1 / k.C1);
+    fused_lag(s.T0, s.T1, batch, s);
+    s.launches = 1;
+    snprintf(buf, sizeof buf, "fused1d(%s): N=256 x %lld, phase0 columns R=1 C=16, phase1 16-row groups R=%d, lag %d, %d slots",
+             split ? "split" : "plain", (long long)s.N2, k.R1, s.D, s.S);
+    s.text = buf;
+    return TCFFT_SUCCESS;
+  }
   if (lg >= 16 && lg <= 22) {
     const int64_t n1 = int64_t(1) << ((lg + 1) / 2), n2 = n / n1;
     FusedKey k;
@@ -183,6 +207,37 @@ tcfftStatus choose_1d(int64_t n, int64_t batch, int precision, Schedule& s) {
     return TCFFT_SUCCESS;
   }
   return TCFFT_NOT_SUPPORTED;
+}
+
+// Host-only schedule selection for a 2D size.
+tcfftStatus choose_2d(int64_t nx, int64_t ny, int64_t batch, int precision, Schedule& s) {
+  if (!is_pow2(nx) || !is_pow2(ny) || nx < 256 || ny < 256 || nx > 2048 || ny > 2048) return TCFFT_INVALID_SIZE;
+  if (batch < 1 || batch > (int64_t(1) << 40) / (nx * ny)) return TCFFT_INVALID_SIZE;
+  const bool split = precision == TCFFT_PRECISION_SPLIT;
+  const int es = split ? 8 : 4;
+  s = Schedule();
+  FusedKey k;
+  k.role0 = kRoleRow;
+  k.R0 = (int)(ny / 256);
+  k.C0 = 16 * 256 * k.R0 * es <= 64 * 1024 ? 16 : 8;
+  k.role1 = kRoleCol;
+  k.R1 = (int)(nx / 256);
+  k.C1 = fused_cols(k.R1, split);
+  k.split = split;
+  if (k.C1 == 0 || k.C0 * 256 * k.R0 * es > 64 * 1024 || (split && (k.R0 > 4 || k.R1 > 4))) return TCFFT_NOT_SUPPORTED;
+  s.kind = Schedule::kFused2d;
+  s.N1 = nx;
+  s.N2 = ny;
+  s.key = k;
+  s.T0 = (int)(nx / k.C0);
+  s.T1 = (int)(ny / k.C1);
+  fused_lag(s.T0, s.T1, batch, s);
+  s.launches = 1;
+  char buf[160];
+  snprintf(buf, sizeof buf, "fused2d(%s): %lld x %lld, phase0 rows R=%d C=%d, phase1 columns R=%d C=%d, lag %d",
+           split ? "split" : "plain", (long long)nx, (long long)ny, k.R0, k.C0, k.R1, k.C1, s.D);
+  s.text = buf;
+  return TCFFT_SUCCESS;
 }
 
 tcfftStatus validate_opts(const tcfftOptions* o) {
@@ -235,7 +290,15 @@ tcfftStatus exec_plan(tcfftPlan plan, void* data, void* stream, int dir) {
         if (cu_status(encode_tmap(&plan->fmaps.load0, dt, 2, data, dims, str, box, sw(k.C0)), "tmap load0"))
           return TCFFT_CUDA_ERROR;
       }
-      {  // phase-1 store: X[k1 + N1 k2], k2 = q + R1 (k0 + 16 k1'): dims [N1][k1'][k0][q][B]
+      if (k.role1 == kRoleRow16T) {  // phase-1 store: X[k1 + N1 k2], k2 = q + R1 k0: dims [N1][k0][q][B]
+        const uint64_t rowb = (uint64_t)s.N1 * es;
+        uint64_t dims[4] = {(uint64_t)s.N1, 16, (uint64_t)k.R1, (uint64_t)plan->batch};
+        uint64_t str[3] = {rowb * k.R1, rowb, rowb * s.N2};
+        uint32_t box[4] = {(uint32_t)(128 / es), 16, (uint32_t)k.R1, 1};
+        if (cu_status(encode_tmap(&plan->fmaps.store1, dt, 4, data, dims, str, box, CU_TENSOR_MAP_SWIZZLE_128B),
+                      "tmap store1"))
+          return TCFFT_CUDA_ERROR;
+      } else {  // phase-1 store: X[k1 + N1 k2], k2 = q + R1 (k0 + 16 k1'): dims [N1][k1'][k0][q][B]
         const uint64_t rowb = (uint64_t)s.N1 * es;
         uint64_t dims[5] = {(uint64_t)s.N1, 16, 16, (uint64_t)k.R1, (uint64_t)plan->batch};
         uint64_t str[4] = {rowb * 16 * k.R1, rowb * k.R1, rowb, rowb * s.N2};
@@ -287,6 +350,64 @@ tcfftStatus exec_plan(tcfftPlan plan, void* data, void* stream, int dir) {
       return TCFFT_CUDA_ERROR;
     int grid = 0;
     return cuda_status(launch_fused(s.key, plan->fmaps, fp, plan->num_sms, st, &grid), "fused launch");
+  }
+  if (s.kind == Schedule::kFused2d) {
+    const int es = split ? 8 : 4, er = 128 / es;
+    const CUtensorMapDataType dt = split ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_UINT32;
+    const FusedKey& k = s.key;
+    const int64_t nx = s.N1, ny = s.N2;
+    if (plan->tmap_ptr != data) {
+      auto sw = [&](int c) {
+        return c * es == 32 ? CU_TENSOR_MAP_SWIZZLE_32B
+                            : (c * es == 64 ? CU_TENSOR_MAP_SWIZZLE_64B : CU_TENSOR_MAP_SWIZZLE_128B);
+      };
+      {  // phase 0 (rows, in place): contiguous 128-byte rows, one tile per box group
+        const int64_t tile_rows = (int64_t)k.C0 * ny / er;
+        uint64_t dims[2] = {(uint64_t)er, (uint64_t)(plan->batch * nx * ny / er)};
+        uint64_t str[1] = {128};
+        uint32_t box[2] = {(uint32_t)er, (uint32_t)(tile_rows < 256 ? tile_rows : 256)};
+        if (cu_status(encode_tmap(&plan->fmaps.load0, dt, 2, data, dims, str, box, CU_TENSOR_MAP_SWIZZLE_128B),
+                      "tmap2d load0"))
+          return TCFFT_CUDA_ERROR;
+        plan->fmaps.store0 = plan->fmaps.load0;
+      }
+      {  // phase 1 load: data as [B*NX][NY]
+        uint64_t dims[2] = {(uint64_t)ny, (uint64_t)(plan->batch * nx)};
+        uint64_t str[1] = {(uint64_t)(ny * es)};
+        uint32_t box[2] = {(uint32_t)k.C1, 256};
+        if (cu_status(encode_tmap(&plan->fmaps.load1, dt, 2, data, dims, str, box, sw(k.C1)), "tmap2d load1"))
+          return TCFFT_CUDA_ERROR;
+      }
+      {  // phase 1 store: rows k = q + R1 (k0 + 16 k1'): dims [NY][k1'][k0][q][B]
+        const uint64_t rowb = (uint64_t)ny * es;
+        uint64_t dims[5] = {(uint64_t)ny, 16, 16, (uint64_t)k.R1, (uint64_t)plan->batch};
+        uint64_t str[4] = {rowb * 16 * k.R1, rowb * k.R1, rowb, rowb * nx};
+        uint32_t box[5] = {(uint32_t)k.C1, 16, 16, (uint32_t)k.R1, 1};
+        if (cu_status(encode_tmap(&plan->fmaps.store1, dt, 5, data, dims, str, box, sw(k.C1)), "tmap2d store1"))
+          return TCFFT_CUDA_ERROR;
+      }
+      plan->tmap_ptr = data;
+    }
+    FusedParams fp;
+    memset(&fp, 0, sizeof fp);
+    fp.tw2048 = tw;
+    fp.batch = (int)plan->batch;
+    fp.D = s.D;
+    fp.S = s.S;
+    fp.T0 = s.T0;
+    fp.T1 = s.T1;
+    fp.rows0 = (int)nx;
+    fp.rows1 = (int)nx;
+    fp.cols0 = s.T0;
+    fp.cols1 = s.T1;
+    fp.cnt0 = plan->counters;
+    fp.cnt1 = plan->counters + s.S;
+    fp.err = plan->tables.err;
+    fp.dsign = dsign;
+    if (cuda_status(cudaMemsetAsync(plan->counters, 0, sizeof(int) * 2 * s.S, st), "counter reset"))
+      return TCFFT_CUDA_ERROR;
+    int grid = 0;
+    return cuda_status(launch_fused(s.key, plan->fmaps, fp, plan->num_sms, st, &grid), "fused2d launch");
   }
   return TCFFT_NOT_SUPPORTED;
 }
@@ -405,11 +526,35 @@ tcfftStatus tcfftPlan1d(tcfftPlan* out, int64_t n, int64_t batch, const tcfftOpt
 tcfftStatus tcfftPlan2d(tcfftPlan* out, int64_t nx, int64_t ny, int64_t batch, const tcfftOptions* opts) {
   if (!out) return TCFFT_INVALID_VALUE;
   *out = nullptr;
-  (void)nx;
-  (void)ny;
-  (void)batch;
-  (void)opts;
-  return TCFFT_NOT_SUPPORTED;
+  tcfftStatus st = validate_opts(opts);
+  if (st != TCFFT_SUCCESS) return st;
+  tcfftOptions o;
+  tcfftOptionsDefault(&o);
+  if (opts) o = *opts;
+  Schedule s;
+  st = choose_2d(nx, ny, batch, o.precision, s);
+  if (st != TCFFT_SUCCESS) return st;
+  if (o.input_order == TCFFT_ORDER_REFERENCE_DIGIT_REVERSED) return TCFFT_NOT_SUPPORTED;
+  tcfftPlanImpl* p = new (std::nothrow) tcfftPlanImpl();
+  if (!p) return TCFFT_ALLOC_FAILED;
+  p->kind = 2;
+  p->nx = nx;
+  p->ny = ny;
+  p->n = nx * ny;
+  p->batch = batch;
+  p->precision = o.precision;
+  p->input_order = o.input_order;
+  p->total_elems = nx * ny * batch;
+  p->sched = s;
+  st = alloc_tables(p);
+  if (st == TCFFT_SUCCESS) st = alloc_fused(p);
+  if (st != TCFFT_SUCCESS) {
+    free_tables(p);
+    delete p;
+    return st;
+  }
+  *out = p;
+  return TCFFT_SUCCESS;
 }
 
 tcfftStatus tcfftPlanMany(tcfftPlan* out, int64_t count, const int32_t* ranks, const int64_t* nx, const int64_t* ny,

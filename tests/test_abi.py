@@ -53,6 +53,11 @@ def test_describe_small(n):
     assert "small" in tc.describe_1d(n, 4)
 
 
+@pytest.mark.parametrize("n", [4096, 1 << 15, 1 << 16, 1 << 20, 1 << 22])
+def test_describe_fused(n):
+    assert "fused1d" in tc.describe_1d(n, 4)
+
+
 @pytest.mark.parametrize("n,batch", [(100, 1), (128, 1), (0, 1), (256, 0), (1 << 28, 1)])
 def test_describe_rejects_bad_sizes(n, batch):
     with pytest.raises(tc.TcfftError) as e:
