@@ -1,0 +1,394 @@
+"""Benchmark: batched half-precision FFT throughput on GB300.
+
+Workload (default): 1D complex-to-complex forward FFT, N = 2^20, batch 256,
+so one call transforms 2^28 complex fp16 elements (1 GiB, larger than the
+126 MB L2); real/imag iid uniform[-1, 1) (numpy PCG64, seed 0), generated
+synthetically (no dataset).  Metric: GFLOP/s = 5 N log2(N) batch / t.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--n N] [--batch B]
+                  [--precision plain|split] [--impl ours|reference] [--no-sweep]
+
+One JSON line is printed by rank 0.  Under torchrun (N > 1) every rank runs
+an independent replica on its own GPU (the path shards by transform, no
+collective), timing is max over ranks and `value` is the whole-job
+aggregate ("scaling": "weak").
+
+Keys beyond the base contract: `roofline` (dominant kernel vs the measured
+HBM copy bandwidth), `cpu_baseline` (the FP64 CPU FFT of oracle/ on the host
+cores, bounded sample), `e2e` (host buffers through the public API, copies
+inside the timed region), `clocks` (nvidia-smi sampled during the timed
+region), `sweep` (N = 2^8 .. 2^22 at 2^28 elements per call) and `accuracy`
+(rel-L2 vs numpy's FP64 FFT on a sample, plain and split).
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+FALLBACK_HBM_GBS = 6800.0
+
+
+def measured_peak():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:  # noqa: BLE001 - file optional
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+def profile_traffic(workload_key):
+    """Per-launch DRAM bytes of the dominant kernel from the committed ncu
+    summary (profiles/traffic.txt: '<workload> <bytes_per_launch>')."""
+    path = os.path.join(ROOT, "profiles", "traffic.txt")
+    try:
+        with open(path) as f:
+            for line in f:
+                parts = line.split()
+                if len(parts) >= 2 and parts[0] == workload_key:
+                    return float(parts[1])
+    except OSError:
+        pass
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle sampling during the timed region."""
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index):
+        self.device_index = device_index
+        self.proc = None
+        self.lines = []
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device_index), "--query-gpu=" + self.QUERY,
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for name, val in zip(names, f[5:9]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def flops_per_call(size, batch):
+    return 5.0 * size * math.log2(size) * batch
+
+
+def make_plan(tc, args, size_args, batch):
+    return tc.Plan(batch=batch, precision=args.precision, **size_args)
+
+
+def time_device(torch, plan, x, steps, warmup, dist=None):
+    """W warm-up calls, then K calls timed with CUDA events on the current stream."""
+    for _ in range(warmup):
+        plan.exec(x)
+    torch.cuda.synchronize()
+    if dist is not None:
+        dist.barrier()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(steps):
+        plan.exec(x)
+    e1.record()
+    torch.cuda.synchronize()
+    if dist is not None:
+        dist.barrier()
+    plan.check_device()
+    return e0.elapsed_time(e1) / 1000.0  # seconds for K calls
+
+
+def rel_l2_numpy(y, ref):
+    import numpy as np
+    return float(np.linalg.norm((y - ref).ravel()) / np.linalg.norm(ref.ravel()))
+
+
+def accuracy_sample(torch, tc, size_args, precision, seed=0, count=2):
+    """rel-L2 against numpy's FP64 FFT on `count` transforms of the workload."""
+    import numpy as np
+    n = size_args.get("n")
+    shape = (count, n) if n else (count, size_args["nx"], size_args["ny"])
+    rng = np.random.default_rng(seed)
+    x = rng.uniform(-1.0, 1.0, shape + (2,))
+    dt = np.float16 if precision == "plain" else np.float32
+    xq = x.astype(dt).astype(np.float64)
+    t = torch.from_numpy(x.astype(dt)).cuda()
+    with tc.Plan(batch=count, precision=precision, **size_args) as p:
+        p.exec(t)
+        p.check_device()
+    y = t.double().cpu().numpy()
+    yc = y[..., 0] + 1j * y[..., 1]
+    xc = xq[..., 0] + 1j * xq[..., 1]
+    xu = x[..., 0] + 1j * x[..., 1]
+    if n:
+        ref, refu = np.fft.fft(xc, axis=-1), np.fft.fft(xu, axis=-1)
+    else:
+        ref, refu = np.fft.fft2(xc), np.fft.fft2(xu)
+    return {"rel_l2_vs_fp64_on_rounded_inputs": rel_l2_numpy(yc, ref),
+            "rel_l2_vs_fp64_on_unrounded_inputs": rel_l2_numpy(yc, refu),
+            "nonfinite": int((~np.isfinite(yc)).sum()), "transforms": count}
+
+
+def cpu_baseline(size_args, budget_s=10.0):
+    """The oracle's FP64 CPU FFT (oracle/fft64.c, OpenMP) on the host cores,
+    timed on a bounded sample of the workload's transforms."""
+    import numpy as np
+    import oracle
+    n = size_args.get("n")
+    size = n if n else size_args["nx"] * size_args["ny"]
+    threads = oracle.num_threads()
+    rng = np.random.default_rng(0)
+    per = max(1, threads)
+    x = rng.uniform(-1, 1, (per, size)) + 1j * rng.uniform(-1, 1, (per, size))
+    if n:
+        run = lambda: oracle.fft_1d(x)  # noqa: E731
+    else:
+        xx = x.reshape(per, size_args["nx"], size_args["ny"])
+        run = lambda: oracle.fft_2d(xx)  # noqa: E731
+    run()  # warm
+    done, t0 = 0, time.perf_counter()
+    while True:
+        run()
+        done += per
+        el = time.perf_counter() - t0
+        if el > budget_s or done >= 4096:
+            break
+    gflops = flops_per_call(size, done) / el / 1e9
+    return {"value": gflops, "unit": "GFLOP/s", "cores": threads, "kind": "port",
+            "sample": "%d transforms of the workload size (FP64, oracle/fft64.c, %d OpenMP threads), %.1f s"
+                      % (done, threads, el)}
+
+
+def sweep(torch, tc, precision):
+    out = []
+    peak, _ = measured_peak()
+    es = 4 if precision == "plain" else 8
+    for lg in range(8, 23):
+        n = 1 << lg
+        batch = (1 << 28) // n
+        dt = torch.float16 if precision == "plain" else torch.float32
+        x = torch.empty((batch, n, 2), dtype=dt, device="cuda").uniform_(-1, 1)
+        with tc.Plan(n=n, batch=batch, precision=precision) as p:
+            sec = time_device(torch, p, x, 5, 3) / 5
+        out.append({"n": n, "batch": batch, "us": round(sec * 1e6, 1),
+                    "gflops": round(flops_per_call(n, batch) / sec / 1e9, 1),
+                    "hbm_frac_of_measured": round(2 * es * n * batch / sec / 1e9 / peak, 3)})
+        del x
+        torch.cuda.empty_cache()
+    return out
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--n", type=int, default=1 << 20)
+    ap.add_argument("--nx", type=int, default=0)
+    ap.add_argument("--ny", type=int, default=0)
+    ap.add_argument("--batch", type=int, default=0, help="default: 2^28 elements per call")
+    ap.add_argument("--precision", default="plain", choices=["plain", "split"])
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-sweep", action="store_true")
+    ap.add_argument("--cpu-budget", type=float, default=10.0)
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+
+    if args.nx and args.ny:
+        size_args = {"nx": args.nx, "ny": args.ny}
+        size = args.nx * args.ny
+        wl = "2D C2C forward FFT %dx%d" % (args.nx, args.ny)
+    else:
+        size_args = {"n": args.n}
+        size = args.n
+        wl = "1D C2C forward FFT N=2^%d" % int(math.log2(args.n))
+    batch = args.batch or max(1, (1 << 28) // size)
+    es = 4 if args.precision == "plain" else 8
+    metric = "FFT GFLOP/s (5Nlog2N/t)"
+    config = {"workload": "%s, batch %d (%d complex elements per call), %s, interleaved %s"
+                          % (wl, batch, batch * size, args.precision,
+                             "half2" if args.precision == "plain" else "float2 (hi/lo fp16 products)"),
+              "n": size_args.get("n"), "nx": size_args.get("nx"), "ny": size_args.get("ny"),
+              "batch": batch, "precision": args.precision,
+              "l2": "inputs larger than L2 (%d MiB per call vs 126 MB L2), no flush" % (batch * size * es >> 20),
+              "parallelism": "replicas x%d" % world}
+
+    if args.impl == "reference":
+        # The reference's CPU path is FFTW fp64 (accuracy.cpp:11-23), absent here;
+        # its restatement in oracle/ runs on the host cores with all threads.
+        if rank != 0:
+            return
+        base = cpu_baseline(size_args, budget_s=args.cpu_budget)
+        steps = args.steps
+        ms = flops_per_call(size, batch) / (base["value"] * 1e9) * 1e3
+        line = {"impl": "reference", "metric": metric, "value": base["value"], "unit": "GFLOP/s", "n_gpus": world,
+                "steps": steps, "warmup": args.warmup, "ms_per_step": round(ms, 3), "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "fp64", "data": "synthetic uniform[-1,1)",
+                "config": config, "cpu_baseline": base,
+                "e2e": {"value": base["value"], "unit": "GFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return
+
+    import torch
+    import tcfft_gb300 as tc
+
+    dist = None
+    if world > 1:
+        import torch.distributed as tdist
+        torch.cuda.set_device(local_rank)
+        tdist.init_process_group("nccl")
+        dist = tdist
+    else:
+        torch.cuda.set_device(0)
+    dev_index = torch.cuda.current_device()
+
+    dt = torch.float16 if args.precision == "plain" else torch.float32
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(rank)
+    shape = (batch, size, 2)
+    x = torch.empty(shape, dtype=dt, device="cuda").uniform_(-1, 1, generator=gen)
+    plan = make_plan(tc, args, size_args, batch)
+    info = plan.info
+
+    # ---------------- device-resident timing (value) + clocks
+    sampler = ClockSampler(dev_index)
+    sampler.start()
+    time.sleep(0.3)  # let nvidia-smi start sampling before the timed region
+    secs = time_device(torch, plan, x, args.steps, args.warmup, dist)
+    clocks = sampler.stop()
+    if dist is not None:
+        t = torch.tensor([secs], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        secs = float(t.item())
+    per_call = secs / args.steps
+    value = flops_per_call(size, batch) * world / per_call / 1e9
+
+    # ---------------- roofline of the dominant (only) kernel per call
+    peak, peak_kind = measured_peak()
+    alg_bytes = 2 * es * size * batch
+    achieved = alg_bytes / per_call / 1e9
+    wkey = "%s_%s_%d" % (args.precision, "x".join(str(v) for v in ([args.nx, args.ny] if args.nx else [args.n])),
+                         batch)
+    traffic = profile_traffic(wkey)
+    roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 4), "traffic": traffic,
+                "peak_kind": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind,
+                "algorithmic_bytes_per_launch": alg_bytes,
+                "kernel": info["schedule"]}
+
+    # ---------------- e2e through the public API with host buffers
+    host_in = torch.empty(shape, dtype=dt, pin_memory=True)
+    host_in.uniform_(-1, 1)
+    host_out = torch.empty_like(host_in, pin_memory=True)
+    for _ in range(2):
+        x.copy_(host_in, non_blocking=True)
+        plan.exec(x)
+        host_out.copy_(x, non_blocking=True)
+    torch.cuda.synchronize()
+    if dist is not None:
+        dist.barrier()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e2e_steps = max(3, args.steps // 4)
+    e0.record()
+    for _ in range(e2e_steps):
+        x.copy_(host_in, non_blocking=True)
+        plan.exec(x)
+        host_out.copy_(x, non_blocking=True)
+    e1.record()
+    torch.cuda.synchronize()
+    e2e_s = e0.elapsed_time(e1) / 1000.0 / e2e_steps
+    if dist is not None:
+        t = torch.tensor([e2e_s], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e = {"value": round(flops_per_call(size, batch) * world / e2e_s / 1e9, 1), "unit": "GFLOP/s",
+           "h2d_bytes_per_step": host_in.numel() * host_in.element_size(),
+           "d2h_bytes_per_step": host_out.numel() * host_out.element_size(),
+           "ms_per_step": round(e2e_s * 1e3, 3)}
+    del host_in, host_out
+
+    extra = {}
+    if rank == 0:
+        extra["accuracy"] = {p: accuracy_sample(torch, tc, size_args, p) for p in ("plain", "split")}
+        if not args.no_sweep and "n" in size_args:
+            try:
+                extra["sweep"] = sweep(torch, tc, args.precision)
+            except Exception as e:  # noqa: BLE001 - the sweep is informational
+                extra["sweep_error"] = str(e)
+    plan.destroy()
+    del x
+    torch.cuda.empty_cache()
+
+    if rank == 0:
+        base = cpu_baseline(size_args, budget_s=args.cpu_budget)
+        line = {"metric": metric, "value": round(value, 1), "unit": "GFLOP/s", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": round(per_call * 1e3, 4), "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "fp16" if args.precision == "plain" else "fp16x3",
+                "data": "synthetic: uniform[-1,1) real/imag generated on device",
+                "config": config, "roofline": roofline, "cpu_baseline": base, "e2e": e2e,
+                "gpu_launches": info["launches_per_exec"] * args.steps, "clocks": clocks}
+        line.update(extra)
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()
