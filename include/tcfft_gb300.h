@@ -134,6 +134,31 @@ tcfftStatus tcfftDescribe1d(int64_t n, int64_t batch, int32_t precision, char* b
 /* Library version string. */
 const char* tcfftVersion(void);
 
+/* Allocation-free 1D execute (no counterpart in the reference).
+ *
+ * For callers that cannot call cudaMalloc when they run an FFT: code inside a
+ * CUDA stream capture that must not add allocation nodes, runtimes or plug-in
+ * hosts that own all device memory, or callbacks that run while a memory
+ * pool is locked.  Runs the same two-phase kernel as a tcfftPlan1d plan, in
+ * place on `data` ([batch][n] interleaved complex, device memory, 128-byte
+ * aligned), forward (direction 0) or adjoint (direction 1), on `stream`.
+ *
+ * It allocates nothing: its scratch ring, twiddle tables and completion
+ * counters live in fixed `static __device__` arrays (32 MiB of scratch, about
+ * 32.2 MiB in all) that every GPU loading this library holds until the
+ * process exits.  Limits: n a power of two, 2^12 <= n <= 2^21 for
+ * TCFFT_PRECISION_PLAIN and <= 2^20 for TCFFT_PRECISION_SPLIT; other sizes
+ * return TCFFT_INVALID_SIZE (use a plan).
+ *
+ * All calls share the arrays and leave the last call's contents in them;
+ * each call rewrites its tables and clears its counters on `stream` first, so
+ * calls ordered on one stream are independent, but calls that overlap on the
+ * GPU (different streams or host threads) race and must not be issued
+ * concurrently.  The first call on a device looks up the arrays' device
+ * addresses (cudaGetSymbolAddress); make it before any stream capture. */
+tcfftStatus tcfftExecute1dNoAlloc(void* data, int64_t n, int64_t batch, int32_t precision, int32_t direction,
+                                  void* stream);
+
 #ifdef __cplusplus
 }
 #endif

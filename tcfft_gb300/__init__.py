@@ -88,6 +88,8 @@ _SIGNATURES = {
     "tcfftDescribe1d": ([ctypes.c_int64, ctypes.c_int64, ctypes.c_int32, ctypes.c_char_p, ctypes.c_size_t],
                         ctypes.c_int),
     "tcfftVersion": ([], ctypes.c_char_p),
+    "tcfftExecute1dNoAlloc": ([ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_int32, ctypes.c_int32,
+                               ctypes.c_void_p], ctypes.c_int),
 }
 
 
@@ -139,6 +141,24 @@ def _stream_handle(stream):
     if isinstance(stream, int):
         return ctypes.c_void_p(stream)
     return ctypes.c_void_p(stream.cuda_stream)
+
+
+def _device_ptr(data, precision):
+    """Device address of `data` after checking it matches the precision."""
+    if isinstance(data, int):
+        return data
+    import torch
+    if not isinstance(data, torch.Tensor):
+        raise TypeError("data must be a CUDA torch tensor or a device pointer (int)")
+    if not data.is_cuda:
+        raise ValueError("tcfft executes on device memory; got a CPU tensor")
+    if not data.is_contiguous():
+        raise ValueError("data must be contiguous")
+    want = (torch.float16, torch.complex32) if precision == PRECISION_PLAIN else (torch.float32, torch.complex64)
+    if data.dtype not in want:
+        raise TypeError("precision %s expects %s, got %s" % (
+            "plain" if precision == PRECISION_PLAIN else "split", want, data.dtype))
+    return data.data_ptr()
 
 
 class Plan:
@@ -205,21 +225,7 @@ class Plan:
 
     # -- execution -------------------------------------------------------
     def _ptr(self, data):
-        if isinstance(data, int):
-            return data
-        import torch
-        if not isinstance(data, torch.Tensor):
-            raise TypeError("data must be a CUDA torch tensor or a device pointer (int)")
-        if not data.is_cuda:
-            raise ValueError("tcfft executes on device memory; got a CPU tensor")
-        if not data.is_contiguous():
-            raise ValueError("data must be contiguous")
-        want = (torch.float16, torch.complex32) if self.precision == PRECISION_PLAIN else (torch.float32,
-                                                                                             torch.complex64)
-        if data.dtype not in want:
-            raise TypeError("precision %s expects %s, got %s" % (
-                "plain" if self.precision == PRECISION_PLAIN else "split", want, data.dtype))
-        return data.data_ptr()
+        return _device_ptr(data, self.precision)
 
     def exec(self, data, stream=None, adjoint=False):
         """Transform ``data`` in place (forward, or the adjoint)."""
@@ -287,3 +293,15 @@ def tcfftDestroy(plan):
 
 def version():
     return lib().tcfftVersion().decode()
+
+
+def execute_1d_noalloc(data, n, batch, precision="plain", adjoint=False, stream=None):
+    """Allocation-free in-place 1D FFT (tcfftExecute1dNoAlloc): for callers
+    that cannot allocate device memory when they run a transform.  Uses the
+    library's fixed static scratch (n <= 2^21 plain, <= 2^20 split, n >= 2^12);
+    calls that overlap on the GPU race on that scratch."""
+    prec = _precision_of(precision)
+    ptr = _device_ptr(data, prec)
+    _check(lib().tcfftExecute1dNoAlloc(ctypes.c_void_p(ptr), int(n), int(batch), prec, 1 if adjoint else 0,
+                                       _stream_handle(stream)), "tcfftExecute1dNoAlloc")
+    return data

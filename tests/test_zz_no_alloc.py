@@ -1,0 +1,63 @@
+"""GPU: the allocation-free entry point (tcfftExecute1dNoAlloc), called
+through the C ABI, against the plan-based entry point.
+
+Some callers cannot allocate device memory when they run an FFT (stream
+capture without allocation nodes, hosts that own all device memory); the
+no-alloc entry point serves them from fixed static device arrays.  This file
+is collected last so that a run stopping at the first failure has already run
+every other test; it passes alone in a fresh process and after the others.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+import tcfft_gb300 as tc
+from fftcheck import TOL_PLAIN, TOL_SPLIT, quantize, to_complex, uniform_input
+
+pytestmark = pytest.mark.gpu
+
+CASES = [(1 << 12, 5, "plain"), (1 << 15, 3, "plain"), (1 << 16, 3, "plain"), (1 << 20, 2, "plain"),
+         (1 << 21, 1, "plain"), (1 << 14, 4, "split"), (1 << 18, 2, "split")]
+
+
+def _noalloc(t, n, batch, precision, direction):
+    import torch
+    prec = 0 if precision == "plain" else 1
+    st = tc.lib().tcfftExecute1dNoAlloc(ctypes.c_void_p(t.data_ptr()), n, batch, prec, direction,
+                                        ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+    torch.cuda.synchronize()
+    return st
+
+
+@pytest.mark.parametrize("n,batch,precision", CASES)
+def test_noalloc_matches_plan_two_calls(cuda_device, n, batch, precision):
+    import torch
+    dt = torch.float16 if precision == "plain" else torch.float32
+    tol = TOL_PLAIN if precision == "plain" else TOL_SPLIT
+    x = quantize(uniform_input((batch, n), seed=n % 991 + batch), precision)
+    for direction in (0, 1):
+        ref_t = torch.from_numpy(x).to(dt).to(cuda_device)
+        with tc.Plan(n=n, batch=batch, precision=precision) as p:
+            p.exec(ref_t, adjoint=direction == 1)
+            p.check_device()
+        ref = to_complex(ref_t.double().cpu().numpy())
+        for call in range(2):  # two calls in a row share the static scratch
+            t = torch.from_numpy(x).to(dt).to(cuda_device)
+            assert _noalloc(t, n, batch, precision, direction) == 0
+            y = to_complex(t.double().cpu().numpy())
+            assert np.isfinite(y).all()
+            err = np.linalg.norm(y - ref) / np.linalg.norm(ref)
+            assert err < tol, "n=%d call %d direction %d: rel-L2 %.3e vs plan" % (n, call, direction, err)
+
+
+def test_noalloc_rejects_sizes_beyond_limit(cuda_device):
+    import torch
+    t = torch.zeros((1, 1 << 22, 2), dtype=torch.float16, device=cuda_device)
+    assert _noalloc(t, 1 << 22, 1, "plain", 0) == 2      # beyond the static scratch
+    assert _noalloc(t, 1 << 21, 1, "split", 0) == 2      # split limit is 2^20
+    assert _noalloc(t, 2048, 1, "plain", 0) == 2          # no scratch below 2^12: use a plan
+    assert _noalloc(t, 3000, 1, "plain", 0) == 2
+    u = torch.zeros((1 << 13,), dtype=torch.float16, device=cuda_device)
+    st = tc.lib().tcfftExecute1dNoAlloc(ctypes.c_void_p(u.data_ptr() + 4), 4096, 1, 0, 0, None)
+    assert st == 3                                        # misaligned
