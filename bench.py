@@ -242,6 +242,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-sweep", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=10.0)
+    ap.add_argument("--profile", action="store_true",
+                    help="only the warm-up and timed calls (for ncu captures); prints the time per call")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
 
@@ -304,6 +306,12 @@ def main():
     x = torch.empty(shape, dtype=dt, device="cuda").uniform_(-1, 1, generator=gen)
     plan = make_plan(tc, args, size_args, batch)
     info = plan.info
+    if args.profile:
+        secs = time_device(torch, plan, x, args.steps, args.warmup, dist)
+        if rank == 0:
+            print(json.dumps({"profile_run": info["schedule"], "ms_per_call": secs / args.steps * 1e3}), flush=True)
+        plan.destroy()
+        return
 
     # ---------------- device-resident timing (value) + clocks
     sampler = ClockSampler(dev_index)

@@ -225,29 +225,31 @@ __global__ void __launch_bounds__(384, 1)  // 12 warps at launch: 168 registers 
     // auxiliary warpgroup: give registers back; each path below ends in return,
     // so the compute code is reached only through the setmaxnreg.inc further down
     asm volatile("setmaxnreg.dec.sync.aligned.u32 %0;" ::"n"(Cfg::kAuxRegs));
-    if (warp >= 10) return;  // spare warps
   }
 
+  // Warp 8 is the TMA producer, warp 9 the TMA storer; warps 10-11 idle.
+  if (warp >= 10) return;
   if (warp == 8) {
     // ------------------------------------------------------------ TMA producer
     if (lane == 0) {
       prefetch_tmap(&maps.load0);
       prefetch_tmap(&maps.load1);
-      int cnt = 0;
+      int cnt = 0, issued = 0;
       for (long long idx = blockIdx.x; idx < total; idx += gridDim.x) {
         const Item it = decode_item(idx, p);
         if (!it.valid) continue;
         const int s = cnt % NST;
-        if (!mbar_wait(&empty[s], ((cnt / NST) + 1) & 1, p.err)) break;
         const int slot = it.b % p.S, epoch = it.b / p.S;
+        // dependencies first (their latency overlaps the wait for a free stage)
         if (it.phase == 0) {
           // the previous occupant of this slot (transform b - S) must be finished, so that
           // the slot's scratch (1D) and completion counters (1D and 2D) are free
           if (epoch > 0 && !wait_counter(&p.cnt1[slot], epoch * p.T1, p.err)) break;
         } else {
           if (!wait_counter(&p.cnt0[slot], (epoch + 1) * p.T0, p.err)) break;
-          fence_proxy_async_global();
         }
+        if (!mbar_wait(&empty[s], ((cnt / NST) + 1) & 1, p.err)) break;
+        if (it.phase == 1) fence_proxy_async_global();
         unsigned char* dst = smem + s * Cfg::kStageBytes;
         if (it.phase == 0) {
           mbar_arrive_expect_tx(&full[s], Cfg::kTile0 * ES);
@@ -279,9 +281,11 @@ __global__ void __launch_bounds__(384, 1)  // 12 warps at launch: 168 registers 
           }
         }
         ++cnt;
+        ++issued;
       }
-      // on an early exit let loads still in flight land before the CTA ends (bounded)
+      // on an early exit let this warp's loads still in flight land before the CTA ends (bounded)
       for (int i = (cnt > NST ? cnt - NST : 0); i < cnt; ++i) mbar_wait(&full[i % NST], (i / NST) & 1, nullptr);
+      (void)issued;
     }
     return;
   }
@@ -302,7 +306,6 @@ __global__ void __launch_bounds__(384, 1)  // 12 warps at launch: 168 registers 
         if (npend == 0) return;
         bulk_wait<0>();
         fence_proxy_async_global();
-        __threadfence();
         for (int i = 0; i < npend; ++i) red_release_add(pend[i], 1);
         npend = 0;
       };
@@ -312,10 +315,10 @@ __global__ void __launch_bounds__(384, 1)  // 12 warps at launch: 168 registers 
         const Item it = decode_item(idx, p);
         if (!it.valid) continue;
         const int s = cnt % NST;
-        const uint32_t par = (cnt / NST) & 1;
-        if (!mbar_try_wait(&computed[s], par)) {
+        const uint32_t cpar = (cnt / NST) & 1;
+        if (!mbar_try_wait(&computed[s], cpar)) {
           release_all();
-          if (!mbar_wait(&computed[s], par, p.err)) {
+          if (!mbar_wait(&computed[s], cpar, p.err)) {
             failed = true;
             break;
           }
@@ -354,7 +357,6 @@ __global__ void __launch_bounds__(384, 1)  // 12 warps at launch: 168 registers 
           // the oldest group is complete once at most kMaxPending remain
           bulk_wait<kMaxPending>();
           fence_proxy_async_global();
-          __threadfence();
           red_release_add(pend[0], 1);
           for (int i = 1; i < npend; ++i) pend[i - 1] = pend[i];
           --npend;
@@ -370,8 +372,10 @@ __global__ void __launch_bounds__(384, 1)  // 12 warps at launch: 168 registers 
   asm volatile("setmaxnreg.inc.sync.aligned.u32 %0;" ::"n"(Cfg::kComputeRegs));
   using PI = typename Cfg::PI;
   using RHO = typename Cfg::RHO;
+  using Hold = typename std::conditional<SPLIT, float2, uint32_t>::type;
   JobConsts<SPLIT> jc;
   init_job_consts<SPLIT, PI, RHO>(jc, p.tw2048);
+  const uint32_t twR = smem_addr(s_twR);
   int cnt = 0;
   for (long long idx = blockIdx.x; idx < total; idx += gridDim.x) {
     const Item it = decode_item(idx, p);
@@ -383,86 +387,87 @@ __global__ void __launch_bounds__(384, 1)  // 12 warps at launch: 168 registers 
     if (ok) {
       if (it.phase == 0) {
         if constexpr (ROLE0 == kRoleCol) {
-          // columns in place; 1D adds the four-step twiddle W_N^(n2 k1)
+          // columns j = warp + 8 jn in place; 1D adds the four-step twiddle W_N^(n2 k1)
+          constexpr int JN = C0 / 8;
           const int cg = it.tile % p.cols0;
-#pragma unroll 1
-          for (int j = warp; j < C0; j += 8) {
-            const int n2 = cg * C0 + j;
-            auto ld = [&](int n) { return lds_elem<SPLIT>(base + col_tile_off<C0, ES>(n, j)); };
-            if constexpr (Cfg::k1D) {
-              // four-step twiddle W_N^(n2 k), k = q + R0 k':  W^(n2 q) * W^(n2 R0 k'), factors per job
-              const int nmask = (int)p.n_mask;
-              auto wn = [&](int e) {
-                e &= nmask;
-                return cmul(s_twhi[e >> Cfg::kTwShift], s_twlo[e & ((1 << Cfg::kTwShift) - 1)]);
-              };
-              float2 fk[8], fq[R0];
-#pragma unroll
-              for (int sl = 0; sl < 8; ++sl) fk[sl] = wn(n2 * R0 * jc.kval[sl >> 2][(sl >> 1) & 1][sl & 1]);
-#pragma unroll
-              for (int q = 0; q < R0; ++q) fq[q] = wn(n2 * q);
-              auto st = [&](int k, int q, int sl, float2 v) {
-                v = cmul(v, cmul(fk[sl], fq[q]));
-                sts_elem<SPLIT>(base + col_tile_off<C0, ES>(out_row((k - q) / R0, q), j), v);
-              };
-              fft256r_job<R0, SPLIT, Cfg::kLmax / (256 * R0)>(jc, s_twR, p.dsign, ld, st);
-            } else {
-              auto st = [&](int k, int q, int sl, float2 v) {
-                sts_elem<SPLIT>(base + col_tile_off<C0, ES>(out_row((k - q) / R0, q), j), v);
-              };
-              fft256r_job<R0, SPLIT, Cfg::kLmax / (256 * R0)>(jc, s_twR, p.dsign, ld, st);
-            }
-          }
-        } else {  // kRoleRow: contiguous rows in place (2D phase 0)
-#pragma unroll 1
-          for (int j = warp; j < C0; j += 8) {
-            const uint32_t rb = base + (uint32_t)(j * 256 * R0 * ES);
-            auto ld = [&](int n) { return lds_elem<SPLIT>(rb + swz_w<ES>(n) * ES); };
-            // outputs k = q + R0 k' of one slot are R0 consecutive elements: hold all q, then
-            // store each slot's run with vector stores (conflict-free, like the single-pass kernel)
-            using Hold = typename std::conditional<SPLIT, float2, uint32_t>::type;
-            Hold out[R0][8];
-            auto st = [&](int k, int q, int sl, float2 v) {
-              if constexpr (SPLIT) out[q][sl] = v;
-              else out[q][sl] = pack_h2(v.x, v.y);
+          auto ld = [&](int jn, int n) { return lds_elem<SPLIT>(base + col_tile_off<C0, ES>(n, warp + 8 * jn)); };
+          if constexpr (Cfg::k1D) {
+            // W^(n2 k), k = q + R0 k' = W^(n2 q) * W^(n2 R0 k'): factors per job and thread
+            const int nmask = (int)p.n_mask;
+            const uint32_t a_hi = smem_addr(s_twhi), a_lo = smem_addr(s_twlo);
+            auto wn = [&](int e) {
+              e &= nmask;
+              return cmul(lds64f(a_hi + (e >> Cfg::kTwShift) * 8), lds64f(a_lo + (e & ((1 << Cfg::kTwShift) - 1)) * 8));
             };
-            fft256r_job<R0, SPLIT, Cfg::kLmax / (256 * R0)>(jc, s_twR, p.dsign, ld, st);
+            float2 fk[JN][8], fq[JN][R0];
+#pragma unroll
+            for (int jn = 0; jn < JN; ++jn) {
+              const int n2 = cg * C0 + warp + 8 * jn;
+#pragma unroll
+              for (int sl = 0; sl < 8; ++sl) fk[jn][sl] = wn(n2 * R0 * jc.kval[sl >> 2][(sl >> 1) & 1][sl & 1]);
+#pragma unroll
+              for (int q = 0; q < R0; ++q) fq[jn][q] = wn(n2 * q);
+            }
+            auto st = [&](int jn, int k, int q, int sl, float2 v) {
+              v = cmul(v, cmul(fk[jn][sl], fq[jn][q]));
+              sts_elem<SPLIT>(base + col_tile_off<C0, ES>(out_row((k - q) / R0, q), warp + 8 * jn), v);
+            };
+            fft256r_jobs<R0, SPLIT, Cfg::kLmax / (256 * R0), JN>(jc, twR, p.dsign, ld, st);
+          } else {
+            auto st = [&](int jn, int k, int q, int sl, float2 v) {
+              sts_elem<SPLIT>(base + col_tile_off<C0, ES>(out_row((k - q) / R0, q), warp + 8 * jn), v);
+            };
+            fft256r_jobs<R0, SPLIT, Cfg::kLmax / (256 * R0), JN>(jc, twR, p.dsign, ld, st);
+          }
+        } else {  // kRoleRow: contiguous rows j = warp + 8 jn in place (2D phase 0)
+          constexpr int JN = C0 / 8;
+          auto rowb = [&](int jn) { return base + (uint32_t)((warp + 8 * jn) * 256 * R0 * ES); };
+          auto ld = [&](int jn, int n) { return lds_elem<SPLIT>(rowb(jn) + swz_w<ES>(n) * ES); };
+          // outputs k = q + R0 k' of one slot are R0 consecutive elements: hold all q, then
+          // store each slot's run with vector stores (conflict-free, like the single-pass kernel)
+          Hold out[JN][R0][8];
+          auto st = [&](int jn, int k, int q, int sl, float2 v) {
+            if constexpr (SPLIT) out[jn][q][sl] = v;
+            else out[jn][q][sl] = pack_h2(v.x, v.y);
+          };
+          fft256r_jobs<R0, SPLIT, Cfg::kLmax / (256 * R0), JN>(jc, twR, p.dsign, ld, st);
+#pragma unroll
+          for (int jn = 0; jn < JN; ++jn)
 #pragma unroll
             for (int sl = 0; sl < 8; ++sl) {
+              const uint32_t rb = rowb(jn);
               const int k0 = R0 * jc.kval[sl >> 2][(sl >> 1) & 1][sl & 1];
               if constexpr (!SPLIT) {
-                if constexpr (R0 == 1) sts32(rb + swz_w<4>(k0) * 4, out[0][sl]);
-                else if constexpr (R0 == 2) sts64(rb + swz_w<4>(k0) * 4, out[0][sl], out[1][sl]);
+                if constexpr (R0 == 1) sts32(rb + swz_w<4>(k0) * 4, out[jn][0][sl]);
+                else if constexpr (R0 == 2) sts64(rb + swz_w<4>(k0) * 4, out[jn][0][sl], out[jn][1][sl]);
                 else {
 #pragma unroll
                   for (int q4 = 0; q4 < R0; q4 += 4)
-                    sts128(rb + swz_w<4>(k0 + q4) * 4, out[q4][sl], out[q4 + 1][sl], out[q4 + 2][sl], out[q4 + 3][sl]);
+                    sts128(rb + swz_w<4>(k0 + q4) * 4, out[jn][q4][sl], out[jn][q4 + 1][sl], out[jn][q4 + 2][sl],
+                           out[jn][q4 + 3][sl]);
                 }
               } else {
-                if constexpr (R0 == 1) sts64f(rb + swz_w<8>(k0) * 8, out[0][sl]);
+                if constexpr (R0 == 1) sts64f(rb + swz_w<8>(k0) * 8, out[jn][0][sl]);
                 else {
 #pragma unroll
-                  for (int q2 = 0; q2 < R0; q2 += 2) sts128f(rb + swz_w<8>(k0 + q2) * 8, out[q2][sl], out[q2 + 1][sl]);
+                  for (int q2 = 0; q2 < R0; q2 += 2)
+                    sts128f(rb + swz_w<8>(k0 + q2) * 8, out[jn][q2][sl], out[jn][q2 + 1][sl]);
                 }
               }
             }
-          }
         }
       } else {
         if constexpr (ROLE1 == kRoleCol) {
-#pragma unroll 1
-          for (int j = warp; j < C1; j += 8) {
-            auto ld = [&](int n) { return lds_elem<SPLIT>(base + col_tile_off<C1, ES>(n, j)); };
-            auto st = [&](int k, int q, int sl, float2 v) {
-              sts_elem<SPLIT>(base + col_tile_off<C1, ES>(out_row((k - q) / R1, q), j), v);
-            };
-            fft256r_job<R1, SPLIT, Cfg::kLmax / (256 * R1)>(jc, s_twR, p.dsign, ld, st);
-          }
+          constexpr int JN = C1 / 8;
+          auto ld = [&](int jn, int n) { return lds_elem<SPLIT>(base + col_tile_off<C1, ES>(n, warp + 8 * jn)); };
+          auto st = [&](int jn, int k, int q, int sl, float2 v) {
+            sts_elem<SPLIT>(base + col_tile_off<C1, ES>(out_row((k - q) / R1, q), warp + 8 * jn), v);
+          };
+          fft256r_jobs<R1, SPLIT, Cfg::kLmax / (256 * R1), JN>(jc, twR, p.dsign, ld, st);
         } else if constexpr (ROLE1 == kRoleRow16T) {
           // 16 short rows per warp (one S1 job), held in registers, then written
           // transposed as [k0 + 16 q rows][C1 cols] in boxes of kBW columns
           static_assert(C1 == 128, "short-row tiles hold 8 warps x 16 rows");
-          using Hold = typename std::conditional<SPLIT, float2, uint32_t>::type;
           Hold out[8 * R1];
           {
             const uint32_t rb = base + (uint32_t)(warp * 16 * Cfg::kLen1 * ES);
@@ -471,7 +476,7 @@ __global__ void __launch_bounds__(384, 1)  // 12 warps at launch: 168 registers 
               if constexpr (SPLIT) out[8 * q + sl] = val;
               else out[8 * q + sl] = pack_h2(val.x, val.y);
             };
-            fft16r_job<R1, SPLIT, Cfg::kLmax / (16 * R1), PI, RHO>(jc, s_twR, p.dsign, ld, st);
+            fft16r_job<R1, SPLIT, Cfg::kLmax / (16 * R1), PI, RHO>(jc, twR, p.dsign, ld, st);
           }
           named_bar_sync(1, 256);
           {
@@ -489,35 +494,29 @@ __global__ void __launch_bounds__(384, 1)  // 12 warps at launch: 168 registers 
                 else sts32(addr, out[8 * q + sl]);
               }
           }
-        } else {  // kRoleRowT: rows -> transposed output tile in the same stage
-          static_assert(C1 == 16 || C1 == 8, "row-transpose tiles hold 8 or 16 rows");
-          constexpr int JPW = C1 / 8;  // jobs per compute warp
-          using Hold = typename std::conditional<SPLIT, float2, uint32_t>::type;
-          Hold out[JPW][256 * R1 / 32];
-#pragma unroll
-          for (int jj = 0; jj < JPW; ++jj) {
-            const int j = warp + 8 * jj;
-            const uint32_t rb = base + (uint32_t)(j * 256 * R1 * ES);
-            auto ld = [&](int n) { return lds_elem<SPLIT>(rb + swz_w<ES>(n) * ES); };
-            auto st = [&](int k, int q, int sl, float2 v) {
-              if constexpr (SPLIT) out[jj][8 * q + sl] = v;
-              else out[jj][8 * q + sl] = pack_h2(v.x, v.y);
-            };
-            fft256r_job<R1, SPLIT, Cfg::kLmax / (256 * R1)>(jc, s_twR, p.dsign, ld, st);
-          }
+        } else {  // kRoleRowT: rows j = warp + 8 jn -> transposed output tile in the same stage
+          static_assert(C1 % 8 == 0, "row-transpose tiles hold a multiple of 8 rows");
+          constexpr int JN = C1 / 8;
+          Hold out[JN][256 * R1 / 32];
+          auto ld = [&](int jn, int n) {
+            return lds_elem<SPLIT>(base + (uint32_t)((warp + 8 * jn) * 256 * R1 * ES) + swz_w<ES>(n) * ES);
+          };
+          auto st = [&](int jn, int k, int q, int sl, float2 v) {
+            if constexpr (SPLIT) out[jn][8 * q + sl] = v;
+            else out[jn][8 * q + sl] = pack_h2(v.x, v.y);
+          };
+          fft256r_jobs<R1, SPLIT, Cfg::kLmax / (256 * R1), JN>(jc, twR, p.dsign, ld, st);
           named_bar_sync(1, 256);  // every compute warp finished reading the stage
 #pragma unroll
-          for (int jj = 0; jj < JPW; ++jj) {
-            const int j = warp + 8 * jj;
+          for (int jn = 0; jn < JN; ++jn)
 #pragma unroll
             for (int q = 0; q < R1; ++q)
 #pragma unroll
               for (int sl = 0; sl < 8; ++sl) {
                 const int row = out_row(jc.kval[sl >> 2][(sl >> 1) & 1][sl & 1], q);
-                if constexpr (SPLIT) sts64f(base + col_tile_off<C1, ES>(row, j), out[jj][8 * q + sl]);
-                else sts32(base + col_tile_off<C1, ES>(row, j), out[jj][8 * q + sl]);
+                if constexpr (SPLIT) sts64f(base + col_tile_off<C1, ES>(row, warp + 8 * jn), out[jn][8 * q + sl]);
+                else sts32(base + col_tile_off<C1, ES>(row, warp + 8 * jn), out[jn][8 * q + sl]);
               }
-          }
         }
       }
     }

@@ -54,63 +54,89 @@ __device__ __forceinline__ void init_job_consts(JobConsts<SPLIT>& c, const float
         c.kval[h][e][hh] = RHO::apply(2 * t + e + 8 * h) + 16 * RHO::apply(g + 8 * hh);
 }
 
-// LOAD(n) -> float2 element n (0 <= n < 256R) of the job's input.
-// STORE(k, q, slot, float2) receives output k = q + R * kval[slot] in fp32
-// (slot = 4h + 2e + hh, a compile-time constant after unrolling).
-// twR: table with W_{256R}^j at index j*TWS (shared memory), used for the
-// radix-R twiddles.
+// JN independent jobs computed in lockstep by one warp (JN = 1 or 2): their
+// instruction streams interleave, which hides MMA/shared-memory latency when
+// only two warps share a scheduler.
+// LOAD(jn, n) -> float2 element n (0 <= n < 256R) of job jn's input.
+// STORE(jn, k, q, slot, float2) receives output k = q + R * kval[slot] of job
+// jn in fp32 (slot = 4h + 2e + hh; jn, q, slot compile-time after unrolling).
 // All LOADs of the warp complete (and are ordered by __syncwarp) before the
 // first STORE, so a job may write its output over its own input.
-template <int R, bool SPLIT, int TWS = 1, class LoadF, class StoreF>
-__device__ __forceinline__ void fft256r_job(const JobConsts<SPLIT>& c, const float2* __restrict__ twR, float dsign,
-                                            LoadF&& load, StoreF&& store) {
-  uint32_t bhi[R][2][2][2], blo[SPLIT ? R : 1][2][2][2];
+// twR: shared-memory address of a table with W_{256R}^j at index j*TWS (read
+// with ld.shared), used for the radix-R twiddles.
+template <int R, bool SPLIT, int TWS, int JN, class LoadF, class StoreF>
+__device__ __forceinline__ void fft256r_jobs(const JobConsts<SPLIT>& c, uint32_t twR, float dsign, LoadF&& load,
+                                             StoreF&& store) {
+  uint32_t bhi[JN][R][2][2][2], blo[JN][SPLIT ? R : 1][2][2][2];
 #pragma unroll
   for (int kt = 0; kt < 2; ++kt)
 #pragma unroll
     for (int r = 0; r < 2; ++r)
 #pragma unroll
-      for (int j = 0; j < 2; ++j) {
-        float2 x[R];
+      for (int j = 0; j < 2; ++j)
 #pragma unroll
-        for (int a = 0; a < R; ++a) x[a] = load(c.mval[kt][r][j] + 256 * a);
-        if constexpr (R > 1) {
-          dft_small<R>(x, dsign);
+        for (int jn = 0; jn < JN; ++jn) {
+          float2 x[R];
 #pragma unroll
-          for (int q = 1; q < R; ++q) x[q] = cmul(x[q], twR[((c.mval[kt][r][j] * q) & (256 * R - 1)) * TWS]);
+          for (int a = 0; a < R; ++a) x[a] = load(jn, c.mval[kt][r][j] + 256 * a);
+          if constexpr (R > 1) {
+            dft_small<R>(x, dsign);
+#pragma unroll
+            for (int q = 1; q < R; ++q)
+              x[q] = cmul(x[q], lds64f(twR + ((c.mval[kt][r][j] * q) & (256 * R - 1)) * TWS * 8));
+          }
+#pragma unroll
+          for (int q = 0; q < R; ++q) {
+            if constexpr (SPLIT) split_h2(x[q], bhi[jn][q][kt][r][j], blo[jn][q][kt][r][j]);
+            else bhi[jn][q][kt][r][j] = pack_h2(x[q].x, x[q].y);
+          }
         }
-#pragma unroll
-        for (int q = 0; q < R; ++q) {
-          if constexpr (SPLIT) split_h2(x[q], bhi[q][kt][r][j], blo[q][kt][r][j]);
-          else bhi[q][kt][r][j] = pack_h2(x[q].x, x[q].y);
-        }
-      }
-  __syncwarp();  // every lane has read the job's input (stores may alias it)
+  __syncwarp();  // every lane has read the jobs' inputs (stores may alias them)
 #pragma unroll
   for (int q = 0; q < R; ++q) {
-    float acc[2][2][4];
-    if constexpr (SPLIT) dft16_mma_split(c.afr, c.afr_lo, bhi[q], blo[q], acc);
-    else dft16_mma(c.afr, bhi[q], acc);
-    uint32_t b2[2][2][2], b2lo[2][2][2];
+    float acc[JN][2][2][4];
 #pragma unroll
-    for (int kt = 0; kt < 2; ++kt)
+    for (int jn = 0; jn < JN; ++jn) {
+      if constexpr (SPLIT) dft16_mma_split(c.afr, c.afr_lo, bhi[jn][q], blo[jn][q], acc[jn]);
+      else dft16_mma(c.afr, bhi[jn][q], acc[jn]);
+    }
+    uint32_t b2[JN][2][2][2], b2lo[JN][2][2][2];
 #pragma unroll
-      for (int r = 0; r < 2; ++r)
+    for (int jn = 0; jn < JN; ++jn)
 #pragma unroll
-        for (int h = 0; h < 2; ++h) {
-          const float2 v = cmul(acc_get(acc, kt, h, r), c.tw1[kt][h][r]);
-          if constexpr (SPLIT) split_h2(v, b2[kt][r][h], b2lo[kt][r][h]);
-          else b2[kt][r][h] = pack_h2(v.x, v.y);
-        }
-    if constexpr (SPLIT) dft16_mma_split(c.afr, c.afr_lo, b2, b2lo, acc);
-    else dft16_mma(c.afr, b2, acc);
+      for (int kt = 0; kt < 2; ++kt)
 #pragma unroll
-    for (int h = 0; h < 2; ++h)
+        for (int r = 0; r < 2; ++r)
 #pragma unroll
-      for (int e = 0; e < 2; ++e)
+          for (int h = 0; h < 2; ++h) {
+            const float2 v = cmul(acc_get(acc[jn], kt, h, r), c.tw1[kt][h][r]);
+            if constexpr (SPLIT) split_h2(v, b2[jn][kt][r][h], b2lo[jn][kt][r][h]);
+            else b2[jn][kt][r][h] = pack_h2(v.x, v.y);
+          }
 #pragma unroll
-        for (int hh = 0; hh < 2; ++hh) store(q + R * c.kval[h][e][hh], q, 4 * h + 2 * e + hh, acc_get(acc, h, hh, e));
+    for (int jn = 0; jn < JN; ++jn) {
+      if constexpr (SPLIT) dft16_mma_split(c.afr, c.afr_lo, b2[jn], b2lo[jn], acc[jn]);
+      else dft16_mma(c.afr, b2[jn], acc[jn]);
+    }
+#pragma unroll
+    for (int jn = 0; jn < JN; ++jn)
+#pragma unroll
+      for (int h = 0; h < 2; ++h)
+#pragma unroll
+        for (int e = 0; e < 2; ++e)
+#pragma unroll
+          for (int hh = 0; hh < 2; ++hh)
+            store(jn, q + R * c.kval[h][e][hh], q, 4 * h + 2 * e + hh, acc_get(acc[jn], h, hh, e));
   }
+}
+
+// Single job: LOAD(n), STORE(k, q, slot, float2).
+template <int R, bool SPLIT, int TWS = 1, class LoadF, class StoreF>
+__device__ __forceinline__ void fft256r_job(const JobConsts<SPLIT>& c, uint32_t twR, float dsign, LoadF&& load,
+                                            StoreF&& store) {
+  fft256r_jobs<R, SPLIT, TWS, 1>(
+      c, twR, dsign, [&](int, int n) { return load(n); },
+      [&](int, int k, int q, int sl, float2 v) { store(k, q, sl, v); });
 }
 
 }  // namespace tcfft
@@ -126,10 +152,10 @@ namespace tcfft {
 // STORE(v, k, q, slot, float2) receives output k = q + R k0 of transform v;
 // slot = 4j + 2h + e (compile-time after unrolling) with v = 2t + e + 8j,
 // k0 = RHO(g + 8h).
-// tw16R: table with W_{16R}^j at index j*TWS.
+// tw16R: shared-memory address of a table with W_{16R}^j at index j*TWS.
 template <int R, bool SPLIT, int TWS, class PI, class RHO, class LoadF, class StoreF>
-__device__ __forceinline__ void fft16r_job(const JobConsts<SPLIT>& c, const float2* __restrict__ tw16R, float dsign,
-                                           LoadF&& load, StoreF&& store) {
+__device__ __forceinline__ void fft16r_job(const JobConsts<SPLIT>& c, uint32_t tw16R, float dsign, LoadF&& load,
+                                           StoreF&& store) {
   const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
   uint32_t bhi[R][2][2][2], blo[SPLIT ? R : 1][2][2][2];
 #pragma unroll
@@ -146,7 +172,7 @@ __device__ __forceinline__ void fft16r_job(const JobConsts<SPLIT>& c, const floa
         if constexpr (R > 1) {
           dft_small<R>(x, dsign);
 #pragma unroll
-          for (int q = 1; q < R; ++q) x[q] = cmul(x[q], tw16R[((m1 * q) & (16 * R - 1)) * TWS]);
+          for (int q = 1; q < R; ++q) x[q] = cmul(x[q], lds64f(tw16R + ((m1 * q) & (16 * R - 1)) * TWS * 8));
         }
 #pragma unroll
         for (int q = 0; q < R; ++q) {

@@ -33,7 +33,8 @@ struct SmallCfg {
   static constexpr int kBoxes = kTE / kBoxElems;
   static constexpr int kTileBytes = kTE * kES;
   static constexpr int kStages = 3;
-  static constexpr int kSmem = kStages * kTileBytes + 1024 + 64;
+  static constexpr int kTabBytes = R > 1 ? kN * 8 : 0;  // W_N^j table in shared memory (radix-R twiddles)
+  static constexpr int kSmem = kStages * kTileBytes + kTabBytes + 1024 + 64;
   static constexpr int kMinBlocks = (kStages * kTileBytes <= 100 * 1024) ? 2 : 1;
   static_assert(kTE % kBoxElems == 0, "tile must be whole TMA boxes");
   // bank-conflict-free slot permutations (see fft_common.cuh)
@@ -60,7 +61,9 @@ __global__ void __launch_bounds__(256, SmallCfg<R, SPLIT>::kMinBlocks)
   using RHO = typename C::RHO;
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* smem = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-  uint64_t* full = reinterpret_cast<uint64_t*>(smem + C::kStages * C::kTileBytes);
+  float2* s_tw = reinterpret_cast<float2*>(smem + C::kStages * C::kTileBytes);
+  const uint32_t s_tw_addr = smem_addr(s_tw);
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + C::kStages * C::kTileBytes + C::kTabBytes);
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, g = lane >> 2, t = lane & 3;
   const int ntile_cta = (p.num_tiles - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x;
@@ -70,6 +73,8 @@ __global__ void __launch_bounds__(256, SmallCfg<R, SPLIT>::kMinBlocks)
     for (int s = 0; s < C::kStages; ++s) mbar_init(&full[s], 1);
     fence_barrier_init();
   }
+  if constexpr (R > 1)
+    for (int j = tid; j < C::kN; j += blockDim.x) s_tw[j] = p.tw[j * (2048 / C::kN)];
   __syncthreads();
 
   auto issue_load = [&](int i) {  // thread 0 only: tile #i of this CTA into stage i % kStages
@@ -153,7 +158,7 @@ __global__ void __launch_bounds__(256, SmallCfg<R, SPLIT>::kMinBlocks)
                 dft_small<R>(x, p.dsign);
 #pragma unroll
                 for (int q = 1; q < R; ++q)
-                  x[q] = cmul(x[q], p.tw[((2048 / C::kN) * mval[kt][r][j] * q) & 2047]);
+                  x[q] = cmul(x[q], lds64f(s_tw_addr + ((mval[kt][r][j] * q) & (C::kN - 1)) * 8));
               }
 #pragma unroll
               for (int q = 0; q < R; ++q) {

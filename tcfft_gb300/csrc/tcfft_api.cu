@@ -133,7 +133,8 @@ int ilog2_exact(int64_t v) {
 // placed D blocks after its phase 0, and a slot is reused S blocks later, so
 // both D and S - D must exceed the blocks in flight.
 void fused_lag(int T0, int T1, int64_t batch, Schedule& s) {
-  const int in_flight = 152 * 4;  // CTAs x tiles per CTA
+  static const double scale = getenv("TCFFT_LAG_SCALE") ? atof(getenv("TCFFT_LAG_SCALE")) : 1.0;
+  const int in_flight = (int)(152 * 4 * scale);  // CTAs x tiles per CTA
   int D = (in_flight + (T0 + T1) - 1) / (T0 + T1) + 1;
   if (D > batch) D = (int)batch;
   if (D < 1) D = 1;
@@ -190,6 +191,7 @@ tcfftStatus choose_1d(int64_t n, int64_t batch, int precision, Schedule& s) {
     k.role1 = kRoleRowT;
     k.R1 = (int)(n2 / 256);
     k.C1 = fused_cols(k.R1, split);
+    if (getenv("TCFFT_FUSED_C")) k.C0 = k.C1 = atoi(getenv("TCFFT_FUSED_C"));
     k.split = split;
     if (k.C0 == 0 || k.C1 == 0) return TCFFT_NOT_SUPPORTED;
     s.kind = Schedule::kFused1d;
