@@ -183,3 +183,50 @@ def reference_input_order_2d(x, radices_x, radices_y):
     rx = gen_rev(x.shape[-2], radices_x)
     ry = gen_rev(x.shape[-1], radices_y)
     return np.ascontiguousarray(x[..., rx, :][..., :, ry])
+
+
+# ---------------------------------------------------------------- reference kernels on the GPU
+REF_DIR = os.path.join(HERE, "_ref")
+
+
+def reference_gpu_available():
+    return (os.path.exists(os.path.join(REF_DIR, "tcfft_half_ref.cubin"))
+            and os.path.exists(os.path.join(HERE, "_build", "libref_runner.so")))
+
+
+_RUNNER = None
+
+
+def _runner():
+    global _RUNNER
+    if _RUNNER is None:
+        lib = ctypes.CDLL(os.path.join(HERE, "_build", "libref_runner.so"))
+        c = ctypes
+        lib.ref_exec_1d.argtypes = [c.c_char_p, c.c_char_p, c.c_ulonglong, c.c_int, c.c_int, c.c_int, c.c_int]
+        lib.ref_exec_2d.argtypes = [c.c_char_p, c.c_char_p, c.c_ulonglong, c.c_int, c.c_int, c.c_int, c.c_int,
+                                    c.c_int]
+        _RUNNER = lib
+    return _RUNNER
+
+
+# Kernel families of the reference: "volta" is what tcfftCreate binds
+# (tcfft_half.cu:1244-1248); "a100" the sm_80 fragment-map twins it never binds.
+REFERENCE_FAMILIES = {"volta": 0, "a100": 1}
+
+
+def reference_gpu_fft_1d(dev_ptr, n, batch, family="volta", sync=True):
+    """Run the reference's own kernels (compiled from its sources for sm_103a)
+    in place on digit-reversed half2 data at device address `dev_ptr`."""
+    r = _runner().ref_exec_1d(os.path.join(REF_DIR, "tcfft_half_ref.cubin").encode(),
+                              os.path.join(REF_DIR, "tcfft_half_kernels.txt").encode(), dev_ptr, n, batch,
+                              REFERENCE_FAMILIES[family], int(bool(sync)))
+    if r != 0:
+        raise RuntimeError("reference 1D kernels failed: code %d" % r)
+
+
+def reference_gpu_fft_2d(dev_ptr, nx, ny, batch, family="volta", sync=True):
+    r = _runner().ref_exec_2d(os.path.join(REF_DIR, "tcfft_half_2d_ref.cubin").encode(),
+                              os.path.join(REF_DIR, "tcfft_half_2d_kernels.txt").encode(), dev_ptr, nx, ny, batch,
+                              REFERENCE_FAMILIES[family], int(bool(sync)))
+    if r != 0:
+        raise RuntimeError("reference 2D kernels failed: code %d" % r)

@@ -73,15 +73,17 @@ def build_ref(force=False):
     if force or not _newer(host_so, srcs_1d):
         _run([NVCC, "-O2", "-std=c++14", "-Xcompiler", "-fPIC,-fopenmp", "-shared", "-I", REFERENCE,
               *ARCH, "-o", host_so, *srcs_1d, "-lgomp"])
-    for stem in ("tcfft_half", "tcfft_half_2d"):
+    wrapper = os.path.join(HERE, "ref_kernels.cu")  # includes the reference source, adds the _A100 kernels
+    for two_d, stem in ((0, "tcfft_half"), (1, "tcfft_half_2d")):
         src = os.path.join(REFERENCE, stem + ".cu")
         cubin = os.path.join(REF_OUT, stem + "_ref.cubin")
         names = os.path.join(REF_OUT, stem + "_kernels.txt")
-        if force or not (_newer(cubin, [src]) and _newer(names, [src])):
-            _run([NVCC, "-cubin", "-O3", "-std=c++14", "-I", REFERENCE, *ARCH, "-o", cubin, src])
+        flags = ["-std=c++14", "-I", REFERENCE, "-DTCFFT_REF_2D=%d" % two_d, *ARCH]
+        if force or not (_newer(cubin, [src, wrapper]) and _newer(names, [src, wrapper])):
+            _run([NVCC, "-cubin", "-O3", *flags, "-o", cubin, wrapper])
             # kernel symbol names, read from a host object of the same source
             obj = os.path.join(REF_OUT, stem + "_host.o")
-            _run([NVCC, "-c", "-O0", "-std=c++14", "-I", REFERENCE, *ARCH, "-o", obj, src])
+            _run([NVCC, "-c", "-O0", *flags, "-o", obj, wrapper])
             syms = _run(["nm", "--defined-only", obj])
             kern = sorted({m.group(1) for m in re.finditer(r"\s(_Z\d+layer_\w+)$", syms, re.M)})
             with open(names, "w") as f:

@@ -1,0 +1,78 @@
+"""Differentiable FFT: the forward kernel and its hand-written adjoint behind a
+``torch.autograd.Function``, both through the C ABI (``tcfftExecute`` /
+``tcfftExecuteAdjoint``).
+
+Tensors are real views of interleaved complex data, shape ``[..., n, 2]``
+(1D) or ``[..., nx, ny, 2]`` (2D): fp16 for the plain precision, fp32 for the
+split precision.  For y = F x (F the unnormalised forward DFT), the
+real-view Jacobian transpose is the real view of F^H, so the backward pass of
+a real loss is ``grad_x = F^H grad_y`` -- the adjoint (conjugate-direction)
+transform of the incoming gradient, computed by the same kernels with the
+conjugate twiddles (PyTorch's convention for ``torch.fft.fft`` as well).
+
+The reference library has no inverse or adjoint transform and no autograd;
+this is new functionality on the same plan API.
+"""
+import threading
+
+import torch
+
+from . import Plan
+
+_CACHE = {}
+_LOCK = threading.Lock()
+
+
+class TcfftFunction(torch.autograd.Function):
+    """y = FFT(x) with backward grad_x = FFT^H(grad_y) (adjoint kernel)."""
+
+    @staticmethod
+    def forward(ctx, x, plan):
+        y = x.detach().clone().contiguous()
+        plan.exec(y)
+        ctx.plan = plan
+        return y
+
+    @staticmethod
+    def backward(ctx, gy):
+        gx = gy.detach().clone().contiguous()
+        ctx.plan.exec(gx, adjoint=True)
+        return gx, None
+
+
+def _get_plan(x, ndim, precision):
+    if ndim == 1:
+        n = x.shape[-2]
+        batch = x.numel() // (2 * n)
+        key = ("1d", n, batch, precision, x.device.index)
+        kw = {"n": n, "batch": batch}
+    else:
+        nx, ny = x.shape[-3], x.shape[-2]
+        batch = x.numel() // (2 * nx * ny)
+        key = ("2d", nx, ny, batch, precision, x.device.index)
+        kw = {"nx": nx, "ny": ny, "batch": batch}
+    with _LOCK:
+        p = _CACHE.get(key)
+        if p is None:
+            p = Plan(precision=precision, **kw)
+            _CACHE[key] = p
+    return p
+
+
+def fft(x, precision=None):
+    """Differentiable batched 1D FFT over dim -2 of a real view ``[..., n, 2]``."""
+    precision = precision or ("plain" if x.dtype == torch.float16 else "split")
+    return TcfftFunction.apply(x, _get_plan(x, 1, precision))
+
+
+def fft2(x, precision=None):
+    """Differentiable batched 2D FFT over dims (-3, -2) of ``[..., nx, ny, 2]``."""
+    precision = precision or ("plain" if x.dtype == torch.float16 else "split")
+    return TcfftFunction.apply(x, _get_plan(x, 2, precision))
+
+
+def clear_plan_cache():
+    with _LOCK:
+        for p in _CACHE.values():
+            p.destroy()
+        _CACHE.clear()

@@ -200,6 +200,25 @@ __device__ __forceinline__ void split_h2(float2 x, uint32_t& hi, uint32_t& lo) {
   lo = pack_h2(x.x - h.x, x.y - h.y);
 }
 
+// Split precision keeps each stage's operands inside fp16's range with a
+// per-job power-of-two scale: the job's inputs are scaled so that their largest
+// component lies in [512, 1024), which leaves room for the x16 growth of one
+// radix-16 stage before the next hi/lo split (16384 < 65504); the fp32 results
+// are scaled back exactly.
+__device__ __forceinline__ float warp_max(float m) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  return m;
+}
+// scale and inverse scale (powers of two) for a job whose max |component| is m
+__device__ __forceinline__ void split_scale(float m, float& scale, float& inv) {
+  int e = (int)((__float_as_uint(m) >> 23) & 0xff) - 127;  // floor(log2 m) for normal m
+  if (m == 0.f || e < -100) e = 9;
+  if (e > 100) e = 100;
+  scale = __uint_as_float((uint32_t)(127 + 9 - e) << 23);
+  inv = __uint_as_float((uint32_t)(127 - 9 + e) << 23);
+}
+
 // D += A(16x16 fp16, row) * B(16x8 fp16, col), fp32 accumulate.
 __device__ __forceinline__ void mma16816(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1) {
   asm volatile(

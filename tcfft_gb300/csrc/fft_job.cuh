@@ -68,6 +68,8 @@ template <int R, bool SPLIT, int TWS, int JN, class LoadF, class StoreF>
 __device__ __forceinline__ void fft256r_jobs(const JobConsts<SPLIT>& c, uint32_t twR, float dsign, LoadF&& load,
                                              StoreF&& store) {
   uint32_t bhi[JN][R][2][2][2], blo[JN][SPLIT ? R : 1][2][2][2];
+  float2 xs[SPLIT ? JN : 1][SPLIT ? R : 1][2][2][2];  // split: fp32 operands until the scale is known
+  float inv[JN];
 #pragma unroll
   for (int kt = 0; kt < 2; ++kt)
 #pragma unroll
@@ -87,10 +89,41 @@ __device__ __forceinline__ void fft256r_jobs(const JobConsts<SPLIT>& c, uint32_t
           }
 #pragma unroll
           for (int q = 0; q < R; ++q) {
-            if constexpr (SPLIT) split_h2(x[q], bhi[jn][q][kt][r][j], blo[jn][q][kt][r][j]);
+            if constexpr (SPLIT) xs[jn][q][kt][r][j] = x[q];
             else bhi[jn][q][kt][r][j] = pack_h2(x[q].x, x[q].y);
           }
         }
+  if constexpr (SPLIT) {
+#pragma unroll
+    for (int jn = 0; jn < JN; ++jn) {
+      float m = 0.f;
+#pragma unroll
+      for (int q = 0; q < R; ++q)
+#pragma unroll
+        for (int kt = 0; kt < 2; ++kt)
+#pragma unroll
+          for (int r = 0; r < 2; ++r)
+#pragma unroll
+            for (int j = 0; j < 2; ++j)
+              m = fmaxf(m, fmaxf(fabsf(xs[jn][q][kt][r][j].x), fabsf(xs[jn][q][kt][r][j].y)));
+      float sc;
+      split_scale(warp_max(m), sc, inv[jn]);
+#pragma unroll
+      for (int q = 0; q < R; ++q)
+#pragma unroll
+        for (int kt = 0; kt < 2; ++kt)
+#pragma unroll
+          for (int r = 0; r < 2; ++r)
+#pragma unroll
+            for (int j = 0; j < 2; ++j) {
+              const float2 v = xs[jn][q][kt][r][j];
+              split_h2(make_float2(v.x * sc, v.y * sc), bhi[jn][q][kt][r][j], blo[jn][q][kt][r][j]);
+            }
+    }
+  } else {
+#pragma unroll
+    for (int jn = 0; jn < JN; ++jn) inv[jn] = 1.f;
+  }
   __syncwarp();  // every lane has read the jobs' inputs (stores may alias them)
 #pragma unroll
   for (int q = 0; q < R; ++q) {
@@ -125,8 +158,11 @@ __device__ __forceinline__ void fft256r_jobs(const JobConsts<SPLIT>& c, uint32_t
 #pragma unroll
         for (int e = 0; e < 2; ++e)
 #pragma unroll
-          for (int hh = 0; hh < 2; ++hh)
-            store(jn, q + R * c.kval[h][e][hh], q, 4 * h + 2 * e + hh, acc_get(acc[jn], h, hh, e));
+          for (int hh = 0; hh < 2; ++hh) {
+            float2 v = acc_get(acc[jn], h, hh, e);
+            if constexpr (SPLIT) v = make_float2(v.x * inv[jn], v.y * inv[jn]);
+            store(jn, q + R * c.kval[h][e][hh], q, 4 * h + 2 * e + hh, v);
+          }
   }
 }
 
@@ -158,6 +194,8 @@ __device__ __forceinline__ void fft16r_job(const JobConsts<SPLIT>& c, uint32_t t
                                            StoreF&& store) {
   const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
   uint32_t bhi[R][2][2][2], blo[SPLIT ? R : 1][2][2][2];
+  float2 xs[SPLIT ? R : 1][2][2][2];
+  float inv = 1.f;
 #pragma unroll
   for (int kt = 0; kt < 2; ++kt)
 #pragma unroll
@@ -176,10 +214,34 @@ __device__ __forceinline__ void fft16r_job(const JobConsts<SPLIT>& c, uint32_t t
         }
 #pragma unroll
         for (int q = 0; q < R; ++q) {
-          if constexpr (SPLIT) split_h2(x[q], bhi[q][kt][r][j], blo[q][kt][r][j]);
+          if constexpr (SPLIT) xs[q][kt][r][j] = x[q];
           else bhi[q][kt][r][j] = pack_h2(x[q].x, x[q].y);
         }
       }
+  if constexpr (SPLIT) {
+    float m = 0.f;
+#pragma unroll
+    for (int q = 0; q < R; ++q)
+#pragma unroll
+      for (int kt = 0; kt < 2; ++kt)
+#pragma unroll
+        for (int r = 0; r < 2; ++r)
+#pragma unroll
+          for (int j = 0; j < 2; ++j) m = fmaxf(m, fmaxf(fabsf(xs[q][kt][r][j].x), fabsf(xs[q][kt][r][j].y)));
+    float sc;
+    split_scale(warp_max(m), sc, inv);
+#pragma unroll
+    for (int q = 0; q < R; ++q)
+#pragma unroll
+      for (int kt = 0; kt < 2; ++kt)
+#pragma unroll
+        for (int r = 0; r < 2; ++r)
+#pragma unroll
+          for (int j = 0; j < 2; ++j) {
+            const float2 v = xs[q][kt][r][j];
+            split_h2(make_float2(v.x * sc, v.y * sc), bhi[q][kt][r][j], blo[q][kt][r][j]);
+          }
+  }
   __syncwarp();
 #pragma unroll
   for (int q = 0; q < R; ++q) {
@@ -191,8 +253,11 @@ __device__ __forceinline__ void fft16r_job(const JobConsts<SPLIT>& c, uint32_t t
 #pragma unroll
       for (int h = 0; h < 2; ++h)
 #pragma unroll
-        for (int e = 0; e < 2; ++e)
-          store(2 * t + e + 8 * j, q + R * RHO::apply(g + 8 * h), q, 4 * j + 2 * h + e, acc_get(acc, j, h, e));
+        for (int e = 0; e < 2; ++e) {
+          float2 v = acc_get(acc, j, h, e);
+          if constexpr (SPLIT) v = make_float2(v.x * inv, v.y * inv);
+          store(2 * t + e + 8 * j, q + R * RHO::apply(g + 8 * h), q, 4 * j + 2 * h + e, v);
+        }
   }
 }
 

@@ -138,6 +138,8 @@ __global__ void __launch_bounds__(256, SmallCfg<R, SPLIT>::kMinBlocks)
       const uint32_t job = smem_addr(tile_base) + (uint32_t)((warp * C::kJPW + jj) * C::kN * C::kES);
       // ---------------- load + radix-R (DIF) + twiddle -> B operands per tile q
       uint32_t bhi[R][2][2][2], blo[SPLIT ? R : 1][2][2][2];
+      float2 xs[SPLIT ? R : 1][2][2][2];  // split: fp32 operands until the job's scale is known
+      float inv = 1.f;
 #pragma unroll
       for (int kt = 0; kt < 2; ++kt)
 #pragma unroll
@@ -162,11 +164,36 @@ __global__ void __launch_bounds__(256, SmallCfg<R, SPLIT>::kMinBlocks)
               }
 #pragma unroll
               for (int q = 0; q < R; ++q) {
-                if constexpr (SPLIT) split_h2(x[q], bhi[q][kt][r][j], blo[q][kt][r][j]);
+                if constexpr (SPLIT) xs[q][kt][r][j] = x[q];
                 else bhi[q][kt][r][j] = pack_h2(x[q].x, x[q].y);
               }
             }
           }
+      if constexpr (SPLIT) {
+        float m = 0.f;
+#pragma unroll
+        for (int q = 0; q < R; ++q)
+#pragma unroll
+          for (int kt = 0; kt < 2; ++kt)
+#pragma unroll
+            for (int r = 0; r < 2; ++r)
+#pragma unroll
+              for (int j = 0; j < 2; ++j)
+                m = fmaxf(m, fmaxf(fabsf(xs[q][kt][r][j].x), fabsf(xs[q][kt][r][j].y)));
+        float sc;
+        split_scale(warp_max(m), sc, inv);
+#pragma unroll
+        for (int q = 0; q < R; ++q)
+#pragma unroll
+          for (int kt = 0; kt < 2; ++kt)
+#pragma unroll
+            for (int r = 0; r < 2; ++r)
+#pragma unroll
+              for (int j = 0; j < 2; ++j) {
+                const float2 v = xs[q][kt][r][j];
+                split_h2(make_float2(v.x * sc, v.y * sc), bhi[q][kt][r][j], blo[q][kt][r][j]);
+              }
+      }
       __syncwarp();  // all lanes finished reading this job's region (in-place)
 
       // ---------------- two radix-16 tensor-core stages per tile q
@@ -196,7 +223,7 @@ __global__ void __launch_bounds__(256, SmallCfg<R, SPLIT>::kMinBlocks)
 #pragma unroll
             for (int hh = 0; hh < 2; ++hh) {
               const float2 v = acc_get(acc, h, hh, e);
-              if constexpr (SPLIT) res[q][h][e][hh] = v;
+              if constexpr (SPLIT) res[q][h][e][hh] = make_float2(v.x * inv, v.y * inv);
               else res[q][h][e][hh].x = __uint_as_float(pack_h2(v.x, v.y));
             }
       }

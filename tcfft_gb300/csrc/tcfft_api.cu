@@ -117,6 +117,11 @@ void free_tables(tcfftPlanImpl* p) {
   }
   if (p->counters) cudaFree(p->counters);
   p->counters = nullptr;
+  if (p->rev_x) cudaFree(p->rev_x);
+  if (p->rev_y) cudaFree(p->rev_y);
+  if (p->perm_tmp) cudaFree(p->perm_tmp);
+  p->rev_x = p->rev_y = nullptr;
+  p->perm_tmp = nullptr;
   p->tables = DeviceTables();
   p->scratch = nullptr;
 }
@@ -242,6 +247,26 @@ tcfftStatus choose_2d(int64_t nx, int64_t ny, int64_t batch, int precision, Sche
   return TCFFT_SUCCESS;
 }
 
+// Device tables for the reference input order; chains must be supported by the reference.
+tcfftStatus setup_reference_order(tcfftPlanImpl* p) {
+  const int es = p->precision == TCFFT_PRECISION_SPLIT ? 8 : 4;
+  auto upload = [&](const std::vector<int>& h, int** d) -> tcfftStatus {
+    if (cudaMalloc(d, h.size() * sizeof(int)) != cudaSuccess) return TCFFT_ALLOC_FAILED;
+    if (cudaMemcpy(*d, h.data(), h.size() * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess)
+      return TCFFT_CUDA_ERROR;
+    return TCFFT_SUCCESS;
+  };
+  tcfftStatus st;
+  if (p->kind == 1) {
+    if ((st = upload(digit_reversal(p->n, p->radices_x), &p->rev_y)) != TCFFT_SUCCESS) return st;
+  } else {
+    if ((st = upload(digit_reversal(p->nx, p->radices_x), &p->rev_x)) != TCFFT_SUCCESS) return st;
+    if ((st = upload(digit_reversal(p->ny, p->radices_y), &p->rev_y)) != TCFFT_SUCCESS) return st;
+  }
+  if (cudaMalloc(&p->perm_tmp, p->total_elems * es) != cudaSuccess) return TCFFT_ALLOC_FAILED;
+  return TCFFT_SUCCESS;
+}
+
 tcfftStatus validate_opts(const tcfftOptions* o) {
   if (!o) return TCFFT_SUCCESS;
   if (o->precision != TCFFT_PRECISION_PLAIN && o->precision != TCFFT_PRECISION_SPLIT) return TCFFT_INVALID_VALUE;
@@ -259,6 +284,13 @@ tcfftStatus exec_plan(tcfftPlan plan, void* data, void* stream, int dir) {
   const float2* tw = plan->tables.tw2048[dir];
   const float dsign = dir == 0 ? 1.f : -1.f;
   const Schedule& s = plan->sched;
+  if (plan->perm_tmp) {  // reference input order: move the input to natural order first
+    const int64_t nx = plan->kind == 1 ? 1 : plan->nx, ny = plan->kind == 1 ? plan->n : plan->ny;
+    if (cuda_status(to_natural_order(data, plan->perm_tmp, plan->rev_x, plan->rev_y, nx, ny, plan->batch,
+                                     split ? 8 : 4, plan->num_sms, st),
+                    "input reorder"))
+      return TCFFT_CUDA_ERROR;
+  }
   if (s.kind == Schedule::kSmall) {
     // 2D view of the whole batch: rows of 128 bytes
     const int es = split ? 8 : 4, er = 128 / es;
@@ -502,7 +534,11 @@ tcfftStatus tcfftPlan1d(tcfftPlan* out, int64_t n, int64_t batch, const tcfftOpt
   Schedule s;
   st = choose_1d(n, batch, o.precision, s);
   if (st != TCFFT_SUCCESS) return st;
-  if (o.input_order == TCFFT_ORDER_REFERENCE_DIGIT_REVERSED) return TCFFT_NOT_SUPPORTED;
+  std::vector<int> chain = {(int)n};  // natural order reads as a single radix-N digit
+  if (o.input_order == TCFFT_ORDER_REFERENCE_DIGIT_REVERSED) {
+    chain = reference_radices_1d(n);
+    if (chain.empty()) return TCFFT_INVALID_SIZE;  // the reference defines no order for this size
+  }
   tcfftPlanImpl* p = new (std::nothrow) tcfftPlanImpl();
   if (!p) return TCFFT_ALLOC_FAILED;
   p->kind = 1;
@@ -514,8 +550,10 @@ tcfftStatus tcfftPlan1d(tcfftPlan* out, int64_t n, int64_t batch, const tcfftOpt
   p->input_order = o.input_order;
   p->total_elems = n * batch;
   p->sched = s;
+  p->radices_x = chain;
   st = alloc_tables(p);
   if (st == TCFFT_SUCCESS && s.kind != Schedule::kSmall) st = alloc_fused(p);
+  if (st == TCFFT_SUCCESS && o.input_order == TCFFT_ORDER_REFERENCE_DIGIT_REVERSED) st = setup_reference_order(p);
   if (st != TCFFT_SUCCESS) {
     free_tables(p);
     delete p;
@@ -536,7 +574,12 @@ tcfftStatus tcfftPlan2d(tcfftPlan* out, int64_t nx, int64_t ny, int64_t batch, c
   Schedule s;
   st = choose_2d(nx, ny, batch, o.precision, s);
   if (st != TCFFT_SUCCESS) return st;
-  if (o.input_order == TCFFT_ORDER_REFERENCE_DIGIT_REVERSED) return TCFFT_NOT_SUPPORTED;
+  std::vector<int> cx = {(int)nx}, cy = {(int)ny};
+  if (o.input_order == TCFFT_ORDER_REFERENCE_DIGIT_REVERSED) {
+    cx = reference_radices_2d_axis(nx);
+    cy = reference_radices_2d_axis(ny);
+    if (cx.empty() || cy.empty()) return TCFFT_INVALID_SIZE;
+  }
   tcfftPlanImpl* p = new (std::nothrow) tcfftPlanImpl();
   if (!p) return TCFFT_ALLOC_FAILED;
   p->kind = 2;
@@ -548,8 +591,11 @@ tcfftStatus tcfftPlan2d(tcfftPlan* out, int64_t nx, int64_t ny, int64_t batch, c
   p->input_order = o.input_order;
   p->total_elems = nx * ny * batch;
   p->sched = s;
+  p->radices_x = cx;
+  p->radices_y = cy;
   st = alloc_tables(p);
   if (st == TCFFT_SUCCESS) st = alloc_fused(p);
+  if (st == TCFFT_SUCCESS && o.input_order == TCFFT_ORDER_REFERENCE_DIGIT_REVERSED) st = setup_reference_order(p);
   if (st != TCFFT_SUCCESS) {
     free_tables(p);
     delete p;
@@ -607,6 +653,10 @@ tcfftStatus tcfftGetPlanInfo(tcfftPlan plan, tcfftPlanInfo* info) {
   info->element_bytes = plan->precision == TCFFT_PRECISION_SPLIT ? 8 : 4;
   info->launches_per_exec = plan->sched.launches;
   info->scratch_bytes = plan->scratch_bytes;
+  info->n_radices = (int)plan->radices_x.size();
+  for (int i = 0; i < info->n_radices && i < 16; ++i) info->radices[i] = plan->radices_x[i];
+  info->n_radices_y = (int)plan->radices_y.size();
+  for (int i = 0; i < info->n_radices_y && i < 16; ++i) info->radices_y[i] = plan->radices_y[i];
   snprintf(info->schedule, sizeof info->schedule, "%s", plan->sched.text.c_str());
   return TCFFT_SUCCESS;
 }

@@ -40,6 +40,13 @@ cudaError_t launch_fused(const FusedKey& k, const FusedMaps& maps, const FusedPa
 cudaError_t launch_small(int R, bool split, const CUtensorMap& tmap, int64_t total_elems, const float2* tw,
                          float dsign, int* err, int num_sms, cudaStream_t stream, int* launches);
 int small_tile_elems(int R, bool split);
+
+// Reference input-order contract (tcfft_permute.cu).
+std::vector<int> reference_radices_1d(int64_t n);
+std::vector<int> reference_radices_2d_axis(int64_t n);
+std::vector<int> digit_reversal(int64_t n, const std::vector<int>& radices);
+cudaError_t to_natural_order(void* data, void* tmp, const int* rev_x, const int* rev_y, int64_t nx, int64_t ny,
+                             int64_t batch, int es, int num_sms, cudaStream_t st);
 int small_smem_bytes(int R, bool split);
 
 }  // namespace tcfft

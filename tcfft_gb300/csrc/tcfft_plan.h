@@ -1,6 +1,7 @@
 // tcfft_plan.h -- the opaque plan object behind `tcfftPlan`.
 #pragma once
 #include <string>
+#include <vector>
 
 #include "fft_fused.cuh"
 #include "tcfft_host.h"
@@ -37,6 +38,11 @@ struct tcfftPlanImpl {
   int* counters = nullptr;  // [2 * S]
   void* scratch = nullptr;
   int64_t scratch_bytes = 0;
+  // reference input order (TCFFT_ORDER_REFERENCE_DIGIT_REVERSED)
+  std::vector<int> radices_x, radices_y;  // reported chains (x = the 1D chain)
+  int* rev_x = nullptr;                   // device digit-reversal tables (nullptr: natural)
+  int* rev_y = nullptr;
+  void* perm_tmp = nullptr;               // natural-order staging buffer
   // tensor maps encoded for the last data pointer
   void* tmap_ptr = nullptr;
   CUtensorMap tmap0;
