@@ -59,23 +59,34 @@ struct FusedParams {
   float dsign;
 };
 
+// Column tiles: C columns x L rows of C*ES bytes (32, 64 or 128), moved by TMA
+// with the swizzle of that width (the 16-byte chunk bits [4:4+w) of the byte
+// offset XOR bits [7:7+w), w = 1, 2, 3 for 32-, 64-, 128-byte rows).  A column of such a tile
+// reaches only 8 of the 16-byte bank groups, and which one is picked by the low
+// row bits, so rows are placed in a digit order that spreads the rows a warp
+// touches in one instruction over all 8 groups (checked exhaustively for every
+// tile shape: 2 wavefronts per 128 bytes and half-warp, the minimum for two
+// side-by-side jobs):
+//  * input row n = m0 + 16 m1 + 256 a sits at tile row
+//    (m1 bit 3 | m0 << 1 | m1 bits 0-2 << 5 | a << 8);
+//  * output row k = q + R (k0 + 16 k1) sits at tile row
+//    (k0 bits 2-3 | k1 << 2 | k0 bits 0-1 << 6 | q << 8).
+// 5D TMA boxes whose dimensions are these digit groups move the rows between
+// natural order in global memory and this order in the tile.
 template <int C, int ES>
-__device__ __forceinline__ uint32_t col_tile_off(int row, int col) {
-  // tile of C columns; one row = C*ES bytes (32, 64 or 128) with the matching
-  // TMA swizzle (16-byte chunk index XOR address bits [7:9] / [7:8] / [7])
+__device__ __forceinline__ uint32_t ctile_off(int row, int col) {
   constexpr int RB = C * ES;
   static_assert(RB == 32 || RB == 64 || RB == 128, "column tiles are 32-, 64- or 128-byte rows");
-  const int chunk = (col * ES) >> 4;
-  const int within = (col * ES) & 15;
-  const int sw = RB == 128 ? (row & 7) : (RB == 64 ? ((row >> 1) & 3) : ((row >> 2) & 1));
-  return (uint32_t)(row * RB + ((chunk ^ sw) << 4) + within);
+  constexpr uint32_t kMask = RB == 128 ? 7u : (RB == 64 ? 3u : 1u);
+  const uint32_t L = (uint32_t)(row * RB + col * ES);
+  return L ^ (((L >> 7) & kMask) << 4);
 }
-
-// Row of output k = q + R (k0 + 16 k1) inside a column/transposed output tile:
-// rows are stored in (k1, k0, q) order so that the 32 lanes of a warp, whose
-// k1 digits are 8 consecutive values, touch rows with 8 distinct low bits; a
-// 5D TMA store box puts them back in natural order.
-__device__ __forceinline__ int out_row(int kp, int q) { return (kp >> 4) + 16 * (kp & 15) + 256 * q; }
+__device__ __forceinline__ int col_in_row(int n) {
+  return ((n >> 7) & 1) | ((n & 15) << 1) | (((n >> 4) & 7) << 5) | (n & ~255);
+}
+__device__ __forceinline__ int col_out_row(int kp, int q) {
+  return ((kp >> 2) & 3) | ((kp >> 4) << 2) | ((kp & 3) << 6) | (q << 8);
+}
 
 template <bool SPLIT>
 __device__ __forceinline__ float2 lds_elem(uint32_t addr) {
@@ -86,6 +97,23 @@ template <bool SPLIT>
 __device__ __forceinline__ void sts_elem(uint32_t addr, float2 v) {
   if constexpr (SPLIT) sts64f(addr, v);
   else sts32(addr, pack_h2(v.x, v.y));
+}
+// two side-by-side elements (adjacent columns of a column tile)
+template <bool SPLIT>
+__device__ __forceinline__ void lds_pair(uint32_t addr, float2& x0, float2& x1) {
+  if constexpr (SPLIT) {
+    lds128f(addr, x0, x1);
+  } else {
+    uint32_t a, b;
+    lds64(addr, a, b);
+    x0 = unpack_h2(a);
+    x1 = unpack_h2(b);
+  }
+}
+template <bool SPLIT>
+__device__ __forceinline__ void sts_pair(uint32_t addr, float2 v0, float2 v1) {
+  if constexpr (SPLIT) sts128f(addr, v0, v1);
+  else sts64(addr, pack_h2(v0.x, v0.y), pack_h2(v1.x, v1.y));
 }
 
 __device__ __forceinline__ int ld_acquire(const int* p) {
@@ -126,6 +154,116 @@ __device__ __forceinline__ bool named_bar_and(int id, int n, bool pred) {
   return r != 0;
 }
 
+// ---------------------------------------------------------------- plain-precision tile bodies
+// (fft256r_jobs_fold with per-lane slot offsets computed once per tile)
+
+// Input digit m of B-fragment slot 4kt + 2r + j and output index k' of
+// accumulator slot 4h + 2e + hh for this lane (fft_common.cuh conventions).
+template <class PI, class RHO>
+__device__ __forceinline__ int slot_m(int slot) {
+  const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+  return 16 * PI::apply(2 * t + ((slot >> 1) & 1) + 8 * (slot >> 2)) + PI::apply(g + 8 * (slot & 1));
+}
+template <class PI, class RHO>
+__device__ __forceinline__ int slot_kval(int osl) {
+  const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+  return RHO::apply(2 * t + ((osl >> 1) & 1) + 8 * (osl >> 2)) + 16 * RHO::apply(g + 8 * (osl & 1));
+}
+
+// W_N^e from the two-level shared table (e reduced mod N by nmask).
+struct WnTable {
+  uint32_t hi, lo;
+  int shift, nmask;
+  __device__ __forceinline__ float2 operator()(int e) const {
+    e &= nmask;
+    return cmul(lds64f(hi + (e >> shift) * 8), lds64f(lo + (e & ((1 << shift) - 1)) * 8));
+  }
+};
+
+// Column tile, in place: JN = C/8 side-by-side columns col0 = JN warp + jn per
+// warp, each an FFT of length 256R down the tile.  With WN (1D four-step phase
+// 0) the output k of column n2 = n2base + jn is multiplied by W_N^(n2 k).
+template <int R, int C, bool WN, class PI, class RHO>
+__device__ __forceinline__ void plain_col_tile(const JobConsts<false>& jc, uint32_t fold, uint32_t base, int warp,
+                                               float dsign, int n2base, const WnTable& wn) {
+  constexpr int ES = 4, JN = C / 8;
+  constexpr bool PAIR = JN % 2 == 0;
+  constexpr uint32_t kStep = 256 * C * ES;  // one digit a (input) or q (output) further down
+  const int col0 = JN * warp;
+  uint32_t lo[8], so[8];
+#pragma unroll
+  for (int sl = 0; sl < 8; ++sl) {
+    lo[sl] = base + ctile_off<C, ES>(col_in_row(slot_m<PI, RHO>(sl)), col0);
+    so[sl] = base + ctile_off<C, ES>(col_out_row(slot_kval<PI, RHO>(sl), 0), col0);
+  }
+  if constexpr (WN) {
+    // W_N^(n2 (q + R k')), k' = kbase + e + 2h + 32hh (RHO digit structure):
+    // fk[osl] = W^(n2 R kbase) u^(e + 2h) u32^hh with u = W^(n2 R); fq[q] = W^(n2 q)
+    const int kbase = slot_kval<PI, RHO>(0);
+    float2 fk[JN][8], fq[JN][R];
+#pragma unroll
+    for (int jn = 0; jn < JN; ++jn) {
+      const int n2 = n2base + col0 + jn;
+      const float2 F = wn(n2 * R * kbase), u = wn(n2 * R), u32 = wn(32 * n2 * R);
+      const float2 u2 = cmul(u, u), u3 = cmul(u2, u);
+      const float2 f0[4] = {F, cmul(F, u), cmul(F, u2), cmul(F, u3)};
+#pragma unroll
+      for (int osl = 0; osl < 8; ++osl) {
+        const float2 f = f0[((osl >> 1) & 1) + 2 * (osl >> 2)];
+        fk[jn][osl] = (osl & 1) ? cmul(f, u32) : f;
+      }
+      fq[jn][0] = make_float2(1.f, 0.f);
+      if constexpr (R > 1) fq[jn][1] = wn(n2);
+#pragma unroll
+      for (int q = 2; q < R; ++q) fq[jn][q] = cmul(fq[jn][q - 1], fq[jn][1]);
+    }
+    if constexpr (PAIR) {
+      auto ld = [&](int jp, int sl, int a, float2& x0, float2& x1) {
+        lds_pair<false>(lo[sl] + jp * ES + a * kStep, x0, x1);
+      };
+      auto st = [&](int jp, int osl, int q, float2 v0, float2 v1) {
+        v0 = cmul(v0, cmul(fk[jp][osl], fq[jp][q]));
+        v1 = cmul(v1, cmul(fk[jp + 1][osl], fq[jp + 1][q]));
+        sts_pair<false>(so[osl] + jp * ES + q * kStep, v0, v1);
+      };
+      fft256r_jobs_fold<R, JN, true>(jc, fold, dsign, ld, st);
+    } else {
+      auto ld = [&](int jn, int sl, int a) { return lds_elem<false>(lo[sl] + jn * ES + a * kStep); };
+      auto st = [&](int jn, int osl, int q, float2 v) {
+        sts_elem<false>(so[osl] + jn * ES + q * kStep, cmul(v, cmul(fk[jn][osl], fq[jn][q])));
+      };
+      fft256r_jobs_fold<R, JN, false>(jc, fold, dsign, ld, st);
+    }
+  } else {
+    if constexpr (PAIR) {
+      auto ld = [&](int jp, int sl, int a, float2& x0, float2& x1) {
+        lds_pair<false>(lo[sl] + jp * ES + a * kStep, x0, x1);
+      };
+      auto st = [&](int jp, int osl, int q, float2 v0, float2 v1) {
+        sts_pair<false>(so[osl] + jp * ES + q * kStep, v0, v1);
+      };
+      fft256r_jobs_fold<R, JN, true>(jc, fold, dsign, ld, st);
+    } else {
+      auto ld = [&](int jn, int sl, int a) { return lds_elem<false>(lo[sl] + jn * ES + a * kStep); };
+      auto st = [&](int jn, int osl, int q, float2 v) { sts_elem<false>(so[osl] + jn * ES + q * kStep, v); };
+      fft256r_jobs_fold<R, JN, false>(jc, fold, dsign, ld, st);
+    }
+  }
+}
+
+// Contiguous rows of length 256R (JN per warp); the outputs stay in registers
+// (out[jn][q][osl], packed half2) for the caller to store.
+template <int R, int JN, class PI, class RHO>
+__device__ __forceinline__ void plain_row_jobs(const JobConsts<false>& jc, uint32_t fold, uint32_t row_addr0,
+                                               uint32_t row_stride, float dsign, uint32_t (&out)[JN][R][8]) {
+  uint32_t lo[8];
+#pragma unroll
+  for (int sl = 0; sl < 8; ++sl) lo[sl] = row_addr0 + swz_w<4>(slot_m<PI, RHO>(sl)) * 4;
+  auto ld = [&](int jn, int sl, int a) { return lds_elem<false>(lo[sl] + jn * row_stride + a * 1024); };
+  auto st = [&](int jn, int osl, int q, float2 v) { out[jn][q][osl] = pack_h2(v.x, v.y); };
+  fft256r_jobs_fold<R, JN, false>(jc, fold, dsign, ld, st);
+}
+
 template <int ROLE0, int R0, int C0, int ROLE1, int R1, int C1, bool SPLIT>
 struct FusedCfg {
   static constexpr int kES = SPLIT ? 8 : 4;
@@ -136,13 +274,21 @@ struct FusedCfg {
   static constexpr int kTile1 = C1 * kLen1;
   static constexpr int kTileMax = kTile0 > kTile1 ? kTile0 : kTile1;
   static constexpr int kStageBytes = kTileMax * kES;
-  // shared-memory twiddle tables: W_L^j (L = the longer job length) and the two
-  // halves of W_N^j (1D four-step, N = kLen0 * kLen1)
+  // shared-memory tables: W_L^j (L = the longer job length; the fp32 job paths),
+  // the two halves of W_N^j (1D four-step, N = kLen0 * kLen1) and the per-lane
+  // fold tables of the plain 256R-point jobs (one per distinct R)
   static constexpr int kLmax = kLen0 > kLen1 ? kLen0 : kLen1;
   static constexpr int kLog2N = ilog2c(kLen0) + ilog2c(kLen1);
   static constexpr int kTwShift = (kLog2N + 1) / 2;          // log2 of the low table length
   static constexpr int kTwHi = 1 << (kLog2N - kTwShift);     // N >> shift
-  static constexpr int kTabBytes = (kLmax + (k1D ? (1 << kTwShift) + kTwHi : 0)) * 8;
+  static constexpr bool kFold = !SPLIT;                       // plain 256R-point jobs use fft256r_jobs_fold
+  static constexpr bool kFold1Own = kFold && ROLE1 != kRoleRow16T && R1 != R0;
+  static constexpr int kTwRBytes = (SPLIT || ROLE1 == kRoleRow16T) ? kLmax * 8 : 0;
+  static constexpr int kWnBytes = k1D ? ((1 << kTwShift) + kTwHi) * 8 : 0;
+  static constexpr int kFold0Bytes = kFold ? FoldTab<R0>::kBytes : 0;
+  static constexpr int kFold1Bytes = kFold1Own ? FoldTab<R1>::kBytes : 0;
+  static constexpr int kOffWn = kTwRBytes, kOffFold0 = kTwRBytes + kWnBytes, kOffFold1 = kOffFold0 + kFold0Bytes;
+  static constexpr int kTabBytes = kTwRBytes + kWnBytes + kFold0Bytes + kFold1Bytes;
   // kRoleRow16T output boxes: kBW columns (128 bytes) each
   static constexpr int kBW = 128 / kES;
   // contiguous-row tiles move as boxes of [kER elements][kBH rows] (kBH <= 256)
@@ -195,9 +341,12 @@ __global__ void __launch_bounds__(384, 1)  // 12 warps at launch: 168 registers 
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* smem =
       reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-  float2* s_twR = reinterpret_cast<float2*>(smem + NST * Cfg::kStageBytes);  // W_Lmax^j
-  float2* s_twlo = s_twR + Cfg::kLmax;                                       // W_N^j, j < 2^shift
-  float2* s_twhi = s_twlo + (1 << Cfg::kTwShift);                            // W_N^(j << shift)
+  unsigned char* s_tab = smem + NST * Cfg::kStageBytes;
+  float2* s_twR = reinterpret_cast<float2*>(s_tab);                            // W_Lmax^j
+  float2* s_twlo = reinterpret_cast<float2*>(s_tab + Cfg::kOffWn);             // W_N^j, j < 2^shift
+  float2* s_twhi = s_twlo + (1 << Cfg::kTwShift);                              // W_N^(j << shift)
+  unsigned char* s_fold0 = s_tab + Cfg::kOffFold0;                             // fold table for R0
+  unsigned char* s_fold1 = Cfg::kFold1Own ? s_tab + Cfg::kOffFold1 : s_fold0;  // fold table for R1
   uint64_t* full = reinterpret_cast<uint64_t*>(smem + NST * Cfg::kStageBytes + Cfg::kTabBytes);
   uint64_t* computed = full + NST;
   uint64_t* empty = computed + NST;
@@ -214,10 +363,16 @@ __global__ void __launch_bounds__(384, 1)  // 12 warps at launch: 168 registers 
     fence_barrier_init();
   }
   // twiddle tables into shared memory (the inner loops never touch global tables)
-  for (int j = tid; j < Cfg::kLmax; j += blockDim.x) s_twR[j] = p.tw2048[j * (2048 / Cfg::kLmax)];
+  if constexpr (Cfg::kTwRBytes > 0)
+    for (int j = tid; j < Cfg::kLmax; j += blockDim.x) s_twR[j] = p.tw2048[j * (2048 / Cfg::kLmax)];
   if (Cfg::k1D) {
     for (int j = tid; j < (1 << Cfg::kTwShift); j += blockDim.x) s_twlo[j] = p.twlo[j];
     for (int j = tid; j < Cfg::kTwHi; j += blockDim.x) s_twhi[j] = p.twhi[j];
+  }
+  if constexpr (Cfg::kFold) {
+    build_fold_table<R0, typename Cfg::PI, typename Cfg::RHO>(s_fold0, p.tw2048, tid, blockDim.x);
+    if constexpr (Cfg::kFold1Own)
+      build_fold_table<R1, typename Cfg::PI, typename Cfg::RHO>(s_fold1, p.tw2048, tid, blockDim.x);
   }
   __syncthreads();
 
@@ -253,11 +408,9 @@ __global__ void __launch_bounds__(384, 1)  // 12 warps at launch: 168 registers 
         unsigned char* dst = smem + s * Cfg::kStageBytes;
         if (it.phase == 0) {
           mbar_arrive_expect_tx(&full[s], Cfg::kTile0 * ES);
-          if constexpr (ROLE0 == kRoleCol) {
+          if constexpr (ROLE0 == kRoleCol) {  // one 5D box: rows in the column-tile digit order
             const int cg = it.tile % p.cols0;
-#pragma unroll 1
-            for (int i = 0; i < R0; ++i)
-              tma_load_2d(dst + i * (256 * C0 * ES), &maps.load0, cg * C0, it.b * p.rows0 + 256 * i, &full[s]);
+            tma_load_5d(dst, &maps.load0, cg * C0, 0, 0, 0, it.b * R0, &full[s]);
           } else {  // contiguous rows
             const int y0 = (int)(((long long)it.b * p.rows0 + (long long)it.tile * C0) * (256 * R0) / ER);
 #pragma unroll 1
@@ -268,9 +421,7 @@ __global__ void __launch_bounds__(384, 1)  // 12 warps at launch: 168 registers 
           mbar_arrive_expect_tx(&full[s], Cfg::kTile1 * ES);
           if constexpr (ROLE1 == kRoleCol) {
             const int cg = it.tile % p.cols1;
-#pragma unroll 1
-            for (int i = 0; i < R1; ++i)
-              tma_load_2d(dst + i * (256 * C1 * ES), &maps.load1, cg * C1, it.b * p.rows1 + 256 * i, &full[s]);
+            tma_load_5d(dst, &maps.load1, cg * C1, 0, 0, 0, it.b * R1, &full[s]);
           } else {
             // 1D: source is the scratch slot; 2D never has a contiguous phase 1
             const long long row0 = (long long)slot * p.rows1 + (long long)it.tile * C1;
@@ -327,9 +478,9 @@ __global__ void __launch_bounds__(384, 1)  // 12 warps at launch: 168 registers 
         const int slot = it.b % p.S;
         if (it.phase == 0) {
           if constexpr (ROLE0 == kRoleCol) {
-            // 5D box [C0][k1][k0][q][transform]: 1D -> scratch slot, 2D -> the data
+            // 5D box [C0][k0 hi][k1 (+16 transform)][k0 lo][q]: 1D -> scratch slot, 2D -> the data
             const int cg = it.tile % p.cols0;
-            tma_store_5d(&maps.store0, cg * C0, 0, 0, 0, Cfg::k1D ? slot : it.b, src);
+            tma_store_5d(&maps.store0, cg * C0, 0, 16 * (Cfg::k1D ? slot : it.b), 0, 0, src);
           } else {
             const int y0 = (int)(((long long)it.b * p.rows0 + (long long)it.tile * C0) * (256 * R0) / ER);
 #pragma unroll 1
@@ -339,9 +490,9 @@ __global__ void __launch_bounds__(384, 1)  // 12 warps at launch: 168 registers 
         } else {
           if constexpr (ROLE1 == kRoleCol) {
             const int cg = it.tile % p.cols1;
-            tma_store_5d(&maps.store1, cg * C1, 0, 0, 0, it.b, src);
+            tma_store_5d(&maps.store1, cg * C1, 0, 16 * it.b, 0, 0, src);
           } else if constexpr (ROLE1 == kRoleRowT) {  // output columns k1 of data viewed [B][N2 rows k2][N1 cols]
-            tma_store_5d(&maps.store1, it.tile * C1, 0, 0, 0, it.b, src);
+            tma_store_5d(&maps.store1, it.tile * C1, 0, 16 * it.b, 0, 0, src);
           } else {  // kRoleRow16T: C1 columns as boxes of kBW, 4D [cols][k0][q][B]
 #pragma unroll 1
             for (int bx = 0; bx < C1 / Cfg::kBW; ++bx)
@@ -376,6 +527,12 @@ __global__ void __launch_bounds__(384, 1)  // 12 warps at launch: 168 registers 
   JobConsts<SPLIT> jc;
   init_job_consts<SPLIT, PI, RHO>(jc, p.tw2048);
   const uint32_t twR = smem_addr(s_twR);
+  const uint32_t fold0 = smem_addr(s_fold0), fold1 = smem_addr(s_fold1);
+  WnTable wn;
+  wn.hi = smem_addr(s_twhi);
+  wn.lo = smem_addr(s_twlo);
+  wn.shift = Cfg::kTwShift;
+  wn.nmask = (int)p.n_mask;
   int cnt = 0;
   for (long long idx = blockIdx.x; idx < total; idx += gridDim.x) {
     const Item it = decode_item(idx, p);
@@ -386,11 +543,23 @@ __global__ void __launch_bounds__(384, 1)  // 12 warps at launch: 168 registers 
     const uint32_t base = smem_addr(smem + s * Cfg::kStageBytes);
     if (ok) {
       if (it.phase == 0) {
-        if constexpr (ROLE0 == kRoleCol) {
-          // columns j = warp + 8 jn in place; 1D adds the four-step twiddle W_N^(n2 k1)
+        if constexpr (ROLE0 == kRoleCol && !SPLIT) {
+          plain_col_tile<R0, C0, Cfg::k1D, PI, RHO>(jc, fold0, base, warp, p.dsign, (it.tile % p.cols0) * C0, wn);
+        } else if constexpr (ROLE0 == kRoleCol) {
+          // columns JN*warp + jn in place (side by side, moved in pairs); 1D adds the
+          // four-step twiddle W_N^(n2 k1)
           constexpr int JN = C0 / 8;
+          constexpr bool PAIR = JN % 2 == 0;
+          constexpr int TWS = Cfg::kLmax / (256 * R0);
           const int cg = it.tile % p.cols0;
-          auto ld = [&](int jn, int n) { return lds_elem<SPLIT>(base + col_tile_off<C0, ES>(n, warp + 8 * jn)); };
+          const int col0 = JN * warp;
+          auto ld = [&](int jn, int n) { return lds_elem<SPLIT>(base + ctile_off<C0, ES>(col_in_row(n), col0 + jn)); };
+          auto ldp = [&](int jp, int n, float2& x0, float2& x1) {
+            lds_pair<SPLIT>(base + ctile_off<C0, ES>(col_in_row(n), col0 + jp), x0, x1);
+          };
+          auto oaddr = [&](int jn, int k, int q) {
+            return base + ctile_off<C0, ES>(col_out_row((k - q) / R0, q), col0 + jn);
+          };
           if constexpr (Cfg::k1D) {
             // W^(n2 k), k = q + R0 k' = W^(n2 q) * W^(n2 R0 k'): factors per job and thread
             const int nmask = (int)p.n_mask;
@@ -402,22 +571,35 @@ __global__ void __launch_bounds__(384, 1)  // 12 warps at launch: 168 registers 
             float2 fk[JN][8], fq[JN][R0];
 #pragma unroll
             for (int jn = 0; jn < JN; ++jn) {
-              const int n2 = cg * C0 + warp + 8 * jn;
+              const int n2 = cg * C0 + col0 + jn;
 #pragma unroll
               for (int sl = 0; sl < 8; ++sl) fk[jn][sl] = wn(n2 * R0 * jc.kval[sl >> 2][(sl >> 1) & 1][sl & 1]);
 #pragma unroll
               for (int q = 0; q < R0; ++q) fq[jn][q] = wn(n2 * q);
             }
-            auto st = [&](int jn, int k, int q, int sl, float2 v) {
-              v = cmul(v, cmul(fk[jn][sl], fq[jn][q]));
-              sts_elem<SPLIT>(base + col_tile_off<C0, ES>(out_row((k - q) / R0, q), warp + 8 * jn), v);
-            };
-            fft256r_jobs<R0, SPLIT, Cfg::kLmax / (256 * R0), JN>(jc, twR, p.dsign, ld, st);
+            if constexpr (PAIR) {
+              auto st = [&](int jp, int k, int q, int sl, float2 v0, float2 v1) {
+                v0 = cmul(v0, cmul(fk[jp][sl], fq[jp][q]));
+                v1 = cmul(v1, cmul(fk[jp + 1][sl], fq[jp + 1][q]));
+                sts_pair<SPLIT>(oaddr(jp, k, q), v0, v1);
+              };
+              fft256r_jobs<R0, SPLIT, TWS, JN, true>(jc, twR, p.dsign, ldp, st);
+            } else {
+              auto st = [&](int jn, int k, int q, int sl, float2 v) {
+                sts_elem<SPLIT>(oaddr(jn, k, q), cmul(v, cmul(fk[jn][sl], fq[jn][q])));
+              };
+              fft256r_jobs<R0, SPLIT, TWS, JN>(jc, twR, p.dsign, ld, st);
+            }
           } else {
-            auto st = [&](int jn, int k, int q, int sl, float2 v) {
-              sts_elem<SPLIT>(base + col_tile_off<C0, ES>(out_row((k - q) / R0, q), warp + 8 * jn), v);
-            };
-            fft256r_jobs<R0, SPLIT, Cfg::kLmax / (256 * R0), JN>(jc, twR, p.dsign, ld, st);
+            if constexpr (PAIR) {
+              auto st = [&](int jp, int k, int q, int, float2 v0, float2 v1) {
+                sts_pair<SPLIT>(oaddr(jp, k, q), v0, v1);
+              };
+              fft256r_jobs<R0, SPLIT, TWS, JN, true>(jc, twR, p.dsign, ldp, st);
+            } else {
+              auto st = [&](int jn, int k, int q, int, float2 v) { sts_elem<SPLIT>(oaddr(jn, k, q), v); };
+              fft256r_jobs<R0, SPLIT, TWS, JN>(jc, twR, p.dsign, ld, st);
+            }
           }
         } else {  // kRoleRow: contiguous rows j = warp + 8 jn in place (2D phase 0)
           constexpr int JN = C0 / 8;
@@ -426,11 +608,12 @@ __global__ void __launch_bounds__(384, 1)  // 12 warps at launch: 168 registers 
           // outputs k = q + R0 k' of one slot are R0 consecutive elements: hold all q, then
           // store each slot's run with vector stores (conflict-free, like the single-pass kernel)
           Hold out[JN][R0][8];
-          auto st = [&](int jn, int k, int q, int sl, float2 v) {
-            if constexpr (SPLIT) out[jn][q][sl] = v;
-            else out[jn][q][sl] = pack_h2(v.x, v.y);
-          };
-          fft256r_jobs<R0, SPLIT, Cfg::kLmax / (256 * R0), JN>(jc, twR, p.dsign, ld, st);
+          if constexpr (!SPLIT) {
+            plain_row_jobs<R0, JN, PI, RHO>(jc, fold0, rowb(0), 8 * 256 * R0 * ES, p.dsign, out);
+          } else {
+            auto st = [&](int jn, int k, int q, int sl, float2 v) { out[jn][q][sl] = v; };
+            fft256r_jobs<R0, SPLIT, Cfg::kLmax / (256 * R0), JN>(jc, twR, p.dsign, ld, st);
+          }
 #pragma unroll
           for (int jn = 0; jn < JN; ++jn)
 #pragma unroll
@@ -457,13 +640,30 @@ __global__ void __launch_bounds__(384, 1)  // 12 warps at launch: 168 registers 
             }
         }
       } else {
-        if constexpr (ROLE1 == kRoleCol) {
+        if constexpr (ROLE1 == kRoleCol && !SPLIT) {
+          plain_col_tile<R1, C1, false, PI, RHO>(jc, fold1, base, warp, p.dsign, 0, wn);
+        } else if constexpr (ROLE1 == kRoleCol) {
           constexpr int JN = C1 / 8;
-          auto ld = [&](int jn, int n) { return lds_elem<SPLIT>(base + col_tile_off<C1, ES>(n, warp + 8 * jn)); };
-          auto st = [&](int jn, int k, int q, int sl, float2 v) {
-            sts_elem<SPLIT>(base + col_tile_off<C1, ES>(out_row((k - q) / R1, q), warp + 8 * jn), v);
+          constexpr int TWS = Cfg::kLmax / (256 * R1);
+          const int col0 = JN * warp;
+          auto oaddr = [&](int jn, int k, int q) {
+            return base + ctile_off<C1, ES>(col_out_row((k - q) / R1, q), col0 + jn);
           };
-          fft256r_jobs<R1, SPLIT, Cfg::kLmax / (256 * R1), JN>(jc, twR, p.dsign, ld, st);
+          if constexpr (JN % 2 == 0) {
+            auto ldp = [&](int jp, int n, float2& x0, float2& x1) {
+              lds_pair<SPLIT>(base + ctile_off<C1, ES>(col_in_row(n), col0 + jp), x0, x1);
+            };
+            auto st = [&](int jp, int k, int q, int, float2 v0, float2 v1) {
+              sts_pair<SPLIT>(oaddr(jp, k, q), v0, v1);
+            };
+            fft256r_jobs<R1, SPLIT, TWS, JN, true>(jc, twR, p.dsign, ldp, st);
+          } else {
+            auto ld = [&](int jn, int n) {
+              return lds_elem<SPLIT>(base + ctile_off<C1, ES>(col_in_row(n), col0 + jn));
+            };
+            auto st = [&](int jn, int k, int q, int, float2 v) { sts_elem<SPLIT>(oaddr(jn, k, q), v); };
+            fft256r_jobs<R1, SPLIT, TWS, JN>(jc, twR, p.dsign, ld, st);
+          }
         } else if constexpr (ROLE1 == kRoleRow16T) {
           // 16 short rows per warp (one S1 job), held in registers, then written
           // transposed as [k0 + 16 q rows][C1 cols] in boxes of kBW columns
@@ -489,34 +689,48 @@ __global__ void __launch_bounds__(384, 1)  // 12 warps at launch: 168 registers 
                 const int col = warp * 16 + 2 * lane_t + e + 8 * jj;
                 const int row = RHO::apply(lane_g + 8 * h) + 16 * q;
                 const uint32_t addr = base + (uint32_t)((col / Cfg::kBW) * (Cfg::kBW * Cfg::kLen1 * ES)) +
-                                      col_tile_off<Cfg::kBW, ES>(row, col % Cfg::kBW);
+                                      ctile_off<Cfg::kBW, ES>(row, col % Cfg::kBW);
                 if constexpr (SPLIT) sts64f(addr, out[8 * q + sl]);
                 else sts32(addr, out[8 * q + sl]);
               }
           }
-        } else {  // kRoleRowT: rows j = warp + 8 jn -> transposed output tile in the same stage
+        } else {  // kRoleRowT: rows j = JN warp + jn -> transposed output tile in the same stage
           static_assert(C1 % 8 == 0, "row-transpose tiles hold a multiple of 8 rows");
           constexpr int JN = C1 / 8;
-          Hold out[JN][256 * R1 / 32];
-          auto ld = [&](int jn, int n) {
-            return lds_elem<SPLIT>(base + (uint32_t)((warp + 8 * jn) * 256 * R1 * ES) + swz_w<ES>(n) * ES);
-          };
-          auto st = [&](int jn, int k, int q, int sl, float2 v) {
-            if constexpr (SPLIT) out[jn][8 * q + sl] = v;
-            else out[jn][8 * q + sl] = pack_h2(v.x, v.y);
-          };
-          fft256r_jobs<R1, SPLIT, Cfg::kLmax / (256 * R1), JN>(jc, twR, p.dsign, ld, st);
+          constexpr uint32_t kRow = 256 * R1 * ES;   // bytes per input row
+          constexpr uint32_t kStep = 256 * C1 * ES;  // output tile: one q further down
+          const int row0 = JN * warp;                // output columns row0 + jn sit side by side
+          Hold out[JN][R1][8];
+          if constexpr (!SPLIT) {
+            plain_row_jobs<R1, JN, PI, RHO>(jc, fold1, base + row0 * kRow, kRow, p.dsign, out);
+          } else {
+            auto ld = [&](int jn, int n) { return lds_elem<SPLIT>(base + (row0 + jn) * kRow + swz_w<ES>(n) * ES); };
+            auto st = [&](int jn, int k, int q, int sl, float2 v) { out[jn][q][sl] = v; };
+            fft256r_jobs<R1, SPLIT, Cfg::kLmax / (256 * R1), JN>(jc, twR, p.dsign, ld, st);
+          }
           named_bar_sync(1, 256);  // every compute warp finished reading the stage
 #pragma unroll
-          for (int jn = 0; jn < JN; ++jn)
+          for (int sl = 0; sl < 8; ++sl) {
+            const uint32_t so = base + ctile_off<C1, ES>(col_out_row(slot_kval<PI, RHO>(sl), 0), row0);
 #pragma unroll
-            for (int q = 0; q < R1; ++q)
+            for (int q = 0; q < R1; ++q) {
+              if constexpr (JN % 2 == 0) {
 #pragma unroll
-              for (int sl = 0; sl < 8; ++sl) {
-                const int row = out_row(jc.kval[sl >> 2][(sl >> 1) & 1][sl & 1], q);
-                if constexpr (SPLIT) sts64f(base + col_tile_off<C1, ES>(row, warp + 8 * jn), out[jn][8 * q + sl]);
-                else sts32(base + col_tile_off<C1, ES>(row, warp + 8 * jn), out[jn][8 * q + sl]);
+                for (int jp = 0; jp < JN; jp += 2) {
+                  const uint32_t addr = so + jp * ES + q * kStep;
+                  if constexpr (SPLIT) sts128f(addr, out[jp][q][sl], out[jp + 1][q][sl]);
+                  else sts64(addr, out[jp][q][sl], out[jp + 1][q][sl]);
+                }
+              } else {
+#pragma unroll
+                for (int jn = 0; jn < JN; ++jn) {
+                  const uint32_t addr = so + jn * ES + q * kStep;
+                  if constexpr (SPLIT) sts64f(addr, out[jn][q][sl]);
+                  else sts32(addr, out[jn][q][sl]);
+                }
               }
+            }
+          }
         }
       }
     }

@@ -60,13 +60,17 @@ __device__ __forceinline__ void init_job_consts(JobConsts<SPLIT>& c, const float
 // LOAD(jn, n) -> float2 element n (0 <= n < 256R) of job jn's input.
 // STORE(jn, k, q, slot, float2) receives output k = q + R * kval[slot] of job
 // jn in fp32 (slot = 4h + 2e + hh; jn, q, slot compile-time after unrolling).
+// PAIR (JN even): jobs 2i and 2i+1 sit side by side in memory and move together,
+// LOAD(2i, n, float2& x0, float2& x1) and STORE(2i, k, q, slot, v0, v1), so one
+// 8- or 16-byte shared access serves both.
 // All LOADs of the warp complete (and are ordered by __syncwarp) before the
 // first STORE, so a job may write its output over its own input.
 // twR: shared-memory address of a table with W_{256R}^j at index j*TWS (read
 // with ld.shared), used for the radix-R twiddles.
-template <int R, bool SPLIT, int TWS, int JN, class LoadF, class StoreF>
+template <int R, bool SPLIT, int TWS, int JN, bool PAIR = false, class LoadF, class StoreF>
 __device__ __forceinline__ void fft256r_jobs(const JobConsts<SPLIT>& c, uint32_t twR, float dsign, LoadF&& load,
                                              StoreF&& store) {
+  static_assert(!PAIR || JN % 2 == 0, "paired jobs come in twos");
   uint32_t bhi[JN][R][2][2][2], blo[JN][SPLIT ? R : 1][2][2][2];
   float2 xs[SPLIT ? JN : 1][SPLIT ? R : 1][2][2][2];  // split: fp32 operands until the scale is known
   float inv[JN];
@@ -75,24 +79,38 @@ __device__ __forceinline__ void fft256r_jobs(const JobConsts<SPLIT>& c, uint32_t
 #pragma unroll
     for (int r = 0; r < 2; ++r)
 #pragma unroll
-      for (int j = 0; j < 2; ++j)
+      for (int j = 0; j < 2; ++j) {
+        const int m = c.mval[kt][r][j];
+        float2 x[JN][R];
 #pragma unroll
-        for (int jn = 0; jn < JN; ++jn) {
-          float2 x[R];
+        for (int a = 0; a < R; ++a) {
+          if constexpr (PAIR) {
 #pragma unroll
-          for (int a = 0; a < R; ++a) x[a] = load(jn, c.mval[kt][r][j] + 256 * a);
-          if constexpr (R > 1) {
-            dft_small<R>(x, dsign);
+            for (int jp = 0; jp < JN; jp += 2) load(jp, m + 256 * a, x[jp][a], x[jp + 1][a]);
+          } else {
 #pragma unroll
-            for (int q = 1; q < R; ++q)
-              x[q] = cmul(x[q], lds64f(twR + ((c.mval[kt][r][j] * q) & (256 * R - 1)) * TWS * 8));
-          }
-#pragma unroll
-          for (int q = 0; q < R; ++q) {
-            if constexpr (SPLIT) xs[jn][q][kt][r][j] = x[q];
-            else bhi[jn][q][kt][r][j] = pack_h2(x[q].x, x[q].y);
+            for (int jn = 0; jn < JN; ++jn) x[jn][a] = load(jn, m + 256 * a);
           }
         }
+        if constexpr (R > 1) {
+          float2 w[R];  // W_{256R}^(m q), shared by the jobs
+#pragma unroll
+          for (int q = 1; q < R; ++q) w[q] = lds64f(twR + ((m * q) & (256 * R - 1)) * TWS * 8);
+#pragma unroll
+          for (int jn = 0; jn < JN; ++jn) {
+            dft_small<R>(x[jn], dsign);
+#pragma unroll
+            for (int q = 1; q < R; ++q) x[jn][q] = cmul(x[jn][q], w[q]);
+          }
+        }
+#pragma unroll
+        for (int jn = 0; jn < JN; ++jn)
+#pragma unroll
+          for (int q = 0; q < R; ++q) {
+            if constexpr (SPLIT) xs[jn][q][kt][r][j] = x[jn][q];
+            else bhi[jn][q][kt][r][j] = pack_h2(x[jn][q].x, x[jn][q].y);
+          }
+      }
   if constexpr (SPLIT) {
 #pragma unroll
     for (int jn = 0; jn < JN; ++jn) {
@@ -152,17 +170,26 @@ __device__ __forceinline__ void fft256r_jobs(const JobConsts<SPLIT>& c, uint32_t
       else dft16_mma(c.afr, b2[jn], acc[jn]);
     }
 #pragma unroll
-    for (int jn = 0; jn < JN; ++jn)
+    for (int h = 0; h < 2; ++h)
 #pragma unroll
-      for (int h = 0; h < 2; ++h)
+      for (int e = 0; e < 2; ++e)
 #pragma unroll
-        for (int e = 0; e < 2; ++e)
+        for (int hh = 0; hh < 2; ++hh) {
+          float2 v[JN];
 #pragma unroll
-          for (int hh = 0; hh < 2; ++hh) {
-            float2 v = acc_get(acc[jn], h, hh, e);
-            if constexpr (SPLIT) v = make_float2(v.x * inv[jn], v.y * inv[jn]);
-            store(jn, q + R * c.kval[h][e][hh], q, 4 * h + 2 * e + hh, v);
+          for (int jn = 0; jn < JN; ++jn) {
+            v[jn] = acc_get(acc[jn], h, hh, e);
+            if constexpr (SPLIT) v[jn] = make_float2(v[jn].x * inv[jn], v[jn].y * inv[jn]);
           }
+          const int k = q + R * c.kval[h][e][hh], sl = 4 * h + 2 * e + hh;
+          if constexpr (PAIR) {
+#pragma unroll
+            for (int jp = 0; jp < JN; jp += 2) store(jp, k, q, sl, v[jp], v[jp + 1]);
+          } else {
+#pragma unroll
+            for (int jn = 0; jn < JN; ++jn) store(jn, k, q, sl, v[jn]);
+          }
+        }
   }
 }
 
@@ -173,6 +200,137 @@ __device__ __forceinline__ void fft256r_job(const JobConsts<SPLIT>& c, uint32_t 
   fft256r_jobs<R, SPLIT, TWS, 1>(
       c, twR, dsign, [&](int, int n) { return load(n); },
       [&](int, int k, int q, int sl, float2 v) { store(k, q, sl, v); });
+}
+
+// ---------------------------------------------------------------------------
+// Plain precision with the radix-R twiddle folded into the two MMA stages.
+//
+// W_{256R}^(m q) = W_{16R}^(m1 q) W_{256R}^(m0 q) for m = 16 m1 + m0, so the
+// sub-transform q is computed as
+//   stage 1:  A_q[k0][m1] = W16^(m1 k0) W_{16R}^(m1 q)      (a per-q DFT matrix)
+//   twiddle:  T_q[m0][k0] = W_{256R}^(m0 (R k0 + q))        (= W256^(m0 k0) W_{256R}^(m0 q))
+//   stage 2:  F16 over m0
+// and the radix-R step is only the butterfly.  A_0 = F16 and T_0 = W256 stay in
+// registers (JobConsts); A_q and T_q for q >= 1 are per-lane tables in shared
+// memory, entry-major ([entry][lane]) so that the 32 lanes of a warp read 32
+// consecutive words (no bank conflicts).
+template <int R>
+struct FoldTab {
+  static constexpr int kABytes = (R - 1) * 16 * 32 * 4;  // A_q fragments: [q-1][ct kt reg][lane] u32
+  static constexpr int kTBytes = (R - 1) * 8 * 32 * 8;   // T_q: [q-1][j h e][lane] float2
+  static constexpr int kBytes = kABytes + kTBytes;
+};
+
+// Fill one fold table (all threads of the CTA take part; tw2048 = W_2048^j).
+template <int R, class PI, class RHO>
+__device__ void build_fold_table(unsigned char* tab, const float2* __restrict__ tw2048, int tid, int nthreads) {
+  if constexpr (R > 1) {
+    uint32_t* A = reinterpret_cast<uint32_t*>(tab);
+    for (int idx = tid; idx < (R - 1) * 16 * 32; idx += nthreads) {
+      const int q = idx / 512 + 1, e = (idx >> 5) & 15, lane = idx & 31, g = lane >> 2, t = lane & 3;
+      const int ct = e >> 3, kt = (e >> 2) & 1, reg = e & 3;
+      const int k0 = RHO::apply(g + 8 * (reg & 1)), m1 = PI::apply(2 * t + (reg >> 1) + 8 * kt);
+      const float2 w = tw2048[((m1 * (R * k0 + q)) & (16 * R - 1)) * (128 / R)];  // W_{16R}^(m1 (R k0 + q))
+      A[idx] = ct == 0 ? pack_h2(w.x, -w.y) : pack_h2(w.y, w.x);
+    }
+    float2* T = reinterpret_cast<float2*>(tab + FoldTab<R>::kABytes);
+    for (int idx = tid; idx < (R - 1) * 8 * 32; idx += nthreads) {
+      const int q = idx / 256 + 1, sl = (idx >> 5) & 7, lane = idx & 31, g = lane >> 2, t = lane & 3;
+      const int j = sl >> 2, h = (sl >> 1) & 1, e = sl & 1;
+      const int m0 = PI::apply(2 * t + e + 8 * j), k0 = RHO::apply(g + 8 * h);
+      T[idx] = tw2048[((m0 * (R * k0 + q)) & (256 * R - 1)) * (8 / R)];  // W_{256R}^(m0 (R k0 + q))
+    }
+  }
+}
+
+// JN jobs of length 256R in lockstep, plain precision, folded twiddles.
+// LOAD(jn, slot, a) -> float2 input element m(slot) + 256 a of job jn, where
+// slot = 4 kt + 2 r + j is the B-fragment slot (m = 16 PI(2t + r + 8kt) +
+// PI(g + 8j)); with PAIR, LOAD(jp, slot, a, float2& x0, float2& x1) for jobs
+// jp, jp + 1.  STORE(jn, osl, q, float2) receives output q + R kval(osl) of
+// job jn (osl = 4h + 2e + hh, kval = RHO(2t + e + 8h) + 16 RHO(g + 8hh)); with
+// PAIR, STORE(jp, osl, q, v0, v1).  All loads precede the first store.
+// tab: shared-memory address of this R's fold table.
+template <int R, int JN, bool PAIR, class LoadF, class StoreF>
+__device__ __forceinline__ void fft256r_jobs_fold(const JobConsts<false>& c, uint32_t tab, float dsign, LoadF&& load,
+                                                  StoreF&& store) {
+  static_assert(!PAIR || JN % 2 == 0, "paired jobs come in twos");
+  const uint32_t lane4 = (threadIdx.x & 31) * 4;
+  uint32_t bhi[JN][R][2][2][2];
+#pragma unroll
+  for (int kt = 0; kt < 2; ++kt)
+#pragma unroll
+    for (int r = 0; r < 2; ++r)
+#pragma unroll
+      for (int j = 0; j < 2; ++j) {
+        const int slot = 4 * kt + 2 * r + j;
+        float2 x[JN][R];
+#pragma unroll
+        for (int a = 0; a < R; ++a) {
+          if constexpr (PAIR) {
+#pragma unroll
+            for (int jp = 0; jp < JN; jp += 2) load(jp, slot, a, x[jp][a], x[jp + 1][a]);
+          } else {
+#pragma unroll
+            for (int jn = 0; jn < JN; ++jn) x[jn][a] = load(jn, slot, a);
+          }
+        }
+#pragma unroll
+        for (int jn = 0; jn < JN; ++jn) {
+          if constexpr (R > 1) dft_small<R>(x[jn], dsign);
+#pragma unroll
+          for (int q = 0; q < R; ++q) bhi[jn][q][kt][r][j] = pack_h2(x[jn][q].x, x[jn][q].y);
+        }
+      }
+  __syncwarp();  // every lane has read the jobs' inputs (stores may alias them)
+#pragma unroll
+  for (int q = 0; q < R; ++q) {
+    uint32_t aq[2][2][4];
+    if (q == 0) {
+#pragma unroll
+      for (int i = 0; i < 16; ++i) aq[i >> 3][(i >> 2) & 1][i & 3] = c.afr[i >> 3][(i >> 2) & 1][i & 3];
+    } else {
+#pragma unroll
+      for (int i = 0; i < 16; ++i) aq[i >> 3][(i >> 2) & 1][i & 3] = lds32(tab + ((q - 1) * 16 + i) * 128 + lane4);
+    }
+    float acc[JN][2][2][4];
+#pragma unroll
+    for (int jn = 0; jn < JN; ++jn) dft16_mma(aq, bhi[jn][q], acc[jn]);
+    uint32_t b2[JN][2][2][2];
+#pragma unroll
+    for (int kt = 0; kt < 2; ++kt)
+#pragma unroll
+      for (int h = 0; h < 2; ++h)
+#pragma unroll
+        for (int r = 0; r < 2; ++r) {
+          const float2 w = q == 0 ? c.tw1[kt][h][r]
+                                  : lds64f(tab + FoldTab<R>::kABytes + ((q - 1) * 8 + 4 * kt + 2 * h + r) * 256 +
+                                           lane4 * 2);
+#pragma unroll
+          for (int jn = 0; jn < JN; ++jn) {
+            const float2 v = cmul(acc_get(acc[jn], kt, h, r), w);
+            b2[jn][kt][r][h] = pack_h2(v.x, v.y);
+          }
+        }
+#pragma unroll
+    for (int jn = 0; jn < JN; ++jn) dft16_mma(c.afr, b2[jn], acc[jn]);
+#pragma unroll
+    for (int h = 0; h < 2; ++h)
+#pragma unroll
+      for (int e = 0; e < 2; ++e)
+#pragma unroll
+        for (int hh = 0; hh < 2; ++hh) {
+          const int osl = 4 * h + 2 * e + hh;
+          if constexpr (PAIR) {
+#pragma unroll
+            for (int jp = 0; jp < JN; jp += 2)
+              store(jp, osl, q, acc_get(acc[jp], h, hh, e), acc_get(acc[jp + 1], h, hh, e));
+          } else {
+#pragma unroll
+            for (int jn = 0; jn < JN; ++jn) store(jn, osl, q, acc_get(acc[jn], h, hh, e));
+          }
+        }
+  }
 }
 
 }  // namespace tcfft

@@ -52,12 +52,69 @@ CUresult encode_tmap(CUtensorMap* map, CUtensorMapDataType dtype, int rank, void
                   CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
 }
 
+// Column-tile maps (the digit orders of fft_fused.cuh's ctile_off/col_in_row/
+// col_out_row; the swizzle of the tile's row width C*es).  The global data is
+// rows of `ncols` elements; transforms are blocks of 256R consecutive rows.
+CUtensorMapSwizzle col_swizzle(int C, int es) {
+  return C * es == 32 ? CU_TENSOR_MAP_SWIZZLE_32B
+                      : (C * es == 64 ? CU_TENSOR_MAP_SWIZZLE_64B : CU_TENSOR_MAP_SWIZZLE_128B);
+}
+// Load box [C][m1 bit 3][m0][m1 bits 0-2][a + R block]: input row n = m0 + 16 m1 + 256 a.
+CUresult encode_col_load(CUtensorMap* m, CUtensorMapDataType dt, void* base, int64_t ncols, int64_t nblk, int es,
+                         int C, int R) {
+  const uint64_t rp = (uint64_t)ncols * es;
+  uint64_t dims[5] = {(uint64_t)ncols, 2, 16, 8, (uint64_t)(nblk * R)};
+  uint64_t str[4] = {128 * rp, rp, 16 * rp, 256 * rp};
+  uint32_t box[5] = {(uint32_t)C, 2, 16, 8, (uint32_t)R};
+  return encode_tmap(m, dt, 5, base, dims, str, box, col_swizzle(C, es));
+}
+// Store box [C][k0 bits 2-3][k1 + 16 block][k0 bits 0-1][q]: output row k = q + R (k0 + 16 k1).
+CUresult encode_col_store(CUtensorMap* m, CUtensorMapDataType dt, void* base, int64_t ncols, int64_t nblk, int es,
+                          int C, int R) {
+  const uint64_t rp = (uint64_t)ncols * es;
+  uint64_t dims[5] = {(uint64_t)ncols, 4, (uint64_t)(16 * nblk), 4, (uint64_t)R};
+  uint64_t str[4] = {4 * R * rp, 16 * R * rp, R * rp, rp};
+  uint32_t box[5] = {(uint32_t)C, 4, 16, 4, (uint32_t)R};
+  return encode_tmap(m, dt, 5, base, dims, str, box, col_swizzle(C, es));
+}
+
+// Tensor maps of the 1D fused executor (the plan path and the allocation-free
+// entry point share them): phase 0 reads `data` as column tiles and writes the
+// scratch slots [S][N1 rows][N2 cols]; phase 1 reads scratch rows and writes
+// `data` transposed (X[k1 + N1 k2]).
+CUresult encode_fused1d_maps(FusedMaps* maps, const FusedKey& k, void* data, void* scratch, int64_t n1, int64_t n2,
+                             int64_t batch, int S) {
+  const int es = k.split ? 8 : 4, er = 128 / es;
+  const CUtensorMapDataType dt = k.split ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_UINT32;
+  CUresult r = encode_col_load(&maps->load0, dt, data, n2, batch, es, k.C0, k.R0);
+  if (r != CUDA_SUCCESS) return r;
+  r = encode_col_store(&maps->store0, dt, scratch, n2, S, es, k.C0, k.R0);
+  if (r != CUDA_SUCCESS) return r;
+  {  // phase-1 load: scratch as contiguous 128-byte rows, boxes of one tile (<= 256 rows)
+    const int64_t tile_rows = (int64_t)k.C1 * n2 / er;
+    uint64_t dims[2] = {(uint64_t)er, (uint64_t)(S * n1 * n2 / er)};
+    uint64_t str[1] = {128};
+    uint32_t box[2] = {(uint32_t)er, (uint32_t)(tile_rows < 256 ? tile_rows : 256)};
+    r = encode_tmap(&maps->load1, dt, 2, scratch, dims, str, box, CU_TENSOR_MAP_SWIZZLE_128B);
+    if (r != CUDA_SUCCESS) return r;
+  }
+  if (k.role1 == kRoleRow16T) {  // phase-1 store: X[k1 + N1 k2], k2 = q + R1 k0: dims [N1][k0][q][B]
+    const uint64_t rowb = (uint64_t)n1 * es;
+    uint64_t dims[4] = {(uint64_t)n1, 16, (uint64_t)k.R1, (uint64_t)batch};
+    uint64_t str[3] = {rowb * k.R1, rowb, rowb * n2};
+    uint32_t box[4] = {(uint32_t)(128 / es), 16, (uint32_t)k.R1, 1};
+    return encode_tmap(&maps->store1, dt, 4, data, dims, str, box, CU_TENSOR_MAP_SWIZZLE_128B);
+  }
+  // phase-1 store: data as [B*N2 rows k2][N1 cols k1]
+  return encode_col_store(&maps->store1, dt, data, n1, batch, es, k.C1, k.R1);
+}
 }  // namespace tcfft
 
 using namespace tcfft;
 
 // ------------------------------------------------------------------ helpers
 namespace {
+
 
 bool is_pow2(int64_t v) { return v > 0 && (v & (v - 1)) == 0; }
 
@@ -313,52 +370,9 @@ tcfftStatus exec_plan(tcfftPlan plan, void* data, void* stream, int dir) {
     const CUtensorMapDataType dt = split ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_UINT32;
     if (plan->tmap_ptr != data) {
       const FusedKey& k = s.key;
-      auto sw = [&](int c) {
-        return c * es == 32 ? CU_TENSOR_MAP_SWIZZLE_32B
-                            : (c * es == 64 ? CU_TENSOR_MAP_SWIZZLE_64B : CU_TENSOR_MAP_SWIZZLE_128B);
-      };
-      {  // phase-0 load: data as [B*N1][N2]
-        uint64_t dims[2] = {(uint64_t)s.N2, (uint64_t)(plan->batch * s.N1)};
-        uint64_t str[1] = {(uint64_t)(s.N2 * es)};
-        uint32_t box[2] = {(uint32_t)k.C0, 256};
-        if (cu_status(encode_tmap(&plan->fmaps.load0, dt, 2, data, dims, str, box, sw(k.C0)), "tmap load0"))
-          return TCFFT_CUDA_ERROR;
-      }
-      if (k.role1 == kRoleRow16T) {  // phase-1 store: X[k1 + N1 k2], k2 = q + R1 k0: dims [N1][k0][q][B]
-        const uint64_t rowb = (uint64_t)s.N1 * es;
-        uint64_t dims[4] = {(uint64_t)s.N1, 16, (uint64_t)k.R1, (uint64_t)plan->batch};
-        uint64_t str[3] = {rowb * k.R1, rowb, rowb * s.N2};
-        uint32_t box[4] = {(uint32_t)(128 / es), 16, (uint32_t)k.R1, 1};
-        if (cu_status(encode_tmap(&plan->fmaps.store1, dt, 4, data, dims, str, box, CU_TENSOR_MAP_SWIZZLE_128B),
-                      "tmap store1"))
-          return TCFFT_CUDA_ERROR;
-      } else {  // phase-1 store: X[k1 + N1 k2], k2 = q + R1 (k0 + 16 k1'): dims [N1][k1'][k0][q][B]
-        const uint64_t rowb = (uint64_t)s.N1 * es;
-        uint64_t dims[5] = {(uint64_t)s.N1, 16, 16, (uint64_t)k.R1, (uint64_t)plan->batch};
-        uint64_t str[4] = {rowb * 16 * k.R1, rowb * k.R1, rowb, rowb * s.N2};
-        uint32_t box[5] = {(uint32_t)k.C1, 16, 16, (uint32_t)k.R1, 1};
-        if (cu_status(encode_tmap(&plan->fmaps.store1, dt, 5, data, dims, str, box, sw(k.C1)), "tmap store1"))
-          return TCFFT_CUDA_ERROR;
-      }
-      {  // phase-0 store: scratch rows k1 = q + R0 (k0 + 16 k1'): dims [N2][k1'][k0][q][slot]
-        const uint64_t rowb = (uint64_t)s.N2 * es;
-        uint64_t dims[5] = {(uint64_t)s.N2, 16, 16, (uint64_t)k.R0, (uint64_t)s.S};
-        uint64_t str[4] = {rowb * 16 * k.R0, rowb * k.R0, rowb, rowb * s.N1};
-        uint32_t box[5] = {(uint32_t)k.C0, 16, 16, (uint32_t)k.R0, 1};
-        if (cu_status(encode_tmap(&plan->fmaps.store0, dt, 5, plan->scratch, dims, str, box, sw(k.C0)),
-                      "tmap store0"))
-          return TCFFT_CUDA_ERROR;
-      }
-      {  // phase-1 load: scratch as contiguous 128-byte rows, boxes of one tile (<= 256 rows)
-        const int64_t tile_rows = (int64_t)k.C1 * s.N2 / er;
-        uint64_t dims[2] = {(uint64_t)er, (uint64_t)(s.S * s.N1 * s.N2 / er)};
-        uint64_t str[1] = {128};
-        uint32_t box[2] = {(uint32_t)er, (uint32_t)(tile_rows < 256 ? tile_rows : 256)};
-        if (cu_status(encode_tmap(&plan->fmaps.load1, dt, 2, plan->scratch, dims, str, box,
-                                  CU_TENSOR_MAP_SWIZZLE_128B),
-                      "tmap load1"))
-          return TCFFT_CUDA_ERROR;
-      }
+      if (cu_status(encode_fused1d_maps(&plan->fmaps, k, data, plan->scratch, s.N1, s.N2, plan->batch, s.S),
+                    "tmap fused1d"))
+        return TCFFT_CUDA_ERROR;
       plan->tmap_ptr = data;
     }
     FusedParams fp;
@@ -391,10 +405,6 @@ tcfftStatus exec_plan(tcfftPlan plan, void* data, void* stream, int dir) {
     const FusedKey& k = s.key;
     const int64_t nx = s.N1, ny = s.N2;
     if (plan->tmap_ptr != data) {
-      auto sw = [&](int c) {
-        return c * es == 32 ? CU_TENSOR_MAP_SWIZZLE_32B
-                            : (c * es == 64 ? CU_TENSOR_MAP_SWIZZLE_64B : CU_TENSOR_MAP_SWIZZLE_128B);
-      };
       {  // phase 0 (rows, in place): contiguous 128-byte rows, one tile per box group
         const int64_t tile_rows = (int64_t)k.C0 * ny / er;
         uint64_t dims[2] = {(uint64_t)er, (uint64_t)(plan->batch * nx * ny / er)};
@@ -405,21 +415,12 @@ tcfftStatus exec_plan(tcfftPlan plan, void* data, void* stream, int dir) {
           return TCFFT_CUDA_ERROR;
         plan->fmaps.store0 = plan->fmaps.load0;
       }
-      {  // phase 1 load: data as [B*NX][NY]
-        uint64_t dims[2] = {(uint64_t)ny, (uint64_t)(plan->batch * nx)};
-        uint64_t str[1] = {(uint64_t)(ny * es)};
-        uint32_t box[2] = {(uint32_t)k.C1, 256};
-        if (cu_status(encode_tmap(&plan->fmaps.load1, dt, 2, data, dims, str, box, sw(k.C1)), "tmap2d load1"))
-          return TCFFT_CUDA_ERROR;
-      }
-      {  // phase 1 store: rows k = q + R1 (k0 + 16 k1'): dims [NY][k1'][k0][q][B]
-        const uint64_t rowb = (uint64_t)ny * es;
-        uint64_t dims[5] = {(uint64_t)ny, 16, 16, (uint64_t)k.R1, (uint64_t)plan->batch};
-        uint64_t str[4] = {rowb * 16 * k.R1, rowb * k.R1, rowb, rowb * nx};
-        uint32_t box[5] = {(uint32_t)k.C1, 16, 16, (uint32_t)k.R1, 1};
-        if (cu_status(encode_tmap(&plan->fmaps.store1, dt, 5, data, dims, str, box, sw(k.C1)), "tmap2d store1"))
-          return TCFFT_CUDA_ERROR;
-      }
+      // phase 1 (columns, in place): data as [B*NX][NY], NX = 256 R1 rows per transform
+      if (cu_status(encode_col_load(&plan->fmaps.load1, dt, data, ny, plan->batch, es, k.C1, k.R1), "tmap2d load1"))
+        return TCFFT_CUDA_ERROR;
+      if (cu_status(encode_col_store(&plan->fmaps.store1, dt, data, ny, plan->batch, es, k.C1, k.R1),
+                    "tmap2d store1"))
+        return TCFFT_CUDA_ERROR;
       plan->tmap_ptr = data;
     }
     FusedParams fp;

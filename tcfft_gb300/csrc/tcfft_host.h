@@ -34,6 +34,9 @@ struct FusedKey {
 int fused_cols(int R, bool split);
 cudaError_t launch_fused(const FusedKey& k, const FusedMaps& maps, const FusedParams& p, int num_sms,
                          cudaStream_t st, int* grid_out);
+// Tensor maps of the 1D two-phase executor (N = n1 * n2; S scratch slots of N elements).
+CUresult encode_fused1d_maps(FusedMaps* maps, const FusedKey& k, void* data, void* scratch, int64_t n1, int64_t n2,
+                             int64_t batch, int S);
 
 // Launch entry points implemented in the kernel translation units. Each
 // returns cudaSuccess or the launch error.

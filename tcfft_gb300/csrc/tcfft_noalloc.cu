@@ -183,45 +183,7 @@ extern "C" tcfftStatus tcfftExecute1dNoAlloc(void* data, int64_t n, int64_t batc
 
   // tensor maps (host-side encode, no allocation)
   FusedMaps maps;
-  const CUtensorMapDataType dt = split ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_UINT32;
-  auto sw = [&](int c) {
-    return c * es == 32 ? CU_TENSOR_MAP_SWIZZLE_32B : (c * es == 64 ? CU_TENSOR_MAP_SWIZZLE_64B : CU_TENSOR_MAP_SWIZZLE_128B);
-  };
-  {
-    uint64_t dims[2] = {(uint64_t)n2, (uint64_t)(batch * n1)};
-    uint64_t str[1] = {(uint64_t)(n2 * es)};
-    uint32_t box[2] = {(uint32_t)k.C0, 256};
-    if (encode_tmap(&maps.load0, dt, 2, data, dims, str, box, sw(k.C0)) != CUDA_SUCCESS) return TCFFT_CUDA_ERROR;
-  }
-  {
-    const uint64_t rowb = (uint64_t)n2 * es;
-    uint64_t dims[5] = {(uint64_t)n2, 16, 16, (uint64_t)k.R0, (uint64_t)S};
-    uint64_t str[4] = {rowb * 16 * k.R0, rowb * k.R0, rowb, rowb * n1};
-    uint32_t box[5] = {(uint32_t)k.C0, 16, 16, (uint32_t)k.R0, 1};
-    if (encode_tmap(&maps.store0, dt, 5, d.scratch, dims, str, box, sw(k.C0)) != CUDA_SUCCESS) return TCFFT_CUDA_ERROR;
-  }
-  {
-    const int64_t tile_rows = (int64_t)k.C1 * n2 / er;
-    uint64_t dims[2] = {(uint64_t)er, (uint64_t)(S * n / er)};
-    uint64_t str[1] = {128};
-    uint32_t box[2] = {(uint32_t)er, (uint32_t)(tile_rows < 256 ? tile_rows : 256)};
-    if (encode_tmap(&maps.load1, dt, 2, d.scratch, dims, str, box, CU_TENSOR_MAP_SWIZZLE_128B) != CUDA_SUCCESS)
-      return TCFFT_CUDA_ERROR;
-  }
-  if (k.role1 == kRoleRow16T) {
-    const uint64_t rowb = (uint64_t)n1 * es;
-    uint64_t dims[4] = {(uint64_t)n1, 16, (uint64_t)k.R1, (uint64_t)batch};
-    uint64_t str[3] = {rowb * k.R1, rowb, rowb * n2};
-    uint32_t box[4] = {(uint32_t)(128 / es), 16, (uint32_t)k.R1, 1};
-    if (encode_tmap(&maps.store1, dt, 4, data, dims, str, box, CU_TENSOR_MAP_SWIZZLE_128B) != CUDA_SUCCESS)
-      return TCFFT_CUDA_ERROR;
-  } else {
-    const uint64_t rowb = (uint64_t)n1 * es;
-    uint64_t dims[5] = {(uint64_t)n1, 16, 16, (uint64_t)k.R1, (uint64_t)batch};
-    uint64_t str[4] = {rowb * 16 * k.R1, rowb * k.R1, rowb, rowb * n2};
-    uint32_t box[5] = {(uint32_t)k.C1, 16, 16, (uint32_t)k.R1, 1};
-    if (encode_tmap(&maps.store1, dt, 5, data, dims, str, box, sw(k.C1)) != CUDA_SUCCESS) return TCFFT_CUDA_ERROR;
-  }
+  if (encode_fused1d_maps(&maps, k, data, d.scratch, n1, n2, batch, S) != CUDA_SUCCESS) return TCFFT_CUDA_ERROR;
 
   FusedParams fp;
   fp.tw2048 = d.tw2048;
