@@ -316,6 +316,64 @@ __device__ __forceinline__ float2 acc_get(const float (&acc)[2][2][4], int j, in
   return make_float2(acc[0][j][2 * h + e], acc[1][j][2 * h + e]);
 }
 
+// ---------------------------------------------------------------- packed half2 complex arithmetic
+// A complex value as one 32-bit register: real part in the low half, imaginary
+// part in the high half (the layout of the interleaved half2 data).
+__device__ __forceinline__ uint32_t h2add(uint32_t a, uint32_t b) {
+  uint32_t d;
+  asm("add.rn.f16x2 %0, %1, %2;" : "=r"(d) : "r"(a), "r"(b));
+  return d;
+}
+__device__ __forceinline__ uint32_t h2sub(uint32_t a, uint32_t b) {
+  uint32_t d;
+  asm("sub.rn.f16x2 %0, %1, %2;" : "=r"(d) : "r"(a), "r"(b));
+  return d;
+}
+__device__ __forceinline__ uint32_t h2mul(uint32_t a, uint32_t b) {
+  uint32_t d;
+  asm("mul.rn.f16x2 %0, %1, %2;" : "=r"(d) : "r"(a), "r"(b));
+  return d;
+}
+// v * (-i * dsign): swap the halves, then negate one of them; negmask =
+// 0x80000000 for dsign = +1 ((re, im) -> (im, -re)), 0x00008000 for dsign = -1.
+__device__ __forceinline__ uint32_t h2mi(uint32_t v, uint32_t negmask) { return __byte_perm(v, 0, 0x1032) ^ negmask; }
+
+// In-place radix-R DFT on packed half2 values (same convention as dft_small).
+// c8 = cos(pi/4) broadcast to both halves (used by R = 8).
+template <int R>
+__device__ __forceinline__ void dft_small_h(uint32_t (&x)[R], uint32_t negmask, uint32_t c8) {
+  if constexpr (R == 2) {
+    const uint32_t a = x[0], b = x[1];
+    x[0] = h2add(a, b);
+    x[1] = h2sub(a, b);
+  } else if constexpr (R == 4) {
+    const uint32_t a0 = h2add(x[0], x[2]), a1 = h2sub(x[0], x[2]);
+    const uint32_t b0 = h2add(x[1], x[3]), b1 = h2mi(h2sub(x[1], x[3]), negmask);
+    x[0] = h2add(a0, b0);
+    x[2] = h2sub(a0, b0);
+    x[1] = h2add(a1, b1);
+    x[3] = h2sub(a1, b1);
+  } else if constexpr (R == 8) {
+    uint32_t u[4], v[4];
+#pragma unroll
+    for (int a = 0; a < 4; ++a) {
+      u[a] = h2add(x[a], x[a + 4]);
+      v[a] = h2sub(x[a], x[a + 4]);
+    }
+    // v[a] *= W8^a: W8 = c (1 - i dsign) -> c (v + mi(v)); W8^2 = -i dsign; W8^3 = c (mi(v) - v)
+    v[1] = h2mul(h2add(v[1], h2mi(v[1], negmask)), c8);
+    v[2] = h2mi(v[2], negmask);
+    v[3] = h2mul(h2sub(h2mi(v[3], negmask), v[3]), c8);
+    dft_small_h<4>(u, negmask, c8);
+    dft_small_h<4>(v, negmask, c8);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      x[2 * q] = u[q];
+      x[2 * q + 1] = v[q];
+    }
+  }
+}
+
 // ---------------------------------------------------------------- small radix-R DFT (fp32)
 // In-place DFT of R values, x_q <- sum_a x_a W_R^(a q) (W_R = exp(-2 pi i dsign / R)).
 template <int R>

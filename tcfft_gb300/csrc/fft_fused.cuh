@@ -218,9 +218,7 @@ __device__ __forceinline__ void plain_col_tile(const JobConsts<false>& jc, uint3
       for (int q = 2; q < R; ++q) fq[jn][q] = cmul(fq[jn][q - 1], fq[jn][1]);
     }
     if constexpr (PAIR) {
-      auto ld = [&](int jp, int sl, int a, float2& x0, float2& x1) {
-        lds_pair<false>(lo[sl] + jp * ES + a * kStep, x0, x1);
-      };
+      auto ld = [&](int jp, int sl, int a, uint32_t& x0, uint32_t& x1) { lds64(lo[sl] + jp * ES + a * kStep, x0, x1); };
       auto st = [&](int jp, int osl, int q, float2 v0, float2 v1) {
         v0 = cmul(v0, cmul(fk[jp][osl], fq[jp][q]));
         v1 = cmul(v1, cmul(fk[jp + 1][osl], fq[jp + 1][q]));
@@ -228,7 +226,7 @@ __device__ __forceinline__ void plain_col_tile(const JobConsts<false>& jc, uint3
       };
       fft256r_jobs_fold<R, JN, true>(jc, fold, dsign, ld, st);
     } else {
-      auto ld = [&](int jn, int sl, int a) { return lds_elem<false>(lo[sl] + jn * ES + a * kStep); };
+      auto ld = [&](int jn, int sl, int a) { return lds32(lo[sl] + jn * ES + a * kStep); };
       auto st = [&](int jn, int osl, int q, float2 v) {
         sts_elem<false>(so[osl] + jn * ES + q * kStep, cmul(v, cmul(fk[jn][osl], fq[jn][q])));
       };
@@ -236,15 +234,13 @@ __device__ __forceinline__ void plain_col_tile(const JobConsts<false>& jc, uint3
     }
   } else {
     if constexpr (PAIR) {
-      auto ld = [&](int jp, int sl, int a, float2& x0, float2& x1) {
-        lds_pair<false>(lo[sl] + jp * ES + a * kStep, x0, x1);
-      };
+      auto ld = [&](int jp, int sl, int a, uint32_t& x0, uint32_t& x1) { lds64(lo[sl] + jp * ES + a * kStep, x0, x1); };
       auto st = [&](int jp, int osl, int q, float2 v0, float2 v1) {
         sts_pair<false>(so[osl] + jp * ES + q * kStep, v0, v1);
       };
       fft256r_jobs_fold<R, JN, true>(jc, fold, dsign, ld, st);
     } else {
-      auto ld = [&](int jn, int sl, int a) { return lds_elem<false>(lo[sl] + jn * ES + a * kStep); };
+      auto ld = [&](int jn, int sl, int a) { return lds32(lo[sl] + jn * ES + a * kStep); };
       auto st = [&](int jn, int osl, int q, float2 v) { sts_elem<false>(so[osl] + jn * ES + q * kStep, v); };
       fft256r_jobs_fold<R, JN, false>(jc, fold, dsign, ld, st);
     }
@@ -259,7 +255,7 @@ __device__ __forceinline__ void plain_row_jobs(const JobConsts<false>& jc, uint3
   uint32_t lo[8];
 #pragma unroll
   for (int sl = 0; sl < 8; ++sl) lo[sl] = row_addr0 + swz_w<4>(slot_m<PI, RHO>(sl)) * 4;
-  auto ld = [&](int jn, int sl, int a) { return lds_elem<false>(lo[sl] + jn * row_stride + a * 1024); };
+  auto ld = [&](int jn, int sl, int a) { return lds32(lo[sl] + jn * row_stride + a * 1024); };
   auto st = [&](int jn, int osl, int q, float2 v) { out[jn][q][osl] = pack_h2(v.x, v.y); };
   fft256r_jobs_fold<R, JN, false>(jc, fold, dsign, ld, st);
 }

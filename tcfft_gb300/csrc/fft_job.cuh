@@ -243,10 +243,11 @@ __device__ void build_fold_table(unsigned char* tab, const float2* __restrict__ 
   }
 }
 
-// JN jobs of length 256R in lockstep, plain precision, folded twiddles.
-// LOAD(jn, slot, a) -> float2 input element m(slot) + 256 a of job jn, where
-// slot = 4 kt + 2 r + j is the B-fragment slot (m = 16 PI(2t + r + 8kt) +
-// PI(g + 8j)); with PAIR, LOAD(jp, slot, a, float2& x0, float2& x1) for jobs
+// JN jobs of length 256R in lockstep, plain precision, folded twiddles; the
+// radix-R butterfly runs on the packed half2 inputs (no fp32 round trip).
+// LOAD(jn, slot, a) -> packed half2 input element m(slot) + 256 a of job jn,
+// where slot = 4 kt + 2 r + j is the B-fragment slot (m = 16 PI(2t + r + 8kt) +
+// PI(g + 8j)); with PAIR, LOAD(jp, slot, a, uint32_t& x0, uint32_t& x1) for jobs
 // jp, jp + 1.  STORE(jn, osl, q, float2) receives output q + R kval(osl) of
 // job jn (osl = 4h + 2e + hh, kval = RHO(2t + e + 8h) + 16 RHO(g + 8hh)); with
 // PAIR, STORE(jp, osl, q, v0, v1).  All loads precede the first store.
@@ -256,6 +257,8 @@ __device__ __forceinline__ void fft256r_jobs_fold(const JobConsts<false>& c, uin
                                                   StoreF&& store) {
   static_assert(!PAIR || JN % 2 == 0, "paired jobs come in twos");
   const uint32_t lane4 = (threadIdx.x & 31) * 4;
+  const uint32_t negmask = dsign > 0.f ? 0x80000000u : 0x00008000u;
+  const uint32_t c8 = pack_h2(0.70710678118654752440f, 0.70710678118654752440f);
   uint32_t bhi[JN][R][2][2][2];
 #pragma unroll
   for (int kt = 0; kt < 2; ++kt)
@@ -264,7 +267,7 @@ __device__ __forceinline__ void fft256r_jobs_fold(const JobConsts<false>& c, uin
 #pragma unroll
       for (int j = 0; j < 2; ++j) {
         const int slot = 4 * kt + 2 * r + j;
-        float2 x[JN][R];
+        uint32_t x[JN][R];
 #pragma unroll
         for (int a = 0; a < R; ++a) {
           if constexpr (PAIR) {
@@ -277,9 +280,9 @@ __device__ __forceinline__ void fft256r_jobs_fold(const JobConsts<false>& c, uin
         }
 #pragma unroll
         for (int jn = 0; jn < JN; ++jn) {
-          if constexpr (R > 1) dft_small<R>(x[jn], dsign);
+          if constexpr (R > 1) dft_small_h<R>(x[jn], negmask, c8);
 #pragma unroll
-          for (int q = 0; q < R; ++q) bhi[jn][q][kt][r][j] = pack_h2(x[jn][q].x, x[jn][q].y);
+          for (int q = 0; q < R; ++q) bhi[jn][q][kt][r][j] = x[jn][q];
         }
       }
   __syncwarp();  // every lane has read the jobs' inputs (stores may alias them)
