@@ -43,6 +43,7 @@ struct FusedMaps {
 
 struct FusedParams {
   const float2* tw2048;
+  unsigned char* scratch;  // 1D: the scratch ring (phase-0 output, phase-1 input); 2D: unused
   const float2* twlo;  // W_N^j, j < 2^tw_shift        (1D phase-0 twiddle)
   const float2* twhi;  // W_N^(j << tw_shift)
   int tw_shift;
@@ -537,6 +538,16 @@ __global__ void __launch_bounds__(384, 1)  // 12 warps at launch: 168 registers 
     // all compute warps agree on success before any of them enters a named barrier
     const bool ok = named_bar_and(2, 256, mbar_wait(&full[s], (cnt / NST) & 1, p.err));
     const uint32_t base = smem_addr(smem + s * Cfg::kStageBytes);
+    if constexpr (Cfg::k1D) {
+      if (ok && it.phase == 1) {
+        // the tile's scratch rows are in shared memory now and never read again: drop
+        // them from L2 without writing them back to HBM
+        const long long row0 = (long long)(it.b % p.S) * p.rows1 + (long long)it.tile * C1;
+        const unsigned char* src = p.scratch + row0 * Cfg::kLen1 * ES;
+        for (int i = threadIdx.x; i < Cfg::kTile1 * ES / 128; i += 256)
+          asm volatile("discard.global.L2 [%0], 128;" ::"l"(src + i * 128) : "memory");
+      }
+    }
     if (ok) {
       if (it.phase == 0) {
         if constexpr (ROLE0 == kRoleCol && !SPLIT) {

@@ -377,6 +377,7 @@ tcfftStatus exec_plan(tcfftPlan plan, void* data, void* stream, int dir) {
     }
     FusedParams fp;
     fp.tw2048 = tw;
+    fp.scratch = static_cast<unsigned char*>(plan->scratch);
     fp.twlo = plan->twlo[dir];
     fp.twhi = plan->twhi[dir];
     fp.tw_shift = plan->tw_shift;

@@ -187,6 +187,7 @@ extern "C" tcfftStatus tcfftExecute1dNoAlloc(void* data, int64_t n, int64_t batc
 
   FusedParams fp;
   fp.tw2048 = d.tw2048;
+  fp.scratch = reinterpret_cast<unsigned char*>(d.scratch);
   fp.twlo = d.twlo;
   fp.twhi = d.twhi;
   fp.tw_shift = shift;
