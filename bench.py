@@ -288,6 +288,7 @@ def main():
 
     import torch
     import tcfft_gb300 as tc
+    from tcfft_gb300.replicas import max_over_ranks
 
     dist = None
     if world > 1:
@@ -319,10 +320,7 @@ def main():
     time.sleep(0.3)  # let nvidia-smi start sampling before the timed region
     secs = time_device(torch, plan, x, args.steps, args.warmup, dist)
     clocks = sampler.stop()
-    if dist is not None:
-        t = torch.tensor([secs], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        secs = float(t.item())
+    secs = max_over_ranks(secs, dist, device="cuda")
     per_call = secs / args.steps
     value = flops_per_call(size, batch) * world / per_call / 1e9
 
@@ -361,10 +359,7 @@ def main():
     e1.record()
     torch.cuda.synchronize()
     e2e_s = e0.elapsed_time(e1) / 1000.0 / e2e_steps
-    if dist is not None:
-        t = torch.tensor([e2e_s], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = max_over_ranks(e2e_s, dist, device="cuda")
     e2e = {"value": round(flops_per_call(size, batch) * world / e2e_s / 1e9, 1), "unit": "GFLOP/s",
            "h2d_bytes_per_step": host_in.numel() * host_in.element_size(),
            "d2h_bytes_per_step": host_out.numel() * host_out.element_size(),
