@@ -47,6 +47,8 @@ struct FusedParams {
   const float2* twlo;  // W_N^j, j < 2^tw_shift        (1D phase-0 twiddle)
   const float2* twhi;  // W_N^(j << tw_shift)
   int tw_shift;
+  int wn_global;       // 1: W_N factors read from twlo/twhi in global memory (tables too large to
+                       //    stage in shared memory: the column pass of N > 2^22); 0: staged
   long long n_mask;    // N - 1 (1D)
   int batch;           // transforms
   int D;               // lag in blocks between phase 0 and phase 1 of a transform
@@ -171,12 +173,17 @@ __device__ __forceinline__ int slot_kval(int osl) {
   return RHO::apply(2 * t + ((osl >> 1) & 1) + 8 * (osl >> 2)) + 16 * RHO::apply(g + 8 * (osl & 1));
 }
 
-// W_N^e from the two-level shared table (e reduced mod N by nmask).
+// W_N^e from the two-level table (e reduced mod N by nmask): staged in shared
+// memory (hi, lo addresses) or, for very large N, read from global memory.
 struct WnTable {
   uint32_t hi, lo;
+  const float2* ghi;
+  const float2* glo;
   int shift, nmask;
+  bool global;
   __device__ __forceinline__ float2 operator()(int e) const {
     e &= nmask;
+    if (global) return cmul(__ldg(ghi + (e >> shift)), __ldg(glo + (e & ((1 << shift) - 1))));
     return cmul(lds64f(hi + (e >> shift) * 8), lds64f(lo + (e & ((1 << shift) - 1)) * 8));
   }
 };
@@ -362,7 +369,7 @@ __global__ void __launch_bounds__(384, 1)  // 12 warps at launch: 168 registers 
   // twiddle tables into shared memory (the inner loops never touch global tables)
   if constexpr (Cfg::kTwRBytes > 0)
     for (int j = tid; j < Cfg::kLmax; j += blockDim.x) s_twR[j] = p.tw2048[j * (2048 / Cfg::kLmax)];
-  if (Cfg::k1D) {
+  if (Cfg::k1D && !p.wn_global) {
     for (int j = tid; j < (1 << Cfg::kTwShift); j += blockDim.x) s_twlo[j] = p.twlo[j];
     for (int j = tid; j < Cfg::kTwHi; j += blockDim.x) s_twhi[j] = p.twhi[j];
   }
@@ -528,7 +535,10 @@ __global__ void __launch_bounds__(384, 1)  // 12 warps at launch: 168 registers 
   WnTable wn;
   wn.hi = smem_addr(s_twhi);
   wn.lo = smem_addr(s_twlo);
-  wn.shift = Cfg::kTwShift;
+  wn.ghi = p.twhi;
+  wn.glo = p.twlo;
+  wn.global = p.wn_global != 0;
+  wn.shift = wn.global ? p.tw_shift : Cfg::kTwShift;
   wn.nmask = (int)p.n_mask;
   int cnt = 0;
   for (long long idx = blockIdx.x; idx < total; idx += gridDim.x) {
@@ -569,12 +579,6 @@ __global__ void __launch_bounds__(384, 1)  // 12 warps at launch: 168 registers 
           };
           if constexpr (Cfg::k1D) {
             // W^(n2 k), k = q + R0 k' = W^(n2 q) * W^(n2 R0 k'): factors per job and thread
-            const int nmask = (int)p.n_mask;
-            const uint32_t a_hi = smem_addr(s_twhi), a_lo = smem_addr(s_twlo);
-            auto wn = [&](int e) {
-              e &= nmask;
-              return cmul(lds64f(a_hi + (e >> Cfg::kTwShift) * 8), lds64f(a_lo + (e & ((1 << Cfg::kTwShift) - 1)) * 8));
-            };
             float2 fk[JN][8], fq[JN][R0];
 #pragma unroll
             for (int jn = 0; jn < JN; ++jn) {

@@ -181,6 +181,10 @@ void free_tables(tcfftPlanImpl* p) {
   p->perm_tmp = nullptr;
   p->tables = DeviceTables();
   p->scratch = nullptr;
+  if (p->big) cudaFree(p->big);
+  p->big = nullptr;
+  for (tcfftPlanImpl* sp : p->subs) tcfftDestroy(sp);
+  p->subs.clear();
 }
 
 int ilog2_exact(int64_t v) {
@@ -206,11 +210,21 @@ void fused_lag(int T0, int T1, int64_t batch, Schedule& s) {
 
 // Host-only schedule selection for a 1D size (no CUDA calls).
 tcfftStatus choose_1d(int64_t n, int64_t batch, int precision, Schedule& s) {
-  if (!is_pow2(n) || n < 256 || n > (int64_t(1) << 27)) return TCFFT_INVALID_SIZE;
+  if (!is_pow2(n) || n < 16 || n > (int64_t(1) << 27)) return TCFFT_INVALID_SIZE;
   if (batch < 1 || batch > (int64_t(1) << 40) / n) return TCFFT_INVALID_SIZE;
   const bool split = precision == TCFFT_PRECISION_SPLIT;
   s = Schedule();
   char buf[160];
+  if (n < 256) {
+    if (!tiny_supported(n, split)) return TCFFT_NOT_SUPPORTED;
+    s.kind = Schedule::kTiny;
+    s.R = (int)(n / 16);
+    s.launches = 1;
+    snprintf(buf, sizeof buf, "tiny(N=%lld,%s): 16 transforms per warp, 1 mma stage + radix-%d", (long long)n,
+             split ? "split" : "plain", s.R);
+    s.text = buf;
+    return TCFFT_SUCCESS;
+  }
   if (n <= 2048 && !(split && n == 2048)) {
     s.kind = Schedule::kSmall;
     s.R = (int)(n / 256);
@@ -267,6 +281,33 @@ tcfftStatus choose_1d(int64_t n, int64_t batch, int precision, Schedule& s) {
     snprintf(buf, sizeof buf,
              "fused1d(%s): N=%lld x %lld, phase0 columns R=%d C=%d, phase1 rows R=%d C=%d, lag %d, %d slots",
              split ? "split" : "plain", (long long)n1, (long long)n2, k.R0, k.C0, k.R1, k.C1, s.D, s.S);
+    s.text = buf;
+    return TCFFT_SUCCESS;
+  }
+  if (lg >= 23 && lg <= 27) {
+    // N = N1 x N2, N1 = 2048 (split 1024): column FFTs of N1 with the W_N twiddle into a full-size
+    // scratch (fused kernel, phase 0 only), N1 rows of N2 by a 1D sub-plan, transpose back
+    const int64_t n1 = split ? 1024 : 2048, n2 = n / n1;
+    if (batch > (1 << 30)) return TCFFT_INVALID_SIZE;
+    FusedKey k;
+    k.role0 = kRoleCol;
+    k.R0 = (int)(n1 / 256);
+    k.C0 = 8;
+    k.role1 = kRoleRowT;
+    k.R1 = k.R0;
+    k.C1 = 8;
+    k.split = split;
+    s.kind = Schedule::kLarge1d;
+    s.N1 = n1;
+    s.N2 = n2;
+    s.key = k;
+    s.T0 = (int)(n2 / k.C0);
+    s.T1 = 0;
+    s.D = 0;
+    s.S = (int)batch;
+    s.launches = 3;  // updated with the sub-plan's count at plan time
+    snprintf(buf, sizeof buf, "large1d(%s): N=%lld x %lld, column pass R=%d C=8 -> rows of %lld (sub-plan) -> transpose",
+             split ? "split" : "plain", (long long)n1, (long long)n2, k.R0, (long long)n2);
     s.text = buf;
     return TCFFT_SUCCESS;
   }
@@ -347,6 +388,63 @@ tcfftStatus exec_plan(tcfftPlan plan, void* data, void* stream, int dir) {
                                      split ? 8 : 4, plan->num_sms, st),
                     "input reorder"))
       return TCFFT_CUDA_ERROR;
+  }
+  const int es = split ? 8 : 4;
+  if (s.kind == Schedule::kTiny)
+    return cuda_status(launch_tiny(plan->n, split, data, plan->batch, tw, dsign, plan->num_sms, st), "tiny launch");
+  if (s.kind == Schedule::kLarge1d) {
+    const FusedKey& k = s.key;
+    if (plan->tmap_ptr != data) {
+      const CUtensorMapDataType dt = split ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_UINT32;
+      if (cu_status(encode_col_load(&plan->fmaps.load0, dt, data, s.N2, plan->batch, es, k.C0, k.R0), "tmap load0") ||
+          cu_status(encode_col_store(&plan->fmaps.store0, dt, plan->big, s.N2, plan->batch, es, k.C0, k.R0),
+                    "tmap store0"))
+        return TCFFT_CUDA_ERROR;
+      plan->fmaps.load1 = plan->fmaps.load0;  // phase 1 has no work items
+      plan->fmaps.store1 = plan->fmaps.store0;
+      plan->tmap_ptr = data;
+    }
+    FusedParams fp;
+    memset(&fp, 0, sizeof fp);
+    fp.tw2048 = tw;
+    fp.scratch = static_cast<unsigned char*>(plan->big);
+    fp.twlo = plan->twlo[dir];
+    fp.twhi = plan->twhi[dir];
+    fp.tw_shift = plan->tw_shift;
+    fp.wn_global = 1;
+    fp.n_mask = (long long)(plan->n - 1);
+    fp.batch = (int)plan->batch;
+    fp.D = 0;
+    fp.S = s.S;
+    fp.T0 = s.T0;
+    fp.T1 = 0;
+    fp.rows0 = (int)s.N1;
+    fp.rows1 = (int)s.N1;
+    fp.cols0 = s.T0;
+    fp.cols1 = 1;
+    fp.cnt0 = plan->counters;
+    fp.cnt1 = plan->counters + s.S;
+    fp.err = plan->tables.err;
+    fp.dsign = dsign;
+    if (cuda_status(cudaMemsetAsync(plan->counters, 0, sizeof(int) * 2 * s.S, st), "counter reset"))
+      return TCFFT_CUDA_ERROR;
+    int grid = 0;
+    if (cuda_status(launch_fused(k, plan->fmaps, fp, plan->num_sms, st, &grid), "column pass")) return TCFFT_CUDA_ERROR;
+    tcfftStatus r = exec_plan(plan->subs[0], plan->big, stream, dir);  // rows of N2, natural order
+    if (r != TCFFT_SUCCESS) return r;
+    // [B][N1 rows k1][N2 cols k2] -> X[k1 + N1 k2] = [B][N2][N1]
+    return cuda_status(launch_transpose(plan->big, data, plan->batch, s.N1, s.N2, es, plan->num_sms, st), "transpose");
+  }
+  if (s.kind == Schedule::kGeneric2d) {
+    tcfftStatus r = exec_plan(plan->subs[0], data, stream, dir);  // rows of ny
+    if (r != TCFFT_SUCCESS) return r;
+    if (cuda_status(launch_transpose(data, plan->big, plan->batch, plan->nx, plan->ny, es, plan->num_sms, st),
+                    "transpose"))
+      return TCFFT_CUDA_ERROR;
+    r = exec_plan(plan->subs[1], plan->big, stream, dir);  // columns of nx, now rows
+    if (r != TCFFT_SUCCESS) return r;
+    return cuda_status(launch_transpose(plan->big, data, plan->batch, plan->ny, plan->nx, es, plan->num_sms, st),
+                       "transpose");
   }
   if (s.kind == Schedule::kSmall) {
     // 2D view of the whole batch: rows of 128 bytes
@@ -487,6 +585,49 @@ tcfftStatus alloc_fused(tcfftPlanImpl* p) {
   return TCFFT_SUCCESS;
 }
 
+// Large 1D: full-size intermediate, counters (one slot per transform), W_N
+// tables for N (read from global memory by the column pass) and the row plan.
+tcfftStatus setup_large1d(tcfftPlanImpl* p) {
+  const Schedule& s = p->sched;
+  const int es = p->precision == TCFFT_PRECISION_SPLIT ? 8 : 4;
+  if (cudaMalloc(&p->counters, sizeof(int) * 2 * s.S) != cudaSuccess) return TCFFT_ALLOC_FAILED;
+  tcfftStatus st = alloc_wn_tables(p, p->n);
+  if (st != TCFFT_SUCCESS) return st;
+  p->scratch_bytes = p->n * p->batch * es;
+  if (cudaMalloc(&p->big, p->scratch_bytes) != cudaSuccess) return TCFFT_ALLOC_FAILED;
+  tcfftOptions o;
+  tcfftOptionsDefault(&o);
+  o.precision = p->precision;
+  tcfftPlan rows = nullptr;
+  st = tcfftPlan1d(&rows, s.N2, s.N1 * p->batch, &o);
+  if (st != TCFFT_SUCCESS) return st;
+  p->subs.push_back(rows);
+  p->sched.launches = 2 + rows->sched.launches;
+  p->scratch_bytes += rows->scratch_bytes;
+  return TCFFT_SUCCESS;
+}
+
+// Generic 2D: row plan over ny, column plan over nx (run on the transpose), one
+// full-size intermediate.
+tcfftStatus setup_generic2d(tcfftPlanImpl* p) {
+  const int es = p->precision == TCFFT_PRECISION_SPLIT ? 8 : 4;
+  p->scratch_bytes = p->nx * p->ny * p->batch * es;
+  if (cudaMalloc(&p->big, p->scratch_bytes) != cudaSuccess) return TCFFT_ALLOC_FAILED;
+  tcfftOptions o;
+  tcfftOptionsDefault(&o);
+  o.precision = p->precision;
+  tcfftPlan rows = nullptr, cols = nullptr;
+  tcfftStatus st = tcfftPlan1d(&rows, p->ny, p->nx * p->batch, &o);
+  if (st != TCFFT_SUCCESS) return st;
+  p->subs.push_back(rows);
+  st = tcfftPlan1d(&cols, p->nx, p->ny * p->batch, &o);
+  if (st != TCFFT_SUCCESS) return st;
+  p->subs.push_back(cols);
+  p->sched.launches = rows->sched.launches + cols->sched.launches + 2;
+  p->scratch_bytes += rows->scratch_bytes + cols->scratch_bytes;
+  return TCFFT_SUCCESS;
+}
+
 }  // namespace
 
 // ------------------------------------------------------------------ C ABI
@@ -554,7 +695,8 @@ tcfftStatus tcfftPlan1d(tcfftPlan* out, int64_t n, int64_t batch, const tcfftOpt
   p->sched = s;
   p->radices_x = chain;
   st = alloc_tables(p);
-  if (st == TCFFT_SUCCESS && s.kind != Schedule::kSmall) st = alloc_fused(p);
+  if (st == TCFFT_SUCCESS && (s.kind == Schedule::kFused1d || s.kind == Schedule::kFused2d)) st = alloc_fused(p);
+  if (st == TCFFT_SUCCESS && s.kind == Schedule::kLarge1d) st = setup_large1d(p);
   if (st == TCFFT_SUCCESS && o.input_order == TCFFT_ORDER_REFERENCE_DIGIT_REVERSED) st = setup_reference_order(p);
   if (st != TCFFT_SUCCESS) {
     free_tables(p);
@@ -575,7 +717,22 @@ tcfftStatus tcfftPlan2d(tcfftPlan* out, int64_t nx, int64_t ny, int64_t batch, c
   if (opts) o = *opts;
   Schedule s;
   st = choose_2d(nx, ny, batch, o.precision, s);
-  if (st != TCFFT_SUCCESS) return st;
+  if (st != TCFFT_SUCCESS) {
+    // shapes outside the fused 2D range: compose from 1D plans (both axes must be valid 1D sizes)
+    Schedule sx, sy;
+    if (!is_pow2(nx) || !is_pow2(ny) || batch < 1 || nx * ny > (int64_t(1) << 40) / batch) return TCFFT_INVALID_SIZE;
+    tcfftStatus ex = choose_1d(nx, ny * batch, o.precision, sx), ey = choose_1d(ny, nx * batch, o.precision, sy);
+    if (ex != TCFFT_SUCCESS) return ex;
+    if (ey != TCFFT_SUCCESS) return ey;
+    s = Schedule();
+    s.kind = Schedule::kGeneric2d;
+    s.N1 = nx;
+    s.N2 = ny;
+    char buf[160];
+    snprintf(buf, sizeof buf, "generic2d(%s): rows of %lld, transpose, rows of %lld, transpose",
+             o.precision == TCFFT_PRECISION_SPLIT ? "split" : "plain", (long long)ny, (long long)nx);
+    s.text = buf;
+  }
   std::vector<int> cx = {(int)nx}, cy = {(int)ny};
   if (o.input_order == TCFFT_ORDER_REFERENCE_DIGIT_REVERSED) {
     cx = reference_radices_2d_axis(nx);
@@ -596,7 +753,7 @@ tcfftStatus tcfftPlan2d(tcfftPlan* out, int64_t nx, int64_t ny, int64_t batch, c
   p->radices_x = cx;
   p->radices_y = cy;
   st = alloc_tables(p);
-  if (st == TCFFT_SUCCESS) st = alloc_fused(p);
+  if (st == TCFFT_SUCCESS) st = s.kind == Schedule::kGeneric2d ? setup_generic2d(p) : alloc_fused(p);
   if (st == TCFFT_SUCCESS && o.input_order == TCFFT_ORDER_REFERENCE_DIGIT_REVERSED) st = setup_reference_order(p);
   if (st != TCFFT_SUCCESS) {
     free_tables(p);

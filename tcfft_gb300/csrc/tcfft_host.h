@@ -38,6 +38,14 @@ cudaError_t launch_fused(const FusedKey& k, const FusedMaps& maps, const FusedPa
 CUresult encode_fused1d_maps(FusedMaps* maps, const FusedKey& k, void* data, void* scratch, int64_t n1, int64_t n2,
                              int64_t batch, int S);
 
+// Short 1D transforms N = 16..128 (fft_tiny.cu); N = 128 is plain only.
+bool tiny_supported(int64_t n, bool split);
+cudaError_t launch_tiny(int64_t n, bool split, void* data, int64_t batch, const float2* tw, float dsign, int num_sms,
+                        cudaStream_t st);
+// Batched out-of-place transpose [B][R][C] -> [B][C][R] of es-byte elements (tcfft_transpose.cu).
+cudaError_t launch_transpose(const void* in, void* out, int64_t B, int64_t R, int64_t C, int es, int num_sms,
+                             cudaStream_t st);
+
 // Launch entry points implemented in the kernel translation units. Each
 // returns cudaSuccess or the launch error.
 cudaError_t launch_small(int R, bool split, const CUtensorMap& tmap, int64_t total_elems, const float2* tw,

@@ -191,6 +191,7 @@ extern "C" tcfftStatus tcfftExecute1dNoAlloc(void* data, int64_t n, int64_t batc
   fp.twlo = d.twlo;
   fp.twhi = d.twhi;
   fp.tw_shift = shift;
+  fp.wn_global = 0;
   fp.n_mask = (long long)(n - 1);
   fp.batch = (int)batch;
   fp.D = D;

@@ -10,7 +10,12 @@ namespace tcfft {
 
 // Execution schedule chosen at plan time (host-only, no CUDA calls).
 struct Schedule {
-  enum Kind { kNone = 0, kSmall = 1, kFused1d = 2, kFused2d = 3 } kind = kNone;
+  // kTiny: N = 16..128, one launch (fft_tiny.cu).
+  // kLarge1d: N = N1 N2 with N2 > 2048: column pass (fused kernel, phase 0 only) into a
+  //   full-size scratch, row FFTs of length N2 by a sub-plan, transpose back.
+  // kGeneric2d: axes outside the fused 2D range: row FFTs (sub-plan), transpose, row FFTs of
+  //   the other axis (sub-plan), transpose back.
+  enum Kind { kNone = 0, kSmall = 1, kFused1d = 2, kFused2d = 3, kTiny = 4, kLarge1d = 5, kGeneric2d = 6 } kind = kNone;
   int R = 1;             // small: N = 256 R
   int64_t N1 = 0, N2 = 0;  // fused 1D: N = N1 N2 (phase 0 columns of N1, phase 1 rows of N2)
   FusedKey key;          // fused: kernel instantiation
@@ -38,6 +43,9 @@ struct tcfftPlanImpl {
   int* counters = nullptr;  // [2 * S]
   void* scratch = nullptr;
   int64_t scratch_bytes = 0;
+  // composite schedules (kLarge1d, kGeneric2d): full-size intermediate and sub-plans
+  void* big = nullptr;
+  std::vector<tcfftPlanImpl*> subs;
   // reference input order (TCFFT_ORDER_REFERENCE_DIGIT_REVERSED)
   std::vector<int> radices_x, radices_y;  // reported chains (x = the 1D chain)
   int* rev_x = nullptr;                   // device digit-reversal tables (nullptr: natural)

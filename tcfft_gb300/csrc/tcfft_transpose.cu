@@ -1,0 +1,57 @@
+// tcfft_transpose.cu -- batched out-of-place transpose [B][R][C] -> [B][C][R].
+//
+// Used where a transform is composed from smaller plans: the last step of the
+// large 1D sizes (N = N1 N2 with N2 > 2048 is computed as row FFTs of a
+// [N1][N2] array whose result X[k1 + N1 k2] is its transpose) and the column
+// pass of 2D shapes outside the fused 2D range.  32 x 32 tiles through shared
+// memory: 128-byte coalesced rows on both sides for 4-byte elements.
+#include "tcfft_host.h"
+
+namespace tcfft {
+namespace {
+
+template <typename E>
+__global__ void __launch_bounds__(256) transpose_kernel(const E* __restrict__ in, E* __restrict__ out, long long B,
+                                                        long long R, long long C) {
+  __shared__ E tile[32][33];
+  const long long tr = (R + 31) / 32, tc = (C + 31) / 32, per = tr * tc, total = B * per;
+  for (long long t = blockIdx.x; t < total; t += gridDim.x) {
+    const long long b = t / per, rem = t - b * per;
+    const long long r0 = (rem / tc) * 32, c0 = (rem % tc) * 32;
+    const E* ib = in + b * R * C;
+    E* ob = out + b * R * C;
+#pragma unroll
+    for (int i = threadIdx.y; i < 32; i += 8) {
+      const long long r = r0 + i, c = c0 + threadIdx.x;
+      if (r < R && c < C) tile[i][threadIdx.x] = ib[r * C + c];
+    }
+    __syncthreads();
+#pragma unroll
+    for (int i = threadIdx.y; i < 32; i += 8) {
+      const long long c = c0 + i, r = r0 + threadIdx.x;
+      if (r < R && c < C) ob[c * R + r] = tile[threadIdx.x][i];
+    }
+    __syncthreads();
+  }
+}
+
+}  // namespace
+
+cudaError_t launch_transpose(const void* in, void* out, int64_t B, int64_t R, int64_t C, int es, int num_sms,
+                             cudaStream_t st) {
+  const long long tiles = B * ((R + 31) / 32) * ((C + 31) / 32);
+  long long blocks = tiles < (long long)num_sms * 16 ? tiles : (long long)num_sms * 16;
+  if (blocks < 1) blocks = 1;
+  const dim3 block(32, 8);
+  if (es == 4)
+    transpose_kernel<uint32_t><<<(unsigned)blocks, block, 0, st>>>(static_cast<const uint32_t*>(in),
+                                                                   static_cast<uint32_t*>(out), B, R, C);
+  else if (es == 8)
+    transpose_kernel<uint2><<<(unsigned)blocks, block, 0, st>>>(static_cast<const uint2*>(in),
+                                                                static_cast<uint2*>(out), B, R, C);
+  else
+    return cudaErrorInvalidValue;
+  return cudaGetLastError();
+}
+
+}  // namespace tcfft
