@@ -58,7 +58,7 @@ def test_describe_fused(n):
     assert "fused1d" in tc.describe_1d(n, 4)
 
 
-@pytest.mark.parametrize("n,batch", [(100, 1), (128, 1), (0, 1), (256, 0), (1 << 28, 1)])
+@pytest.mark.parametrize("n,batch", [(100, 1), (8, 1), (0, 1), (256, 0), (1 << 28, 1)])
 def test_describe_rejects_bad_sizes(n, batch):
     with pytest.raises(tc.TcfftError) as e:
         tc.describe_1d(n, batch)
