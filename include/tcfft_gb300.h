@@ -80,10 +80,15 @@ typedef struct tcfftPlanImpl* tcfftPlan;
 /* Fill `opts` with defaults (plain, natural order, no autotune). */
 tcfftStatus tcfftOptionsDefault(tcfftOptions* opts);
 
-/* 1D batched plan: `batch` transforms of length n (power of two, 256 <= n <= 2^27). */
+/* 1D batched plan: `batch` transforms of length n (power of two, 16 <= n <= 2^27;
+ * the split precision stops at n = 64 below 256). The reference plans ten sizes
+ * (tcfft_half.cu:1250-1330: 2^8..2^10, 2^17..2^19, 2^24..2^27); all of them are
+ * included. */
 tcfftStatus tcfftPlan1d(tcfftPlan* plan, int64_t n, int64_t batch, const tcfftOptions* opts);
 
-/* 2D batched plan: `batch` transforms of nx x ny (powers of two, 128 <= nx, ny). */
+/* 2D batched plan: `batch` transforms of nx x ny (powers of two, each a valid
+ * 1D size). Axes 256..2048 run fused (one HBM round trip); other shapes are
+ * composed from 1D plans and transposes. */
 tcfftStatus tcfftPlan2d(tcfftPlan* plan, int64_t nx, int64_t ny, int64_t batch, const tcfftOptions* opts);
 
 /* Uneven batch in one launch: `count` independent transforms, transform i has
