@@ -16,6 +16,12 @@
 #include <vector>
 
 #include "tcfft_host.h"
+#include <algorithm>
+#include <map>
+#include <mutex>
+#include <set>
+#include <tuple>
+
 #include "tcfft_plan.h"
 
 namespace tcfft {
@@ -185,6 +191,14 @@ void free_tables(tcfftPlanImpl* p) {
   p->big = nullptr;
   for (tcfftPlanImpl* sp : p->subs) tcfftDestroy(sp);
   p->subs.clear();
+  p->runs.clear();
+  for (int d = 0; d < 2; ++d) {
+    if (p->graph_exec[d]) cudaGraphExecDestroy(p->graph_exec[d]);
+    p->graph_exec[d] = nullptr;
+    p->graph_ptr[d] = nullptr;
+  }
+  if (p->cap_stream) cudaStreamDestroy(p->cap_stream);
+  p->cap_stream = nullptr;
 }
 
 int ilog2_exact(int64_t v) {
@@ -198,8 +212,12 @@ int ilog2_exact(int64_t v) {
 // Tiles in flight span about (CTAs x stages) items; a transform's phase 1 is
 // placed D blocks after its phase 0, and a slot is reused S blocks later, so
 // both D and S - D must exceed the blocks in flight.
+// Lag multiplier chosen by the autotuner while it times candidates (0: none).
+thread_local double g_lag_override = 0.0;
+
 void fused_lag(int T0, int T1, int64_t batch, Schedule& s) {
-  static const double scale = getenv("TCFFT_LAG_SCALE") ? atof(getenv("TCFFT_LAG_SCALE")) : 1.0;
+  static const double env_scale = getenv("TCFFT_LAG_SCALE") ? atof(getenv("TCFFT_LAG_SCALE")) : 1.0;
+  const double scale = g_lag_override > 0.0 ? g_lag_override : env_scale;
   const int in_flight = (int)(152 * 4 * scale);  // CTAs x tiles per CTA
   int D = (in_flight + (T0 + T1) - 1) / (T0 + T1) + 1;
   if (D > batch) D = (int)batch;
@@ -373,11 +391,14 @@ tcfftStatus validate_opts(const tcfftOptions* o) {
   return TCFFT_SUCCESS;
 }
 
+tcfftStatus exec_many(tcfftPlanImpl* plan, void* data, cudaStream_t st, int dir);
+
 tcfftStatus exec_plan(tcfftPlan plan, void* data, void* stream, int dir) {
   if (!plan || plan->magic != tcfftPlanImpl::kMagic) return TCFFT_INVALID_PLAN;
   if (!data) return TCFFT_INVALID_VALUE;
   if ((reinterpret_cast<uintptr_t>(data) & 127) != 0) return TCFFT_MISALIGNED;
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  if (plan->kind == 3) return exec_many(plan, data, st, dir);
   const bool split = plan->precision == TCFFT_PRECISION_SPLIT;
   const float2* tw = plan->tables.tw2048[dir];
   const float dsign = dir == 0 ? 1.f : -1.f;
@@ -572,17 +593,30 @@ tcfftStatus alloc_wn_tables(tcfftPlanImpl* p, int64_t n) {
   return TCFFT_SUCCESS;
 }
 
-tcfftStatus alloc_fused(tcfftPlanImpl* p) {
+// Counters and (1D) scratch ring for the current schedule's slot count.
+tcfftStatus alloc_ring(tcfftPlanImpl* p) {
   const Schedule& s = p->sched;
   const int es = p->precision == TCFFT_PRECISION_SPLIT ? 8 : 4;
+  if (p->counters) cudaFree(p->counters);
+  if (p->scratch) cudaFree(p->scratch);
+  p->counters = nullptr;
+  p->scratch = nullptr;
+  p->scratch_bytes = 0;
+  p->tmap_ptr = nullptr;  // the maps name the scratch
   if (cudaMalloc(&p->counters, sizeof(int) * 2 * s.S) != cudaSuccess) return TCFFT_ALLOC_FAILED;
   if (s.kind == Schedule::kFused1d) {
-    tcfftStatus st = alloc_wn_tables(p, p->n);
-    if (st != TCFFT_SUCCESS) return st;
     p->scratch_bytes = (int64_t)s.S * p->n * es;
     if (cudaMalloc(&p->scratch, p->scratch_bytes) != cudaSuccess) return TCFFT_ALLOC_FAILED;
   }
   return TCFFT_SUCCESS;
+}
+
+tcfftStatus alloc_fused(tcfftPlanImpl* p) {
+  if (p->sched.kind == Schedule::kFused1d) {
+    tcfftStatus st = alloc_wn_tables(p, p->n);
+    if (st != TCFFT_SUCCESS) return st;
+  }
+  return alloc_ring(p);
 }
 
 // Large 1D: full-size intermediate, counters (one slot per transform), W_N
@@ -626,6 +660,153 @@ tcfftStatus setup_generic2d(tcfftPlanImpl* p) {
   p->sched.launches = rows->sched.launches + cols->sched.launches + 2;
   p->scratch_bytes += rows->scratch_bytes + cols->scratch_bytes;
   return TCFFT_SUCCESS;
+}
+
+// ------------------------------------------------------------------ autotuner
+// For the fused executor the free parameter with the largest measured effect
+// is the lag (how many transforms are between their first and second phase,
+// which sets the L2 footprint of the intermediate and the slack of the
+// cross-CTA dependency).  At plan time, with tcfftOptions.autotune = 1, the
+// plan times a few lag multipliers on a scratch buffer of its own size and
+// keeps the fastest; results are cached per (shape, batch, precision) in the
+// process and, if tune_cache_path is set, in that text file ("key scale" lines).
+std::mutex g_tune_mu;
+std::map<std::string, double> g_tune_cache;
+std::set<std::string> g_tune_files_read;
+
+void load_tune_file(const char* path) {
+  if (!path || g_tune_files_read.count(path)) return;
+  g_tune_files_read.insert(path);
+  FILE* f = fopen(path, "r");
+  if (!f) return;
+  char line[256];
+  while (fgets(line, sizeof line, f)) {
+    char key[200];
+    double v = 0;
+    if (sscanf(line, "%199[^|]|%lf", key, &v) == 2 && v > 0) g_tune_cache[key] = v;
+  }
+  fclose(f);
+}
+
+tcfftStatus choose_again(tcfftPlanImpl* p, double scale, Schedule& s) {
+  g_lag_override = scale;
+  tcfftStatus st = p->kind == 1 ? choose_1d(p->n, p->batch, p->precision, s)
+                                : choose_2d(p->nx, p->ny, p->batch, p->precision, s);
+  g_lag_override = 0.0;
+  return st;
+}
+
+tcfftStatus apply_lag(tcfftPlanImpl* p, double scale) {
+  Schedule s;
+  tcfftStatus st = choose_again(p, scale, s);
+  if (st != TCFFT_SUCCESS) return st;
+  p->sched = s;
+  p->lag_scale = scale;
+  return alloc_ring(p);
+}
+
+tcfftStatus autotune_plan(tcfftPlanImpl* p, const tcfftOptions& o) {
+  if (p->sched.kind != Schedule::kFused1d && p->sched.kind != Schedule::kFused2d) return TCFFT_SUCCESS;
+  char kb[200];
+  snprintf(kb, sizeof kb, "%d %lld %lld %lld %d", p->kind, (long long)p->nx, (long long)p->ny, (long long)p->batch,
+           p->precision);
+  const std::string key = kb;
+  std::lock_guard<std::mutex> lock(g_tune_mu);
+  load_tune_file(o.tune_cache_path);
+  double best = 1.0;
+  auto it = g_tune_cache.find(key);
+  if (it != g_tune_cache.end()) {
+    best = it->second;
+  } else {
+    const int es = p->precision == TCFFT_PRECISION_SPLIT ? 8 : 4;
+    void* tmp = nullptr;
+    if (cudaMalloc(&tmp, p->total_elems * es) != cudaSuccess) {
+      cudaGetLastError();
+      return TCFFT_SUCCESS;  // not enough memory to time: keep the built-in lag
+    }
+    cudaMemset(tmp, 0, p->total_elems * es);
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    float best_ms = 1e30f;
+    std::set<int> seen_d;
+    for (double c : {1.0, 0.6, 1.6, 2.5}) {
+      Schedule s;
+      if (choose_again(p, c, s) != TCFFT_SUCCESS || seen_d.count(s.D)) continue;
+      seen_d.insert(s.D);
+      if (apply_lag(p, c) != TCFFT_SUCCESS) break;
+      if (exec_plan(p, tmp, nullptr, 0) != TCFFT_SUCCESS) break;
+      cudaEventRecord(e0, nullptr);
+      for (int r = 0; r < 3; ++r) exec_plan(p, tmp, nullptr, 0);
+      cudaEventRecord(e1, nullptr);
+      if (cudaEventSynchronize(e1) != cudaSuccess) break;
+      float ms = 0;
+      cudaEventElapsedTime(&ms, e0, e1);
+      if (ms < best_ms) {
+        best_ms = ms;
+        best = c;
+      }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(tmp);
+    g_tune_cache[key] = best;
+    if (o.tune_cache_path) {
+      FILE* f = fopen(o.tune_cache_path, "a");
+      if (f) {
+        fprintf(f, "%s|%.3f\n", key.c_str(), best);
+        fclose(f);
+      }
+    }
+  }
+  tcfftStatus st = apply_lag(p, best);
+  if (st != TCFFT_SUCCESS) return st;
+  char buf[48];
+  snprintf(buf, sizeof buf, " [tuned: lag x%.2g]", best);
+  p->sched.text += buf;
+  return TCFFT_SUCCESS;
+}
+
+tcfftStatus check_errors(tcfftPlanImpl* p) {
+  int e = 0;
+  if (cudaMemcpy(&e, p->tables.err, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return TCFFT_CUDA_ERROR;
+  tcfftStatus r = TCFFT_SUCCESS;
+  if (e != 0) {
+    cudaMemset(p->tables.err, 0, sizeof(int));
+    r = TCFFT_TIMEOUT;
+  }
+  for (tcfftPlanImpl* sp : p->subs) {
+    tcfftStatus rs = check_errors(sp);
+    if (r == TCFFT_SUCCESS) r = rs;
+  }
+  return r;
+}
+
+tcfftStatus exec_many(tcfftPlanImpl* plan, void* data, cudaStream_t st, int dir) {
+  const int es = plan->precision == TCFFT_PRECISION_SPLIT ? 8 : 4;
+  if (!plan->graph_exec[dir] || plan->graph_ptr[dir] != data) {
+    if (plan->graph_exec[dir]) cudaGraphExecDestroy(plan->graph_exec[dir]);
+    plan->graph_exec[dir] = nullptr;
+    plan->graph_ptr[dir] = nullptr;
+    if (cuda_status(cudaStreamBeginCapture(plan->cap_stream, cudaStreamCaptureModeThreadLocal), "graph capture"))
+      return TCFFT_CUDA_ERROR;
+    tcfftStatus r = TCFFT_SUCCESS;
+    for (const auto& run : plan->runs) {
+      r = exec_plan(run.sub, static_cast<unsigned char*>(data) + run.offset * es, plan->cap_stream, dir);
+      if (r != TCFFT_SUCCESS) break;
+    }
+    cudaGraph_t g = nullptr;
+    cudaError_t ce = cudaStreamEndCapture(plan->cap_stream, &g);
+    if (r != TCFFT_SUCCESS || ce != cudaSuccess) {
+      if (g) cudaGraphDestroy(g);
+      return r != TCFFT_SUCCESS ? r : cuda_status(ce, "graph capture");
+    }
+    ce = cudaGraphInstantiate(&plan->graph_exec[dir], g, 0);
+    cudaGraphDestroy(g);
+    if (cuda_status(ce, "graph instantiate")) return TCFFT_CUDA_ERROR;
+    plan->graph_ptr[dir] = data;
+  }
+  return cuda_status(cudaGraphLaunch(plan->graph_exec[dir], st), "graph launch");
 }
 
 }  // namespace
@@ -697,6 +878,7 @@ tcfftStatus tcfftPlan1d(tcfftPlan* out, int64_t n, int64_t batch, const tcfftOpt
   st = alloc_tables(p);
   if (st == TCFFT_SUCCESS && (s.kind == Schedule::kFused1d || s.kind == Schedule::kFused2d)) st = alloc_fused(p);
   if (st == TCFFT_SUCCESS && s.kind == Schedule::kLarge1d) st = setup_large1d(p);
+  if (st == TCFFT_SUCCESS && o.autotune) st = autotune_plan(p, o);
   if (st == TCFFT_SUCCESS && o.input_order == TCFFT_ORDER_REFERENCE_DIGIT_REVERSED) st = setup_reference_order(p);
   if (st != TCFFT_SUCCESS) {
     free_tables(p);
@@ -754,6 +936,7 @@ tcfftStatus tcfftPlan2d(tcfftPlan* out, int64_t nx, int64_t ny, int64_t batch, c
   p->radices_y = cy;
   st = alloc_tables(p);
   if (st == TCFFT_SUCCESS) st = s.kind == Schedule::kGeneric2d ? setup_generic2d(p) : alloc_fused(p);
+  if (st == TCFFT_SUCCESS && o.autotune) st = autotune_plan(p, o);
   if (st == TCFFT_SUCCESS && o.input_order == TCFFT_ORDER_REFERENCE_DIGIT_REVERSED) st = setup_reference_order(p);
   if (st != TCFFT_SUCCESS) {
     free_tables(p);
@@ -768,13 +951,80 @@ tcfftStatus tcfftPlanMany(tcfftPlan* out, int64_t count, const int32_t* ranks, c
                           const int64_t* offsets, const tcfftOptions* opts) {
   if (!out) return TCFFT_INVALID_VALUE;
   *out = nullptr;
-  (void)count;
-  (void)ranks;
-  (void)nx;
-  (void)ny;
-  (void)offsets;
-  (void)opts;
-  return TCFFT_NOT_SUPPORTED;
+  if (count < 1 || !ranks || !nx || !offsets) return TCFFT_INVALID_VALUE;
+  tcfftStatus st = validate_opts(opts);
+  if (st != TCFFT_SUCCESS) return st;
+  tcfftOptions o;
+  tcfftOptionsDefault(&o);
+  if (opts) o = *opts;
+  if (o.input_order != TCFFT_ORDER_NATURAL) return TCFFT_INVALID_VALUE;
+  const int es = o.precision == TCFFT_PRECISION_SPLIT ? 8 : 4;
+  std::vector<int64_t> size(count);
+  for (int64_t i = 0; i < count; ++i) {
+    if (ranks[i] != 1 && ranks[i] != 2) return TCFFT_INVALID_VALUE;
+    if (ranks[i] == 2 && !ny) return TCFFT_INVALID_VALUE;
+    const int64_t y = ranks[i] == 2 ? ny[i] : 1;
+    if (!is_pow2(nx[i]) || !is_pow2(y)) return TCFFT_INVALID_SIZE;
+    size[i] = nx[i] * y;
+    if (offsets[i] < 0 || (offsets[i] * es) % 128 != 0) return TCFFT_MISALIGNED;
+  }
+  std::vector<int64_t> order(count);
+  for (int64_t i = 0; i < count; ++i) order[i] = i;
+  std::sort(order.begin(), order.end(), [&](int64_t a, int64_t b) { return offsets[a] < offsets[b]; });
+  for (int64_t k = 1; k < count; ++k)
+    if (offsets[order[k]] < offsets[order[k - 1]] + size[order[k - 1]]) return TCFFT_INVALID_VALUE;  // overlap
+  tcfftPlanImpl* p = new (std::nothrow) tcfftPlanImpl();
+  if (!p) return TCFFT_ALLOC_FAILED;
+  p->kind = 3;
+  p->precision = o.precision;
+  p->batch = count;
+  st = alloc_tables(p);
+  tcfftOptions os = o;
+  std::map<std::tuple<int, int64_t, int64_t, int64_t>, tcfftPlanImpl*> by_key;
+  int launches = 0, nsub = 0;
+  for (int64_t k = 0; k < count && st == TCFFT_SUCCESS;) {
+    // a run: same shape, each transform right after the previous one
+    const int64_t i0 = order[k];
+    const int r = ranks[i0];
+    const int64_t x = nx[i0], y = r == 2 ? ny[i0] : 1;
+    int64_t len = 1;
+    while (k + len < count) {
+      const int64_t j = order[k + len], prev = order[k + len - 1];
+      if (ranks[j] != r || nx[j] != x || (r == 2 ? ny[j] : 1) != y || offsets[j] != offsets[prev] + size[prev]) break;
+      ++len;
+    }
+    const auto key = std::make_tuple(r, x, y, len);
+    tcfftPlanImpl* sub = nullptr;
+    auto it = by_key.find(key);
+    if (it != by_key.end()) {
+      sub = it->second;
+    } else {
+      st = r == 1 ? tcfftPlan1d(&sub, x, len, &os) : tcfftPlan2d(&sub, x, y, len, &os);
+      if (st != TCFFT_SUCCESS) break;
+      p->subs.push_back(sub);
+      by_key[key] = sub;
+      ++nsub;
+    }
+    p->runs.push_back({sub, offsets[i0]});
+    launches += sub->sched.launches;
+    p->total_elems += size[i0] * len;
+    k += len;
+  }
+  if (st == TCFFT_SUCCESS && cudaStreamCreateWithFlags(&p->cap_stream, cudaStreamNonBlocking) != cudaSuccess)
+    st = TCFFT_CUDA_ERROR;
+  if (st != TCFFT_SUCCESS) {
+    free_tables(p);
+    delete p;
+    return st;
+  }
+  p->sched.launches = launches;
+  char buf[160];
+  snprintf(buf, sizeof buf, "many(%s): %lld transforms in %d runs, %d sub-plans, %d launches per graph replay",
+           o.precision == TCFFT_PRECISION_SPLIT ? "split" : "plain", (long long)count, (int)p->runs.size(), nsub,
+           launches);
+  p->sched.text = buf;
+  *out = p;
+  return TCFFT_SUCCESS;
 }
 
 tcfftStatus tcfftExecute(tcfftPlan plan, void* data, void* stream) { return exec_plan(plan, data, stream, 0); }
@@ -787,13 +1037,7 @@ tcfftStatus tcfftCheckDevice(tcfftPlan plan, void* stream) {
   if (!plan || plan->magic != tcfftPlanImpl::kMagic) return TCFFT_INVALID_PLAN;
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
   if (cudaStreamSynchronize(st) != cudaSuccess) return TCFFT_CUDA_ERROR;
-  int e = 0;
-  if (cudaMemcpy(&e, plan->tables.err, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return TCFFT_CUDA_ERROR;
-  if (e != 0) {
-    cudaMemset(plan->tables.err, 0, sizeof(int));
-    return TCFFT_TIMEOUT;
-  }
-  return TCFFT_SUCCESS;
+  return check_errors(plan);
 }
 
 tcfftStatus tcfftDestroy(tcfftPlan plan) {

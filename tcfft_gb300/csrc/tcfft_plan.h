@@ -46,6 +46,20 @@ struct tcfftPlanImpl {
   // composite schedules (kLarge1d, kGeneric2d): full-size intermediate and sub-plans
   void* big = nullptr;
   std::vector<tcfftPlanImpl*> subs;
+  // tcfftPlanMany: runs of same-shape, back-to-back transforms, each executed by a
+  // sub-plan shared by every run of that shape and length (owned in `subs`); the
+  // sequence is captured once per (data pointer, direction) into a CUDA graph on a
+  // private stream and replayed with one graph launch.
+  struct Run {
+    tcfftPlanImpl* sub;
+    int64_t offset;  // elements
+  };
+  std::vector<Run> runs;
+  cudaStream_t cap_stream = nullptr;
+  void* graph_ptr[2] = {nullptr, nullptr};
+  cudaGraphExec_t graph_exec[2] = {nullptr, nullptr};
+  // autotuner: chosen lag multiplier of the fused executor (1 = built-in)
+  double lag_scale = 1.0;
   // reference input order (TCFFT_ORDER_REFERENCE_DIGIT_REVERSED)
   std::vector<int> radices_x, radices_y;  // reported chains (x = the 1D chain)
   int* rev_x = nullptr;                   // device digit-reversal tables (nullptr: natural)

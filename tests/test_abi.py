@@ -77,3 +77,23 @@ def test_null_arguments():
     assert lib.tcfftExecute(None, None, None) == 8
     assert lib.tcfftDestroy(None) == 8
     assert lib.tcfftOptionsDefault(None) == 1
+
+
+def test_plan_many_rejects_bad_layouts():
+    """Argument checks of tcfftPlanMany happen before any device work."""
+    import ctypes
+    lib = tc.lib()
+
+    def call(shapes, offsets):
+        n = len(shapes)
+        ranks = (ctypes.c_int32 * max(n, 1))(*[len(s) for s in shapes])
+        nx = (ctypes.c_int64 * max(n, 1))(*[s[0] for s in shapes])
+        ny = (ctypes.c_int64 * max(n, 1))(*[s[1] if len(s) > 1 else 1 for s in shapes])
+        off = (ctypes.c_int64 * max(n, 1))(*offsets)
+        h = ctypes.c_void_p(None)
+        return lib.tcfftPlanMany(ctypes.byref(h), n, ranks, nx, ny, off, None)
+
+    assert call([], []) == 1                              # TCFFT_INVALID_VALUE: empty
+    assert call([(256,)], [3]) == 3                       # TCFFT_MISALIGNED: 12-byte offset
+    assert call([(256,), (256,)], [0, 128]) == 1          # overlapping transforms
+    assert call([(100,)], [0]) == 2                       # TCFFT_INVALID_SIZE

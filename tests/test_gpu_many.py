@@ -1,0 +1,122 @@
+"""GPU: uneven batches in one plan (tcfftPlanMany) -- the mixed 1D/2D
+workload of 512 1D transforms of 2^8..2^16 points and 64 2D transforms of
+128..1024 per axis (seed 2), packed back to back in one device buffer, run
+through a CUDA graph replayed on every execute -- and the plan-time
+autotuner.  No reference counterpart (the reference plans one size per
+handle)."""
+import numpy as np
+import pytest
+import torch
+
+import oracle
+import tcfft_gb300 as tc
+from fftcheck import TOL_PLAIN, TOL_SPLIT, quantize, to_complex
+
+pytestmark = pytest.mark.gpu
+
+
+def mixed_shapes(seed=2):
+    rng = np.random.default_rng(seed)
+    shapes = [(1 << int(e),) for e in rng.integers(8, 17, size=512)]
+    shapes += [(1 << int(a), 1 << int(b)) for a, b in rng.integers(7, 11, size=(64, 2))]
+    order = rng.permutation(len(shapes))
+    return [shapes[i] for i in order]
+
+
+def pack(shapes, seed, precision):
+    rng = np.random.default_rng(seed)
+    parts = [quantize(rng.uniform(-1, 1, tuple(s) + (2,)), precision) for s in shapes]
+    flat = np.concatenate([p.reshape(-1, 2) for p in parts])
+    return parts, flat
+
+
+def unpack(flat, shapes):
+    out, off = [], 0
+    for s in shapes:
+        n = int(np.prod(s))
+        out.append(flat[off:off + n].reshape(tuple(s) + (2,)))
+        off += n
+    return out
+
+
+def check(parts, ys, tol, adjoint=False):
+    sign = +1 if adjoint else -1
+    worst = 0.0
+    for x, y in zip(parts, ys):
+        ref = oracle.fft_1d(to_complex(x), sign) if x.ndim == 2 else oracle.fft_2d(to_complex(x), sign)
+        worst = max(worst, oracle.rel_l2(to_complex(y), ref))
+    assert worst < tol, worst
+    return worst
+
+
+@pytest.mark.parametrize("precision", ["plain", "split"])
+def test_mixed_batch(cuda_device, precision):
+    shapes = mixed_shapes()
+    if precision == "split":  # the split mode stops at 64 points below 256: keep axes >= 256
+        shapes = [s for s in shapes if all(v >= 256 for v in s)]
+    parts, flat = pack(shapes, 5, precision)
+    dt = torch.float16 if precision == "plain" else torch.float32
+    tol = TOL_PLAIN if precision == "plain" else TOL_SPLIT
+    p = tc.Plan.many(shapes, precision=precision)
+    try:
+        assert "many" in p.info["schedule"]
+        base = torch.from_numpy(flat).to(dt).cuda()
+        for _ in range(2):  # first call captures the graph, the second replays it
+            buf = base.clone()
+            p.exec(buf)
+            p.check_device()
+            check(parts, unpack(buf.double().cpu().numpy(), shapes), tol)
+        buf = base.clone()
+        p.exec(buf, adjoint=True)
+        p.check_device()
+        check(parts, unpack(buf.double().cpu().numpy(), shapes), tol, adjoint=True)
+        other = torch.zeros(flat.shape[0] + 64, 2, dtype=dt, device="cuda")[64:]  # another pointer
+        other.copy_(base)
+        p.exec(other)
+        p.check_device()
+        check(parts, unpack(other.double().cpu().numpy(), shapes), tol)
+    finally:
+        p.destroy()
+
+
+def test_contiguous_runs_share_one_launch(cuda_device):
+    shapes = [(256,)] * 10 + [(1024,)] * 5 + [(64, 128)] * 3
+    parts, flat = pack(shapes, 9, "plain")
+    with tc.Plan.many(shapes) as p:
+        assert "in 3 runs" in p.info["schedule"], p.info["schedule"]
+        buf = torch.from_numpy(flat).half().cuda()
+        p.exec(buf)
+        p.check_device()
+    check(parts, unpack(buf.double().cpu().numpy(), shapes), TOL_PLAIN)
+
+
+def test_gapped_offsets(cuda_device):
+    shapes = [(512,), (512,), (2048,)]
+    offsets = [0, 1024, 4096]  # a gap between every transform: three runs
+    parts, _ = pack(shapes, 4, "plain")
+    buf = torch.full((8192, 2), 7.0, dtype=torch.float16, device="cuda")
+    for x, o in zip(parts, offsets):
+        buf[o:o + x.shape[0]] = torch.from_numpy(x).half()
+    with tc.Plan.many(shapes, offsets=offsets) as p:
+        p.exec(buf)
+        p.check_device()
+    got = buf.double().cpu().numpy()
+    ys = [got[o:o + x.shape[0]] for x, o in zip(parts, offsets)]
+    check(parts, ys, TOL_PLAIN)
+    assert (got[512:1024] == 7.0).all() and (got[2048:4096] == 7.0).all()  # gaps untouched
+
+
+def test_autotune(cuda_device, tmp_path):
+    cache = str(tmp_path / "tune.txt")
+    n, batch = 1 << 16, 64
+    rng = np.random.default_rng(3)
+    xq = quantize(rng.uniform(-1, 1, (batch, n, 2)), "plain")
+    with tc.Plan(n=n, batch=batch, autotune=True, tune_cache_path=cache) as p:
+        assert "tuned" in p.info["schedule"]
+        t = torch.from_numpy(xq).half().cuda()
+        p.exec(t)
+        p.check_device()
+    err = oracle.rel_l2(to_complex(t.double().cpu().numpy()), oracle.fft_1d(to_complex(xq)))
+    assert err < TOL_PLAIN
+    with open(cache) as f:
+        assert "|" in f.read()
