@@ -252,6 +252,16 @@ tcfftStatus choose_1d(int64_t n, int64_t batch, int precision, Schedule& s) {
     return TCFFT_SUCCESS;
   }
   const int lg = ilog2_exact(n);
+  if (n == 2048 && split) {
+    // the single-pass kernel's split mode stops at 1024: 2048 = 32 x 64 from two tiny sub-plans
+    s.kind = Schedule::kFourStep;
+    s.N1 = 32;
+    s.N2 = 64;
+    s.launches = 5;
+    snprintf(buf, sizeof buf, "fourstep(split): N=32 x 64, tiny sub-plans, 3 transposes (one with the twiddle)");
+    s.text = buf;
+    return TCFFT_SUCCESS;
+  }
   if (lg >= 12 && lg <= 15) {
     // N = 256 x N2 with short rows N2 = 16 R1: phase 0 columns of 256, phase 1 16 rows per warp
     FusedKey k;
@@ -456,6 +466,24 @@ tcfftStatus exec_plan(tcfftPlan plan, void* data, void* stream, int dir) {
     // [B][N1 rows k1][N2 cols k2] -> X[k1 + N1 k2] = [B][N2][N1]
     return cuda_status(launch_transpose(plan->big, data, plan->batch, s.N1, s.N2, es, plan->num_sms, st), "transpose");
   }
+  if (s.kind == Schedule::kFourStep) {
+    // x[n1 N2 + n2]: [B][N1][N2] -> [B][N2][N1]; rows of N1 -> Y[n2][k1]; times W_N^(n2 k1)
+    // and transposed -> [B][N1][N2]; rows of N2 -> Z[k1][k2]; X[k1 + N1 k2] = [B][N2][N1]
+    if (cuda_status(launch_transpose(data, plan->big, plan->batch, s.N1, s.N2, es, plan->num_sms, st), "transpose"))
+      return TCFFT_CUDA_ERROR;
+    tcfftStatus r = exec_plan(plan->subs[0], plan->big, stream, dir);
+    if (r != TCFFT_SUCCESS) return r;
+    if (cuda_status(launch_transpose_twiddle(plan->big, data, plan->batch, s.N2, s.N1, plan->n, dsign, split,
+                                             plan->num_sms, st),
+                    "transpose-twiddle"))
+      return TCFFT_CUDA_ERROR;
+    r = exec_plan(plan->subs[1], data, stream, dir);
+    if (r != TCFFT_SUCCESS) return r;
+    if (cuda_status(launch_transpose(data, plan->big, plan->batch, s.N1, s.N2, es, plan->num_sms, st), "transpose"))
+      return TCFFT_CUDA_ERROR;
+    return cuda_status(cudaMemcpyAsync(data, plan->big, plan->total_elems * es, cudaMemcpyDeviceToDevice, st),
+                       "copy back");
+  }
   if (s.kind == Schedule::kGeneric2d) {
     tcfftStatus r = exec_plan(plan->subs[0], data, stream, dir);  // rows of ny
     if (r != TCFFT_SUCCESS) return r;
@@ -638,6 +666,27 @@ tcfftStatus setup_large1d(tcfftPlanImpl* p) {
   p->subs.push_back(rows);
   p->sched.launches = 2 + rows->sched.launches;
   p->scratch_bytes += rows->scratch_bytes;
+  return TCFFT_SUCCESS;
+}
+
+// Four-step from two short sub-plans (rows of N1, rows of N2), one full-size
+// intermediate.
+tcfftStatus setup_fourstep(tcfftPlanImpl* p) {
+  const Schedule& s = p->sched;
+  const int es = p->precision == TCFFT_PRECISION_SPLIT ? 8 : 4;
+  p->scratch_bytes = p->n * p->batch * es;
+  if (cudaMalloc(&p->big, p->scratch_bytes) != cudaSuccess) return TCFFT_ALLOC_FAILED;
+  tcfftOptions o;
+  tcfftOptionsDefault(&o);
+  o.precision = p->precision;
+  tcfftPlan a = nullptr, b = nullptr;
+  tcfftStatus st = tcfftPlan1d(&a, s.N1, s.N2 * p->batch, &o);
+  if (st != TCFFT_SUCCESS) return st;
+  p->subs.push_back(a);
+  st = tcfftPlan1d(&b, s.N2, s.N1 * p->batch, &o);
+  if (st != TCFFT_SUCCESS) return st;
+  p->subs.push_back(b);
+  p->sched.launches = a->sched.launches + b->sched.launches + 4;
   return TCFFT_SUCCESS;
 }
 
@@ -878,6 +927,7 @@ tcfftStatus tcfftPlan1d(tcfftPlan* out, int64_t n, int64_t batch, const tcfftOpt
   st = alloc_tables(p);
   if (st == TCFFT_SUCCESS && (s.kind == Schedule::kFused1d || s.kind == Schedule::kFused2d)) st = alloc_fused(p);
   if (st == TCFFT_SUCCESS && s.kind == Schedule::kLarge1d) st = setup_large1d(p);
+  if (st == TCFFT_SUCCESS && s.kind == Schedule::kFourStep) st = setup_fourstep(p);
   if (st == TCFFT_SUCCESS && o.autotune) st = autotune_plan(p, o);
   if (st == TCFFT_SUCCESS && o.input_order == TCFFT_ORDER_REFERENCE_DIGIT_REVERSED) st = setup_reference_order(p);
   if (st != TCFFT_SUCCESS) {

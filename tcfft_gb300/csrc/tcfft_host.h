@@ -46,6 +46,10 @@ cudaError_t launch_tiny(int64_t n, bool split, void* data, int64_t batch, const 
 cudaError_t launch_transpose(const void* in, void* out, int64_t B, int64_t R, int64_t C, int es, int num_sms,
                              cudaStream_t st);
 
+// Transpose with the four-step twiddle: out[b][c][r] = in[b][r][c] * W_N^(r c).
+cudaError_t launch_transpose_twiddle(const void* in, void* out, int64_t B, int64_t R, int64_t C, int64_t N,
+                                     float dsign, bool split, int num_sms, cudaStream_t st);
+
 // Launch entry points implemented in the kernel translation units. Each
 // returns cudaSuccess or the launch error.
 cudaError_t launch_small(int R, bool split, const CUtensorMap& tmap, int64_t total_elems, const float2* tw,

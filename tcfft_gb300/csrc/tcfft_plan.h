@@ -15,7 +15,11 @@ struct Schedule {
   //   full-size scratch, row FFTs of length N2 by a sub-plan, transpose back.
   // kGeneric2d: axes outside the fused 2D range: row FFTs (sub-plan), transpose, row FFTs of
   //   the other axis (sub-plan), transpose back.
-  enum Kind { kNone = 0, kSmall = 1, kFused1d = 2, kFused2d = 3, kTiny = 4, kLarge1d = 5, kGeneric2d = 6 } kind = kNone;
+  // kFourStep: N = N1 N2 from two short sub-plans: transpose, rows of N1, transpose with the
+  //   W_N twiddle, rows of N2, transpose (the split precision at N = 2048).
+  enum Kind {
+    kNone = 0, kSmall = 1, kFused1d = 2, kFused2d = 3, kTiny = 4, kLarge1d = 5, kGeneric2d = 6, kFourStep = 7
+  } kind = kNone;
   int R = 1;             // small: N = 256 R
   int64_t N1 = 0, N2 = 0;  // fused 1D: N = N1 N2 (phase 0 columns of N1, phase 1 rows of N2)
   FusedKey key;          // fused: kernel instantiation

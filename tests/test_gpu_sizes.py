@@ -125,3 +125,19 @@ def test_generic_2d_split(cuda_device, nx, ny):
     with tc.Plan(nx=nx, ny=ny, batch=2, precision="split") as p:
         y = run_gpu(p, xq, "split")
     assert oracle.rel_l2(y, oracle_2d(xq)) < TOL_SPLIT
+
+
+def test_split_2048_fourstep(cuda_device):
+    """Split precision at N = 2048 (beyond the single-pass kernel's split
+    range): four-step from two short sub-plans; also as a 2D axis."""
+    xq = quantize(uniform_input((5, 2048), seed=21), "split")
+    with tc.Plan(n=2048, batch=5, precision="split") as p:
+        assert "fourstep" in p.info["schedule"]
+        y = run_gpu(p, xq, "split")
+        ya = run_gpu(p, xq, "split", adjoint=True)
+    assert oracle.rel_l2(y, oracle_1d(xq)) < TOL_SPLIT
+    assert oracle.rel_l2(ya, oracle_1d(xq, adjoint=True)) < TOL_SPLIT
+    x2 = quantize(uniform_input((1, 256, 2048), seed=22), "split")
+    with tc.Plan(nx=256, ny=2048, batch=1, precision="split") as p:
+        y2 = run_gpu(p, x2, "split")
+    assert oracle.rel_l2(y2, oracle_2d(x2)) < TOL_SPLIT
