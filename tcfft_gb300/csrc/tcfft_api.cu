@@ -252,13 +252,15 @@ tcfftStatus choose_1d(int64_t n, int64_t batch, int precision, Schedule& s) {
     return TCFFT_SUCCESS;
   }
   const int lg = ilog2_exact(n);
-  if (n == 2048 && split) {
-    // the single-pass kernel's split mode stops at 1024: 2048 = 32 x 64 from two tiny sub-plans
+  if (split && (n == 2048 || n == 32768)) {
+    // beyond the split range of the single-pass kernel (1024) and of the short-row phase
+    // (16 R with R <= 4): N = N1 x 64 from two sub-plans
     s.kind = Schedule::kFourStep;
-    s.N1 = 32;
+    s.N1 = n / 64;
     s.N2 = 64;
     s.launches = 5;
-    snprintf(buf, sizeof buf, "fourstep(split): N=32 x 64, tiny sub-plans, 3 transposes (one with the twiddle)");
+    snprintf(buf, sizeof buf, "fourstep(split): N=%lld x 64, two sub-plans, 3 transposes (one with the twiddle)",
+             (long long)s.N1);
     s.text = buf;
     return TCFFT_SUCCESS;
   }

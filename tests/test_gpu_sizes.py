@@ -127,16 +127,20 @@ def test_generic_2d_split(cuda_device, nx, ny):
     assert oracle.rel_l2(y, oracle_2d(xq)) < TOL_SPLIT
 
 
-def test_split_2048_fourstep(cuda_device):
-    """Split precision at N = 2048 (beyond the single-pass kernel's split
-    range): four-step from two short sub-plans; also as a 2D axis."""
-    xq = quantize(uniform_input((5, 2048), seed=21), "split")
-    with tc.Plan(n=2048, batch=5, precision="split") as p:
+@pytest.mark.parametrize("n", [2048, 32768])
+def test_split_fourstep(cuda_device, n):
+    """Split precision at N = 2048 and 2^15 (beyond the split range of the
+    single-pass kernel and of the short-row phase): four-step from two
+    sub-plans; 2048 also as a 2D axis."""
+    xq = quantize(uniform_input((5, n), seed=21), "split")
+    with tc.Plan(n=n, batch=5, precision="split") as p:
         assert "fourstep" in p.info["schedule"]
         y = run_gpu(p, xq, "split")
         ya = run_gpu(p, xq, "split", adjoint=True)
     assert oracle.rel_l2(y, oracle_1d(xq)) < TOL_SPLIT
     assert oracle.rel_l2(ya, oracle_1d(xq, adjoint=True)) < TOL_SPLIT
+    if n != 2048:
+        return
     x2 = quantize(uniform_input((1, 256, 2048), seed=22), "split")
     with tc.Plan(nx=256, ny=2048, batch=1, precision="split") as p:
         y2 = run_gpu(p, x2, "split")
