@@ -288,7 +288,7 @@ tcfftStatus choose_1d(int64_t n, int64_t batch, int precision, Schedule& s) {
     s.text = buf;
     return TCFFT_SUCCESS;
   }
-  if (lg >= 16 && lg <= 22) {
+  if (lg >= 16 && lg <= 22 && !(split && lg >= 21)) {
     const int64_t n1 = int64_t(1) << ((lg + 1) / 2), n2 = n / n1;
     FusedKey k;
     k.role0 = kRoleCol;
@@ -314,7 +314,7 @@ tcfftStatus choose_1d(int64_t n, int64_t batch, int precision, Schedule& s) {
     s.text = buf;
     return TCFFT_SUCCESS;
   }
-  if (lg >= 23 && lg <= 27) {
+  if ((lg >= 23 || (split && lg >= 21)) && lg <= 27) {
     // N = N1 x N2, N1 = 2048 (split 1024): column FFTs of N1 with the W_N twiddle into a full-size
     // scratch (fused kernel, phase 0 only), N1 rows of N2 by a 1D sub-plan, transpose back
     const int64_t n1 = split ? 1024 : 2048, n2 = n / n1;

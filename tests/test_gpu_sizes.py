@@ -55,8 +55,8 @@ def test_large_plain(cuda_device, n, batch):
     assert err < TOL_PLAIN, "n=%d rel-L2 %.3e" % (n, err)
 
 
-def test_large_split_and_adjoint(cuda_device):
-    n = 1 << 23
+@pytest.mark.parametrize("n", [1 << 21, 1 << 23])
+def test_large_split_and_adjoint(cuda_device, n):
     xq = quantize(uniform_input((1, n), seed=12), "split")
     with tc.Plan(n=n, batch=1, precision="split") as p:
         y = run_gpu(p, xq, "split")
