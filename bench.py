@@ -210,13 +210,14 @@ def cpu_baseline(size_args, budget_s=10.0):
                       % (done, threads, el)}
 
 
-def sweep(torch, tc, precision):
+def sweep(torch, tc, precision, lgs=range(8, 25), total=1 << 28):
+    """1D sizes at `total` elements per call (BASELINE's config 2)."""
     out = []
     peak, _ = measured_peak()
     es = 4 if precision == "plain" else 8
-    for lg in range(8, 23):
+    for lg in lgs:
         n = 1 << lg
-        batch = (1 << 28) // n
+        batch = max(1, total // n)
         dt = torch.float16 if precision == "plain" else torch.float32
         x = torch.empty((batch, n, 2), dtype=dt, device="cuda").uniform_(-1, 1)
         with tc.Plan(n=n, batch=batch, precision=precision) as p:
@@ -227,6 +228,75 @@ def sweep(torch, tc, precision):
         del x
         torch.cuda.empty_cache()
     return out
+
+
+def flops_2d(nx, ny, batch):
+    return 5.0 * nx * ny * math.log2(nx * ny) * batch
+
+
+def sweep_2d(torch, tc):
+    """BASELINE's 2D configuration: 1024^2 x 16, 4096^2 x 1, 256^2 x 1024 (plain; 1024^2 also split)."""
+    out = []
+    peak, _ = measured_peak()
+    for nx, ny, batch, prec in ((1024, 1024, 16, "plain"), (4096, 4096, 1, "plain"), (256, 256, 1024, "plain"),
+                                (1024, 1024, 16, "split")):
+        es = 4 if prec == "plain" else 8
+        dt = torch.float16 if prec == "plain" else torch.float32
+        x = torch.empty((batch, nx, ny, 2), dtype=dt, device="cuda").uniform_(-1, 1)
+        with tc.Plan(nx=nx, ny=ny, batch=batch, precision=prec) as p:
+            sec = time_device(torch, p, x, 10, 3) / 10
+            sched = p.info["schedule"]
+        out.append({"nx": nx, "ny": ny, "batch": batch, "precision": prec, "us": round(sec * 1e6, 1),
+                    "gflops": round(flops_2d(nx, ny, batch) / sec / 1e9, 1),
+                    "hbm_frac_of_measured": round(2 * es * nx * ny * batch / sec / 1e9 / peak, 3),
+                    "schedule": sched.split(":")[0]})
+        del x
+        torch.cuda.empty_cache()
+    return out
+
+
+def uneven_batch(torch, tc):
+    """BASELINE's uneven-batch configuration: 512 1D transforms of 2^8..2^16 and 64 2D transforms
+    of 2^7..2^10 per axis (seed 2), back to back in one buffer, one plan, graph-replayed."""
+    import numpy as np
+    rng = np.random.default_rng(2)
+    shapes = [(1 << int(e),) for e in rng.integers(8, 17, size=512)]
+    shapes += [(1 << int(a), 1 << int(b)) for a, b in rng.integers(7, 11, size=(64, 2))]
+    shapes = [shapes[i] for i in rng.permutation(len(shapes))]
+    elems = sum(int(np.prod(sh)) for sh in shapes)
+    flops = sum(5.0 * int(np.prod(sh)) * math.log2(int(np.prod(sh))) for sh in shapes)
+    x = torch.empty((elems, 2), dtype=torch.float16, device="cuda").uniform_(-1, 1)
+    peak, _ = measured_peak()
+    with tc.Plan.many(shapes) as p:
+        sec = time_device(torch, p, x, 20, 3) / 20
+        info = p.info
+    return {"transforms": len(shapes), "elements": elems, "us": round(sec * 1e6, 1),
+            "gflops": round(flops / sec / 1e9, 1), "hbm_frac_of_measured": round(8 * elems / sec / 1e9 / peak, 3),
+            "launches_per_replay": info["launches_per_exec"], "schedule": info["schedule"]}
+
+
+def cufft_fp16(torch, size_args, batch):
+    """cuFFT half precision (through torch.fft on complex32) on the same workload: a reported
+    GPU baseline (out of place), not the reference."""
+    n = size_args.get("n")
+    if not n:
+        return None
+    x = torch.empty((batch, n, 2), dtype=torch.float16, device="cuda").uniform_(-1, 1)
+    xc = torch.view_as_complex(x)
+    for _ in range(3):
+        y = torch.fft.fft(xc)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(10):
+        y = torch.fft.fft(xc)
+    e1.record()
+    torch.cuda.synchronize()
+    sec = e0.elapsed_time(e1) / 1000.0 / 10
+    del y, xc, x
+    torch.cuda.empty_cache()
+    return {"gflops": round(flops_per_call(n, batch) / sec / 1e9, 1), "us": round(sec * 1e6, 1),
+            "what": "torch.fft.fft on complex32 (cuFFT fp16), out of place"}
 
 
 def main():
@@ -370,10 +440,16 @@ def main():
     if rank == 0:
         extra["accuracy"] = {p: accuracy_sample(torch, tc, size_args, p) for p in ("plain", "split")}
         if not args.no_sweep and "n" in size_args:
-            try:
-                extra["sweep"] = sweep(torch, tc, args.precision)
-            except Exception as e:  # noqa: BLE001 - the sweep is informational
-                extra["sweep_error"] = str(e)
+            for key, fn in (("sweep", lambda: sweep(torch, tc, args.precision)),
+                            ("sweep_split", lambda: sweep(torch, tc, "split", lgs=(10, 12, 14, 16, 18, 20, 22))),
+                            ("sweep_2d", lambda: sweep_2d(torch, tc)),
+                            ("uneven_batch", lambda: uneven_batch(torch, tc)),
+                            ("cufft_fp16", lambda: cufft_fp16(torch, size_args, batch))):
+                try:  # informational
+                    extra[key] = fn()
+                except Exception as e:  # noqa: BLE001
+                    extra[key + "_error"] = str(e)[:200]
+                torch.cuda.empty_cache()
     plan.destroy()
     del x
     torch.cuda.empty_cache()

@@ -192,6 +192,11 @@ void free_tables(tcfftPlanImpl* p) {
   for (tcfftPlanImpl* sp : p->subs) tcfftDestroy(sp);
   p->subs.clear();
   p->runs.clear();
+  for (long long** q : {&p->mv_user, &p->mv_big, &p->mv_cum}) {
+    if (*q) cudaFree(*q);
+    *q = nullptr;
+  }
+  p->mv_n = 0;
   for (int d = 0; d < 2; ++d) {
     if (p->graph_exec[d]) cudaGraphExecDestroy(p->graph_exec[d]);
     p->graph_exec[d] = nullptr;
@@ -842,10 +847,19 @@ tcfftStatus exec_many(tcfftPlanImpl* plan, void* data, cudaStream_t st, int dir)
     if (cuda_status(cudaStreamBeginCapture(plan->cap_stream, cudaStreamCaptureModeThreadLocal), "graph capture"))
       return TCFFT_CUDA_ERROR;
     tcfftStatus r = TCFFT_SUCCESS;
+    if (plan->mv_n > 0)
+      r = cuda_status(launch_move_blocks(data, plan->big, plan->mv_user, plan->mv_big, plan->mv_cum, plan->mv_n,
+                                         plan->mv_chunks, plan->num_sms, plan->cap_stream),
+                      "gather");
     for (const auto& run : plan->runs) {
-      r = exec_plan(run.sub, static_cast<unsigned char*>(data) + run.offset * es, plan->cap_stream, dir);
       if (r != TCFFT_SUCCESS) break;
+      unsigned char* base = static_cast<unsigned char*>(run.in_big ? plan->big : data);
+      r = exec_plan(run.sub, base + run.offset * es, plan->cap_stream, dir);
     }
+    if (r == TCFFT_SUCCESS && plan->mv_n > 0)
+      r = cuda_status(launch_move_blocks(plan->big, data, plan->mv_big, plan->mv_user, plan->mv_cum, plan->mv_n,
+                                         plan->mv_chunks, plan->num_sms, plan->cap_stream),
+                      "scatter");
     cudaGraph_t g = nullptr;
     cudaError_t ce = cudaStreamEndCapture(plan->cap_stream, &g);
     if (r != TCFFT_SUCCESS || ce != cudaSuccess) {
@@ -1032,35 +1046,71 @@ tcfftStatus tcfftPlanMany(tcfftPlan* out, int64_t count, const int32_t* ranks, c
   p->batch = count;
   st = alloc_tables(p);
   tcfftOptions os = o;
+  // group by shape (in offset order); a group that is one back-to-back run executes in place,
+  // any other group with several members is gathered into `big`, run as one batch, scattered back
+  std::map<std::tuple<int, int64_t, int64_t>, std::vector<int64_t>> groups;
+  for (int64_t k = 0; k < count; ++k) {
+    const int64_t i = order[k];
+    groups[std::make_tuple(ranks[i], nx[i], ranks[i] == 2 ? ny[i] : 1)].push_back(i);
+  }
   std::map<std::tuple<int, int64_t, int64_t, int64_t>, tcfftPlanImpl*> by_key;
+  std::vector<long long> mv_user, mv_big, mv_cum;
+  int64_t big_elems = 0;
+  long long chunks = 0;
   int launches = 0, nsub = 0;
-  for (int64_t k = 0; k < count && st == TCFFT_SUCCESS;) {
-    // a run: same shape, each transform right after the previous one
-    const int64_t i0 = order[k];
-    const int r = ranks[i0];
-    const int64_t x = nx[i0], y = r == 2 ? ny[i0] : 1;
-    int64_t len = 1;
-    while (k + len < count) {
-      const int64_t j = order[k + len], prev = order[k + len - 1];
-      if (ranks[j] != r || nx[j] != x || (r == 2 ? ny[j] : 1) != y || offsets[j] != offsets[prev] + size[prev]) break;
-      ++len;
-    }
-    const auto key = std::make_tuple(r, x, y, len);
-    tcfftPlanImpl* sub = nullptr;
-    auto it = by_key.find(key);
-    if (it != by_key.end()) {
-      sub = it->second;
+  for (auto& g : groups) {
+    if (st != TCFFT_SUCCESS) break;
+    const int r = std::get<0>(g.first);
+    const int64_t x = std::get<1>(g.first), y = std::get<2>(g.first), sz = x * y;
+    const std::vector<int64_t>& idx = g.second;
+    bool contiguous = true;
+    for (size_t j = 1; j < idx.size(); ++j) contiguous = contiguous && offsets[idx[j]] == offsets[idx[j - 1]] + sz;
+    std::vector<std::pair<int64_t, int64_t>> todo;  // (offset, run length)
+    bool in_big = false;
+    if (contiguous || idx.size() == 1) {
+      todo.push_back({offsets[idx[0]], (int64_t)idx.size()});
     } else {
-      st = r == 1 ? tcfftPlan1d(&sub, x, len, &os) : tcfftPlan2d(&sub, x, y, len, &os);
-      if (st != TCFFT_SUCCESS) break;
-      p->subs.push_back(sub);
-      by_key[key] = sub;
-      ++nsub;
+      in_big = true;
+      todo.push_back({big_elems, (int64_t)idx.size()});
+      for (size_t j = 0; j < idx.size(); ++j) {
+        mv_user.push_back(offsets[idx[j]] * es);
+        mv_big.push_back((big_elems + (int64_t)j * sz) * es);
+        mv_cum.push_back(chunks);
+        chunks += sz * es / 16;
+      }
+      big_elems += sz * (int64_t)idx.size();
     }
-    p->runs.push_back({sub, offsets[i0]});
-    launches += sub->sched.launches;
-    p->total_elems += size[i0] * len;
-    k += len;
+    for (const auto& t : todo) {
+      const auto key = std::make_tuple(r, x, y, t.second);
+      tcfftPlanImpl* sub = nullptr;
+      auto it = by_key.find(key);
+      if (it != by_key.end()) {
+        sub = it->second;
+      } else {
+        st = r == 1 ? tcfftPlan1d(&sub, x, t.second, &os) : tcfftPlan2d(&sub, x, y, t.second, &os);
+        if (st != TCFFT_SUCCESS) break;
+        p->subs.push_back(sub);
+        by_key[key] = sub;
+        ++nsub;
+      }
+      p->runs.push_back({sub, t.first, in_big});
+      launches += sub->sched.launches;
+    }
+    p->total_elems += sz * (int64_t)idx.size();
+  }
+  if (st == TCFFT_SUCCESS && !mv_user.empty()) {
+    const size_t nb = mv_user.size() * sizeof(long long);
+    if (cudaMalloc(&p->big, big_elems * es) != cudaSuccess || cudaMalloc(&p->mv_user, nb) != cudaSuccess ||
+        cudaMalloc(&p->mv_big, nb) != cudaSuccess || cudaMalloc(&p->mv_cum, nb) != cudaSuccess)
+      st = TCFFT_ALLOC_FAILED;
+    else if (cudaMemcpy(p->mv_user, mv_user.data(), nb, cudaMemcpyHostToDevice) != cudaSuccess ||
+             cudaMemcpy(p->mv_big, mv_big.data(), nb, cudaMemcpyHostToDevice) != cudaSuccess ||
+             cudaMemcpy(p->mv_cum, mv_cum.data(), nb, cudaMemcpyHostToDevice) != cudaSuccess)
+      st = TCFFT_CUDA_ERROR;
+    p->mv_n = (int)mv_user.size();
+    p->mv_chunks = chunks;
+    p->scratch_bytes = big_elems * es;
+    launches += 2;
   }
   if (st == TCFFT_SUCCESS && cudaStreamCreateWithFlags(&p->cap_stream, cudaStreamNonBlocking) != cudaSuccess)
     st = TCFFT_CUDA_ERROR;
@@ -1071,9 +1121,9 @@ tcfftStatus tcfftPlanMany(tcfftPlan* out, int64_t count, const int32_t* ranks, c
   }
   p->sched.launches = launches;
   char buf[160];
-  snprintf(buf, sizeof buf, "many(%s): %lld transforms in %d runs, %d sub-plans, %d launches per graph replay",
-           o.precision == TCFFT_PRECISION_SPLIT ? "split" : "plain", (long long)count, (int)p->runs.size(), nsub,
-           launches);
+  snprintf(buf, sizeof buf, "many(%s): %lld transforms in %d runs (%d gathered), %d sub-plans, %d launches per graph replay",
+           o.precision == TCFFT_PRECISION_SPLIT ? "split" : "plain", (long long)count, (int)p->runs.size(), p->mv_n,
+           nsub, launches);
   p->sched.text = buf;
   *out = p;
   return TCFFT_SUCCESS;

@@ -50,6 +50,11 @@ cudaError_t launch_transpose(const void* in, void* out, int64_t B, int64_t R, in
 cudaError_t launch_transpose_twiddle(const void* in, void* out, int64_t B, int64_t R, int64_t C, int64_t N,
                                      float dsign, bool split, int num_sms, cudaStream_t st);
 
+// Copies nblocks variable-size blocks (byte offsets, 16-byte aligned) in one launch (tcfft_gather.cu).
+cudaError_t launch_move_blocks(const void* src, void* dst, const long long* src_off, const long long* dst_off,
+                               const long long* cum, int nblocks, long long total_chunks, int num_sms,
+                               cudaStream_t st);
+
 // Launch entry points implemented in the kernel translation units. Each
 // returns cudaSuccess or the launch error.
 cudaError_t launch_small(int R, bool split, const CUtensorMap& tmap, int64_t total_elems, const float2* tw,

@@ -56,9 +56,19 @@ struct tcfftPlanImpl {
   // private stream and replayed with one graph launch.
   struct Run {
     tcfftPlanImpl* sub;
-    int64_t offset;  // elements
+    int64_t offset;  // elements, in the caller's buffer or (in_big) in `big`
+    bool in_big;
   };
   std::vector<Run> runs;
+  // same-shape transforms that are not back to back are gathered into `big`
+  // (one launch), transformed as one batch and scattered back (one launch):
+  // per moved transform its byte offset in the caller's buffer and in `big`,
+  // and the 16-byte chunks before it (device tables)
+  long long* mv_user = nullptr;
+  long long* mv_big = nullptr;
+  long long* mv_cum = nullptr;
+  int mv_n = 0;
+  long long mv_chunks = 0;
   cudaStream_t cap_stream = nullptr;
   void* graph_ptr[2] = {nullptr, nullptr};
   cudaGraphExec_t graph_exec[2] = {nullptr, nullptr};
