@@ -1,0 +1,249 @@
+// fft_resident.cu -- 1D FFTs of N = 256 x 16 R1 (R1 = 1, 2, 4: N = 4096, 8192,
+// 16384) held entirely in one CTA's shared memory.
+//
+// Same four-step factorisation as the two-phase kernel (fft_fused.cuh), but a
+// whole transform (16-64 KiB) fits in one 64 KiB stage, so both phases run on
+// the stage in place: no scratch ring, no cross-CTA dependency, and HBM is
+// touched once per element each way with contiguous TMA copies.  (The
+// reference has no sizes between 1024 and 2^17, tcfft_half.cu:1250-1330.)
+//
+//   stage = T transforms (T = 16 KiB-transforms per 64 KiB), loaded as column
+//           tiles of the [256 rows n1][N2 cols n2] view (5D boxes in the
+//           digit-ordered row layout of the column role, one box per group of
+//           C <= 32 columns);
+//   phase 0: 256-point column FFTs (plain_col_tile) times W_N^(n2 k1);
+//   phase 1: N2-point FFTs of the 256 rows k1, 16 rows per warp job
+//           (fft16r_job), results held in registers;
+//   output: after a barrier, X[k1 + 256 k2] written in natural order into the
+//           stage and stored with a 2D TMA box of 128-byte rows.
+#include <mutex>
+
+#include "fft_fused.cuh"
+#include "tcfft_host.h"
+
+namespace tcfft {
+namespace {
+
+template <int R1>
+struct ResCfg {
+  static constexpr int kN2 = 16 * R1;
+  static constexpr int kN = 256 * kN2;
+  static constexpr int kC = kN2 < 32 ? kN2 : 32;          // columns per column tile
+  static constexpr int kCG = kN2 / kC;                     // column tiles per transform
+  static constexpr int kT = 65536 / (kN * 4);              // transforms per stage
+  static constexpr int kTileBytes = 256 * kC * 4;          // one column tile
+  static constexpr int kStageBytes = 65536;
+  static constexpr int kStages = 3;
+  static constexpr int kLog2N = 8 + 4 + (R1 == 1 ? 0 : (R1 == 2 ? 1 : 2));
+  static constexpr int kTwShift = (kLog2N + 1) / 2;
+  static constexpr int kTwLo = 1 << kTwShift, kTwHi = kN >> kTwShift;
+  static constexpr int kTabBytes = (kTwLo + kTwHi + kN2) * 8 + FoldTab<1>::kBytes;
+  static constexpr int kSmem = kStages * kStageBytes + kTabBytes + 1024 + 256;
+  static constexpr int kThreads = 384;
+  using PI = BitPerm<0, 1, 3, 2>;
+  using RHO = BitPerm<0, 2, 3, 1>;
+  static_assert(kT >= 1 && kT * kN * 4 == kStageBytes, "a stage holds whole transforms");
+};
+
+struct ResParams {
+  const float2* tw2048;
+  const float2* twlo;
+  const float2* twhi;
+  long long batch;
+  int* err;
+  float dsign;
+};
+
+template <int R1>
+__global__ void __launch_bounds__(384, 1) fft_resident_kernel(const __grid_constant__ CUtensorMap load_map,
+                                                               const __grid_constant__ CUtensorMap store_map,
+                                                               const ResParams p) {
+  using Cfg = ResCfg<R1>;
+  using PI = typename Cfg::PI;
+  using RHO = typename Cfg::RHO;
+  constexpr int NST = Cfg::kStages, T = Cfg::kT, CG = Cfg::kCG, C = Cfg::kC, N = Cfg::kN;
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  unsigned char* smem =
+      reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  unsigned char* tab = smem + NST * Cfg::kStageBytes;
+  float2* s_twlo = reinterpret_cast<float2*>(tab);
+  float2* s_twhi = s_twlo + Cfg::kTwLo;
+  float2* s_tw16 = s_twhi + Cfg::kTwHi;  // W_{N2}^j
+  unsigned char* s_fold = reinterpret_cast<unsigned char*>(s_tw16 + Cfg::kN2);
+  uint64_t* full = reinterpret_cast<uint64_t*>(tab + Cfg::kTabBytes);
+  uint64_t* computed = full + NST;
+  uint64_t* empty = computed + NST;
+
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const long long tiles = (p.batch + T - 1) / T;
+  if (tid == 0) {
+    for (int s = 0; s < NST; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&computed[s], 8);
+      mbar_init(&empty[s], 1);
+    }
+    fence_barrier_init();
+  }
+  for (int j = tid; j < Cfg::kTwLo; j += blockDim.x) s_twlo[j] = p.twlo[j];
+  for (int j = tid; j < Cfg::kTwHi; j += blockDim.x) s_twhi[j] = p.twhi[j];
+  for (int j = tid; j < Cfg::kN2; j += blockDim.x) s_tw16[j] = p.tw2048[j * (2048 / Cfg::kN2)];
+  build_fold_table<1, PI, RHO>(s_fold, p.tw2048, tid, blockDim.x);
+  __syncthreads();
+
+  if (warp >= 8) asm volatile("setmaxnreg.dec.sync.aligned.u32 %0;" ::"n"(56));
+  if (warp >= 10) return;
+  if (warp == 8) {  // ------------------------------------------------ TMA producer
+    if (lane == 0) {
+      prefetch_tmap(&load_map);
+      int cnt = 0;
+      for (long long it = blockIdx.x; it < tiles; it += gridDim.x, ++cnt) {
+        const int s = cnt % NST;
+        if (!mbar_wait(&empty[s], ((cnt / NST) + 1) & 1, p.err)) break;
+        unsigned char* dst = smem + s * Cfg::kStageBytes;
+        mbar_arrive_expect_tx(&full[s], Cfg::kStageBytes);
+#pragma unroll 1
+        for (int t = 0; t < T; ++t)
+#pragma unroll 1
+          for (int cg = 0; cg < CG; ++cg)
+            tma_load_5d(dst + (t * CG + cg) * Cfg::kTileBytes, &load_map, cg * C, 0, 0, 0, (int)(it * T + t),
+                        &full[s]);
+      }
+      for (int i = (cnt > NST ? cnt - NST : 0); i < cnt; ++i) mbar_wait(&full[i % NST], (i / NST) & 1, nullptr);
+    }
+    return;
+  }
+  if (warp == 9) {  // ------------------------------------------------ TMA storer
+    if (lane == 0) {
+      prefetch_tmap(&store_map);
+      int cnt = 0;
+      for (long long it = blockIdx.x; it < tiles; it += gridDim.x, ++cnt) {
+        const int s = cnt % NST;
+        if (!mbar_wait(&computed[s], (cnt / NST) & 1, p.err)) break;
+        const unsigned char* src = smem + s * Cfg::kStageBytes;
+        const int row0 = (int)(it * (Cfg::kStageBytes / 128));
+#pragma unroll 1
+        for (int b = 0; b < Cfg::kStageBytes / (256 * 128); ++b)
+          tma_store_2d(&store_map, 0, row0 + 256 * b, src + b * 256 * 128);
+        bulk_commit();
+        bulk_wait_read<0>();
+        mbar_arrive(&empty[s]);
+      }
+      bulk_wait<0>();
+    }
+    return;
+  }
+
+  // ------------------------------------------------------------------ compute warps
+  asm volatile("setmaxnreg.inc.sync.aligned.u32 %0;" ::"n"(224));
+  JobConsts<false> jc;
+  init_job_consts<false, PI, RHO>(jc, p.tw2048);
+  const uint32_t fold = smem_addr(s_fold), tw16 = smem_addr(s_tw16);
+  WnTable wn;
+  wn.hi = smem_addr(s_twhi);
+  wn.lo = smem_addr(s_twlo);
+  wn.ghi = p.twhi;
+  wn.glo = p.twlo;
+  wn.global = false;
+  wn.shift = Cfg::kTwShift;
+  wn.nmask = N - 1;
+  const int g = lane >> 2, tq = lane & 3;
+  int cnt = 0;
+  for (long long it = blockIdx.x; it < tiles; it += gridDim.x, ++cnt) {
+    const int s = cnt % NST;
+    const bool ok = named_bar_and(2, 256, mbar_wait(&full[s], (cnt / NST) & 1, p.err));
+    const uint32_t base = smem_addr(smem + s * Cfg::kStageBytes);
+    if (ok) {
+      // phase 0: columns of 256 (in place, digit-ordered rows), twiddle W_N^(n2 k1)
+#pragma unroll 1
+      for (int tile = 0; tile < T * CG; ++tile)
+        plain_col_tile<1, C, true, PI, RHO>(jc, fold, base + tile * Cfg::kTileBytes, warp, p.dsign,
+                                            (tile % CG) * C, wn);
+      named_bar_sync(1, 256);
+      // phase 1: 16 rows k1 per job, FFT over n2 (length 16 R1); jobs j = warp + 8 i
+      constexpr int JOBS = 2 * T;  // per warp: 16 T jobs per stage / 8 warps
+      uint32_t out[JOBS][8 * R1];
+#pragma unroll
+      for (int i = 0; i < JOBS; ++i) {
+        const int job = warp + 8 * i, t = job >> 4, k1base = (job & 15) * 16;
+        const uint32_t tbase = base + t * (CG * Cfg::kTileBytes);
+        auto ld = [&](int v, int n) {
+          const uint32_t a = tbase + (n / C) * Cfg::kTileBytes + ctile_off<C, 4>(col_out_row(k1base + v, 0), n % C);
+          return unpack_h2(lds32(a));
+        };
+        auto st = [&](int, int, int q, int slot, float2 val) { out[i][8 * q + slot] = pack_h2(val.x, val.y); };
+        fft16r_job<R1, false, 1, PI, RHO>(jc, tw16, p.dsign, ld, st);
+      }
+      named_bar_sync(1, 256);  // every warp has read the stage
+      // natural order X[k1 + 256 k2] of transform t at element t N + k1 + 256 k2 (128B-swizzled rows)
+#pragma unroll
+      for (int i = 0; i < JOBS; ++i) {
+        const int job = warp + 8 * i, t = job >> 4, k1base = (job & 15) * 16;
+#pragma unroll
+        for (int q = 0; q < R1; ++q)
+#pragma unroll
+          for (int slot = 0; slot < 8; ++slot) {
+            const int jj = slot >> 2, h = (slot >> 1) & 1, e = slot & 1;
+            const int v = 2 * tq + e + 8 * jj, k = q + R1 * RHO::apply(g + 8 * h);
+            const uint32_t el = (uint32_t)(t * N + k1base + v + 256 * k);
+            sts32(base + swz_w<4>(el) * 4, out[i][8 * q + slot]);
+          }
+      }
+    }
+    fence_proxy_async_smem();
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&computed[s]);
+    if (!ok) break;
+  }
+}
+
+template <int R1>
+cudaError_t launch_resident_t(const CUtensorMap& lm, const CUtensorMap& sm, const ResParams& p, int num_sms,
+                              cudaStream_t st) {
+  using Cfg = ResCfg<R1>;
+  auto kern = fft_resident_kernel<R1>;
+  static std::once_flag once;
+  static cudaError_t init_err = cudaSuccess;
+  std::call_once(once, [&] { init_err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg::kSmem); });
+  if (init_err != cudaSuccess) return init_err;
+  const long long tiles = (p.batch + Cfg::kT - 1) / Cfg::kT;
+  const long long grid = tiles < num_sms ? tiles : num_sms;
+  kern<<<(int)grid, Cfg::kThreads, Cfg::kSmem, st>>>(lm, sm, p);
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+bool resident_supported(int64_t n, bool split) { return !split && (n == 4096 || n == 8192 || n == 16384); }
+
+// Tensor maps: column-tile loads of the [B*256 rows][N2 cols] view and 128-byte-row stores.
+cudaError_t launch_resident(int64_t n, void* data, int64_t batch, const float2* tw2048, const float2* twlo,
+                            const float2* twhi, float dsign, int* err, int num_sms, cudaStream_t st,
+                            CUtensorMap* lm, CUtensorMap* sm, bool encode) {
+  const int64_t n2 = n / 256;
+  const int C = n2 < 32 ? (int)n2 : 32;
+  if (encode) {
+    if (encode_col_load(lm, CU_TENSOR_MAP_DATA_TYPE_UINT32, data, n2, batch, 4, C, 1) != CUDA_SUCCESS)
+      return cudaErrorInvalidValue;
+    uint64_t dims[2] = {32, (uint64_t)(n * batch / 32)};
+    uint64_t str[1] = {128};
+    uint32_t box[2] = {32, 256};
+    if (encode_tmap(sm, CU_TENSOR_MAP_DATA_TYPE_UINT32, 2, data, dims, str, box, CU_TENSOR_MAP_SWIZZLE_128B) !=
+        CUDA_SUCCESS)
+      return cudaErrorInvalidValue;
+  }
+  ResParams p;
+  p.tw2048 = tw2048;
+  p.twlo = twlo;
+  p.twhi = twhi;
+  p.batch = batch;
+  p.err = err;
+  p.dsign = dsign;
+  switch (n) {
+    case 4096: return launch_resident_t<1>(*lm, *sm, p, num_sms, st);
+    case 8192: return launch_resident_t<2>(*lm, *sm, p, num_sms, st);
+    case 16384: return launch_resident_t<4>(*lm, *sm, p, num_sms, st);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+}  // namespace tcfft

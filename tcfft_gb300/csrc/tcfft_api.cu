@@ -269,6 +269,16 @@ tcfftStatus choose_1d(int64_t n, int64_t batch, int precision, Schedule& s) {
     s.text = buf;
     return TCFFT_SUCCESS;
   }
+  if (resident_supported(n, split) && !getenv("TCFFT_NO_RESIDENT")) {
+    s.kind = Schedule::kResident;
+    s.N1 = 256;
+    s.N2 = n / 256;
+    s.launches = 1;
+    snprintf(buf, sizeof buf, "resident(plain): N=256 x %lld, whole transforms in shared memory, one HBM pass",
+             (long long)s.N2);
+    s.text = buf;
+    return TCFFT_SUCCESS;
+  }
   if (lg >= 12 && lg <= 15) {
     // N = 256 x N2 with short rows N2 = 16 R1: phase 0 columns of 256, phase 1 16 rows per warp
     FusedKey k;
@@ -428,6 +438,13 @@ tcfftStatus exec_plan(tcfftPlan plan, void* data, void* stream, int dir) {
       return TCFFT_CUDA_ERROR;
   }
   const int es = split ? 8 : 4;
+  if (s.kind == Schedule::kResident) {
+    const bool enc = plan->tmap_ptr != data;
+    cudaError_t e = launch_resident(plan->n, data, plan->batch, tw, plan->twlo[dir], plan->twhi[dir], dsign,
+                                    plan->tables.err, plan->num_sms, st, &plan->fmaps.load0, &plan->fmaps.store0, enc);
+    if (e == cudaSuccess) plan->tmap_ptr = data;
+    return cuda_status(e, "resident launch");
+  }
   if (s.kind == Schedule::kTiny)
     return cuda_status(launch_tiny(plan->n, split, data, plan->batch, tw, dsign, plan->num_sms, st), "tiny launch");
   if (s.kind == Schedule::kLarge1d) {
@@ -944,6 +961,7 @@ tcfftStatus tcfftPlan1d(tcfftPlan* out, int64_t n, int64_t batch, const tcfftOpt
   if (st == TCFFT_SUCCESS && (s.kind == Schedule::kFused1d || s.kind == Schedule::kFused2d)) st = alloc_fused(p);
   if (st == TCFFT_SUCCESS && s.kind == Schedule::kLarge1d) st = setup_large1d(p);
   if (st == TCFFT_SUCCESS && s.kind == Schedule::kFourStep) st = setup_fourstep(p);
+  if (st == TCFFT_SUCCESS && s.kind == Schedule::kResident) st = alloc_wn_tables(p, n);
   if (st == TCFFT_SUCCESS && o.autotune) st = autotune_plan(p, o);
   if (st == TCFFT_SUCCESS && o.input_order == TCFFT_ORDER_REFERENCE_DIGIT_REVERSED) st = setup_reference_order(p);
   if (st != TCFFT_SUCCESS) {

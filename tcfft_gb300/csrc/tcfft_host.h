@@ -55,6 +55,17 @@ cudaError_t launch_move_blocks(const void* src, void* dst, const long long* src_
                                const long long* cum, int nblocks, long long total_chunks, int num_sms,
                                cudaStream_t st);
 
+// Column-tile tensor maps (tcfft_api.cu): rows of `ncols` elements, blocks of 256R rows.
+CUresult encode_col_load(CUtensorMap* m, CUtensorMapDataType dt, void* base, int64_t ncols, int64_t nblk, int es,
+                         int C, int R);
+CUresult encode_col_store(CUtensorMap* m, CUtensorMapDataType dt, void* base, int64_t ncols, int64_t nblk, int es,
+                          int C, int R);
+// Whole-transform-in-shared-memory kernel, N = 4096, 8192, 16384 plain (fft_resident.cu).
+bool resident_supported(int64_t n, bool split);
+cudaError_t launch_resident(int64_t n, void* data, int64_t batch, const float2* tw2048, const float2* twlo,
+                            const float2* twhi, float dsign, int* err, int num_sms, cudaStream_t st,
+                            CUtensorMap* lm, CUtensorMap* sm, bool encode);
+
 // Launch entry points implemented in the kernel translation units. Each
 // returns cudaSuccess or the launch error.
 cudaError_t launch_small(int R, bool split, const CUtensorMap& tmap, int64_t total_elems, const float2* tw,
