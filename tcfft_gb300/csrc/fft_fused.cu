@@ -38,9 +38,12 @@ cudaError_t launch_fused_1d(const FusedKey& k, const FusedMaps& maps, const Fuse
   // 1D four-step: phase 0 = columns of N1 = 256*R0, phase 1 = rows of N2 = 256*R1 (N1 >= N2)
   TCFFT_FUSED_CASE(kRoleCol, 1, 16, kRoleRowT, 1, 16, false)
   TCFFT_FUSED_CASE(kRoleCol, 1, 32, kRoleRowT, 1, 32, false)
+  TCFFT_FUSED_CASE(kRoleCol, 2, 32, kRoleRowT, 1, 32, false)
+  TCFFT_FUSED_CASE(kRoleCol, 2, 32, kRoleRowT, 2, 32, false)
   TCFFT_FUSED_CASE(kRoleCol, 2, 16, kRoleRowT, 1, 16, false)
   TCFFT_FUSED_CASE(kRoleCol, 2, 16, kRoleRowT, 2, 16, false)
   TCFFT_FUSED_CASE(kRoleCol, 4, 16, kRoleRowT, 2, 16, false)
+  TCFFT_FUSED_CASE(kRoleCol, 4, 16, kRoleRowT, 2, 32, false)
   TCFFT_FUSED_CASE(kRoleCol, 4, 16, kRoleRowT, 4, 16, false)
   TCFFT_FUSED_CASE(kRoleCol, 8, 8, kRoleRowT, 4, 16, false)
   TCFFT_FUSED_CASE(kRoleCol, 8, 8, kRoleRowT, 8, 8, false)

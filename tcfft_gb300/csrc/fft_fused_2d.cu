@@ -36,20 +36,20 @@ cudaError_t launch_fused_2d_plain(const FusedKey& k, const FusedMaps& maps, cons
                 int* grid_out, bool* handled) {
   *handled = false;
   // 2D [NX][NY]: phase 0 = rows of NY = 256*R0 (C0 rows per tile), phase 1 = columns of NX = 256*R1
-  TCFFT_FUSED_CASE(kRoleRow, 1, 16, kRoleCol, 1, 16, false)
-  TCFFT_FUSED_CASE(kRoleRow, 1, 16, kRoleCol, 2, 16, false)
-  TCFFT_FUSED_CASE(kRoleRow, 1, 16, kRoleCol, 4, 16, false)
-  TCFFT_FUSED_CASE(kRoleRow, 1, 16, kRoleCol, 8, 8, false)
-  TCFFT_FUSED_CASE(kRoleRow, 2, 16, kRoleCol, 1, 16, false)
-  TCFFT_FUSED_CASE(kRoleRow, 2, 16, kRoleCol, 2, 16, false)
-  TCFFT_FUSED_CASE(kRoleRow, 2, 16, kRoleCol, 4, 16, false)
-  TCFFT_FUSED_CASE(kRoleRow, 2, 16, kRoleCol, 8, 8, false)
-  TCFFT_FUSED_CASE(kRoleRow, 4, 16, kRoleCol, 1, 16, false)
-  TCFFT_FUSED_CASE(kRoleRow, 4, 16, kRoleCol, 2, 16, false)
+  TCFFT_FUSED_CASE(kRoleRow, 1, 32, kRoleCol, 1, 32, false)
+  TCFFT_FUSED_CASE(kRoleRow, 1, 32, kRoleCol, 2, 32, false)
+  TCFFT_FUSED_CASE(kRoleRow, 1, 32, kRoleCol, 4, 16, false)
+  TCFFT_FUSED_CASE(kRoleRow, 1, 32, kRoleCol, 8, 8, false)
+  TCFFT_FUSED_CASE(kRoleRow, 2, 32, kRoleCol, 1, 32, false)
+  TCFFT_FUSED_CASE(kRoleRow, 2, 32, kRoleCol, 2, 32, false)
+  TCFFT_FUSED_CASE(kRoleRow, 2, 32, kRoleCol, 4, 16, false)
+  TCFFT_FUSED_CASE(kRoleRow, 2, 32, kRoleCol, 8, 8, false)
+  TCFFT_FUSED_CASE(kRoleRow, 4, 16, kRoleCol, 1, 32, false)
+  TCFFT_FUSED_CASE(kRoleRow, 4, 16, kRoleCol, 2, 32, false)
   TCFFT_FUSED_CASE(kRoleRow, 4, 16, kRoleCol, 4, 16, false)
   TCFFT_FUSED_CASE(kRoleRow, 4, 16, kRoleCol, 8, 8, false)
-  TCFFT_FUSED_CASE(kRoleRow, 8, 8, kRoleCol, 1, 16, false)
-  TCFFT_FUSED_CASE(kRoleRow, 8, 8, kRoleCol, 2, 16, false)
+  TCFFT_FUSED_CASE(kRoleRow, 8, 8, kRoleCol, 1, 32, false)
+  TCFFT_FUSED_CASE(kRoleRow, 8, 8, kRoleCol, 2, 32, false)
   TCFFT_FUSED_CASE(kRoleRow, 8, 8, kRoleCol, 4, 16, false)
   TCFFT_FUSED_CASE(kRoleRow, 8, 8, kRoleCol, 8, 8, false)
   return cudaErrorNotSupported;

@@ -369,10 +369,11 @@ tcfftStatus choose_2d(int64_t nx, int64_t ny, int64_t batch, int precision, Sche
   FusedKey k;
   k.role0 = kRoleRow;
   k.R0 = (int)(ny / 256);
-  k.C0 = 16 * 256 * k.R0 * es <= 64 * 1024 ? 16 : 8;
+  k.C0 = fused_cols(k.R0, split);
   k.role1 = kRoleCol;
   k.R1 = (int)(nx / 256);
   k.C1 = fused_cols(k.R1, split);
+  if (getenv("TCFFT_FUSED_C")) k.C0 = k.C1 = atoi(getenv("TCFFT_FUSED_C"));
   k.split = split;
   if (k.C1 == 0 || k.C0 * 256 * k.R0 * es > 64 * 1024 || (split && (k.R0 > 4 || k.R1 > 4))) return TCFFT_NOT_SUPPORTED;
   s.kind = Schedule::kFused2d;
