@@ -439,6 +439,13 @@ tcfftStatus exec_plan(tcfftPlan plan, void* data, void* stream, int dir) {
       return TCFFT_CUDA_ERROR;
   }
   const int es = split ? 8 : 4;
+  if (s.kind == Schedule::kCluster) {
+    const bool enc = plan->tmap_ptr != data;
+    cudaError_t e = launch_cluster(plan->n, data, plan->batch, tw, plan->twlo[dir], plan->twhi[dir], dsign,
+                                   plan->tables.err, plan->num_sms, st, &plan->fmaps.load0, &plan->fmaps.store0, enc);
+    if (e == cudaSuccess) plan->tmap_ptr = data;
+    return cuda_status(e, "cluster launch");
+  }
   if (s.kind == Schedule::kResident) {
     const bool enc = plan->tmap_ptr != data;
     cudaError_t e = launch_resident(plan->n, data, plan->batch, tw, plan->twlo[dir], plan->twhi[dir], dsign,
@@ -959,7 +966,25 @@ tcfftStatus tcfftPlan1d(tcfftPlan* out, int64_t n, int64_t batch, const tcfftOpt
   p->sched = s;
   p->radices_x = chain;
   st = alloc_tables(p);
-  if (st == TCFFT_SUCCESS && (s.kind == Schedule::kFused1d || s.kind == Schedule::kFused2d)) st = alloc_fused(p);
+  const char* cl_env = getenv("TCFFT_CLUSTER");
+  if (st == TCFFT_SUCCESS && s.kind == Schedule::kFused1d && cl_env && atoi(cl_env) != 0 &&
+      cluster_supported(n, o.precision == TCFFT_PRECISION_SPLIT, p->num_sms)) {
+    // opt-in: clusters of N / 2^14 CTAs, one transform per cluster, no L2 round trip.  Correct at
+    // N = 2^15..2^18 but slower than the two-phase kernel above 2^15 (remote shared-memory loads
+    // and the cluster-wide barrier between the phases), so the planner does not pick it by itself.
+    p->sched = Schedule();
+    p->sched.kind = Schedule::kCluster;
+    p->sched.N1 = 256;
+    p->sched.N2 = n / 256;
+    p->sched.launches = 1;
+    char buf[160];
+    snprintf(buf, sizeof buf, "cluster(plain): N=256 x %lld on %lld CTAs sharing shared memory, one HBM pass",
+             (long long)(n / 256), (long long)(n >> 14));
+    p->sched.text = buf;
+    st = alloc_wn_tables(p, n);
+  }
+  if (st == TCFFT_SUCCESS && (p->sched.kind == Schedule::kFused1d || p->sched.kind == Schedule::kFused2d))
+    st = alloc_fused(p);
   if (st == TCFFT_SUCCESS && s.kind == Schedule::kLarge1d) st = setup_large1d(p);
   if (st == TCFFT_SUCCESS && s.kind == Schedule::kFourStep) st = setup_fourstep(p);
   if (st == TCFFT_SUCCESS && s.kind == Schedule::kResident) st = alloc_wn_tables(p, n);

@@ -66,6 +66,12 @@ cudaError_t launch_resident(int64_t n, void* data, int64_t batch, const float2* 
                             const float2* twhi, float dsign, int* err, int num_sms, cudaStream_t st,
                             CUtensorMap* lm, CUtensorMap* sm, bool encode);
 
+// One transform per thread-block cluster, N = 2^15..2^18 plain (fft_cluster.cu).
+bool cluster_supported(int64_t n, bool split, int num_sms);
+cudaError_t launch_cluster(int64_t n, void* data, int64_t batch, const float2* tw2048, const float2* twlo,
+                           const float2* twhi, float dsign, int* err, int num_sms, cudaStream_t st, CUtensorMap* lm,
+                           CUtensorMap* sm, bool encode);
+
 // Launch entry points implemented in the kernel translation units. Each
 // returns cudaSuccess or the launch error.
 cudaError_t launch_small(int R, bool split, const CUtensorMap& tmap, int64_t total_elems, const float2* tw,

@@ -19,7 +19,8 @@ struct Schedule {
   //   W_N twiddle, rows of N2, transpose (the split precision at N = 2048).
   enum Kind {
     kNone = 0, kSmall = 1, kFused1d = 2, kFused2d = 3, kTiny = 4, kLarge1d = 5, kGeneric2d = 6, kFourStep = 7,
-    kResident = 8  // N = 4096..16384 plain: whole transforms in one CTA's shared memory (fft_resident.cu)
+    kResident = 8,  // N = 4096..16384 plain: whole transforms in one CTA's shared memory (fft_resident.cu)
+    kCluster = 9    // N = 2^15..2^18 plain: one transform per thread-block cluster (fft_cluster.cu)
   } kind = kNone;
   int R = 1;             // small: N = 256 R
   int64_t N1 = 0, N2 = 0;  // fused 1D: N = N1 N2 (phase 0 columns of N1, phase 1 rows of N2)

@@ -145,3 +145,21 @@ def test_split_fourstep(cuda_device, n):
     with tc.Plan(nx=256, ny=2048, batch=1, precision="split") as p:
         y2 = run_gpu(p, x2, "split")
     assert oracle.rel_l2(y2, oracle_2d(x2)) < TOL_SPLIT
+
+
+@pytest.mark.parametrize("n", [1 << 15, 1 << 16, 1 << 17, 1 << 18])
+def test_cluster_opt_in(cuda_device, monkeypatch, n):
+    """The thread-block-cluster kernel (one transform per cluster of N / 2^14
+    CTAs, phases exchanged through distributed shared memory), selected with
+    TCFFT_CLUSTER=1 where the device can co-schedule the cluster."""
+    monkeypatch.setenv("TCFFT_CLUSTER", "1")
+    batch = 5
+    xq = quantize(uniform_input((batch, n), seed=n % 97), "plain")
+    with tc.Plan(n=n, batch=batch) as p:
+        sched = p.info["schedule"]
+        y = run_gpu(p, xq, "plain")
+        ya = run_gpu(p, xq, "plain", adjoint=True)
+    if not sched.startswith("cluster"):
+        pytest.skip("cluster of %d CTAs not schedulable here: %s" % (n >> 14, sched))
+    assert oracle.rel_l2(y, oracle_1d(xq)) < TOL_PLAIN
+    assert oracle.rel_l2(ya, oracle_1d(xq, adjoint=True)) < TOL_PLAIN
