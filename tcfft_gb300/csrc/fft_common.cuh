@@ -169,6 +169,10 @@ __device__ __forceinline__ void sts32(uint32_t addr, uint32_t v) {
 __device__ __forceinline__ void lds64(uint32_t addr, uint32_t& a, uint32_t& b) {
   asm volatile("ld.shared.v2.b32 {%0, %1}, [%2];" : "=r"(a), "=r"(b) : "r"(addr) : "memory");
 }
+__device__ __forceinline__ void lds128(uint32_t addr, uint32_t (&w)[4]) {
+  asm volatile("ld.shared.v4.b32 {%0, %1, %2, %3}, [%4];" : "=r"(w[0]), "=r"(w[1]), "=r"(w[2]), "=r"(w[3]) : "r"(addr)
+               : "memory");
+}
 __device__ __forceinline__ void lds128f(uint32_t addr, float2& a, float2& b) {
   asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];" : "=f"(a.x), "=f"(a.y), "=f"(b.x), "=f"(b.y) : "r"(addr)
                : "memory");

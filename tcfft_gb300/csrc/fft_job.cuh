@@ -422,4 +422,55 @@ __device__ __forceinline__ void fft16r_job(const JobConsts<SPLIT>& c, uint32_t t
   }
 }
 
+// fft16r_job (plain precision) with each lane's inputs read as 16-byte quads:
+// with PI = BitPerm<0, 2, 3, 1> the slots (kt, r) of lane t are the points
+// m1 = 4t + r + 2kt, i.e. the four consecutive points 4t .. 4t + 3 (the word
+// r + 2kt of the quad).  LOAD4(v, a, w) fills w[0..3] with the half2 words of
+// points 16a + 4t .. 16a + 4t + 3 of transform v.  STORE as in fft16r_job.
+template <int R, int TWS, class PI, class RHO, class Load4F, class StoreF>
+__device__ __forceinline__ void fft16r_job_q(const JobConsts<false>& c, uint32_t tw16R, float dsign, Load4F&& load4,
+                                             StoreF&& store) {
+  static_assert(PI::apply(1) == 1 && PI::apply(2) == 4 && PI::apply(4) == 8 && PI::apply(8) == 2,
+                "quad loads need PI = BitPerm<0, 2, 3, 1>");
+  const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+  uint32_t bhi[R][2][2][2];
+#pragma unroll
+  for (int j = 0; j < 2; ++j) {
+    uint32_t w[R][4];
+#pragma unroll
+    for (int a = 0; a < R; ++a) load4(g + 8 * j, a, w[a]);
+#pragma unroll
+    for (int kt = 0; kt < 2; ++kt)
+#pragma unroll
+      for (int r = 0; r < 2; ++r) {
+        if constexpr (R == 1) {
+          bhi[0][kt][r][j] = w[0][r + 2 * kt];
+        } else {
+          const int m1 = 4 * t + r + 2 * kt;
+          float2 x[R];
+#pragma unroll
+          for (int a = 0; a < R; ++a) x[a] = unpack_h2(w[a][r + 2 * kt]);
+          dft_small<R>(x, dsign);
+#pragma unroll
+          for (int q = 1; q < R; ++q) x[q] = cmul(x[q], lds64f(tw16R + ((m1 * q) & (16 * R - 1)) * TWS * 8));
+#pragma unroll
+          for (int q = 0; q < R; ++q) bhi[q][kt][r][j] = pack_h2(x[q].x, x[q].y);
+        }
+      }
+  }
+  __syncwarp();
+#pragma unroll
+  for (int q = 0; q < R; ++q) {
+    float acc[2][2][4];
+    dft16_mma(c.afr, bhi[q], acc);
+#pragma unroll
+    for (int j = 0; j < 2; ++j)
+#pragma unroll
+      for (int h = 0; h < 2; ++h)
+#pragma unroll
+        for (int e = 0; e < 2; ++e) store(2 * t + e + 8 * j, q + R * RHO::apply(g + 8 * h), q, 4 * j + 2 * h + e,
+                                          acc_get(acc, j, h, e));
+  }
+}
+
 }  // namespace tcfft

@@ -13,9 +13,16 @@
 //           C <= 32 columns);
 //   phase 0: 256-point column FFTs (plain_col_tile) times W_N^(n2 k1);
 //   phase 1: N2-point FFTs of the 256 rows k1, 16 rows per warp job
-//           (fft16r_job), results held in registers;
-//   output: after a barrier, X[k1 + 256 k2] written in natural order into the
-//           stage and stored with a 2D TMA box of 128-byte rows.
+//           (fft16r_job_q, 16-byte loads), results held in registers;
+//   output: after a barrier, X[k1 + 256 k2] written into the stage in a
+//           digit order of (k1, k2) and stored with one 5D TMA box per stage.
+//
+// Bank conflicts (the former natural-order write-back hit one bank 8 times
+// per instruction): a job's 16 rows are the k1 of one 16-aligned group with
+// the row digits permuted (kap_of) so that the two rows a quarter-warp reads
+// sit in different halves of the 128-byte bank window, and the lanes of one
+// output store differ in k1 bits 0-1 (one 16-byte chunk) and in the k2 bits
+// that select the stage row's swizzle phase (8 different chunks).
 #include <mutex>
 
 #include "fft_fused.cuh"
@@ -40,10 +47,23 @@ struct ResCfg {
   static constexpr int kTabBytes = (kTwLo + kTwHi + kN2) * 8 + FoldTab<1>::kBytes;
   static constexpr int kSmem = kStages * kStageBytes + kTabBytes + 1024 + 256;
   static constexpr int kThreads = 384;
-  using PI = BitPerm<0, 1, 3, 2>;
+  static constexpr int kL = R1 == 1 ? 0 : (R1 == 2 ? 1 : 2);  // log2 R1
+  using PI = BitPerm<0, 1, 3, 2>;   // phase 0 (column jobs)
+  using PI1 = BitPerm<0, 2, 3, 1>;  // phase 1: lane t reads points 4t .. 4t + 3
   using RHO = BitPerm<0, 2, 3, 1>;
   static_assert(kT >= 1 && kT * kN * 4 == kStageBytes, "a stage holds whole transforms");
 };
+
+// Row k1 of transform-row v (0..15) in phase-1 job jl (0..15): a bit permutation
+// of k1 = 16 jl + v.  v bit 0 goes to the k1 bit that makes the tile rows of
+// v and v + 1 differ in the bank half (tile row bit 0 for 64-byte rows, bit 2
+// for 128-byte rows); v bits 1-2 go to k1 bits 0-1 (the output chunk).
+template <int C>
+__device__ __forceinline__ int kap_of(int v, int jl) {
+  const int v0 = v & 1, v1 = (v >> 1) & 1, v2 = (v >> 2) & 1, v3 = (v >> 3) & 1;
+  if constexpr (C == 16) return v1 | (v2 << 1) | (v0 << 2) | (v3 << 3) | (jl << 4);
+  else return v1 | (v2 << 1) | ((jl & 1) << 2) | (v3 << 3) | (v0 << 4) | ((jl >> 1) << 5);
+}
 
 struct ResParams {
   const float2* tw2048;
@@ -60,8 +80,9 @@ __global__ void __launch_bounds__(384, 1) fft_resident_kernel(const __grid_const
                                                                const ResParams p) {
   using Cfg = ResCfg<R1>;
   using PI = typename Cfg::PI;
+  using PI1 = typename Cfg::PI1;
   using RHO = typename Cfg::RHO;
-  constexpr int NST = Cfg::kStages, T = Cfg::kT, CG = Cfg::kCG, C = Cfg::kC, N = Cfg::kN;
+  constexpr int NST = Cfg::kStages, T = Cfg::kT, CG = Cfg::kCG, C = Cfg::kC, L = Cfg::kL;
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* smem =
       reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
@@ -120,10 +141,7 @@ __global__ void __launch_bounds__(384, 1) fft_resident_kernel(const __grid_const
         const int s = cnt % NST;
         if (!mbar_wait(&computed[s], (cnt / NST) & 1, p.err)) break;
         const unsigned char* src = smem + s * Cfg::kStageBytes;
-        const int row0 = (int)(it * (Cfg::kStageBytes / 128));
-#pragma unroll 1
-        for (int b = 0; b < Cfg::kStageBytes / (256 * 128); ++b)
-          tma_store_2d(&store_map, 0, row0 + 256 * b, src + b * 256 * 128);
+        tma_store_5d(&store_map, 0, 0, (int)(4 * T * it), 0, 0, src);
         bulk_commit();
         bulk_wait_read<0>();
         mbar_arrive(&empty[s]);
@@ -135,8 +153,9 @@ __global__ void __launch_bounds__(384, 1) fft_resident_kernel(const __grid_const
 
   // ------------------------------------------------------------------ compute warps
   asm volatile("setmaxnreg.inc.sync.aligned.u32 %0;" ::"n"(224));
-  JobConsts<false> jc;
+  JobConsts<false> jc, jc1;
   init_job_consts<false, PI, RHO>(jc, p.tw2048);
+  init_job_consts<false, PI1, RHO>(jc1, p.tw2048);
   const uint32_t fold = smem_addr(s_fold), tw16 = smem_addr(s_tw16);
   WnTable wn;
   wn.hi = smem_addr(s_twhi);
@@ -145,7 +164,7 @@ __global__ void __launch_bounds__(384, 1) fft_resident_kernel(const __grid_const
   wn.glo = p.twlo;
   wn.global = false;
   wn.shift = Cfg::kTwShift;
-  wn.nmask = N - 1;
+  wn.nmask = Cfg::kN - 1;
   const int g = lane >> 2, tq = lane & 3;
   int cnt = 0;
   for (long long it = blockIdx.x; it < tiles; it += gridDim.x, ++cnt) {
@@ -164,28 +183,32 @@ __global__ void __launch_bounds__(384, 1) fft_resident_kernel(const __grid_const
       uint32_t out[JOBS][8 * R1];
 #pragma unroll
       for (int i = 0; i < JOBS; ++i) {
-        const int job = warp + 8 * i, t = job >> 4, k1base = (job & 15) * 16;
+        const int job = warp + 8 * i, t = job >> 4, jl = job & 15;
         const uint32_t tbase = base + t * (CG * Cfg::kTileBytes);
-        auto ld = [&](int v, int n) {
-          const uint32_t a = tbase + (n / C) * Cfg::kTileBytes + ctile_off<C, 4>(col_out_row(k1base + v, 0), n % C);
-          return unpack_h2(lds32(a));
+        auto ld4 = [&](int v, int a, uint32_t(&w)[4]) {
+          const int n = 4 * tq + 16 * a;
+          lds128(tbase + (n / C) * Cfg::kTileBytes + ctile_off<C, 4>(col_out_row(kap_of<C>(v, jl), 0), n % C), w);
         };
         auto st = [&](int, int, int q, int slot, float2 val) { out[i][8 * q + slot] = pack_h2(val.x, val.y); };
-        fft16r_job<R1, false, 1, PI, RHO>(jc, tw16, p.dsign, ld, st);
+        fft16r_job_q<R1, 1, PI1, RHO>(jc1, tw16, p.dsign, ld4, st);
       }
       named_bar_sync(1, 256);  // every warp has read the stage
-      // natural order X[k1 + 256 k2] of transform t at element t N + k1 + 256 k2 (128B-swizzled rows)
+      // X[k1 + 256 k2] of transform t at stage row rho (128-byte rows of 32 k1, 128B swizzle):
+      // rho = k2 bit L | (k2 bits L+2..L+3, t) << 1 | k2 bit L+1 << (3 + log2 T) |
+      //       (k1 >> 5 | (k2 & (R1 - 1)) << 3) << (4 + log2 T); the store box has these digits as dims
 #pragma unroll
       for (int i = 0; i < JOBS; ++i) {
-        const int job = warp + 8 * i, t = job >> 4, k1base = (job & 15) * 16;
+        const int job = warp + 8 * i, t = job >> 4, jl = job & 15;
 #pragma unroll
         for (int q = 0; q < R1; ++q)
 #pragma unroll
           for (int slot = 0; slot < 8; ++slot) {
             const int jj = slot >> 2, h = (slot >> 1) & 1, e = slot & 1;
-            const int v = 2 * tq + e + 8 * jj, k = q + R1 * RHO::apply(g + 8 * h);
-            const uint32_t el = (uint32_t)(t * N + k1base + v + 256 * k);
-            sts32(base + swz_w<4>(el) * 4, out[i][8 * q + slot]);
+            const int kap = kap_of<C>(2 * tq + e + 8 * jj, jl), k2 = q + R1 * RHO::apply(g + 8 * h);
+            const int rho = ((k2 >> L) & 1) +
+                            2 * ((((k2 >> (L + 2)) & 3) + 4 * t) +
+                                 4 * T * (((k2 >> (L + 1)) & 1) + 2 * ((kap >> 5) + 8 * (k2 & (R1 - 1)))));
+            sts32(base + swz_w<4>((uint32_t)((kap & 31) + 32 * rho)) * 4, out[i][8 * q + slot]);
           }
       }
     }
@@ -215,7 +238,10 @@ cudaError_t launch_resident_t(const CUtensorMap& lm, const CUtensorMap& sm, cons
 
 bool resident_supported(int64_t n, bool split) { return !split && (n == 4096 || n == 8192 || n == 16384); }
 
-// Tensor maps: column-tile loads of the [B*256 rows][N2 cols] view and 128-byte-row stores.
+// Tensor maps: column-tile loads of the [B*256 rows][N2 cols] view; stores of
+// X[k1 + 256 k2] as a 5D box with dims (k1 bits 0-4, k2 bit L, k2 bits L+2..L+3
+// together with the transform index, k2 bit L+1, k1 bits 5-7 together with
+// k2 bits 0..L-1), L = log2(N2 / 16), matching the stage layout above.
 cudaError_t launch_resident(int64_t n, void* data, int64_t batch, const float2* tw2048, const float2* twlo,
                             const float2* twhi, float dsign, int* err, int num_sms, cudaStream_t st,
                             CUtensorMap* lm, CUtensorMap* sm, bool encode) {
@@ -224,10 +250,12 @@ cudaError_t launch_resident(int64_t n, void* data, int64_t batch, const float2* 
   if (encode) {
     if (encode_col_load(lm, CU_TENSOR_MAP_DATA_TYPE_UINT32, data, n2, batch, 4, C, 1) != CUDA_SUCCESS)
       return cudaErrorInvalidValue;
-    uint64_t dims[2] = {32, (uint64_t)(n * batch / 32)};
-    uint64_t str[1] = {128};
-    uint32_t box[2] = {32, 256};
-    if (encode_tmap(sm, CU_TENSOR_MAP_DATA_TYPE_UINT32, 2, data, dims, str, box, CU_TENSOR_MAP_SWIZZLE_128B) !=
+    const uint64_t r1 = (uint64_t)(n2 / 16), row = 256 * 4;  // R1; bytes per k2 step
+    const uint32_t T = (uint32_t)(4 / r1);                    // transforms per stage
+    uint64_t dims[5] = {32, 2, (uint64_t)(4 * batch), 2, 8 * r1};
+    uint64_t str[4] = {row * r1, row * r1 * 4, row * r1 * 2, 128};
+    uint32_t box[5] = {32, 2, 4 * T, 2, (uint32_t)(8 * r1)};
+    if (encode_tmap(sm, CU_TENSOR_MAP_DATA_TYPE_UINT32, 5, data, dims, str, box, CU_TENSOR_MAP_SWIZZLE_128B) !=
         CUDA_SUCCESS)
       return cudaErrorInvalidValue;
   }
