@@ -268,6 +268,12 @@ __device__ __forceinline__ void plain_row_jobs(const JobConsts<false>& jc, uint3
   fft256r_jobs_fold<R, JN, false>(jc, fold, dsign, ld, st);
 }
 
+// Tiles per work item of a 1D row-transpose schedule: as many tiles as fill a
+// 64 KiB stage (at most 4); other schedules move one tile per item.
+__host__ __device__ constexpr int fused_sub_of(bool sub_ok, int tile_bytes) {
+  return !sub_ok || tile_bytes >= 65536 ? 1 : (65536 / tile_bytes > 4 ? 4 : 65536 / tile_bytes);
+}
+
 template <int ROLE0, int R0, int C0, int ROLE1, int R1, int C1, bool SPLIT>
 struct FusedCfg {
   static constexpr int kES = SPLIT ? 8 : 4;
@@ -276,7 +282,15 @@ struct FusedCfg {
   static constexpr int kLen0 = role_len(ROLE0, R0), kLen1 = role_len(ROLE1, R1);  // FFT lengths
   static constexpr int kTile0 = C0 * kLen0;  // elements per tile
   static constexpr int kTile1 = C1 * kLen1;
-  static constexpr int kTileMax = kTile0 > kTile1 ? kTile0 : kTile1;
+  // 1D row-transpose schedules move up to 4 tiles per work item (kSub0/kSub1),
+  // so that every item fills a 64 KiB stage: fewer, larger TMA transactions and
+  // fewer per-item waits for tiles smaller than a stage (host T0/T1 count tiles;
+  // the launcher passes items)
+  static constexpr bool kSubOK = k1D && ROLE1 == kRoleRowT;
+  static constexpr int kSub0 = fused_sub_of(kSubOK, kTile0 * kES);
+  static constexpr int kSub1 = fused_sub_of(kSubOK, kTile1 * kES);
+  static constexpr int kItem0 = kSub0 * kTile0, kItem1 = kSub1 * kTile1;  // elements per work item
+  static constexpr int kTileMax = kItem0 > kItem1 ? kItem0 : kItem1;
   static constexpr int kStageBytes = kTileMax * kES;
   // shared-memory tables: W_L^j (L = the longer job length; the fp32 job paths),
   // the two halves of W_N^j (1D four-step, N = kLen0 * kLen1) and the per-lane
@@ -411,10 +425,13 @@ __global__ void __launch_bounds__(384, 1)  // 12 warps at launch: 168 registers 
         if (it.phase == 1) fence_proxy_async_global();
         unsigned char* dst = smem + s * Cfg::kStageBytes;
         if (it.phase == 0) {
-          mbar_arrive_expect_tx(&full[s], Cfg::kTile0 * ES);
-          if constexpr (ROLE0 == kRoleCol) {  // one 5D box: rows in the column-tile digit order
-            const int cg = it.tile % p.cols0;
-            tma_load_5d(dst, &maps.load0, cg * C0, 0, 0, 0, it.b * R0, &full[s]);
+          mbar_arrive_expect_tx(&full[s], Cfg::kItem0 * ES);
+          if constexpr (ROLE0 == kRoleCol) {  // 5D boxes: rows in the column-tile digit order
+#pragma unroll 1
+            for (int u = 0; u < Cfg::kSub0; ++u) {
+              const int cg = (it.tile * Cfg::kSub0 + u) % p.cols0;
+              tma_load_5d(dst + u * (Cfg::kTile0 * ES), &maps.load0, cg * C0, 0, 0, 0, it.b * R0, &full[s]);
+            }
           } else {  // contiguous rows
             const int y0 = (int)(((long long)it.b * p.rows0 + (long long)it.tile * C0) * (256 * R0) / ER);
 #pragma unroll 1
@@ -422,16 +439,16 @@ __global__ void __launch_bounds__(384, 1)  // 12 warps at launch: 168 registers 
               tma_load_2d(dst + i * (ER * Cfg::kBH0 * ES), &maps.load0, 0, y0 + Cfg::kBH0 * i, &full[s]);
           }
         } else {
-          mbar_arrive_expect_tx(&full[s], Cfg::kTile1 * ES);
+          mbar_arrive_expect_tx(&full[s], Cfg::kItem1 * ES);
           if constexpr (ROLE1 == kRoleCol) {
             const int cg = it.tile % p.cols1;
             tma_load_5d(dst, &maps.load1, cg * C1, 0, 0, 0, it.b * R1, &full[s]);
           } else {
             // 1D: source is the scratch slot; 2D never has a contiguous phase 1
-            const long long row0 = (long long)slot * p.rows1 + (long long)it.tile * C1;
+            const long long row0 = (long long)slot * p.rows1 + (long long)it.tile * (Cfg::kSub1 * C1);
             const int y0 = (int)(row0 * Cfg::kLen1 / ER);
 #pragma unroll 1
-            for (int i = 0; i < Cfg::kTile1 / (ER * Cfg::kBH1); ++i)
+            for (int i = 0; i < Cfg::kItem1 / (ER * Cfg::kBH1); ++i)
               tma_load_2d(dst + i * (ER * Cfg::kBH1 * ES), &maps.load1, 0, y0 + Cfg::kBH1 * i, &full[s]);
           }
         }
@@ -483,8 +500,12 @@ __global__ void __launch_bounds__(384, 1)  // 12 warps at launch: 168 registers 
         if (it.phase == 0) {
           if constexpr (ROLE0 == kRoleCol) {
             // 5D box [C0][k0 hi][k1 (+16 transform)][k0 lo][q]: 1D -> scratch slot, 2D -> the data
-            const int cg = it.tile % p.cols0;
-            tma_store_5d(&maps.store0, cg * C0, 0, 16 * (Cfg::k1D ? slot : it.b), 0, 0, src);
+#pragma unroll 1
+            for (int u = 0; u < Cfg::kSub0; ++u) {
+              const int cg = (it.tile * Cfg::kSub0 + u) % p.cols0;
+              tma_store_5d(&maps.store0, cg * C0, 0, 16 * (Cfg::k1D ? slot : it.b), 0, 0,
+                           src + u * (Cfg::kTile0 * ES));
+            }
           } else {
             const int y0 = (int)(((long long)it.b * p.rows0 + (long long)it.tile * C0) * (256 * R0) / ER);
 #pragma unroll 1
@@ -496,7 +517,10 @@ __global__ void __launch_bounds__(384, 1)  // 12 warps at launch: 168 registers 
             const int cg = it.tile % p.cols1;
             tma_store_5d(&maps.store1, cg * C1, 0, 16 * it.b, 0, 0, src);
           } else if constexpr (ROLE1 == kRoleRowT) {  // output columns k1 of data viewed [B][N2 rows k2][N1 cols]
-            tma_store_5d(&maps.store1, it.tile * C1, 0, 16 * it.b, 0, 0, src);
+#pragma unroll 1
+            for (int u = 0; u < Cfg::kSub1; ++u)
+              tma_store_5d(&maps.store1, (it.tile * Cfg::kSub1 + u) * C1, 0, 16 * it.b, 0, 0,
+                           src + u * (Cfg::kTile1 * ES));
           } else {  // kRoleRow16T: C1 columns as boxes of kBW, 4D [cols][k0][q][B]
 #pragma unroll 1
             for (int bx = 0; bx < C1 / Cfg::kBW; ++bx)
@@ -552,23 +576,29 @@ __global__ void __launch_bounds__(384, 1)  // 12 warps at launch: 168 registers 
       if (ok && it.phase == 1) {
         // the tile's scratch rows are in shared memory now and never read again: drop
         // them from L2 without writing them back to HBM
-        const long long row0 = (long long)(it.b % p.S) * p.rows1 + (long long)it.tile * C1;
+        const long long row0 = (long long)(it.b % p.S) * p.rows1 + (long long)it.tile * (Cfg::kSub1 * C1);
         const unsigned char* src = p.scratch + row0 * Cfg::kLen1 * ES;
-        for (int i = threadIdx.x; i < Cfg::kTile1 * ES / 128; i += 256)
+        for (int i = threadIdx.x; i < Cfg::kItem1 * ES / 128; i += 256)
           asm volatile("discard.global.L2 [%0], 128;" ::"l"(src + i * 128) : "memory");
       }
     }
     if (ok) {
       if (it.phase == 0) {
         if constexpr (ROLE0 == kRoleCol && !SPLIT) {
-          plain_col_tile<R0, C0, Cfg::k1D, PI, RHO>(jc, fold0, base, warp, p.dsign, (it.tile % p.cols0) * C0, wn);
+#pragma unroll 1
+          for (int u = 0; u < Cfg::kSub0; ++u)
+            plain_col_tile<R0, C0, Cfg::k1D, PI, RHO>(jc, fold0, base + u * (Cfg::kTile0 * ES), warp, p.dsign,
+                                                      ((it.tile * Cfg::kSub0 + u) % p.cols0) * C0, wn);
         } else if constexpr (ROLE0 == kRoleCol) {
+#pragma unroll 1
+         for (int u = 0; u < Cfg::kSub0; ++u) {
+          const uint32_t base = smem_addr(smem + s * Cfg::kStageBytes) + u * (Cfg::kTile0 * ES);
           // columns JN*warp + jn in place (side by side, moved in pairs); 1D adds the
           // four-step twiddle W_N^(n2 k1)
           constexpr int JN = C0 / 8;
           constexpr bool PAIR = JN % 2 == 0;
           constexpr int TWS = Cfg::kLmax / (256 * R0);
-          const int cg = it.tile % p.cols0;
+          const int cg = (it.tile * Cfg::kSub0 + u) % p.cols0;
           const int col0 = JN * warp;
           auto ld = [&](int jn, int n) { return lds_elem<SPLIT>(base + ctile_off<C0, ES>(col_in_row(n), col0 + jn)); };
           auto ldp = [&](int jp, int n, float2& x0, float2& x1) {
@@ -612,6 +642,7 @@ __global__ void __launch_bounds__(384, 1)  // 12 warps at launch: 168 registers 
               fft256r_jobs<R0, SPLIT, TWS, JN>(jc, twR, p.dsign, ld, st);
             }
           }
+         }
         } else {  // kRoleRow: contiguous rows j = warp + 8 jn in place (2D phase 0)
           constexpr int JN = C0 / 8;
           auto rowb = [&](int jn) { return base + (uint32_t)((warp + 8 * jn) * 256 * R0 * ES); };
@@ -711,6 +742,9 @@ __global__ void __launch_bounds__(384, 1)  // 12 warps at launch: 168 registers 
           constexpr uint32_t kRow = 256 * R1 * ES;   // bytes per input row
           constexpr uint32_t kStep = 256 * C1 * ES;  // output tile: one q further down
           const int row0 = JN * warp;                // output columns row0 + jn sit side by side
+#pragma unroll 1
+         for (int u = 0; u < Cfg::kSub1; ++u) {       // the item's tiles, one after the other
+          const uint32_t base = smem_addr(smem + s * Cfg::kStageBytes) + u * (Cfg::kTile1 * ES);
           Hold out[JN][R1][8];
           if constexpr (!SPLIT) {
             plain_row_jobs<R1, JN, PI, RHO>(jc, fold1, base + row0 * kRow, kRow, p.dsign, out);
@@ -742,6 +776,7 @@ __global__ void __launch_bounds__(384, 1)  // 12 warps at launch: 168 registers 
               }
             }
           }
+         }
         }
       }
     }
