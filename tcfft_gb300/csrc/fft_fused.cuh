@@ -196,6 +196,7 @@ __device__ __forceinline__ void plain_col_tile(const JobConsts<false>& jc, uint3
                                                float dsign, int n2base, const WnTable& wn) {
   constexpr int ES = 4, JN = C / 8;
   constexpr bool PAIR = JN % 2 == 0;
+  constexpr bool QUAD = JN == 4;  // 128-byte rows: the four columns move as one 16-byte access
   constexpr uint32_t kStep = 256 * C * ES;  // one digit a (input) or q (output) further down
   const int col0 = JN * warp;
   uint32_t lo[8], so[8];
@@ -225,7 +226,25 @@ __device__ __forceinline__ void plain_col_tile(const JobConsts<false>& jc, uint3
 #pragma unroll
       for (int q = 2; q < R; ++q) fq[jn][q] = cmul(fq[jn][q - 1], fq[jn][1]);
     }
-    if constexpr (PAIR) {
+    if constexpr (QUAD) {
+      auto ld = [&](int, int sl, int a, uint32_t& x0, uint32_t& x1, uint32_t& x2, uint32_t& x3) {
+        uint32_t w[4];
+        lds128(lo[sl] + a * kStep, w);
+        x0 = w[0];
+        x1 = w[1];
+        x2 = w[2];
+        x3 = w[3];
+      };
+      auto st = [&](int, int osl, int q, float2 v0, float2 v1, float2 v2, float2 v3) {
+        v0 = cmul(v0, cmul(fk[0][osl], fq[0][q]));
+        v1 = cmul(v1, cmul(fk[1][osl], fq[1][q]));
+        v2 = cmul(v2, cmul(fk[2][osl], fq[2][q]));
+        v3 = cmul(v3, cmul(fk[3][osl], fq[3][q]));
+        sts128(so[osl] + q * kStep, pack_h2(v0.x, v0.y), pack_h2(v1.x, v1.y), pack_h2(v2.x, v2.y),
+               pack_h2(v3.x, v3.y));
+      };
+      fft256r_jobs_fold_quad<R>(jc, fold, dsign, ld, st);
+    } else if constexpr (PAIR) {
       auto ld = [&](int jp, int sl, int a, uint32_t& x0, uint32_t& x1) { lds64(lo[sl] + jp * ES + a * kStep, x0, x1); };
       auto st = [&](int jp, int osl, int q, float2 v0, float2 v1) {
         v0 = cmul(v0, cmul(fk[jp][osl], fq[jp][q]));
@@ -241,7 +260,21 @@ __device__ __forceinline__ void plain_col_tile(const JobConsts<false>& jc, uint3
       fft256r_jobs_fold<R, JN, false>(jc, fold, dsign, ld, st);
     }
   } else {
-    if constexpr (PAIR) {
+    if constexpr (QUAD) {
+      auto ld = [&](int, int sl, int a, uint32_t& x0, uint32_t& x1, uint32_t& x2, uint32_t& x3) {
+        uint32_t w[4];
+        lds128(lo[sl] + a * kStep, w);
+        x0 = w[0];
+        x1 = w[1];
+        x2 = w[2];
+        x3 = w[3];
+      };
+      auto st = [&](int, int osl, int q, float2 v0, float2 v1, float2 v2, float2 v3) {
+        sts128(so[osl] + q * kStep, pack_h2(v0.x, v0.y), pack_h2(v1.x, v1.y), pack_h2(v2.x, v2.y),
+               pack_h2(v3.x, v3.y));
+      };
+      fft256r_jobs_fold_quad<R>(jc, fold, dsign, ld, st);
+    } else if constexpr (PAIR) {
       auto ld = [&](int jp, int sl, int a, uint32_t& x0, uint32_t& x1) { lds64(lo[sl] + jp * ES + a * kStep, x0, x1); };
       auto st = [&](int jp, int osl, int q, float2 v0, float2 v1) {
         sts_pair<false>(so[osl] + jp * ES + q * kStep, v0, v1);
@@ -759,7 +792,9 @@ __global__ void __launch_bounds__(384, 1)  // 12 warps at launch: 168 registers 
             const uint32_t so = base + ctile_off<C1, ES>(col_out_row(slot_kval<PI, RHO>(sl), 0), row0);
 #pragma unroll
             for (int q = 0; q < R1; ++q) {
-              if constexpr (JN % 2 == 0) {
+              if constexpr (!SPLIT && JN == 4) {  // 128-byte rows: one 16-byte store per slot
+                sts128(so + q * kStep, out[0][q][sl], out[1][q][sl], out[2][q][sl], out[3][q][sl]);
+              } else if constexpr (JN % 2 == 0) {
 #pragma unroll
                 for (int jp = 0; jp < JN; jp += 2) {
                   const uint32_t addr = so + jp * ES + q * kStep;

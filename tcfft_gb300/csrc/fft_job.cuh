@@ -252,10 +252,13 @@ __device__ void build_fold_table(unsigned char* tab, const float2* __restrict__ 
 // job jn (osl = 4h + 2e + hh, kval = RHO(2t + e + 8h) + 16 RHO(g + 8hh)); with
 // PAIR, STORE(jp, osl, q, v0, v1).  All loads precede the first store.
 // tab: shared-memory address of this R's fold table.
-template <int R, int JN, bool PAIR, class LoadF, class StoreF>
-__device__ __forceinline__ void fft256r_jobs_fold(const JobConsts<false>& c, uint32_t tab, float dsign, LoadF&& load,
-                                                  StoreF&& store) {
+// QUAD (JN = 4, with PAIR): the four jobs' elements of one slot move together,
+// LOAD(0, slot, a, x0, x1, x2, x3) and STORE(0, osl, q, v0, v1, v2, v3).
+template <int R, int JN, bool PAIR, class LoadF, class StoreF, bool QUAD = false>
+__device__ __forceinline__ void fft256r_jobs_fold_impl(const JobConsts<false>& c, uint32_t tab, float dsign,
+                                                       LoadF&& load, StoreF&& store) {
   static_assert(!PAIR || JN % 2 == 0, "paired jobs come in twos");
+  static_assert(!QUAD || (PAIR && JN == 4), "quads are four paired jobs");
   const uint32_t lane4 = (threadIdx.x & 31) * 4;
   const uint32_t negmask = dsign > 0.f ? 0x80000000u : 0x00008000u;
   const uint32_t c8 = pack_h2(0.70710678118654752440f, 0.70710678118654752440f);
@@ -270,7 +273,9 @@ __device__ __forceinline__ void fft256r_jobs_fold(const JobConsts<false>& c, uin
         uint32_t x[JN][R];
 #pragma unroll
         for (int a = 0; a < R; ++a) {
-          if constexpr (PAIR) {
+          if constexpr (QUAD) {
+            load(0, slot, a, x[0][a], x[1][a], x[2][a], x[3][a]);
+          } else if constexpr (PAIR) {
 #pragma unroll
             for (int jp = 0; jp < JN; jp += 2) load(jp, slot, a, x[jp][a], x[jp + 1][a]);
           } else {
@@ -324,7 +329,10 @@ __device__ __forceinline__ void fft256r_jobs_fold(const JobConsts<false>& c, uin
 #pragma unroll
         for (int hh = 0; hh < 2; ++hh) {
           const int osl = 4 * h + 2 * e + hh;
-          if constexpr (PAIR) {
+          if constexpr (QUAD) {
+            store(0, osl, q, acc_get(acc[0], h, hh, e), acc_get(acc[1], h, hh, e), acc_get(acc[2], h, hh, e),
+                  acc_get(acc[3], h, hh, e));
+          } else if constexpr (PAIR) {
 #pragma unroll
             for (int jp = 0; jp < JN; jp += 2)
               store(jp, osl, q, acc_get(acc[jp], h, hh, e), acc_get(acc[jp + 1], h, hh, e));
@@ -334,6 +342,19 @@ __device__ __forceinline__ void fft256r_jobs_fold(const JobConsts<false>& c, uin
           }
         }
   }
+}
+
+template <int R, int JN, bool PAIR, class LoadF, class StoreF>
+__device__ __forceinline__ void fft256r_jobs_fold(const JobConsts<false>& c, uint32_t tab, float dsign, LoadF&& load,
+                                                  StoreF&& store) {
+  fft256r_jobs_fold_impl<R, JN, PAIR, LoadF, StoreF, false>(c, tab, dsign, static_cast<LoadF&&>(load),
+                                                            static_cast<StoreF&&>(store));
+}
+template <int R, class LoadF, class StoreF>
+__device__ __forceinline__ void fft256r_jobs_fold_quad(const JobConsts<false>& c, uint32_t tab, float dsign,
+                                                       LoadF&& load, StoreF&& store) {
+  fft256r_jobs_fold_impl<R, 4, true, LoadF, StoreF, true>(c, tab, dsign, static_cast<LoadF&&>(load),
+                                                          static_cast<StoreF&&>(store));
 }
 
 }  // namespace tcfft
