@@ -226,6 +226,9 @@ __device__ __forceinline__ void plain_col_tile(const JobConsts<false>& jc, uint3
 #pragma unroll
       for (int q = 2; q < R; ++q) fq[jn][q] = cmul(fq[jn][q - 1], fq[jn][1]);
     }
+    // W_N^(n2 (q + R k')) of job jn, output slot osl (q is a compile-time constant after
+    // unrolling: q = 0 needs no product)
+    auto wfac = [&](int jn, int osl, int q) { return q == 0 ? fk[jn][osl] : cmul(fk[jn][osl], fq[jn][q]); };
     if constexpr (QUAD) {
       auto ld = [&](int, int sl, int a, uint32_t& x0, uint32_t& x1, uint32_t& x2, uint32_t& x3) {
         uint32_t w[4];
@@ -236,10 +239,10 @@ __device__ __forceinline__ void plain_col_tile(const JobConsts<false>& jc, uint3
         x3 = w[3];
       };
       auto st = [&](int, int osl, int q, float2 v0, float2 v1, float2 v2, float2 v3) {
-        v0 = cmul(v0, cmul(fk[0][osl], fq[0][q]));
-        v1 = cmul(v1, cmul(fk[1][osl], fq[1][q]));
-        v2 = cmul(v2, cmul(fk[2][osl], fq[2][q]));
-        v3 = cmul(v3, cmul(fk[3][osl], fq[3][q]));
+        v0 = cmul(v0, wfac(0, osl, q));
+        v1 = cmul(v1, wfac(1, osl, q));
+        v2 = cmul(v2, wfac(2, osl, q));
+        v3 = cmul(v3, wfac(3, osl, q));
         sts128(so[osl] + q * kStep, pack_h2(v0.x, v0.y), pack_h2(v1.x, v1.y), pack_h2(v2.x, v2.y),
                pack_h2(v3.x, v3.y));
       };
@@ -247,15 +250,15 @@ __device__ __forceinline__ void plain_col_tile(const JobConsts<false>& jc, uint3
     } else if constexpr (PAIR) {
       auto ld = [&](int jp, int sl, int a, uint32_t& x0, uint32_t& x1) { lds64(lo[sl] + jp * ES + a * kStep, x0, x1); };
       auto st = [&](int jp, int osl, int q, float2 v0, float2 v1) {
-        v0 = cmul(v0, cmul(fk[jp][osl], fq[jp][q]));
-        v1 = cmul(v1, cmul(fk[jp + 1][osl], fq[jp + 1][q]));
+        v0 = cmul(v0, wfac(jp, osl, q));
+        v1 = cmul(v1, wfac(jp + 1, osl, q));
         sts_pair<false>(so[osl] + jp * ES + q * kStep, v0, v1);
       };
       fft256r_jobs_fold<R, JN, true>(jc, fold, dsign, ld, st);
     } else {
       auto ld = [&](int jn, int sl, int a) { return lds32(lo[sl] + jn * ES + a * kStep); };
       auto st = [&](int jn, int osl, int q, float2 v) {
-        sts_elem<false>(so[osl] + jn * ES + q * kStep, cmul(v, cmul(fk[jn][osl], fq[jn][q])));
+        sts_elem<false>(so[osl] + jn * ES + q * kStep, cmul(v, wfac(jn, osl, q)));
       };
       fft256r_jobs_fold<R, JN, false>(jc, fold, dsign, ld, st);
     }
