@@ -62,6 +62,7 @@ cudaError_t launch_fused_1d(const FusedKey& k, const FusedMaps& maps, const Fuse
   TCFFT_FUSED_CASE(kRoleCol, 1, 16, kRoleRow16T, 2, 128, false)
   TCFFT_FUSED_CASE(kRoleCol, 1, 16, kRoleRow16T, 4, 128, false)
   TCFFT_FUSED_CASE(kRoleCol, 1, 16, kRoleRow16T, 8, 128, false)
+  TCFFT_FUSED_CASE(kRoleCol, 2, 32, kRoleRow16T, 4, 128, false)
   TCFFT_FUSED_CASE(kRoleCol, 1, 16, kRoleRow16T, 1, 128, true)
   TCFFT_FUSED_CASE(kRoleCol, 1, 16, kRoleRow16T, 2, 128, true)
   TCFFT_FUSED_CASE(kRoleCol, 1, 16, kRoleRow16T, 4, 128, true)

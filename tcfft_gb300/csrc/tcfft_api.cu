@@ -289,24 +289,27 @@ tcfftStatus choose_1d(int64_t n, int64_t batch, int precision, Schedule& s) {
   if (lg >= 12 && lg <= 15) {
     // N = 256 x N2 with short rows N2 = 16 R1: phase 0 columns of 256, phase 1 16 rows per warp
     FusedKey k;
+    // plain 2^15: 512 x 64 (measured 1.24 ms for 2^28 elements against 1.48 ms for 256 x 128
+    // and 1.38 ms for 1024 x 32: 64 KiB column tiles and a radix-4 short-row phase)
+    const int64_t n1 = (!split && lg == 15) ? 512 : 256;
     k.role0 = kRoleCol;
-    k.R0 = 1;
-    k.C0 = 16;
+    k.R0 = (int)(n1 / 256);
+    k.C0 = n1 == 512 ? 32 : 16;
     k.role1 = kRoleRow16T;
-    k.R1 = (int)(n / 256 / 16);
+    k.R1 = (int)(n / n1 / 16);
     k.C1 = 128;
     k.split = split;
     if (split && k.R1 > 4) return TCFFT_NOT_SUPPORTED;
     s.kind = Schedule::kFused1d;
-    s.N1 = 256;
-    s.N2 = n / 256;
+    s.N1 = n1;
+    s.N2 = n / n1;
     s.key = k;
     s.T0 = (int)(s.N2 / k.C0 > 0 ? s.N2 / k.C0 : 1);
     s.T1 = (int)(s.N1 / k.C1);
     fused_lag(s.T0, s.T1, batch, s);
     s.launches = 1;
-    snprintf(buf, sizeof buf, "fused1d(%s): N=256 x %lld, phase0 columns R=1 C=16, phase1 16-row groups R=%d, lag %d, %d slots",
-             split ? "split" : "plain", (long long)s.N2, k.R1, s.D, s.S);
+    snprintf(buf, sizeof buf, "fused1d(%s): N=%lld x %lld, phase0 columns R=%d C=%d, phase1 16-row groups R=%d, lag %d, %d slots",
+             split ? "split" : "plain", (long long)s.N1, (long long)s.N2, k.R0, k.C0, k.R1, s.D, s.S);
     s.text = buf;
     return TCFFT_SUCCESS;
   }
