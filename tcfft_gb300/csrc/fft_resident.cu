@@ -65,16 +65,34 @@ __device__ __forceinline__ int kap_of(int v, int jl) {
   else return v1 | (v2 << 1) | ((jl & 1) << 2) | (v3 << 3) | (v0 << 4) | ((jl >> 1) << 5);
 }
 
+// Stage row (128-byte rows of 32 k1, 128B swizzle) of output X[k1 + 256 k2] of
+// stage transform t: rho = k2 bit L | (k2 bits L+2..L+3, t) << 1 |
+// (k2 bit L+1 | (k1 >> 5 | (k2 & (R1 - 1)) << 3) << 1) << (3 + log2 T).
+template <int R1>
+__device__ __forceinline__ int res_rho(int kap, int k2, int t) {
+  constexpr int L = ResCfg<R1>::kL, T = ResCfg<R1>::kT;
+  return ((k2 >> L) & 1) +
+         2 * ((((k2 >> (L + 2)) & 3) + 4 * t) + 4 * T * (((k2 >> (L + 1)) & 1) + 2 * ((kap >> 5) + 8 * (k2 & (R1 - 1)))));
+}
+
 struct ResParams {
   const float2* tw2048;
   const float2* twlo;
   const float2* twhi;
   long long batch;
+  long long rows;  // transposed output: transforms per matrix (the destination's row length)
   int* err;
   float dsign;
 };
 
-template <int R1>
+// TOUT (N = 4096): the output is written transposed, as dst[m][k][r] for transform
+// m * rows + r (a [rows][4096] matrix of transforms becomes the [4096][rows] matrix of
+// their outputs), out of place.  The stage's four transforms are adjacent rows r, so
+// after the natural-order write-back all compute threads re-read it as 16-byte
+// groups of 4 outputs of one transform and write 16-byte groups of one output of the
+// 4 transforms, in the layout of a 5D box (r: 4, k bits 2-4, k bits 0-1, k bits 5-11,
+// matrix): both passes one wavefront per quarter-warp.
+template <int R1, bool TOUT>
 __global__ void __launch_bounds__(384, 1) fft_resident_kernel(const __grid_constant__ CUtensorMap load_map,
                                                                const __grid_constant__ CUtensorMap store_map,
                                                                const ResParams p) {
@@ -141,7 +159,12 @@ __global__ void __launch_bounds__(384, 1) fft_resident_kernel(const __grid_const
         const int s = cnt % NST;
         if (!mbar_wait(&computed[s], (cnt / NST) & 1, p.err)) break;
         const unsigned char* src = smem + s * Cfg::kStageBytes;
-        tma_store_5d(&store_map, 0, 0, (int)(4 * T * it), 0, 0, src);
+        if constexpr (TOUT) {
+          const long long m0 = it * T;  // first transform of the stage
+          tma_store_5d(&store_map, (int)(m0 % p.rows), 0, 0, 0, (int)(m0 / p.rows), src);
+        } else {
+          tma_store_5d(&store_map, 0, 0, (int)(4 * T * it), 0, 0, src);
+        }
         bulk_commit();
         bulk_wait_read<0>();
         mbar_arrive(&empty[s]);
@@ -205,11 +228,30 @@ __global__ void __launch_bounds__(384, 1) fft_resident_kernel(const __grid_const
           for (int slot = 0; slot < 8; ++slot) {
             const int jj = slot >> 2, h = (slot >> 1) & 1, e = slot & 1;
             const int kap = kap_of<C>(2 * tq + e + 8 * jj, jl), k2 = q + R1 * RHO::apply(g + 8 * h);
-            const int rho = ((k2 >> L) & 1) +
-                            2 * ((((k2 >> (L + 2)) & 3) + 4 * t) +
-                                 4 * T * (((k2 >> (L + 1)) & 1) + 2 * ((kap >> 5) + 8 * (k2 & (R1 - 1)))));
+            const int rho = res_rho<R1>(kap, k2, t);
             sts32(base + swz_w<4>((uint32_t)((kap & 31) + 32 * rho)) * 4, out[i][8 * q + slot]);
           }
+      }
+      if constexpr (TOUT) {
+        static_assert(R1 == 1 && T == 4, "transposed output: four 4096-point transforms per stage");
+        named_bar_sync(1, 256);  // natural-order write-back complete
+        uint32_t w[4][4][4];     // [group][transform][output]
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          const int gi = threadIdx.x + 256 * i, K = 4 * (gi & 7) + 32 * (gi >> 3);
+#pragma unroll
+          for (int t = 0; t < 4; ++t)
+            lds128(base + swz_w<4>((uint32_t)((K & 31) + 32 * res_rho<1>(K & 255, K >> 8, t))) * 4, w[i][t]);
+        }
+        named_bar_sync(1, 256);  // every group read before any is overwritten
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          const int gi = threadIdx.x + 256 * i, K = 4 * (gi & 7) + 32 * (gi >> 3);
+#pragma unroll
+          for (int j = 0; j < 4; ++j)
+            sts128(base + 16 * (((K >> 2) & 7) + 8 * j + 32 * (K >> 5)), w[i][0][j], w[i][1][j], w[i][2][j],
+                   w[i][3][j]);
+        }
       }
     }
     fence_proxy_async_smem();
@@ -219,11 +261,11 @@ __global__ void __launch_bounds__(384, 1) fft_resident_kernel(const __grid_const
   }
 }
 
-template <int R1>
+template <int R1, bool TOUT = false>
 cudaError_t launch_resident_t(const CUtensorMap& lm, const CUtensorMap& sm, const ResParams& p, int num_sms,
                               cudaStream_t st) {
   using Cfg = ResCfg<R1>;
-  auto kern = fft_resident_kernel<R1>;
+  auto kern = fft_resident_kernel<R1, TOUT>;
   static std::once_flag once;
   static cudaError_t init_err = cudaSuccess;
   std::call_once(once, [&] { init_err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg::kSmem); });
@@ -264,6 +306,7 @@ cudaError_t launch_resident(int64_t n, void* data, int64_t batch, const float2* 
   p.twlo = twlo;
   p.twhi = twhi;
   p.batch = batch;
+  p.rows = 0;
   p.err = err;
   p.dsign = dsign;
   switch (n) {
@@ -272,6 +315,38 @@ cudaError_t launch_resident(int64_t n, void* data, int64_t batch, const float2* 
     case 16384: return launch_resident_t<4>(*lm, *sm, p, num_sms, st);
     default: return cudaErrorInvalidValue;
   }
+}
+
+// N = 4096 with transposed output: transform m * rows + r of `in` (batch = rows x
+// matrices) goes to out[m][k][r], k < 4096 (out of place; rows a multiple of 4).
+bool resident_tout_supported(int64_t n, int64_t batch, int64_t rows) {
+  return n == 4096 && rows >= 4 && rows % 4 == 0 && batch % rows == 0;
+}
+cudaError_t launch_resident_tout(int64_t n, const void* in, void* out, int64_t batch, int64_t rows,
+                                 const float2* tw2048, const float2* twlo, const float2* twhi, float dsign, int* err,
+                                 int num_sms, cudaStream_t st, CUtensorMap* lm, CUtensorMap* sm, bool encode) {
+  if (!resident_tout_supported(n, batch, rows)) return cudaErrorInvalidValue;
+  if (encode) {
+    if (encode_col_load(lm, CU_TENSOR_MAP_DATA_TYPE_UINT32, const_cast<void*>(in), 16, batch, 4, 16, 1) !=
+        CUDA_SUCCESS)
+      return cudaErrorInvalidValue;
+    const uint64_t rb = (uint64_t)rows * 4;  // bytes per output k
+    uint64_t dims[5] = {(uint64_t)rows, 8, 4, 128, (uint64_t)(batch / rows)};
+    uint64_t str[4] = {4 * rb, rb, 32 * rb, 4096 * rb};
+    uint32_t box[5] = {4, 8, 4, 128, 1};
+    if (encode_tmap(sm, CU_TENSOR_MAP_DATA_TYPE_UINT32, 5, out, dims, str, box, CU_TENSOR_MAP_SWIZZLE_NONE) !=
+        CUDA_SUCCESS)
+      return cudaErrorInvalidValue;
+  }
+  ResParams p;
+  p.tw2048 = tw2048;
+  p.twlo = twlo;
+  p.twhi = twhi;
+  p.batch = batch;
+  p.rows = rows;
+  p.err = err;
+  p.dsign = dsign;
+  return launch_resident_t<1, true>(*lm, *sm, p, num_sms, st);
 }
 
 }  // namespace tcfft

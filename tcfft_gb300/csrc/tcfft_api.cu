@@ -431,6 +431,18 @@ tcfftStatus validate_opts(const tcfftOptions* o) {
 
 tcfftStatus exec_many(tcfftPlanImpl* plan, void* data, cudaStream_t st, int dir);
 
+// Composite schedules whose 4096-point row pass writes its output transposed
+// (resident kernel, plain): 1D N1 x 4096 (no final transpose) and 2D axes of 4096.
+bool large1d_tout(const tcfftPlanImpl* p) {
+  return p->precision == TCFFT_PRECISION_PLAIN && p->sched.N2 == 4096 &&
+         resident_tout_supported(4096, p->sched.N1 * p->batch, p->sched.N1);
+}
+bool generic2d_tout(const tcfftPlanImpl* p, int axis) {
+  if (p->precision != TCFFT_PRECISION_PLAIN) return false;
+  return axis == 0 ? p->ny == 4096 && resident_tout_supported(4096, p->nx * p->batch, p->nx)
+                   : p->nx == 4096 && resident_tout_supported(4096, p->ny * p->batch, p->ny);
+}
+
 tcfftStatus exec_plan(tcfftPlan plan, void* data, void* stream, int dir) {
   if (!plan || plan->magic != tcfftPlanImpl::kMagic) return TCFFT_INVALID_PLAN;
   if (!data) return TCFFT_INVALID_VALUE;
@@ -467,7 +479,8 @@ tcfftStatus exec_plan(tcfftPlan plan, void* data, void* stream, int dir) {
     return cuda_status(launch_tiny(plan->n, split, data, plan->batch, tw, dsign, plan->num_sms, st), "tiny launch");
   if (s.kind == Schedule::kLarge1d) {
     const FusedKey& k = s.key;
-    if (plan->tmap_ptr != data) {
+    const bool fresh = plan->tmap_ptr != data;
+    if (fresh) {
       const CUtensorMapDataType dt = split ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_UINT32;
       if (cu_status(encode_col_load(&plan->fmaps.load0, dt, data, s.N2, plan->batch, es, k.C0, k.R0), "tmap load0") ||
           cu_status(encode_col_store(&plan->fmaps.store0, dt, plan->big, s.N2, plan->batch, es, k.C0, k.R0),
@@ -503,6 +516,14 @@ tcfftStatus exec_plan(tcfftPlan plan, void* data, void* stream, int dir) {
       return TCFFT_CUDA_ERROR;
     int grid = 0;
     if (cuda_status(launch_fused(k, plan->fmaps, fp, plan->num_sms, st, &grid), "column pass")) return TCFFT_CUDA_ERROR;
+    if (large1d_tout(plan)) {
+      // rows of N2 = 4096 written transposed straight into data: X[k1 + N1 k2]
+      const tcfftPlanImpl* rp = plan->subs[0];
+      return cuda_status(launch_resident_tout(4096, plan->big, data, s.N1 * plan->batch, s.N1, tw, rp->twlo[dir],
+                                              rp->twhi[dir], dsign, plan->tables.err, plan->num_sms, st,
+                                              &plan->fmaps.load1, &plan->fmaps.store1, fresh),
+                         "rows (transposed output)");
+    }
     tcfftStatus r = exec_plan(plan->subs[0], plan->big, stream, dir);  // rows of N2, natural order
     if (r != TCFFT_SUCCESS) return r;
     // [B][N1 rows k1][N2 cols k2] -> X[k1 + N1 k2] = [B][N2][N1]
@@ -527,15 +548,34 @@ tcfftStatus exec_plan(tcfftPlan plan, void* data, void* stream, int dir) {
                        "copy back");
   }
   if (s.kind == Schedule::kGeneric2d) {
-    tcfftStatus r = exec_plan(plan->subs[0], data, stream, dir);  // rows of ny
+    // an axis of 4096 runs as the resident kernel with transposed output, which
+    // replaces that axis' transpose
+    const bool fresh = plan->tmap_ptr != data;
+    plan->tmap_ptr = data;
+    const int64_t nx = plan->nx, ny = plan->ny, B = plan->batch;
+    if (generic2d_tout(plan, 0)) {  // rows of ny -> big = [B][ny][nx]
+      const tcfftPlanImpl* rp = plan->subs[0];
+      if (cuda_status(launch_resident_tout(4096, data, plan->big, nx * B, nx, tw, rp->twlo[dir], rp->twhi[dir], dsign,
+                                           plan->tables.err, plan->num_sms, st, &plan->fmaps.load0,
+                                           &plan->fmaps.store0, fresh),
+                      "rows (transposed output)"))
+        return TCFFT_CUDA_ERROR;
+    } else {
+      tcfftStatus r = exec_plan(plan->subs[0], data, stream, dir);  // rows of ny
+      if (r != TCFFT_SUCCESS) return r;
+      if (cuda_status(launch_transpose(data, plan->big, B, nx, ny, es, plan->num_sms, st), "transpose"))
+        return TCFFT_CUDA_ERROR;
+    }
+    if (generic2d_tout(plan, 1)) {  // columns of nx (rows of big) -> data = [B][nx][ny]
+      const tcfftPlanImpl* cp = plan->subs[1];
+      return cuda_status(launch_resident_tout(4096, plan->big, data, ny * B, ny, tw, cp->twlo[dir], cp->twhi[dir],
+                                              dsign, plan->tables.err, plan->num_sms, st, &plan->fmaps.load1,
+                                              &plan->fmaps.store1, fresh),
+                         "columns (transposed output)");
+    }
+    tcfftStatus r = exec_plan(plan->subs[1], plan->big, stream, dir);  // columns of nx, now rows
     if (r != TCFFT_SUCCESS) return r;
-    if (cuda_status(launch_transpose(data, plan->big, plan->batch, plan->nx, plan->ny, es, plan->num_sms, st),
-                    "transpose"))
-      return TCFFT_CUDA_ERROR;
-    r = exec_plan(plan->subs[1], plan->big, stream, dir);  // columns of nx, now rows
-    if (r != TCFFT_SUCCESS) return r;
-    return cuda_status(launch_transpose(plan->big, data, plan->batch, plan->ny, plan->nx, es, plan->num_sms, st),
-                       "transpose");
+    return cuda_status(launch_transpose(plan->big, data, B, ny, nx, es, plan->num_sms, st), "transpose");
   }
   if (s.kind == Schedule::kSmall) {
     // 2D view of the whole batch: rows of 128 bytes
@@ -707,6 +747,10 @@ tcfftStatus setup_large1d(tcfftPlanImpl* p) {
   if (st != TCFFT_SUCCESS) return st;
   p->subs.push_back(rows);
   p->sched.launches = 2 + rows->sched.launches;
+  if (large1d_tout(p)) {
+    p->sched.launches = 2;
+    p->sched.text += ", rows written transposed (no transpose pass)";
+  }
   p->scratch_bytes += rows->scratch_bytes;
   return TCFFT_SUCCESS;
 }
@@ -749,6 +793,12 @@ tcfftStatus setup_generic2d(tcfftPlanImpl* p) {
   if (st != TCFFT_SUCCESS) return st;
   p->subs.push_back(cols);
   p->sched.launches = rows->sched.launches + cols->sched.launches + 2;
+  if (generic2d_tout(p, 0) || generic2d_tout(p, 1)) {
+    p->sched.launches = (generic2d_tout(p, 0) ? 1 : rows->sched.launches + 1) +
+                        (generic2d_tout(p, 1) ? 1 : cols->sched.launches + 1);
+    p->sched.text += generic2d_tout(p, 0) && generic2d_tout(p, 1) ? " (both axes: 4096-point rows written transposed)"
+                                                                  : " (one 4096 axis written transposed)";
+  }
   p->scratch_bytes += rows->scratch_bytes + cols->scratch_bytes;
   return TCFFT_SUCCESS;
 }

@@ -65,6 +65,10 @@ bool resident_supported(int64_t n, bool split);
 cudaError_t launch_resident(int64_t n, void* data, int64_t batch, const float2* tw2048, const float2* twlo,
                             const float2* twhi, float dsign, int* err, int num_sms, cudaStream_t st,
                             CUtensorMap* lm, CUtensorMap* sm, bool encode);
+bool resident_tout_supported(int64_t n, int64_t batch, int64_t rows);
+cudaError_t launch_resident_tout(int64_t n, const void* in, void* out, int64_t batch, int64_t rows,
+                                 const float2* tw2048, const float2* twlo, const float2* twhi, float dsign, int* err,
+                                 int num_sms, cudaStream_t st, CUtensorMap* lm, CUtensorMap* sm, bool encode);
 
 // One transform per thread-block cluster, N = 2^15..2^18 plain (fft_cluster.cu).
 bool cluster_supported(int64_t n, bool split, int num_sms);

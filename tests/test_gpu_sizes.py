@@ -3,8 +3,9 @@
 * 1D N = 16..128 (tiny kernel; batches that leave a partial group of 16);
 * 1D N = 2^23..2^27 (column pass + row sub-plan + transpose; 2^24..2^27 are
   sizes the reference supports, tcfft_half.cu:1310-1326);
-* 2D shapes outside 256..2048 per axis (row plans and transposes): the
-  128 x 128 .. 1024 x 1024 mix of the uneven-batch workload and 4096 x 4096.
+* 2D shapes outside 256..2048 per axis (row plans and transposes; an axis of
+  4096 as the resident kernel with transposed output): the 128 x 128 ..
+  1024 x 1024 mix of the uneven-batch workload and 4096 x 4096.
 
 Checked against the FP64 oracle on the rounded inputs; at 2^27, where a full
 FP64 reference is costly, through size-independent properties (linearity,
@@ -99,7 +100,7 @@ def test_largest_size_properties(cuda_device):
 
 
 @pytest.mark.parametrize("nx,ny,batch", [(128, 128, 8), (128, 1024, 2), (512, 128, 3), (64, 256, 4),
-                                         (1024, 4096, 1)])
+                                         (1024, 4096, 1), (4096, 256, 2), (4096, 4096, 1)])
 def test_generic_2d_plain(cuda_device, nx, ny, batch):
     xq = quantize(uniform_input((batch, nx, ny), seed=nx + ny), "plain")
     with tc.Plan(nx=nx, ny=ny, batch=batch) as p:
