@@ -261,6 +261,205 @@ __global__ void __launch_bounds__(384, 1) fft_resident_kernel(const __grid_const
   }
 }
 
+// ---------------------------------------------------------------------------
+// Split precision (fp32 complex in and out, hi/lo fp16 operands, three tensor-core
+// products per stage): N = 4096 (two transforms per 64 KiB stage) and 8192 (one).
+// Same schedule as the plain kernel: column tiles of 16 columns (128-byte rows of
+// 8-byte elements), the 256-point split column jobs with W_N, the 16 R1-point
+// split row jobs of 16 rows, natural-order write-back, 128-byte-row stores.
+template <int R1>
+struct ResSplitCfg {
+  static constexpr int kES = 8;
+  static constexpr int kN2 = 16 * R1, kN = 256 * kN2;
+  static constexpr int kC = 16;
+  static constexpr int kCG = kN2 / kC;
+  static constexpr int kTileBytes = 256 * kC * kES;
+  static constexpr int kStageBytes = 65536;
+  static constexpr int kT = kStageBytes / (kN * kES);
+  static constexpr int kStages = 3;
+  static constexpr int kLog2N = R1 == 1 ? 12 : 13;
+  static constexpr int kTwShift = (kLog2N + 1) / 2;
+  static constexpr int kTwLo = 1 << kTwShift, kTwHi = kN >> kTwShift;
+  static constexpr int kTabBytes = (kTwLo + kTwHi + kN2) * 8;
+  static constexpr int kSmem = kStages * kStageBytes + kTabBytes + 1024 + 256;
+  static constexpr int kThreads = 384;
+  using PI = BitPerm<0, 1, 2, 3>;
+  using RHO = BitPerm<0, 2, 3, 1>;
+  static_assert(kT >= 1 && kT * kN * kES == kStageBytes, "a stage holds whole transforms");
+};
+
+template <int R1>
+__global__ void __launch_bounds__(384, 1) fft_resident_split_kernel(const __grid_constant__ CUtensorMap load_map,
+                                                                     const __grid_constant__ CUtensorMap store_map,
+                                                                     const ResParams p) {
+  using Cfg = ResSplitCfg<R1>;
+  using PI = typename Cfg::PI;
+  using RHO = typename Cfg::RHO;
+  constexpr int NST = Cfg::kStages, T = Cfg::kT, CG = Cfg::kCG, C = Cfg::kC, ES = Cfg::kES;
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  unsigned char* smem =
+      reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  unsigned char* tab = smem + NST * Cfg::kStageBytes;
+  float2* s_twlo = reinterpret_cast<float2*>(tab);
+  float2* s_twhi = s_twlo + Cfg::kTwLo;
+  float2* s_tw16 = s_twhi + Cfg::kTwHi;  // W_{N2}^j
+  uint64_t* full = reinterpret_cast<uint64_t*>(tab + Cfg::kTabBytes);
+  uint64_t* computed = full + NST;
+  uint64_t* empty = computed + NST;
+
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const long long tiles = (p.batch + T - 1) / T;
+  if (tid == 0) {
+    for (int s = 0; s < NST; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&computed[s], 8);
+      mbar_init(&empty[s], 1);
+    }
+    fence_barrier_init();
+  }
+  for (int j = tid; j < Cfg::kTwLo; j += blockDim.x) s_twlo[j] = p.twlo[j];
+  for (int j = tid; j < Cfg::kTwHi; j += blockDim.x) s_twhi[j] = p.twhi[j];
+  for (int j = tid; j < Cfg::kN2; j += blockDim.x) s_tw16[j] = p.tw2048[j * (2048 / Cfg::kN2)];
+  __syncthreads();
+
+  if (warp >= 8) asm volatile("setmaxnreg.dec.sync.aligned.u32 %0;" ::"n"(56));
+  if (warp >= 10) return;
+  if (warp == 8) {  // ------------------------------------------------ TMA producer
+    if (lane == 0) {
+      prefetch_tmap(&load_map);
+      int cnt = 0;
+      for (long long it = blockIdx.x; it < tiles; it += gridDim.x, ++cnt) {
+        const int s = cnt % NST;
+        if (!mbar_wait(&empty[s], ((cnt / NST) + 1) & 1, p.err)) break;
+        unsigned char* dst = smem + s * Cfg::kStageBytes;
+        mbar_arrive_expect_tx(&full[s], Cfg::kStageBytes);
+#pragma unroll 1
+        for (int t = 0; t < T; ++t)
+#pragma unroll 1
+          for (int cg = 0; cg < CG; ++cg)
+            tma_load_5d(dst + (t * CG + cg) * Cfg::kTileBytes, &load_map, cg * C, 0, 0, 0, (int)(it * T + t),
+                        &full[s]);
+      }
+      for (int i = (cnt > NST ? cnt - NST : 0); i < cnt; ++i) mbar_wait(&full[i % NST], (i / NST) & 1, nullptr);
+    }
+    return;
+  }
+  if (warp == 9) {  // ------------------------------------------------ TMA storer
+    if (lane == 0) {
+      prefetch_tmap(&store_map);
+      int cnt = 0;
+      for (long long it = blockIdx.x; it < tiles; it += gridDim.x, ++cnt) {
+        const int s = cnt % NST;
+        if (!mbar_wait(&computed[s], (cnt / NST) & 1, p.err)) break;
+        const unsigned char* src = smem + s * Cfg::kStageBytes;
+        const int row0 = (int)(it * (Cfg::kStageBytes / 128));
+#pragma unroll 1
+        for (int b = 0; b < Cfg::kStageBytes / (256 * 128); ++b)
+          tma_store_2d(&store_map, 0, row0 + 256 * b, src + b * 256 * 128);
+        bulk_commit();
+        bulk_wait_read<0>();
+        mbar_arrive(&empty[s]);
+      }
+      bulk_wait<0>();
+    }
+    return;
+  }
+
+  // ------------------------------------------------------------------ compute warps
+  asm volatile("setmaxnreg.inc.sync.aligned.u32 %0;" ::"n"(224));
+  JobConsts<true> jc;
+  init_job_consts<true, PI, RHO>(jc, p.tw2048);
+  const uint32_t tw16 = smem_addr(s_tw16);
+  WnTable wn;
+  wn.hi = smem_addr(s_twhi);
+  wn.lo = smem_addr(s_twlo);
+  wn.ghi = p.twhi;
+  wn.glo = p.twlo;
+  wn.global = false;
+  wn.shift = Cfg::kTwShift;
+  wn.nmask = Cfg::kN - 1;
+  const int g = lane >> 2, tq = lane & 3;
+  constexpr int JN = C / 8;  // two side-by-side columns per warp
+  const int col0 = JN * warp;
+  int cnt = 0;
+  for (long long it = blockIdx.x; it < tiles; it += gridDim.x, ++cnt) {
+    const int s = cnt % NST;
+    const bool ok = named_bar_and(2, 256, mbar_wait(&full[s], (cnt / NST) & 1, p.err));
+    const uint32_t base = smem_addr(smem + s * Cfg::kStageBytes);
+    if (ok) {
+      // phase 0: columns of 256 in place, times W_N^(n2 k1)
+#pragma unroll 1
+      for (int tile = 0; tile < T * CG; ++tile) {
+        const uint32_t tb = base + tile * Cfg::kTileBytes;
+        float2 fk[JN][8];
+#pragma unroll
+        for (int jn = 0; jn < JN; ++jn) {
+          const int n2 = (tile % CG) * C + col0 + jn;
+#pragma unroll
+          for (int sl = 0; sl < 8; ++sl) fk[jn][sl] = wn(n2 * jc.kval[sl >> 2][(sl >> 1) & 1][sl & 1]);
+        }
+        auto ldp = [&](int jp, int n, float2& x0, float2& x1) {
+          lds_pair<true>(tb + ctile_off<C, ES>(col_in_row(n), col0 + jp), x0, x1);
+        };
+        auto st = [&](int jp, int k, int, int sl, float2 v0, float2 v1) {
+          sts_pair<true>(tb + ctile_off<C, ES>(col_out_row(k, 0), col0 + jp), cmul(v0, fk[jp][sl]),
+                         cmul(v1, fk[jp + 1][sl]));
+        };
+        fft256r_jobs<1, true, 1, JN, true>(jc, tw16, p.dsign, ldp, st);
+      }
+      named_bar_sync(1, 256);
+      // phase 1: 16 rows k1 per job, FFT over n2 (length 16 R1); jobs j = warp + 8 i
+      constexpr int JOBS = 2 * T;
+      float2 out[JOBS][8 * R1];
+#pragma unroll
+      for (int i = 0; i < JOBS; ++i) {
+        const int job = warp + 8 * i, t = job >> 4, k1base = (job & 15) * 16;
+        const uint32_t tbase = base + t * (CG * Cfg::kTileBytes);
+        auto ld = [&](int v, int n) {
+          return lds_elem<true>(tbase + (n / C) * Cfg::kTileBytes +
+                                ctile_off<C, ES>(col_out_row(k1base + v, 0), n % C));
+        };
+        auto st = [&](int, int, int q, int slot, float2 val) { out[i][8 * q + slot] = val; };
+        fft16r_job<R1, true, 1, PI, RHO>(jc, tw16, p.dsign, ld, st);
+      }
+      named_bar_sync(1, 256);  // every warp has read the stage
+      // natural order X[k1 + 256 k2] of transform t at element t N + k1 + 256 k2 (128B-swizzled rows)
+#pragma unroll
+      for (int i = 0; i < JOBS; ++i) {
+        const int job = warp + 8 * i, t = job >> 4, k1base = (job & 15) * 16;
+#pragma unroll
+        for (int q = 0; q < R1; ++q)
+#pragma unroll
+          for (int slot = 0; slot < 8; ++slot) {
+            const int jj = slot >> 2, h = (slot >> 1) & 1, e = slot & 1;
+            const int v = 2 * tq + e + 8 * jj, k = q + R1 * RHO::apply(g + 8 * h);
+            const uint32_t el = (uint32_t)(t * Cfg::kN + k1base + v + 256 * k);
+            sts64f(base + swz_w<8>(el) * 8, out[i][8 * q + slot]);
+          }
+      }
+    }
+    fence_proxy_async_smem();
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&computed[s]);
+    if (!ok) break;
+  }
+}
+
+template <int R1>
+cudaError_t launch_resident_split_t(const CUtensorMap& lm, const CUtensorMap& sm, const ResParams& p, int num_sms,
+                                    cudaStream_t st) {
+  using Cfg = ResSplitCfg<R1>;
+  auto kern = fft_resident_split_kernel<R1>;
+  static std::once_flag once;
+  static cudaError_t init_err = cudaSuccess;
+  std::call_once(once, [&] { init_err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg::kSmem); });
+  if (init_err != cudaSuccess) return init_err;
+  const long long tiles = (p.batch + Cfg::kT - 1) / Cfg::kT;
+  const long long grid = tiles < num_sms ? tiles : num_sms;
+  kern<<<(int)grid, Cfg::kThreads, Cfg::kSmem, st>>>(lm, sm, p);
+  return cudaGetLastError();
+}
+
 template <int R1, bool TOUT = false>
 cudaError_t launch_resident_t(const CUtensorMap& lm, const CUtensorMap& sm, const ResParams& p, int num_sms,
                               cudaStream_t st) {
@@ -278,12 +477,43 @@ cudaError_t launch_resident_t(const CUtensorMap& lm, const CUtensorMap& sm, cons
 
 }  // namespace
 
-bool resident_supported(int64_t n, bool split) { return !split && (n == 4096 || n == 8192 || n == 16384); }
+bool resident_supported(int64_t n, bool split) {
+  return split ? (n == 4096 || n == 8192) : (n == 4096 || n == 8192 || n == 16384);
+}
 
 // Tensor maps: column-tile loads of the [B*256 rows][N2 cols] view; stores of
 // X[k1 + 256 k2] as a 5D box with dims (k1 bits 0-4, k2 bit L, k2 bits L+2..L+3
 // together with the transform index, k2 bit L+1, k1 bits 5-7 together with
 // k2 bits 0..L-1), L = log2(N2 / 16), matching the stage layout above.
+cudaError_t launch_resident_split(int64_t n, void* data, int64_t batch, const float2* tw2048, const float2* twlo,
+                                  const float2* twhi, float dsign, int* err, int num_sms, cudaStream_t st,
+                                  CUtensorMap* lm, CUtensorMap* sm, bool encode) {
+  const int64_t n2 = n / 256;
+  if (encode) {
+    if (encode_col_load(lm, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, data, n2, batch, 8, 16, 1) != CUDA_SUCCESS)
+      return cudaErrorInvalidValue;
+    uint64_t dims[2] = {16, (uint64_t)(n * batch / 16)};
+    uint64_t str[1] = {128};
+    uint32_t box[2] = {16, 256};
+    if (encode_tmap(sm, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 2, data, dims, str, box, CU_TENSOR_MAP_SWIZZLE_128B) !=
+        CUDA_SUCCESS)
+      return cudaErrorInvalidValue;
+  }
+  ResParams p;
+  p.tw2048 = tw2048;
+  p.twlo = twlo;
+  p.twhi = twhi;
+  p.batch = batch;
+  p.rows = 0;
+  p.err = err;
+  p.dsign = dsign;
+  switch (n) {
+    case 4096: return launch_resident_split_t<1>(*lm, *sm, p, num_sms, st);
+    case 8192: return launch_resident_split_t<2>(*lm, *sm, p, num_sms, st);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
 cudaError_t launch_resident(int64_t n, void* data, int64_t batch, const float2* tw2048, const float2* twlo,
                             const float2* twhi, float dsign, int* err, int num_sms, cudaStream_t st,
                             CUtensorMap* lm, CUtensorMap* sm, bool encode) {

@@ -281,8 +281,8 @@ tcfftStatus choose_1d(int64_t n, int64_t batch, int precision, Schedule& s) {
     s.N1 = 256;
     s.N2 = n / 256;
     s.launches = 1;
-    snprintf(buf, sizeof buf, "resident(plain): N=256 x %lld, whole transforms in shared memory, one HBM pass",
-             (long long)s.N2);
+    snprintf(buf, sizeof buf, "resident(%s): N=256 x %lld, whole transforms in shared memory, one HBM pass",
+             split ? "split" : "plain", (long long)s.N2);
     s.text = buf;
     return TCFFT_SUCCESS;
   }
@@ -470,8 +470,11 @@ tcfftStatus exec_plan(tcfftPlan plan, void* data, void* stream, int dir) {
   }
   if (s.kind == Schedule::kResident) {
     const bool enc = plan->tmap_ptr != data;
-    cudaError_t e = launch_resident(plan->n, data, plan->batch, tw, plan->twlo[dir], plan->twhi[dir], dsign,
-                                    plan->tables.err, plan->num_sms, st, &plan->fmaps.load0, &plan->fmaps.store0, enc);
+    cudaError_t e =
+        split ? launch_resident_split(plan->n, data, plan->batch, tw, plan->twlo[dir], plan->twhi[dir], dsign,
+                                      plan->tables.err, plan->num_sms, st, &plan->fmaps.load0, &plan->fmaps.store0, enc)
+              : launch_resident(plan->n, data, plan->batch, tw, plan->twlo[dir], plan->twhi[dir], dsign,
+                                plan->tables.err, plan->num_sms, st, &plan->fmaps.load0, &plan->fmaps.store0, enc);
     if (e == cudaSuccess) plan->tmap_ptr = data;
     return cuda_status(e, "resident launch");
   }

@@ -60,11 +60,14 @@ CUresult encode_col_load(CUtensorMap* m, CUtensorMapDataType dt, void* base, int
                          int C, int R);
 CUresult encode_col_store(CUtensorMap* m, CUtensorMapDataType dt, void* base, int64_t ncols, int64_t nblk, int es,
                           int C, int R);
-// Whole-transform-in-shared-memory kernel, N = 4096, 8192, 16384 plain (fft_resident.cu).
+// Whole-transform-in-shared-memory kernel, N = 4096, 8192, 16384 plain, 4096 and 8192 split (fft_resident.cu).
 bool resident_supported(int64_t n, bool split);
 cudaError_t launch_resident(int64_t n, void* data, int64_t batch, const float2* tw2048, const float2* twlo,
                             const float2* twhi, float dsign, int* err, int num_sms, cudaStream_t st,
                             CUtensorMap* lm, CUtensorMap* sm, bool encode);
+cudaError_t launch_resident_split(int64_t n, void* data, int64_t batch, const float2* tw2048, const float2* twlo,
+                                  const float2* twhi, float dsign, int* err, int num_sms, cudaStream_t st,
+                                  CUtensorMap* lm, CUtensorMap* sm, bool encode);
 bool resident_tout_supported(int64_t n, int64_t batch, int64_t rows);
 cudaError_t launch_resident_tout(int64_t n, const void* in, void* out, int64_t batch, int64_t rows,
                                  const float2* tw2048, const float2* twlo, const float2* twhi, float dsign, int* err,
