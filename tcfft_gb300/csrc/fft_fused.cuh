@@ -208,27 +208,44 @@ __device__ __forceinline__ void plain_col_tile(const JobConsts<false>& jc, uint3
   if constexpr (WN) {
     // W_N^(n2 (q + R k')), k' = kbase + e + 2h + 32hh (RHO digit structure):
     // fk[osl] = W^(n2 R kbase) u^(e + 2h) u32^hh with u = W^(n2 R); fq[q] = W^(n2 q)
+    // (four jobs: only the even-slot factors and u32 are held, 40 registers instead of 64,
+    // the odd slots cost one product at the store)
     const int kbase = slot_kval<PI, RHO>(0);
-    float2 fk[JN][8], fq[JN][R];
+    constexpr int NK = QUAD ? 4 : 8;
+    float2 fk[JN][NK], fu[JN], fq[JN][R];
 #pragma unroll
     for (int jn = 0; jn < JN; ++jn) {
       const int n2 = n2base + col0 + jn;
       const float2 F = wn(n2 * R * kbase), u = wn(n2 * R), u32 = wn(32 * n2 * R);
       const float2 u2 = cmul(u, u), u3 = cmul(u2, u);
       const float2 f0[4] = {F, cmul(F, u), cmul(F, u2), cmul(F, u3)};
+      fu[jn] = u32;
 #pragma unroll
-      for (int osl = 0; osl < 8; ++osl) {
-        const float2 f = f0[((osl >> 1) & 1) + 2 * (osl >> 2)];
-        fk[jn][osl] = (osl & 1) ? cmul(f, u32) : f;
+      for (int osl = 0; osl < NK; ++osl) {
+        if constexpr (QUAD) {
+          fk[jn][osl] = f0[osl];
+        } else {
+          const float2 f = f0[((osl >> 1) & 1) + 2 * (osl >> 2)];
+          fk[jn][osl] = (osl & 1) ? cmul(f, u32) : f;
+        }
       }
       fq[jn][0] = make_float2(1.f, 0.f);
       if constexpr (R > 1) fq[jn][1] = wn(n2);
 #pragma unroll
       for (int q = 2; q < R; ++q) fq[jn][q] = cmul(fq[jn][q - 1], fq[jn][1]);
     }
-    // W_N^(n2 (q + R k')) of job jn, output slot osl (q is a compile-time constant after
-    // unrolling: q = 0 needs no product)
-    auto wfac = [&](int jn, int osl, int q) { return q == 0 ? fk[jn][osl] : cmul(fk[jn][osl], fq[jn][q]); };
+    // W_N^(n2 (q + R k')) of job jn, output slot osl (osl and q are compile-time constants
+    // after unrolling: q = 0 needs no product)
+    auto wfac = [&](int jn, int osl, int q) {
+      float2 f;
+      if constexpr (QUAD) {
+        f = fk[jn][((osl >> 1) & 1) + 2 * (osl >> 2)];
+        if (osl & 1) f = cmul(f, fu[jn]);
+      } else {
+        f = fk[jn][osl];
+      }
+      return q == 0 ? f : cmul(f, fq[jn][q]);
+    };
     if constexpr (QUAD) {
       auto ld = [&](int, int sl, int a, uint32_t& x0, uint32_t& x1, uint32_t& x2, uint32_t& x3) {
         uint32_t w[4];
