@@ -204,6 +204,14 @@ void free_tables(tcfftPlanImpl* p) {
   }
   if (p->cap_stream) cudaStreamDestroy(p->cap_stream);
   p->cap_stream = nullptr;
+  for (int b = 0; b < tcfftPlanImpl::kBranches; ++b) {
+    if (p->branch[b]) cudaStreamDestroy(p->branch[b]);
+    if (p->join_ev[b]) cudaEventDestroy(p->join_ev[b]);
+    p->branch[b] = nullptr;
+    p->join_ev[b] = nullptr;
+  }
+  if (p->fork_ev) cudaEventDestroy(p->fork_ev);
+  p->fork_ev = nullptr;
 }
 
 int ilog2_exact(int64_t v) {
@@ -939,11 +947,29 @@ tcfftStatus exec_many(tcfftPlanImpl* plan, void* data, cudaStream_t st, int dir)
       r = cuda_status(launch_move_blocks(data, plan->big, plan->mv_user, plan->mv_big, plan->mv_cum, plan->mv_n,
                                          plan->mv_chunks, plan->num_sms, plan->cap_stream),
                       "gather");
+    // runs on branch streams: runs of one sub-plan share its scratch, so they stay on one
+    // branch (in order); different sub-plans touch disjoint data and run concurrently
+    if (r == TCFFT_SUCCESS) r = cuda_status(cudaEventRecord(plan->fork_ev, plan->cap_stream), "graph fork");
+    std::map<const tcfftPlanImpl*, int> branch_of;
+    bool used[tcfftPlanImpl::kBranches] = {};
     for (const auto& run : plan->runs) {
       if (r != TCFFT_SUCCESS) break;
+      auto ins = branch_of.emplace(run.sub, (int)(branch_of.size() % tcfftPlanImpl::kBranches));
+      const int b = ins.first->second;
+      if (!used[b]) {
+        used[b] = true;
+        if (cuda_status(cudaStreamWaitEvent(plan->branch[b], plan->fork_ev, 0), "graph fork")) {
+          r = TCFFT_CUDA_ERROR;
+          break;
+        }
+      }
       unsigned char* base = static_cast<unsigned char*>(run.in_big ? plan->big : data);
-      r = exec_plan(run.sub, base + run.offset * es, plan->cap_stream, dir);
+      r = exec_plan(run.sub, base + run.offset * es, plan->branch[b], dir);
     }
+    for (int b = 0; b < tcfftPlanImpl::kBranches; ++b)  // join every forked branch (also after a failure)
+      if (used[b] && (cudaEventRecord(plan->join_ev[b], plan->branch[b]) != cudaSuccess ||
+                      cudaStreamWaitEvent(plan->cap_stream, plan->join_ev[b], 0) != cudaSuccess))
+        r = TCFFT_CUDA_ERROR;
     if (r == TCFFT_SUCCESS && plan->mv_n > 0)
       r = cuda_status(launch_move_blocks(plan->big, data, plan->mv_big, plan->mv_user, plan->mv_cum, plan->mv_n,
                                          plan->mv_chunks, plan->num_sms, plan->cap_stream),
@@ -1221,6 +1247,12 @@ tcfftStatus tcfftPlanMany(tcfftPlan* out, int64_t count, const int32_t* ranks, c
   }
   if (st == TCFFT_SUCCESS && cudaStreamCreateWithFlags(&p->cap_stream, cudaStreamNonBlocking) != cudaSuccess)
     st = TCFFT_CUDA_ERROR;
+  if (st == TCFFT_SUCCESS && cudaEventCreateWithFlags(&p->fork_ev, cudaEventDisableTiming) != cudaSuccess)
+    st = TCFFT_CUDA_ERROR;
+  for (int b = 0; b < tcfftPlanImpl::kBranches && st == TCFFT_SUCCESS; ++b)
+    if (cudaStreamCreateWithFlags(&p->branch[b], cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&p->join_ev[b], cudaEventDisableTiming) != cudaSuccess)
+      st = TCFFT_CUDA_ERROR;
   if (st != TCFFT_SUCCESS) {
     free_tables(p);
     delete p;

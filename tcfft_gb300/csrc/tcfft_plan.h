@@ -72,6 +72,12 @@ struct tcfftPlanImpl {
   int mv_n = 0;
   long long mv_chunks = 0;
   cudaStream_t cap_stream = nullptr;
+  // independent runs are captured on branch streams (forked after the gather, joined
+  // before the scatter), so the graph runs them concurrently
+  static constexpr int kBranches = 8;
+  cudaStream_t branch[kBranches] = {};
+  cudaEvent_t fork_ev = nullptr;
+  cudaEvent_t join_ev[kBranches] = {};
   void* graph_ptr[2] = {nullptr, nullptr};
   cudaGraphExec_t graph_exec[2] = {nullptr, nullptr};
   // autotuner: chosen lag multiplier of the fused executor (1 = built-in)
