@@ -87,6 +87,21 @@ __device__ __forceinline__ uint32_t ctile_off(int row, int col) {
 __device__ __forceinline__ int col_in_row(int n) {
   return ((n >> 7) & 1) | ((n & 15) << 1) | (((n >> 4) & 7) << 5) | (n & ~255);
 }
+// Split precision (8-byte elements, identity slot permutation, 16-byte accesses of
+// two columns): the eight lanes of a quarter-warp read rows n whose bits 0, 5 and 6
+// differ, so those bits are the tile row's low bits (the swizzle phase):
+// tile row (n bits 5-6 | n bit 0 << 2 | n bits 1-4 << 3 | (n >> 7) << 7).
+template <bool SPLIT>
+__device__ __forceinline__ int col_in_row_t(int n) {
+  if constexpr (SPLIT) return ((n >> 5) & 3) | ((n & 1) << 2) | (((n >> 1) & 15) << 3) | ((n >> 7) << 7);
+  else return col_in_row(n);
+}
+// Block coordinate of transform b in a column-load box (the outermost box dimension
+// holds R blocks of 256 rows, 2R half-blocks of 128 in the split order).
+template <bool SPLIT>
+__host__ __device__ constexpr int col_blk(int b, int R) {
+  return SPLIT ? 2 * R * b : R * b;
+}
 __device__ __forceinline__ int col_out_row(int kp, int q) {
   return ((kp >> 2) & 3) | ((kp >> 4) << 2) | ((kp & 3) << 6) | (q << 8);
 }
@@ -483,7 +498,8 @@ __global__ void __launch_bounds__(384, 1)  // 12 warps at launch: 168 registers 
 #pragma unroll 1
             for (int u = 0; u < Cfg::kSub0; ++u) {
               const int cg = (it.tile * Cfg::kSub0 + u) % p.cols0;
-              tma_load_5d(dst + u * (Cfg::kTile0 * ES), &maps.load0, cg * C0, 0, 0, 0, it.b * R0, &full[s]);
+              tma_load_5d(dst + u * (Cfg::kTile0 * ES), &maps.load0, cg * C0, 0, 0, 0, col_blk<SPLIT>(it.b, R0),
+                          &full[s]);
             }
           } else {  // contiguous rows
             const int y0 = (int)(((long long)it.b * p.rows0 + (long long)it.tile * C0) * (256 * R0) / ER);
@@ -495,7 +511,7 @@ __global__ void __launch_bounds__(384, 1)  // 12 warps at launch: 168 registers 
           mbar_arrive_expect_tx(&full[s], Cfg::kItem1 * ES);
           if constexpr (ROLE1 == kRoleCol) {
             const int cg = it.tile % p.cols1;
-            tma_load_5d(dst, &maps.load1, cg * C1, 0, 0, 0, it.b * R1, &full[s]);
+            tma_load_5d(dst, &maps.load1, cg * C1, 0, 0, 0, col_blk<SPLIT>(it.b, R1), &full[s]);
           } else {
             // 1D: source is the scratch slot; 2D never has a contiguous phase 1
             const long long row0 = (long long)slot * p.rows1 + (long long)it.tile * (Cfg::kSub1 * C1);
@@ -653,9 +669,11 @@ __global__ void __launch_bounds__(384, 1)  // 12 warps at launch: 168 registers 
           constexpr int TWS = Cfg::kLmax / (256 * R0);
           const int cg = (it.tile * Cfg::kSub0 + u) % p.cols0;
           const int col0 = JN * warp;
-          auto ld = [&](int jn, int n) { return lds_elem<SPLIT>(base + ctile_off<C0, ES>(col_in_row(n), col0 + jn)); };
+          auto ld = [&](int jn, int n) {
+            return lds_elem<SPLIT>(base + ctile_off<C0, ES>(col_in_row_t<SPLIT>(n), col0 + jn));
+          };
           auto ldp = [&](int jp, int n, float2& x0, float2& x1) {
-            lds_pair<SPLIT>(base + ctile_off<C0, ES>(col_in_row(n), col0 + jp), x0, x1);
+            lds_pair<SPLIT>(base + ctile_off<C0, ES>(col_in_row_t<SPLIT>(n), col0 + jp), x0, x1);
           };
           auto oaddr = [&](int jn, int k, int q) {
             return base + ctile_off<C0, ES>(col_out_row((k - q) / R0, q), col0 + jn);
@@ -746,7 +764,7 @@ __global__ void __launch_bounds__(384, 1)  // 12 warps at launch: 168 registers 
           };
           if constexpr (JN % 2 == 0) {
             auto ldp = [&](int jp, int n, float2& x0, float2& x1) {
-              lds_pair<SPLIT>(base + ctile_off<C1, ES>(col_in_row(n), col0 + jp), x0, x1);
+              lds_pair<SPLIT>(base + ctile_off<C1, ES>(col_in_row_t<SPLIT>(n), col0 + jp), x0, x1);
             };
             auto st = [&](int jp, int k, int q, int, float2 v0, float2 v1) {
               sts_pair<SPLIT>(oaddr(jp, k, q), v0, v1);
@@ -754,7 +772,7 @@ __global__ void __launch_bounds__(384, 1)  // 12 warps at launch: 168 registers 
             fft256r_jobs<R1, SPLIT, TWS, JN, true>(jc, twR, p.dsign, ldp, st);
           } else {
             auto ld = [&](int jn, int n) {
-              return lds_elem<SPLIT>(base + ctile_off<C1, ES>(col_in_row(n), col0 + jn));
+              return lds_elem<SPLIT>(base + ctile_off<C1, ES>(col_in_row_t<SPLIT>(n), col0 + jn));
             };
             auto st = [&](int jn, int k, int q, int, float2 v) { sts_elem<SPLIT>(oaddr(jn, k, q), v); };
             fft256r_jobs<R1, SPLIT, TWS, JN>(jc, twR, p.dsign, ld, st);

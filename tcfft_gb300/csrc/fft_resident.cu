@@ -337,8 +337,8 @@ __global__ void __launch_bounds__(384, 1) fft_resident_split_kernel(const __grid
         for (int t = 0; t < T; ++t)
 #pragma unroll 1
           for (int cg = 0; cg < CG; ++cg)
-            tma_load_5d(dst + (t * CG + cg) * Cfg::kTileBytes, &load_map, cg * C, 0, 0, 0, (int)(it * T + t),
-                        &full[s]);
+            tma_load_5d(dst + (t * CG + cg) * Cfg::kTileBytes, &load_map, cg * C, 0, 0, 0,
+                        col_blk<true>((int)(it * T + t), 1), &full[s]);
       }
       for (int i = (cnt > NST ? cnt - NST : 0); i < cnt; ++i) mbar_wait(&full[i % NST], (i / NST) & 1, nullptr);
     }
@@ -399,7 +399,7 @@ __global__ void __launch_bounds__(384, 1) fft_resident_split_kernel(const __grid
           for (int sl = 0; sl < 8; ++sl) fk[jn][sl] = wn(n2 * jc.kval[sl >> 2][(sl >> 1) & 1][sl & 1]);
         }
         auto ldp = [&](int jp, int n, float2& x0, float2& x1) {
-          lds_pair<true>(tb + ctile_off<C, ES>(col_in_row(n), col0 + jp), x0, x1);
+          lds_pair<true>(tb + ctile_off<C, ES>(col_in_row_t<true>(n), col0 + jp), x0, x1);
         };
         auto st = [&](int jp, int k, int, int sl, float2 v0, float2 v1) {
           sts_pair<true>(tb + ctile_off<C, ES>(col_out_row(k, 0), col0 + jp), cmul(v0, fk[jp][sl]),

@@ -69,6 +69,15 @@ CUtensorMapSwizzle col_swizzle(int C, int es) {
 CUresult encode_col_load(CUtensorMap* m, CUtensorMapDataType dt, void* base, int64_t ncols, int64_t nblk, int es,
                          int C, int R) {
   const uint64_t rp = (uint64_t)ncols * es;
+  if (es == 8) {
+    // split precision (8-byte elements, identity slot permutation): box
+    // [C][n bits 5-6][n bit 0][n bits 1-4][n bit 7 + 2 a]: tile row
+    // (n bits 5-6 | n bit 0 << 2 | n bits 1-4 << 3 | (n >> 7) << 7), see col_in_row_t
+    uint64_t dims[5] = {(uint64_t)ncols, 4, 2, 16, (uint64_t)(2 * nblk * R)};
+    uint64_t str[4] = {32 * rp, rp, 2 * rp, 128 * rp};
+    uint32_t box[5] = {(uint32_t)C, 4, 2, 16, (uint32_t)(2 * R)};
+    return encode_tmap(m, dt, 5, base, dims, str, box, col_swizzle(C, es));
+  }
   uint64_t dims[5] = {(uint64_t)ncols, 2, 16, 8, (uint64_t)(nblk * R)};
   uint64_t str[4] = {128 * rp, rp, 16 * rp, 256 * rp};
   uint32_t box[5] = {(uint32_t)C, 2, 16, 8, (uint32_t)R};
