@@ -106,6 +106,18 @@ tcfftStatus tcfftExecute(tcfftPlan plan, void* data, void* stream);
  * tcfftExecute, i.e. n * inverse DFT), same layout and schedule. */
 tcfftStatus tcfftExecuteAdjoint(tcfftPlan plan, void* data, void* stream);
 
+/* Host-buffer execution: the batch is copied in from `host_in`, transformed
+ * (forward) in the caller's device buffer `work` (the plan's size, 128-byte
+ * aligned) and copied out to `host_out`, pipelined over chunks of the batch on
+ * internal streams (host-to-device copy of chunk c+1, transform of chunk c and
+ * device-to-host copy of chunk c-1 overlap).  Ordered after the work already in
+ * `stream`; work queued in `stream` afterwards waits for the whole call.
+ * host_in and host_out should be pinned (cudaHostAlloc / cudaHostRegister) for
+ * the copies to be asynchronous; host_out may equal host_in.  Uneven-batch plans
+ * run unchunked (copy in, execute, copy out on `stream`).  No counterpart in the
+ * reference, whose tcfftExec takes device memory only. */
+tcfftStatus tcfftExecuteHost(tcfftPlan plan, const void* host_in, void* host_out, void* work, void* stream);
+
 /* Synchronise `stream` and report device-side errors (TCFFT_TIMEOUT) raised
  * by bounded waits since the last check; clears the flag. */
 tcfftStatus tcfftCheckDevice(tcfftPlan plan, void* stream);

@@ -81,6 +81,8 @@ _SIGNATURES = {
                        ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(Options)], ctypes.c_int),
     "tcfftExecute": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
     "tcfftExecuteAdjoint": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
+    "tcfftExecuteHost": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p],
+                         ctypes.c_int),
     "tcfftCheckDevice": ([ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
     "tcfftDestroy": ([ctypes.c_void_p], ctypes.c_int),
     "tcfftGetErrorString": ([ctypes.c_int], ctypes.c_char_p),
@@ -235,6 +237,29 @@ class Plan:
         _check(fn(self._handle, ctypes.c_void_p(self._ptr(data)), _stream_handle(stream)),
                "tcfftExecute%s" % ("Adjoint" if adjoint else ""))
         return data
+
+    def exec_host(self, host_in, host_out, work, stream=None):
+        """Forward transform of a host batch: ``host_in`` is copied into the device
+        buffer ``work``, transformed and copied to ``host_out`` (pinned CPU tensors of
+        the plan's size), pipelined over chunks of the batch (tcfftExecuteHost)."""
+        if not self._handle:
+            raise TcfftError(8, "exec on destroyed plan")
+        inf = self.info
+        if getattr(self, "shapes", None) is not None:  # uneven batch: up to the end of the last transform
+            span = max(int(o) + int(s[0]) * (int(s[1]) if len(s) > 1 else 1) for o, s in zip(self.offsets, self.shapes))
+            nbytes = span * inf["element_bytes"]
+        else:
+            nbytes = inf["total_elements"] * inf["element_bytes"]
+        for t in (host_in, host_out):
+            if t.is_cuda or not t.is_contiguous():
+                raise ValueError("host buffers must be contiguous CPU tensors")
+            if t.numel() * t.element_size() != nbytes:
+                raise ValueError("host buffers must hold the plan's %d bytes" % nbytes)
+        _check(lib().tcfftExecuteHost(self._handle, ctypes.c_void_p(host_in.data_ptr()),
+                                      ctypes.c_void_p(host_out.data_ptr()), ctypes.c_void_p(self._ptr(work)),
+                                      _stream_handle(stream)),
+               "tcfftExecuteHost")
+        return host_out
 
     def check_device(self, stream=None):
         """Synchronise and raise TcfftError(TCFFT_TIMEOUT) if a bounded wait expired."""

@@ -221,6 +221,23 @@ void free_tables(tcfftPlanImpl* p) {
   }
   if (p->fork_ev) cudaEventDestroy(p->fork_ev);
   p->fork_ev = nullptr;
+  for (int i = 0; i < 2; ++i) {
+    if (p->host_sub[i]) tcfftDestroy(p->host_sub[i]);
+    p->host_sub[i] = nullptr;
+    if (p->host_join[i]) cudaEventDestroy(p->host_join[i]);
+    p->host_join[i] = nullptr;
+  }
+  for (int i = 0; i < 3; ++i) {
+    if (p->host_st[i]) cudaStreamDestroy(p->host_st[i]);
+    p->host_st[i] = nullptr;
+  }
+  for (int c = 0; c < tcfftPlanImpl::kHostChunks; ++c) {
+    if (p->host_ev_in[c]) cudaEventDestroy(p->host_ev_in[c]);
+    if (p->host_ev_fft[c]) cudaEventDestroy(p->host_ev_fft[c]);
+    p->host_ev_in[c] = p->host_ev_fft[c] = nullptr;
+  }
+  if (p->host_fork) cudaEventDestroy(p->host_fork);
+  p->host_fork = nullptr;
 }
 
 int ilog2_exact(int64_t v) {
@@ -940,6 +957,11 @@ tcfftStatus check_errors(tcfftPlanImpl* p) {
     tcfftStatus rs = check_errors(sp);
     if (r == TCFFT_SUCCESS) r = rs;
   }
+  for (tcfftPlanImpl* sp : p->host_sub)
+    if (sp) {
+      tcfftStatus rs = check_errors(sp);
+      if (r == TCFFT_SUCCESS) r = rs;
+    }
   return r;
 }
 
@@ -1239,6 +1261,7 @@ tcfftStatus tcfftPlanMany(tcfftPlan* out, int64_t count, const int32_t* ranks, c
       launches += sub->sched.launches;
     }
     p->total_elems += sz * (int64_t)idx.size();
+    for (int64_t i : idx) p->span_elems = std::max(p->span_elems, offsets[i] + sz);
   }
   if (st == TCFFT_SUCCESS && !mv_user.empty()) {
     const size_t nb = mv_user.size() * sizeof(long long);
@@ -1278,6 +1301,85 @@ tcfftStatus tcfftPlanMany(tcfftPlan* out, int64_t count, const int32_t* ranks, c
 }
 
 tcfftStatus tcfftExecute(tcfftPlan plan, void* data, void* stream) { return exec_plan(plan, data, stream, 0); }
+
+tcfftStatus tcfftExecuteHost(tcfftPlan plan, const void* host_in, void* host_out, void* work, void* stream) {
+  if (!plan || plan->magic != tcfftPlanImpl::kMagic) return TCFFT_INVALID_PLAN;
+  if (!host_in || !host_out || !work) return TCFFT_INVALID_VALUE;
+  if ((reinterpret_cast<uintptr_t>(work) & 127) != 0) return TCFFT_MISALIGNED;
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  const int64_t es = plan->precision == TCFFT_PRECISION_SPLIT ? 8 : 4;
+  const int64_t per = plan->kind == 2 ? plan->nx * plan->ny : plan->n;  // elements per transform
+  const int64_t total = (plan->kind == 3 ? plan->span_elems : plan->total_elems) * es;
+  const int K = plan->kind == 3 ? 1 : (int)std::min<int64_t>(tcfftPlanImpl::kHostChunks, plan->batch);
+  if (K <= 1) {  // unchunked
+    if (cuda_status(cudaMemcpyAsync(work, host_in, total, cudaMemcpyHostToDevice, st), "copy in"))
+      return TCFFT_CUDA_ERROR;
+    tcfftStatus r = exec_plan(plan, work, stream, 0);
+    if (r != TCFFT_SUCCESS) return r;
+    return cuda_status(cudaMemcpyAsync(host_out, work, total, cudaMemcpyDeviceToHost, st), "copy out");
+  }
+  const int64_t b0 = plan->batch / K, extra = plan->batch % K;  // chunks 0..extra-1 hold b0 + 1
+  if (!plan->host_st[0] || plan->host_b0 != b0) {
+    for (int i = 0; i < 2; ++i)
+      if (plan->host_sub[i]) {
+        tcfftDestroy(plan->host_sub[i]);
+        plan->host_sub[i] = nullptr;
+      }
+    tcfftOptions o;
+    tcfftOptionsDefault(&o);
+    o.precision = plan->precision;
+    o.input_order = plan->input_order;
+    for (int i = 0; i < 2; ++i) {
+      const int64_t b = b0 + i;
+      if (b == 0 || (i == 1 && extra == 0)) continue;
+      const tcfftStatus r = plan->kind == 2 ? tcfftPlan2d(&plan->host_sub[i], plan->nx, plan->ny, b, &o)
+                                            : tcfftPlan1d(&plan->host_sub[i], plan->n, b, &o);
+      if (r != TCFFT_SUCCESS) return r;
+    }
+    plan->host_b0 = b0;
+    for (int i = 0; i < 3; ++i)
+      if (!plan->host_st[i] && cudaStreamCreateWithFlags(&plan->host_st[i], cudaStreamNonBlocking) != cudaSuccess)
+        return TCFFT_CUDA_ERROR;
+    for (cudaEvent_t* e : {&plan->host_fork, &plan->host_join[0], &plan->host_join[1]})
+      if (!*e && cudaEventCreateWithFlags(e, cudaEventDisableTiming) != cudaSuccess) return TCFFT_CUDA_ERROR;
+    for (int c = 0; c < tcfftPlanImpl::kHostChunks; ++c)
+      if ((!plan->host_ev_in[c] && cudaEventCreateWithFlags(&plan->host_ev_in[c], cudaEventDisableTiming)) ||
+          (!plan->host_ev_fft[c] && cudaEventCreateWithFlags(&plan->host_ev_fft[c], cudaEventDisableTiming)))
+        return TCFFT_CUDA_ERROR;
+  }
+  cudaStream_t sin = plan->host_st[0], sfft = plan->host_st[1], sout = plan->host_st[2];
+  if (cuda_status(cudaEventRecord(plan->host_fork, st), "fork")) return TCFFT_CUDA_ERROR;
+  for (cudaStream_t x : {sin, sfft, sout})
+    if (cuda_status(cudaStreamWaitEvent(x, plan->host_fork, 0), "fork")) return TCFFT_CUDA_ERROR;
+  int64_t first = 0;  // first transform of the chunk
+  for (int c = 0; c < K; ++c) {
+    const int64_t b = b0 + (c < extra ? 1 : 0);
+    const int64_t off = first * per * es, bytes = b * per * es;
+    unsigned char* dev = static_cast<unsigned char*>(work) + off;
+    if (cuda_status(cudaMemcpyAsync(dev, static_cast<const unsigned char*>(host_in) + off, bytes,
+                                    cudaMemcpyHostToDevice, sin),
+                    "copy in") ||
+        cuda_status(cudaEventRecord(plan->host_ev_in[c], sin), "copy in") ||
+        cuda_status(cudaStreamWaitEvent(sfft, plan->host_ev_in[c], 0), "copy in"))
+      return TCFFT_CUDA_ERROR;
+    const tcfftStatus r = exec_plan(plan->host_sub[b == b0 ? 0 : 1], dev, sfft, 0);
+    if (r != TCFFT_SUCCESS) return r;
+    if (cuda_status(cudaEventRecord(plan->host_ev_fft[c], sfft), "transform") ||
+        cuda_status(cudaStreamWaitEvent(sout, plan->host_ev_fft[c], 0), "transform") ||
+        cuda_status(cudaMemcpyAsync(static_cast<unsigned char*>(host_out) + off, dev, bytes, cudaMemcpyDeviceToHost,
+                                    sout),
+                    "copy out"))
+      return TCFFT_CUDA_ERROR;
+    first += b;
+  }
+  // `stream` continues after the last transform and the last copy out
+  if (cuda_status(cudaEventRecord(plan->host_join[0], sfft), "join") ||
+      cuda_status(cudaEventRecord(plan->host_join[1], sout), "join") ||
+      cuda_status(cudaStreamWaitEvent(st, plan->host_join[0], 0), "join") ||
+      cuda_status(cudaStreamWaitEvent(st, plan->host_join[1], 0), "join"))
+    return TCFFT_CUDA_ERROR;
+  return TCFFT_SUCCESS;
+}
 
 tcfftStatus tcfftExecuteAdjoint(tcfftPlan plan, void* data, void* stream) {
   return exec_plan(plan, data, stream, 1);

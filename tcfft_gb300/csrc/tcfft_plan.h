@@ -40,6 +40,7 @@ struct tcfftPlanImpl {
   int precision = 0, input_order = 0;
   int device = -1, num_sms = 0;
   int64_t total_elems = 0;
+  int64_t span_elems = 0;  // elements from the buffer start to the end of the last transform
   tcfft::Schedule sched;
   tcfft::DeviceTables tables;
   // fused executor resources
@@ -80,6 +81,14 @@ struct tcfftPlanImpl {
   cudaEvent_t join_ev[kBranches] = {};
   void* graph_ptr[2] = {nullptr, nullptr};
   cudaGraphExec_t graph_exec[2] = {nullptr, nullptr};
+  // tcfftExecuteHost: sub-plans for the chunk batches (created on first use), copy-in,
+  // compute and copy-out streams, per-chunk events
+  static constexpr int kHostChunks = 8;
+  tcfftPlanImpl* host_sub[2] = {nullptr, nullptr};  // chunk batches b0 and b0 + 1
+  int64_t host_b0 = 0;
+  cudaStream_t host_st[3] = {};
+  cudaEvent_t host_ev_in[kHostChunks] = {}, host_ev_fft[kHostChunks] = {};
+  cudaEvent_t host_fork = nullptr, host_join[2] = {};
   // autotuner: chosen lag multiplier of the fused executor (1 = built-in)
   double lag_scale = 1.0;
   // reference input order (TCFFT_ORDER_REFERENCE_DIGIT_REVERSED)
