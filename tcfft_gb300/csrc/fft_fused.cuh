@@ -350,11 +350,11 @@ struct FusedCfg {
   static constexpr int kLen0 = role_len(ROLE0, R0), kLen1 = role_len(ROLE1, R1);  // FFT lengths
   static constexpr int kTile0 = C0 * kLen0;  // elements per tile
   static constexpr int kTile1 = C1 * kLen1;
-  // 1D row-transpose schedules move up to 4 tiles per work item (kSub0/kSub1),
+  // 1D row-transpose and 2D schedules move up to 4 tiles per work item (kSub0/kSub1),
   // so that every item fills a 64 KiB stage: fewer, larger TMA transactions and
   // fewer per-item waits for tiles smaller than a stage (host T0/T1 count tiles;
   // the launcher passes items)
-  static constexpr bool kSubOK = k1D && ROLE1 == kRoleRowT;
+  static constexpr bool kSubOK = (k1D && ROLE1 == kRoleRowT) || (ROLE0 == kRoleRow && ROLE1 == kRoleCol);
   static constexpr int kSub0 = fused_sub_of(kSubOK, kTile0 * kES);
   static constexpr int kSub1 = fused_sub_of(kSubOK, kTile1 * kES);
   static constexpr int kItem0 = kSub0 * kTile0, kItem1 = kSub1 * kTile1;  // elements per work item
@@ -501,17 +501,22 @@ __global__ void __launch_bounds__(384, 1)  // 12 warps at launch: 168 registers 
               tma_load_5d(dst + u * (Cfg::kTile0 * ES), &maps.load0, cg * C0, 0, 0, 0, col_blk<SPLIT>(it.b, R0),
                           &full[s]);
             }
-          } else {  // contiguous rows
-            const int y0 = (int)(((long long)it.b * p.rows0 + (long long)it.tile * C0) * (256 * R0) / ER);
+          } else {  // contiguous rows (the item's tiles are consecutive row groups)
+            const int y0 =
+                (int)(((long long)it.b * p.rows0 + (long long)it.tile * (Cfg::kSub0 * C0)) * (256 * R0) / ER);
 #pragma unroll 1
-            for (int i = 0; i < Cfg::kTile0 / (ER * Cfg::kBH0); ++i)
+            for (int i = 0; i < Cfg::kItem0 / (ER * Cfg::kBH0); ++i)
               tma_load_2d(dst + i * (ER * Cfg::kBH0 * ES), &maps.load0, 0, y0 + Cfg::kBH0 * i, &full[s]);
           }
         } else {
           mbar_arrive_expect_tx(&full[s], Cfg::kItem1 * ES);
           if constexpr (ROLE1 == kRoleCol) {
-            const int cg = it.tile % p.cols1;
-            tma_load_5d(dst, &maps.load1, cg * C1, 0, 0, 0, col_blk<SPLIT>(it.b, R1), &full[s]);
+#pragma unroll 1
+            for (int u = 0; u < Cfg::kSub1; ++u) {
+              const int cg = (it.tile * Cfg::kSub1 + u) % p.cols1;
+              tma_load_5d(dst + u * (Cfg::kTile1 * ES), &maps.load1, cg * C1, 0, 0, 0, col_blk<SPLIT>(it.b, R1),
+                          &full[s]);
+            }
           } else {
             // 1D: source is the scratch slot; 2D never has a contiguous phase 1
             const long long row0 = (long long)slot * p.rows1 + (long long)it.tile * (Cfg::kSub1 * C1);
@@ -576,15 +581,19 @@ __global__ void __launch_bounds__(384, 1)  // 12 warps at launch: 168 registers 
                            src + u * (Cfg::kTile0 * ES));
             }
           } else {
-            const int y0 = (int)(((long long)it.b * p.rows0 + (long long)it.tile * C0) * (256 * R0) / ER);
+            const int y0 =
+                (int)(((long long)it.b * p.rows0 + (long long)it.tile * (Cfg::kSub0 * C0)) * (256 * R0) / ER);
 #pragma unroll 1
-            for (int i = 0; i < Cfg::kTile0 / (ER * Cfg::kBH0); ++i)
+            for (int i = 0; i < Cfg::kItem0 / (ER * Cfg::kBH0); ++i)
               tma_store_2d(&maps.store0, 0, y0 + Cfg::kBH0 * i, src + i * (ER * Cfg::kBH0 * ES));
           }
         } else {
           if constexpr (ROLE1 == kRoleCol) {
-            const int cg = it.tile % p.cols1;
-            tma_store_5d(&maps.store1, cg * C1, 0, 16 * it.b, 0, 0, src);
+#pragma unroll 1
+            for (int u = 0; u < Cfg::kSub1; ++u) {
+              const int cg = (it.tile * Cfg::kSub1 + u) % p.cols1;
+              tma_store_5d(&maps.store1, cg * C1, 0, 16 * it.b, 0, 0, src + u * (Cfg::kTile1 * ES));
+            }
           } else if constexpr (ROLE1 == kRoleRowT) {  // output columns k1 of data viewed [B][N2 rows k2][N1 cols]
 #pragma unroll 1
             for (int u = 0; u < Cfg::kSub1; ++u)
@@ -715,6 +724,9 @@ __global__ void __launch_bounds__(384, 1)  // 12 warps at launch: 168 registers 
           }
          }
         } else {  // kRoleRow: contiguous rows j = warp + 8 jn in place (2D phase 0)
+#pragma unroll 1
+         for (int u = 0; u < Cfg::kSub0; ++u) {
+          const uint32_t base = smem_addr(smem + s * Cfg::kStageBytes) + u * (Cfg::kTile0 * ES);
           constexpr int JN = C0 / 8;
           auto rowb = [&](int jn) { return base + (uint32_t)((warp + 8 * jn) * 256 * R0 * ES); };
           auto ld = [&](int jn, int n) { return lds_elem<SPLIT>(rowb(jn) + swz_w<ES>(n) * ES); };
@@ -751,11 +763,17 @@ __global__ void __launch_bounds__(384, 1)  // 12 warps at launch: 168 registers 
                 }
               }
             }
+         }
         }
       } else {
         if constexpr (ROLE1 == kRoleCol && !SPLIT) {
-          plain_col_tile<R1, C1, false, PI, RHO>(jc, fold1, base, warp, p.dsign, 0, wn);
+#pragma unroll 1
+          for (int u = 0; u < Cfg::kSub1; ++u)
+            plain_col_tile<R1, C1, false, PI, RHO>(jc, fold1, base + u * (Cfg::kTile1 * ES), warp, p.dsign, 0, wn);
         } else if constexpr (ROLE1 == kRoleCol) {
+#pragma unroll 1
+         for (int u = 0; u < Cfg::kSub1; ++u) {
+          const uint32_t base = smem_addr(smem + s * Cfg::kStageBytes) + u * (Cfg::kTile1 * ES);
           constexpr int JN = C1 / 8;
           constexpr int TWS = Cfg::kLmax / (256 * R1);
           const int col0 = JN * warp;
@@ -777,6 +795,7 @@ __global__ void __launch_bounds__(384, 1)  // 12 warps at launch: 168 registers 
             auto st = [&](int jn, int k, int q, int, float2 v) { sts_elem<SPLIT>(oaddr(jn, k, q), v); };
             fft256r_jobs<R1, SPLIT, TWS, JN>(jc, twR, p.dsign, ld, st);
           }
+         }
         } else if constexpr (ROLE1 == kRoleRow16T) {
           // 16 short rows per warp (one S1 job), held in registers, then written
           // transposed as [k0 + 16 q rows][C1 cols] in boxes of kBW columns

@@ -17,11 +17,16 @@ cudaError_t launch_t(const FusedMaps& maps, const FusedParams& p, int num_sms, c
     init_err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg::kSmem);
   });
   if (init_err != cudaSuccess) return init_err;
-  const long long items = (long long)(p.batch + p.D) * (p.T0 + p.T1);
+  // p.T0 / p.T1 count tiles per transform; the kernel works on items of kSub0 / kSub1 tiles
+  if (p.T0 % Cfg::kSub0 != 0 || p.T1 % Cfg::kSub1 != 0) return cudaErrorInvalidValue;
+  FusedParams q = p;
+  q.T0 = p.T0 / Cfg::kSub0;
+  q.T1 = p.T1 / Cfg::kSub1;
+  const long long items = (long long)(q.batch + q.D) * (q.T0 + q.T1);
   long long grid = num_sms;
   if (grid > items) grid = items;
   if (grid_out) *grid_out = (int)grid;
-  kern<<<(int)grid, Cfg::kThreads, Cfg::kSmem, st>>>(maps, p);
+  kern<<<(int)grid, Cfg::kThreads, Cfg::kSmem, st>>>(maps, q);
   return cudaGetLastError();
 }
 }  // namespace

@@ -259,7 +259,7 @@ thread_local double g_lag_override = 0.0;
 void fused_lag(int T0, int T1, int64_t batch, Schedule& s, const FusedKey* key = nullptr) {
   static const double env_scale = getenv("TCFFT_LAG_SCALE") ? atof(getenv("TCFFT_LAG_SCALE")) : 1.0;
   double scale = g_lag_override > 0.0 ? g_lag_override : env_scale;
-  if (key && key->role1 == kRoleRowT) {
+  if (key && (key->role1 == kRoleRowT || (key->role0 == kRoleRow && key->role1 == kRoleCol))) {
     const int es = key->split ? 8 : 4;
     const int s0 = fused_sub_of(true, key->C0 * 256 * key->R0 * es), s1 = fused_sub_of(true, key->C1 * 256 * key->R1 * es);
     if (s0 > 1 || s1 > 1) scale *= 1.25 * (double)(T0 * s0 + T1 * s1) / (double)(T0 + T1);
@@ -426,7 +426,7 @@ tcfftStatus choose_2d(int64_t nx, int64_t ny, int64_t batch, int precision, Sche
   s.key = k;
   s.T0 = (int)(nx / k.C0);
   s.T1 = (int)(ny / k.C1);
-  fused_lag(s.T0, s.T1, batch, s);
+  fused_lag(s.T0, s.T1, batch, s, &k);
   s.launches = 1;
   char buf[160];
   snprintf(buf, sizeof buf, "fused2d(%s): %lld x %lld, phase0 rows R=%d C=%d, phase1 columns R=%d C=%d, lag %d",
