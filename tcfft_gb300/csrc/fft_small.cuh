@@ -19,6 +19,7 @@
 // the same global rows).
 #pragma once
 #include "fft_common.cuh"
+#include "fft_job.cuh"
 
 namespace tcfft {
 
@@ -33,9 +34,12 @@ struct SmallCfg {
   static constexpr int kBoxes = kTE / kBoxElems;
   static constexpr int kTileBytes = kTE * kES;
   static constexpr int kStages = 3;
-  static constexpr int kTabBytes = R > 1 ? kN * 8 : 0;  // W_N^j table in shared memory (radix-R twiddles)
+  // split: W_N^j table (radix-R twiddles); plain: the folded radix-R tables (per-q DFT
+  // matrices and stage-1 twiddles, fft256r_jobs_fold) in place of it
+  static constexpr bool kFold = !SPLIT && R > 1;
+  static constexpr int kTabBytes = kFold ? FoldTab<R>::kBytes : (R > 1 ? kN * 8 : 0);
   static constexpr int kSmem = kStages * kTileBytes + kTabBytes + 1024 + 64;
-  static constexpr int kMinBlocks = (kStages * kTileBytes <= 100 * 1024) ? 2 : 1;
+  static constexpr int kMinBlocks = (kSmem <= 112 * 1024) ? 2 : 1;
   static_assert(kTE % kBoxElems == 0, "tile must be whole TMA boxes");
   // bank-conflict-free slot permutations (see fft_common.cuh)
   using PI = typename std::conditional<SPLIT, BitPerm<0, 1, 2, 3>, BitPerm<0, 1, 3, 2>>::type;
@@ -73,7 +77,9 @@ __global__ void __launch_bounds__(256, SmallCfg<R, SPLIT>::kMinBlocks)
     for (int s = 0; s < C::kStages; ++s) mbar_init(&full[s], 1);
     fence_barrier_init();
   }
-  if constexpr (R > 1)
+  if constexpr (C::kFold)
+    build_fold_table<R, PI, RHO>(reinterpret_cast<unsigned char*>(s_tw), p.tw, tid, blockDim.x);
+  else if constexpr (R > 1)
     for (int j = tid; j < C::kN; j += blockDim.x) s_tw[j] = p.tw[j * (2048 / C::kN)];
   __syncthreads();
 
@@ -90,6 +96,8 @@ __global__ void __launch_bounds__(256, SmallCfg<R, SPLIT>::kMinBlocks)
     for (int i = 0; i < C::kStages && i < ntile_cta; ++i) issue_load(i);
 
   // ---- per-thread constants
+  JobConsts<false> jc;  // the fold path's fragments and stage-1 twiddles
+  if constexpr (C::kFold) init_job_consts<false, PI, RHO>(jc, p.tw);
   uint32_t afr[2][2][4], afr_lo[2][2][4];
   build_dft_frags<PI, RHO>(p.tw, 128, afr, afr_lo, SPLIT);
   float2 tw1[2][2][2];  // W256^(m0 k0) for stage-1 output (j, h, e)
@@ -136,6 +144,29 @@ __global__ void __launch_bounds__(256, SmallCfg<R, SPLIT>::kMinBlocks)
 #pragma unroll 1
     for (int jj = 0; jj < (ok ? C::kJPW : 0); ++jj) {
       const uint32_t job = smem_addr(tile_base) + (uint32_t)((warp * C::kJPW + jj) * C::kN * C::kES);
+      if constexpr (C::kFold) {
+        // plain R > 1: radix-R butterfly on packed half2, twiddles folded into the
+        // per-q tensor-core stages; outputs k = q + R k' collected, then stored as R-runs
+        uint32_t res[R][8];
+        auto ld = [&](int, int slot, int a) {
+          return lds32(job + (uint32_t)(a * 256 + in_off[slot >> 2][(slot >> 1) & 1][slot & 1]) * 4);
+        };
+        auto st = [&](int, int osl, int q, float2 v) { res[q][osl] = pack_h2(v.x, v.y); };
+        fft256r_jobs_fold<R, 1, false>(jc, s_tw_addr, p.dsign, ld, st);
+#pragma unroll
+        for (int osl = 0; osl < 8; ++osl) {
+          const uint32_t ob = out_off[osl >> 2][(osl >> 1) & 1][osl & 1];
+          if constexpr (R == 2) {
+            sts64(job + ob * 4, res[0][osl], res[1][osl]);
+          } else {
+#pragma unroll
+            for (int q4 = 0; q4 < R; q4 += 4)
+              sts128(job + swz_w<4>(swz_w<4>(ob) + q4) * 4, res[q4][osl], res[q4 + 1][osl], res[q4 + 2][osl],
+                     res[q4 + 3][osl]);
+          }
+        }
+        continue;
+      }
       // ---------------- load + radix-R (DIF) + twiddle -> B operands per tile q
       uint32_t bhi[R][2][2][2], blo[SPLIT ? R : 1][2][2][2];
       float2 xs[SPLIT ? R : 1][2][2][2];  // split: fp32 operands until the job's scale is known
