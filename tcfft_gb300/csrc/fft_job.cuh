@@ -443,6 +443,59 @@ __device__ __forceinline__ void fft16r_job(const JobConsts<SPLIT>& c, uint32_t t
   }
 }
 
+// fft16r_job_q with the radix-R step folded like fft256r_jobs_fold: the butterfly
+// runs on the packed half2 inputs and the twiddle W_{16R}^(m1 q) is part of the
+// per-q DFT matrix A_q (the A part of FoldTab<R>, built with this PI and RHO).
+template <int R, class PI, class RHO, class Load4F, class StoreF>
+__device__ __forceinline__ void fft16r_job_q_fold(const JobConsts<false>& c, uint32_t tab, float dsign,
+                                                  Load4F&& load4, StoreF&& store) {
+  static_assert(PI::apply(1) == 1 && PI::apply(2) == 4 && PI::apply(4) == 8 && PI::apply(8) == 2,
+                "quad loads need PI = BitPerm<0, 2, 3, 1>");
+  const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+  const uint32_t lane4 = (uint32_t)lane * 4;
+  const uint32_t negmask = dsign > 0.f ? 0x80000000u : 0x00008000u;
+  const uint32_t c8 = pack_h2(0.70710678118654752440f, 0.70710678118654752440f);
+  uint32_t bhi[R][2][2][2];
+#pragma unroll
+  for (int j = 0; j < 2; ++j) {
+    uint32_t w[R][4];
+#pragma unroll
+    for (int a = 0; a < R; ++a) load4(g + 8 * j, a, w[a]);
+#pragma unroll
+    for (int kt = 0; kt < 2; ++kt)
+#pragma unroll
+      for (int r = 0; r < 2; ++r) {
+        uint32_t x[R];
+#pragma unroll
+        for (int a = 0; a < R; ++a) x[a] = w[a][r + 2 * kt];
+        if constexpr (R > 1) dft_small_h<R>(x, negmask, c8);
+#pragma unroll
+        for (int q = 0; q < R; ++q) bhi[q][kt][r][j] = x[q];
+      }
+  }
+  __syncwarp();
+#pragma unroll
+  for (int q = 0; q < R; ++q) {
+    uint32_t aq[2][2][4];
+    if (q == 0) {
+#pragma unroll
+      for (int i = 0; i < 16; ++i) aq[i >> 3][(i >> 2) & 1][i & 3] = c.afr[i >> 3][(i >> 2) & 1][i & 3];
+    } else {
+#pragma unroll
+      for (int i = 0; i < 16; ++i) aq[i >> 3][(i >> 2) & 1][i & 3] = lds32(tab + ((q - 1) * 16 + i) * 128 + lane4);
+    }
+    float acc[2][2][4];
+    dft16_mma(aq, bhi[q], acc);
+#pragma unroll
+    for (int j = 0; j < 2; ++j)
+#pragma unroll
+      for (int h = 0; h < 2; ++h)
+#pragma unroll
+        for (int e = 0; e < 2; ++e) store(2 * t + e + 8 * j, q + R * RHO::apply(g + 8 * h), q, 4 * j + 2 * h + e,
+                                          acc_get(acc, j, h, e));
+  }
+}
+
 // fft16r_job (plain precision) with each lane's inputs read as 16-byte quads:
 // with PI = BitPerm<0, 2, 3, 1> the slots (kt, r) of lane t are the points
 // m1 = 4t + r + 2kt, i.e. the four consecutive points 4t .. 4t + 3 (the word

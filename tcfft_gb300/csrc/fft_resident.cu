@@ -44,7 +44,7 @@ struct ResCfg {
   static constexpr int kLog2N = 8 + 4 + (R1 == 1 ? 0 : (R1 == 2 ? 1 : 2));
   static constexpr int kTwShift = (kLog2N + 1) / 2;
   static constexpr int kTwLo = 1 << kTwShift, kTwHi = kN >> kTwShift;
-  static constexpr int kTabBytes = (kTwLo + kTwHi + kN2) * 8 + FoldTab<1>::kBytes;
+  static constexpr int kTabBytes = (kTwLo + kTwHi + kN2) * 8 + FoldTab<R1>::kBytes;  // + phase-1 fold table
   static constexpr int kSmem = kStages * kStageBytes + kTabBytes + 1024 + 256;
   static constexpr int kThreads = 384;
   static constexpr int kL = R1 == 1 ? 0 : (R1 == 2 ? 1 : 2);  // log2 R1
@@ -126,7 +126,7 @@ __global__ void __launch_bounds__(384, 1) fft_resident_kernel(const __grid_const
   for (int j = tid; j < Cfg::kTwLo; j += blockDim.x) s_twlo[j] = p.twlo[j];
   for (int j = tid; j < Cfg::kTwHi; j += blockDim.x) s_twhi[j] = p.twhi[j];
   for (int j = tid; j < Cfg::kN2; j += blockDim.x) s_tw16[j] = p.tw2048[j * (2048 / Cfg::kN2)];
-  build_fold_table<1, PI, RHO>(s_fold, p.tw2048, tid, blockDim.x);
+  build_fold_table<R1, PI1, RHO>(s_fold, p.tw2048, tid, blockDim.x);  // phase-1 radix-R1 fold
   __syncthreads();
 
   if (warp >= 8) asm volatile("setmaxnreg.dec.sync.aligned.u32 %0;" ::"n"(56));
@@ -213,7 +213,7 @@ __global__ void __launch_bounds__(384, 1) fft_resident_kernel(const __grid_const
           lds128(tbase + (n / C) * Cfg::kTileBytes + ctile_off<C, 4>(col_out_row(kap_of<C>(v, jl), 0), n % C), w);
         };
         auto st = [&](int, int, int q, int slot, float2 val) { out[i][8 * q + slot] = pack_h2(val.x, val.y); };
-        fft16r_job_q<R1, 1, PI1, RHO>(jc1, tw16, p.dsign, ld4, st);
+        fft16r_job_q_fold<R1, PI1, RHO>(jc1, fold, p.dsign, ld4, st);
       }
       named_bar_sync(1, 256);  // every warp has read the stage
       // X[k1 + 256 k2] of transform t at stage row rho (128-byte rows of 32 k1, 128B swizzle):
