@@ -368,11 +368,14 @@ struct FusedCfg {
   static constexpr int kTwShift = (kLog2N + 1) / 2;          // log2 of the low table length
   static constexpr int kTwHi = 1 << (kLog2N - kTwShift);     // N >> shift
   static constexpr bool kFold = !SPLIT;                       // plain 256R-point jobs use fft256r_jobs_fold
-  static constexpr bool kFold1Own = kFold && ROLE1 != kRoleRow16T && R1 != R0;
+  // (short-row phases use the A_q part only; with R1 == R0 they share the phase-0 table,
+  // whose A part comes first)
+  static constexpr bool kFold1Own = kFold && R1 != R0 && R1 > 1;
   static constexpr int kTwRBytes = (SPLIT || ROLE1 == kRoleRow16T) ? kLmax * 8 : 0;
   static constexpr int kWnBytes = k1D ? ((1 << kTwShift) + kTwHi) * 8 : 0;
   static constexpr int kFold0Bytes = kFold ? FoldTab<R0>::kBytes : 0;
-  static constexpr int kFold1Bytes = kFold1Own ? FoldTab<R1>::kBytes : 0;
+  static constexpr int kFold1Bytes =
+      kFold1Own ? (ROLE1 == kRoleRow16T ? FoldTab<R1>::kABytes : FoldTab<R1>::kBytes) : 0;
   static constexpr int kOffWn = kTwRBytes, kOffFold0 = kTwRBytes + kWnBytes, kOffFold1 = kOffFold0 + kFold0Bytes;
   static constexpr int kTabBytes = kTwRBytes + kWnBytes + kFold0Bytes + kFold1Bytes;
   // kRoleRow16T output boxes: kBW columns (128 bytes) each
@@ -458,7 +461,8 @@ __global__ void __launch_bounds__(384, 1)  // 12 warps at launch: 168 registers 
   if constexpr (Cfg::kFold) {
     build_fold_table<R0, typename Cfg::PI, typename Cfg::RHO>(s_fold0, p.tw2048, tid, blockDim.x);
     if constexpr (Cfg::kFold1Own)
-      build_fold_table<R1, typename Cfg::PI, typename Cfg::RHO>(s_fold1, p.tw2048, tid, blockDim.x);
+      build_fold_table<R1, typename Cfg::PI, typename Cfg::RHO, ROLE1 != kRoleRow16T>(s_fold1, p.tw2048, tid,
+                                                                                       blockDim.x);
   }
   __syncthreads();
 
@@ -808,7 +812,12 @@ __global__ void __launch_bounds__(384, 1)  // 12 warps at launch: 168 registers 
               if constexpr (SPLIT) out[8 * q + sl] = val;
               else out[8 * q + sl] = pack_h2(val.x, val.y);
             };
-            fft16r_job<R1, SPLIT, Cfg::kLmax / (16 * R1), PI, RHO>(jc, twR, p.dsign, ld, st);
+            if constexpr (SPLIT) {
+              fft16r_job<R1, SPLIT, Cfg::kLmax / (16 * R1), PI, RHO>(jc, twR, p.dsign, ld, st);
+            } else {
+              auto ldr = [&](int v, int n) { return lds32(rb + swz_w<4>(v * Cfg::kLen1 + n) * 4); };
+              fft16r_job_fold<R1, PI, RHO>(jc, fold1, p.dsign, ldr, st);
+            }
           }
           named_bar_sync(1, 256);
           {

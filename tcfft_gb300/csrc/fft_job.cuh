@@ -222,7 +222,8 @@ struct FoldTab {
 };
 
 // Fill one fold table (all threads of the CTA take part; tw2048 = W_2048^j).
-template <int R, class PI, class RHO>
+// WITH_T = false: the A_q part only (16R-point row jobs have no second stage).
+template <int R, class PI, class RHO, bool WITH_T = true>
 __device__ void build_fold_table(unsigned char* tab, const float2* __restrict__ tw2048, int tid, int nthreads) {
   if constexpr (R > 1) {
     uint32_t* A = reinterpret_cast<uint32_t*>(tab);
@@ -234,7 +235,7 @@ __device__ void build_fold_table(unsigned char* tab, const float2* __restrict__ 
       A[idx] = ct == 0 ? pack_h2(w.x, -w.y) : pack_h2(w.y, w.x);
     }
     float2* T = reinterpret_cast<float2*>(tab + FoldTab<R>::kABytes);
-    for (int idx = tid; idx < (R - 1) * 8 * 32; idx += nthreads) {
+    for (int idx = tid; idx < (WITH_T ? (R - 1) * 8 * 32 : 0); idx += nthreads) {
       const int q = idx / 256 + 1, sl = (idx >> 5) & 7, lane = idx & 31, g = lane >> 2, t = lane & 3;
       const int j = sl >> 2, h = (sl >> 1) & 1, e = sl & 1;
       const int m0 = PI::apply(2 * t + e + 8 * j), k0 = RHO::apply(g + 8 * h);
@@ -473,6 +474,53 @@ __device__ __forceinline__ void fft16r_job_q_fold(const JobConsts<false>& c, uin
         for (int q = 0; q < R; ++q) bhi[q][kt][r][j] = x[q];
       }
   }
+  __syncwarp();
+#pragma unroll
+  for (int q = 0; q < R; ++q) {
+    uint32_t aq[2][2][4];
+    if (q == 0) {
+#pragma unroll
+      for (int i = 0; i < 16; ++i) aq[i >> 3][(i >> 2) & 1][i & 3] = c.afr[i >> 3][(i >> 2) & 1][i & 3];
+    } else {
+#pragma unroll
+      for (int i = 0; i < 16; ++i) aq[i >> 3][(i >> 2) & 1][i & 3] = lds32(tab + ((q - 1) * 16 + i) * 128 + lane4);
+    }
+    float acc[2][2][4];
+    dft16_mma(aq, bhi[q], acc);
+#pragma unroll
+    for (int j = 0; j < 2; ++j)
+#pragma unroll
+      for (int h = 0; h < 2; ++h)
+#pragma unroll
+        for (int e = 0; e < 2; ++e) store(2 * t + e + 8 * j, q + R * RHO::apply(g + 8 * h), q, 4 * j + 2 * h + e,
+                                          acc_get(acc, j, h, e));
+  }
+}
+
+// The same with one element per load: LOAD(v, n) -> packed half2 point n of
+// transform v (fft16r_job's slot layout, any PI).
+template <int R, class PI, class RHO, class LoadF, class StoreF>
+__device__ __forceinline__ void fft16r_job_fold(const JobConsts<false>& c, uint32_t tab, float dsign, LoadF&& load,
+                                                StoreF&& store) {
+  const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+  const uint32_t lane4 = (uint32_t)lane * 4;
+  const uint32_t negmask = dsign > 0.f ? 0x80000000u : 0x00008000u;
+  const uint32_t c8 = pack_h2(0.70710678118654752440f, 0.70710678118654752440f);
+  uint32_t bhi[R][2][2][2];
+#pragma unroll
+  for (int kt = 0; kt < 2; ++kt)
+#pragma unroll
+    for (int r = 0; r < 2; ++r)
+#pragma unroll
+      for (int j = 0; j < 2; ++j) {
+        const int m1 = PI::apply(2 * t + r + 8 * kt), v = g + 8 * j;
+        uint32_t x[R];
+#pragma unroll
+        for (int a = 0; a < R; ++a) x[a] = load(v, m1 + 16 * a);
+        if constexpr (R > 1) dft_small_h<R>(x, negmask, c8);
+#pragma unroll
+        for (int q = 0; q < R; ++q) bhi[q][kt][r][j] = x[q];
+      }
   __syncwarp();
 #pragma unroll
   for (int q = 0; q < R; ++q) {
