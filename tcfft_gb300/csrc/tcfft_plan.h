@@ -83,7 +83,7 @@ struct tcfftPlanImpl {
   cudaGraphExec_t graph_exec[2] = {nullptr, nullptr};
   // tcfftExecuteHost: sub-plans for the chunk batches (created on first use), copy-in,
   // compute and copy-out streams, per-chunk events
-  static constexpr int kHostChunks = 8;
+  static constexpr int kHostChunks = 16;
   tcfftPlanImpl* host_sub[2] = {nullptr, nullptr};  // chunk batches b0 and b0 + 1
   int64_t host_b0 = 0;
   cudaStream_t host_st[3] = {};
