@@ -39,6 +39,44 @@ __global__ void __launch_bounds__(256) transpose_kernel(const E* __restrict__ in
   }
 }
 
+// 4-byte elements, R and C multiples of 64: 64 x 64 tiles, every global access a
+// 16-byte vector (16 lanes cover one 256-byte row segment on both sides); the tile
+// goes through shared memory with a one-word row pad, so the column-wise reads of
+// the transposed side spread over the banks.
+__global__ void __launch_bounds__(256) transpose64_kernel(const uint4* __restrict__ in, uint4* __restrict__ out,
+                                                          long long B, long long R, long long C) {
+  __shared__ uint32_t tile[64][65];
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  const long long tr = R / 64, tc = C / 64, per = tr * tc, total = B * per;
+  for (long long t = blockIdx.x; t < total; t += gridDim.x) {
+    const long long b = t / per, rem = t - b * per;
+    const long long r0 = (rem / tc) * 64, c0 = (rem % tc) * 64;
+    const uint4* ib = in + (b * R * C) / 4;
+    uint4* ob = out + (b * R * C) / 4;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const int r = ty + 16 * i;
+      const uint4 v = ib[((r0 + r) * C + c0) / 4 + tx];
+      tile[r][4 * tx] = v.x;
+      tile[r][4 * tx + 1] = v.y;
+      tile[r][4 * tx + 2] = v.z;
+      tile[r][4 * tx + 3] = v.w;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const int c = ty + 16 * i;  // output row (input column)
+      uint4 v;
+      v.x = tile[4 * tx][c];
+      v.y = tile[4 * tx + 1][c];
+      v.z = tile[4 * tx + 2][c];
+      v.w = tile[4 * tx + 3][c];
+      ob[((c0 + c) * R + r0) / 4 + tx] = v;
+    }
+    __syncthreads();
+  }
+}
+
 // out[b][c][r] = in[b][r][c] * W_N^(r c), W_N = exp(-2 pi i dsign / N): the
 // transpose of a four-step FFT with its twiddle (fp32 arithmetic).
 template <bool SPLIT>
@@ -96,6 +134,14 @@ cudaError_t launch_transpose_twiddle(const void* in, void* out, int64_t B, int64
 
 cudaError_t launch_transpose(const void* in, void* out, int64_t B, int64_t R, int64_t C, int es, int num_sms,
                              cudaStream_t st) {
+  if (es == 4 && R % 64 == 0 && C % 64 == 0 &&
+      (reinterpret_cast<uintptr_t>(in) & 15) == 0 && (reinterpret_cast<uintptr_t>(out) & 15) == 0) {
+    const long long tiles64 = B * (R / 64) * (C / 64);
+    const long long blocks64 = tiles64 < (long long)num_sms * 8 ? tiles64 : (long long)num_sms * 8;
+    transpose64_kernel<<<(unsigned)blocks64, 256, 0, st>>>(static_cast<const uint4*>(in), static_cast<uint4*>(out),
+                                                          B, R, C);
+    return cudaGetLastError();
+  }
   const long long tiles = B * ((R + 31) / 32) * ((C + 31) / 32);
   long long blocks = tiles < (long long)num_sms * 16 ? tiles : (long long)num_sms * 16;
   if (blocks < 1) blocks = 1;
