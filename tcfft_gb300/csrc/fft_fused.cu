@@ -52,6 +52,7 @@ cudaError_t launch_fused_1d(const FusedKey& k, const FusedMaps& maps, const Fuse
   TCFFT_FUSED_CASE(kRoleCol, 4, 16, kRoleRowT, 4, 16, false)
   TCFFT_FUSED_CASE(kRoleCol, 8, 8, kRoleRowT, 4, 16, false)
   TCFFT_FUSED_CASE(kRoleCol, 8, 8, kRoleRowT, 8, 8, false)
+  TCFFT_FUSED_CASE(kRoleCol, 4, 16, kRoleRowT, 8, 8, false)
   TCFFT_FUSED_CASE(kRoleCol, 1, 16, kRoleRowT, 1, 16, true)
   TCFFT_FUSED_CASE(kRoleCol, 2, 16, kRoleRowT, 1, 16, true)
   TCFFT_FUSED_CASE(kRoleCol, 2, 16, kRoleRowT, 2, 16, true)
@@ -66,6 +67,7 @@ cudaError_t launch_fused_1d(const FusedKey& k, const FusedMaps& maps, const Fuse
   TCFFT_FUSED_CASE(kRoleCol, 1, 16, kRoleRow16T, 1, 128, true)
   TCFFT_FUSED_CASE(kRoleCol, 1, 16, kRoleRow16T, 2, 128, true)
   TCFFT_FUSED_CASE(kRoleCol, 1, 16, kRoleRow16T, 4, 128, true)
+  TCFFT_FUSED_CASE(kRoleCol, 2, 16, kRoleRow16T, 4, 128, true)
   return cudaErrorNotSupported;
 }
 

@@ -298,9 +298,9 @@ tcfftStatus choose_1d(int64_t n, int64_t batch, int precision, Schedule& s) {
     return TCFFT_SUCCESS;
   }
   const int lg = ilog2_exact(n);
-  if (split && (n == 2048 || n == 32768)) {
-    // beyond the split range of the single-pass kernel (1024) and of the short-row phase
-    // (16 R with R <= 4): N = N1 x 64 from two sub-plans
+  if (split && n == 2048) {
+    // beyond the split range of the single-pass kernel (1024) and below the short-row phase
+    // (16 rows of 16 R): N = N1 x 64 from two sub-plans
     s.kind = Schedule::kFourStep;
     s.N1 = n / 64;
     s.N2 = 64;
@@ -323,12 +323,13 @@ tcfftStatus choose_1d(int64_t n, int64_t batch, int precision, Schedule& s) {
   if (lg >= 12 && lg <= 15) {
     // N = 256 x N2 with short rows N2 = 16 R1: phase 0 columns of 256, phase 1 16 rows per warp
     FusedKey k;
-    // plain 2^15: 512 x 64 (measured 1.24 ms for 2^28 elements against 1.48 ms for 256 x 128
-    // and 1.38 ms for 1024 x 32: 64 KiB column tiles and a radix-4 short-row phase)
-    const int64_t n1 = (!split && lg == 15) ? 512 : 256;
+    // 2^15: 512 x 64 (plain: 1.24 ms for 2^28 elements against 1.48 ms for 256 x 128 and
+    // 1.38 ms for 1024 x 32: 64 KiB column tiles and a radix-4 short-row phase; split: the
+    // short-row phase's R <= 4 limit)
+    const int64_t n1 = lg == 15 ? 512 : 256;
     k.role0 = kRoleCol;
     k.R0 = (int)(n1 / 256);
-    k.C0 = n1 == 512 ? 32 : 16;
+    k.C0 = n1 == 512 ? (split ? 16 : 32) : 16;
     k.role1 = kRoleRow16T;
     k.R1 = (int)(n / n1 / 16);
     k.C1 = 128;
@@ -348,7 +349,10 @@ tcfftStatus choose_1d(int64_t n, int64_t batch, int precision, Schedule& s) {
     return TCFFT_SUCCESS;
   }
   if (lg >= 16 && lg <= 22 && !(split && lg >= 21)) {
-    const int64_t n1 = int64_t(1) << ((lg + 1) / 2), n2 = n / n1;
+    // N1 >= N2 except 2^21: 1024 x 2048 (0.90 ms for 2^28 elements) against 2048 x 1024 (0.94 ms)
+    int64_t n1 = int64_t(1) << ((lg + 1) / 2);
+    if (lg == 21) n1 = 1024;
+    const int64_t n2 = n / n1;
     FusedKey k;
     k.role0 = kRoleCol;
     k.R0 = (int)(n1 / 256);
@@ -374,17 +378,19 @@ tcfftStatus choose_1d(int64_t n, int64_t batch, int precision, Schedule& s) {
     return TCFFT_SUCCESS;
   }
   if ((lg >= 23 || (split && lg >= 21)) && lg <= 27) {
-    // N = N1 x N2, N1 = 2048 (split 1024): column FFTs of N1 with the W_N twiddle into a full-size
-    // scratch (fused kernel, phase 0 only), N1 rows of N2 by a 1D sub-plan, transpose back
-    const int64_t n1 = split ? 1024 : 2048, n2 = n / n1;
+    // N = N1 x N2, N1 = 2048 (split 1024; split 2^21: 512, so that the rows are 4096-point
+    // resident transforms rather than a four-step of 2048): column FFTs of N1 with the W_N
+    // twiddle into a full-size scratch (fused kernel, phase 0 only), N1 rows of N2 by a 1D
+    // sub-plan, transpose back
+    const int64_t n1 = split ? (lg == 21 ? 512 : 1024) : 2048, n2 = n / n1;
     if (batch > (1 << 30)) return TCFFT_INVALID_SIZE;
     FusedKey k;
     k.role0 = kRoleCol;
     k.R0 = (int)(n1 / 256);
-    k.C0 = 8;
+    k.C0 = fused_cols(k.R0, split);
     k.role1 = kRoleRowT;
     k.R1 = k.R0;
-    k.C1 = 8;
+    k.C1 = k.C0;
     k.split = split;
     s.kind = Schedule::kLarge1d;
     s.N1 = n1;
@@ -395,8 +401,8 @@ tcfftStatus choose_1d(int64_t n, int64_t batch, int precision, Schedule& s) {
     s.D = 0;
     s.S = (int)batch;
     s.launches = 3;  // updated with the sub-plan's count at plan time
-    snprintf(buf, sizeof buf, "large1d(%s): N=%lld x %lld, column pass R=%d C=8 -> rows of %lld (sub-plan) -> transpose",
-             split ? "split" : "plain", (long long)n1, (long long)n2, k.R0, (long long)n2);
+    snprintf(buf, sizeof buf, "large1d(%s): N=%lld x %lld, column pass R=%d C=%d -> rows of %lld (sub-plan) -> transpose",
+             split ? "split" : "plain", (long long)n1, (long long)n2, k.R0, k.C0, (long long)n2);
     s.text = buf;
     return TCFFT_SUCCESS;
   }

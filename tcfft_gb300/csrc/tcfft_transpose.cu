@@ -39,39 +39,40 @@ __global__ void __launch_bounds__(256) transpose_kernel(const E* __restrict__ in
   }
 }
 
-// 4-byte elements, R and C multiples of 64: 64 x 64 tiles, every global access a
-// 16-byte vector (16 lanes cover one 256-byte row segment on both sides); the tile
-// goes through shared memory with a one-word row pad, so the column-wise reads of
-// the transposed side spread over the banks.
-__global__ void __launch_bounds__(256) transpose64_kernel(const uint4* __restrict__ in, uint4* __restrict__ out,
-                                                          long long B, long long R, long long C) {
-  __shared__ uint32_t tile[64][65];
+// R and C multiples of T (T = 64 for 4-byte, 32 for 8-byte elements): T x T tiles,
+// every global access a 16-byte vector (16 lanes cover one 256-byte row segment on
+// both sides); the tile goes through shared memory with a one-element row pad, so
+// the column-wise reads of the transposed side spread over the banks.
+template <typename E, int T>
+__global__ void __launch_bounds__(256) transpose_vec_kernel(const uint4* __restrict__ in, uint4* __restrict__ out,
+                                                            long long B, long long R, long long C) {
+  constexpr int V = 16 / sizeof(E);  // elements per 16-byte vector
+  static_assert(V * 16 == T, "16 lanes cover one tile row");
+  __shared__ E tile[T][T + 1];
   const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
-  const long long tr = R / 64, tc = C / 64, per = tr * tc, total = B * per;
+  const long long tr = R / T, tc = C / T, per = tr * tc, total = B * per;
   for (long long t = blockIdx.x; t < total; t += gridDim.x) {
     const long long b = t / per, rem = t - b * per;
-    const long long r0 = (rem / tc) * 64, c0 = (rem % tc) * 64;
-    const uint4* ib = in + (b * R * C) / 4;
-    uint4* ob = out + (b * R * C) / 4;
+    const long long r0 = (rem / tc) * T, c0 = (rem % tc) * T;
+    const uint4* ib = in + (b * R * C) / V;
+    uint4* ob = out + (b * R * C) / V;
 #pragma unroll
-    for (int i = 0; i < 4; ++i) {
+    for (int i = 0; i < T / 16; ++i) {
       const int r = ty + 16 * i;
-      const uint4 v = ib[((r0 + r) * C + c0) / 4 + tx];
-      tile[r][4 * tx] = v.x;
-      tile[r][4 * tx + 1] = v.y;
-      tile[r][4 * tx + 2] = v.z;
-      tile[r][4 * tx + 3] = v.w;
+      const uint4 v = ib[((r0 + r) * C + c0) / V + tx];
+      const E* e = reinterpret_cast<const E*>(&v);
+#pragma unroll
+      for (int k = 0; k < V; ++k) tile[r][V * tx + k] = e[k];
     }
     __syncthreads();
 #pragma unroll
-    for (int i = 0; i < 4; ++i) {
+    for (int i = 0; i < T / 16; ++i) {
       const int c = ty + 16 * i;  // output row (input column)
       uint4 v;
-      v.x = tile[4 * tx][c];
-      v.y = tile[4 * tx + 1][c];
-      v.z = tile[4 * tx + 2][c];
-      v.w = tile[4 * tx + 3][c];
-      ob[((c0 + c) * R + r0) / 4 + tx] = v;
+      E* e = reinterpret_cast<E*>(&v);
+#pragma unroll
+      for (int k = 0; k < V; ++k) e[k] = tile[V * tx + k][c];
+      ob[((c0 + c) * R + r0) / V + tx] = v;
     }
     __syncthreads();
   }
@@ -134,12 +135,17 @@ cudaError_t launch_transpose_twiddle(const void* in, void* out, int64_t B, int64
 
 cudaError_t launch_transpose(const void* in, void* out, int64_t B, int64_t R, int64_t C, int es, int num_sms,
                              cudaStream_t st) {
-  if (es == 4 && R % 64 == 0 && C % 64 == 0 &&
-      (reinterpret_cast<uintptr_t>(in) & 15) == 0 && (reinterpret_cast<uintptr_t>(out) & 15) == 0) {
-    const long long tiles64 = B * (R / 64) * (C / 64);
-    const long long blocks64 = tiles64 < (long long)num_sms * 8 ? tiles64 : (long long)num_sms * 8;
-    transpose64_kernel<<<(unsigned)blocks64, 256, 0, st>>>(static_cast<const uint4*>(in), static_cast<uint4*>(out),
-                                                          B, R, C);
+  const int TV = es == 4 ? 64 : 32;  // vector-kernel tile
+  if ((es == 4 || es == 8) && R % TV == 0 && C % TV == 0 && (reinterpret_cast<uintptr_t>(in) & 15) == 0 &&
+      (reinterpret_cast<uintptr_t>(out) & 15) == 0) {
+    const long long tv = B * (R / TV) * (C / TV);
+    const long long bv = tv < (long long)num_sms * 8 ? tv : (long long)num_sms * 8;
+    if (es == 4)
+      transpose_vec_kernel<uint32_t, 64><<<(unsigned)bv, 256, 0, st>>>(static_cast<const uint4*>(in),
+                                                                       static_cast<uint4*>(out), B, R, C);
+    else
+      transpose_vec_kernel<uint2, 32><<<(unsigned)bv, 256, 0, st>>>(static_cast<const uint4*>(in),
+                                                                    static_cast<uint4*>(out), B, R, C);
     return cudaGetLastError();
   }
   const long long tiles = B * ((R + 31) / 32) * ((C + 31) / 32);
