@@ -211,7 +211,7 @@ def cpu_baseline(size_args, budget_s=10.0):
 
 
 def sweep(torch, tc, precision, lgs=range(8, 25), total=1 << 28):
-    """1D sizes at `total` elements per call (BASELINE's config 2)."""
+    """1D sizes at `total` elements per call (the size-sweep workload)."""
     out = []
     peak, _ = measured_peak()
     es = 4 if precision == "plain" else 8
@@ -235,7 +235,7 @@ def flops_2d(nx, ny, batch):
 
 
 def sweep_2d(torch, tc):
-    """BASELINE's 2D configuration: 1024^2 x 16, 4096^2 x 1, 256^2 x 1024 (plain; 1024^2 also split)."""
+    """The 2D workloads: 1024^2 x 16, 4096^2 x 1, 256^2 x 1024 (plain; 1024^2 also split)."""
     out = []
     peak, _ = measured_peak()
     for nx, ny, batch, prec in ((1024, 1024, 16, "plain"), (4096, 4096, 1, "plain"), (256, 256, 1024, "plain"),
@@ -256,7 +256,7 @@ def sweep_2d(torch, tc):
 
 
 def uneven_batch(torch, tc):
-    """BASELINE's uneven-batch configuration: 512 1D transforms of 2^8..2^16 and 64 2D transforms
+    """The uneven-batch workload: 512 1D transforms of 2^8..2^16 and 64 2D transforms
     of 2^7..2^10 per axis (seed 2), back to back in one buffer, one plan, graph-replayed."""
     import numpy as np
     rng = np.random.default_rng(2)

@@ -12,7 +12,7 @@ TOL_SPLIT = 1e-5
 
 
 def uniform_input(shape, seed):
-    """real, imag iid uniform[-1, 1) in float64 (numpy PCG64, as BASELINE's configs)."""
+    """real, imag iid uniform[-1, 1) in float64 (numpy PCG64, the benchmark workloads' distribution)."""
     rng = np.random.default_rng(seed)
     return rng.uniform(-1.0, 1.0, tuple(shape) + (2,))
 
