@@ -1,6 +1,6 @@
 """CPU: the FP64 analytic gradient used by the GPU autograd tests,
 2 F^H (w * F x), against FP64 central finite differences on 64 random
-coordinates (the differentiation check of the spec configuration)."""
+coordinates (the differentiation workload's check)."""
 import numpy as np
 
 import oracle
