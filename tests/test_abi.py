@@ -85,6 +85,7 @@ def test_null_arguments():
     lib = tc.lib()
     assert lib.tcfftPlan1d(None, 256, 1, None) == 1
     assert lib.tcfftExecute(None, None, None) == 8
+    assert lib.tcfftExecuteHost(None, None, None, None, None) == 8
     assert lib.tcfftDestroy(None) == 8
     assert lib.tcfftOptionsDefault(None) == 1
 
