@@ -206,10 +206,13 @@ struct WnTable {
 // Column tile, in place: JN = C/8 side-by-side columns col0 = JN warp + jn per
 // warp, each an FFT of length 256R down the tile.  With WN (1D four-step phase
 // 0) the output k of column n2 = n2base + jn is multiplied by W_N^(n2 k).
-template <int R, int C, bool WN, class PI, class RHO>
+// JNW: columns per call (default C/8: the 8 warps share the tile in one call; 2 with
+// 32-column tiles: two calls per warp, `warp` and `warp + 8`, fewer live registers).
+template <int R, int C, bool WN, class PI, class RHO, int JNW = C / 8>
 __device__ __forceinline__ void plain_col_tile(const JobConsts<false>& jc, uint32_t fold, uint32_t base, int warp,
                                                float dsign, int n2base, const WnTable& wn) {
-  constexpr int ES = 4, JN = C / 8;
+  constexpr int ES = 4, JN = JNW;
+  static_assert(JN * 8 == C || (JN == 2 && C == 32), "columns per call");
   constexpr bool PAIR = JN % 2 == 0;
   constexpr bool QUAD = JN == 4;  // 128-byte rows: the four columns move as one 16-byte access
   constexpr uint32_t kStep = 256 * C * ES;  // one digit a (input) or q (output) further down
