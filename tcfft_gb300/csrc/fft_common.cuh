@@ -127,11 +127,6 @@ __device__ __forceinline__ void tma_store_2d(const CUtensorMap* map, int x, int 
                "r"(y), "r"(smem_addr(src))
                : "memory");
 }
-__device__ __forceinline__ void tma_store_3d(const CUtensorMap* map, int x, int y, int z, const void* src) {
-  asm volatile("cp.async.bulk.tensor.3d.global.shared::cta.tile.bulk_group [%0, {%1, %2, %3}], [%4];" ::"l"(map),
-               "r"(x), "r"(y), "r"(z), "r"(smem_addr(src))
-               : "memory");
-}
 __device__ __forceinline__ void tma_store_4d(const CUtensorMap* map, int c0, int c1, int c2, int c3, const void* src) {
   asm volatile("cp.async.bulk.tensor.4d.global.shared::cta.tile.bulk_group [%0, {%1, %2, %3, %4}], [%5];" ::"l"(map),
                "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(smem_addr(src))

@@ -193,14 +193,6 @@ __device__ __forceinline__ void fft256r_jobs(const JobConsts<SPLIT>& c, uint32_t
   }
 }
 
-// Single job: LOAD(n), STORE(k, q, slot, float2).
-template <int R, bool SPLIT, int TWS = 1, class LoadF, class StoreF>
-__device__ __forceinline__ void fft256r_job(const JobConsts<SPLIT>& c, uint32_t twR, float dsign, LoadF&& load,
-                                            StoreF&& store) {
-  fft256r_jobs<R, SPLIT, TWS, 1>(
-      c, twR, dsign, [&](int, int n) { return load(n); },
-      [&](int, int k, int q, int sl, float2 v) { store(k, q, sl, v); });
-}
 
 // ---------------------------------------------------------------------------
 // Plain precision with the radix-R twiddle folded into the two MMA stages.
@@ -444,9 +436,15 @@ __device__ __forceinline__ void fft16r_job(const JobConsts<SPLIT>& c, uint32_t t
   }
 }
 
-// fft16r_job_q with the radix-R step folded like fft256r_jobs_fold: the butterfly
-// runs on the packed half2 inputs and the twiddle W_{16R}^(m1 q) is part of the
-// per-q DFT matrix A_q (the A part of FoldTab<R>, built with this PI and RHO).
+// One warp computes 16 FFTs of length 16R (fft16r_job's algorithm and output
+// slots), plain precision, with each lane's inputs read as 16-byte quads and the
+// radix-R step folded like fft256r_jobs_fold: with PI = BitPerm<0, 2, 3, 1> the
+// slots (kt, r) of lane t are the points m1 = 4t + r + 2kt, so LOAD4(v, a, w)
+// fills w[0..3] with the half2 words of points 16a + 4t .. 16a + 4t + 3 of
+// transform v (word r + 2kt is slot (kt, r)); the butterfly runs on the packed
+// half2 inputs and the twiddle W_{16R}^(m1 q) is part of the per-q DFT matrix A_q
+// (the A part of FoldTab<R>, built with this PI and RHO).  STORE(v, k, q, slot,
+// float2) as in fft16r_job.
 template <int R, class PI, class RHO, class Load4F, class StoreF>
 __device__ __forceinline__ void fft16r_job_q_fold(const JobConsts<false>& c, uint32_t tab, float dsign,
                                                   Load4F&& load4, StoreF&& store) {
@@ -534,57 +532,6 @@ __device__ __forceinline__ void fft16r_job_fold(const JobConsts<false>& c, uint3
     }
     float acc[2][2][4];
     dft16_mma(aq, bhi[q], acc);
-#pragma unroll
-    for (int j = 0; j < 2; ++j)
-#pragma unroll
-      for (int h = 0; h < 2; ++h)
-#pragma unroll
-        for (int e = 0; e < 2; ++e) store(2 * t + e + 8 * j, q + R * RHO::apply(g + 8 * h), q, 4 * j + 2 * h + e,
-                                          acc_get(acc, j, h, e));
-  }
-}
-
-// fft16r_job (plain precision) with each lane's inputs read as 16-byte quads:
-// with PI = BitPerm<0, 2, 3, 1> the slots (kt, r) of lane t are the points
-// m1 = 4t + r + 2kt, i.e. the four consecutive points 4t .. 4t + 3 (the word
-// r + 2kt of the quad).  LOAD4(v, a, w) fills w[0..3] with the half2 words of
-// points 16a + 4t .. 16a + 4t + 3 of transform v.  STORE as in fft16r_job.
-template <int R, int TWS, class PI, class RHO, class Load4F, class StoreF>
-__device__ __forceinline__ void fft16r_job_q(const JobConsts<false>& c, uint32_t tw16R, float dsign, Load4F&& load4,
-                                             StoreF&& store) {
-  static_assert(PI::apply(1) == 1 && PI::apply(2) == 4 && PI::apply(4) == 8 && PI::apply(8) == 2,
-                "quad loads need PI = BitPerm<0, 2, 3, 1>");
-  const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-  uint32_t bhi[R][2][2][2];
-#pragma unroll
-  for (int j = 0; j < 2; ++j) {
-    uint32_t w[R][4];
-#pragma unroll
-    for (int a = 0; a < R; ++a) load4(g + 8 * j, a, w[a]);
-#pragma unroll
-    for (int kt = 0; kt < 2; ++kt)
-#pragma unroll
-      for (int r = 0; r < 2; ++r) {
-        if constexpr (R == 1) {
-          bhi[0][kt][r][j] = w[0][r + 2 * kt];
-        } else {
-          const int m1 = 4 * t + r + 2 * kt;
-          float2 x[R];
-#pragma unroll
-          for (int a = 0; a < R; ++a) x[a] = unpack_h2(w[a][r + 2 * kt]);
-          dft_small<R>(x, dsign);
-#pragma unroll
-          for (int q = 1; q < R; ++q) x[q] = cmul(x[q], lds64f(tw16R + ((m1 * q) & (16 * R - 1)) * TWS * 8));
-#pragma unroll
-          for (int q = 0; q < R; ++q) bhi[q][kt][r][j] = pack_h2(x[q].x, x[q].y);
-        }
-      }
-  }
-  __syncwarp();
-#pragma unroll
-  for (int q = 0; q < R; ++q) {
-    float acc[2][2][4];
-    dft16_mma(c.afr, bhi[q], acc);
 #pragma unroll
     for (int j = 0; j < 2; ++j)
 #pragma unroll

@@ -13,7 +13,7 @@
 //           C <= 32 columns);
 //   phase 0: 256-point column FFTs (plain_col_tile) times W_N^(n2 k1);
 //   phase 1: N2-point FFTs of the 256 rows k1, 16 rows per warp job
-//           (fft16r_job_q, 16-byte loads), results held in registers;
+//           (fft16r_job_q_fold, 16-byte loads), results held in registers;
 //   output: after a barrier, X[k1 + 256 k2] written into the stage in a
 //           digit order of (k1, k2) and stored with one 5D TMA box per stage.
 //
