@@ -25,7 +25,12 @@
  * Additions: status codes, stream argument, natural input order by default
  * (the reference expects digit-reversed input, tcfft_doit_half.cpp:38-46;
  * TCFFT_ORDER_REFERENCE_DIGIT_REVERSED reproduces that contract), split
- * precision, the adjoint transform, and uneven batches.
+ * precision, the adjoint transform, uneven batches, host-buffer execution.
+ *
+ * Threads: a plan keeps per-plan device state (scratch, counters, tensor maps
+ * of the last data pointer, lazily built sub-plans), so calls on one plan from
+ * several host threads must be serialised by the caller; different plans are
+ * independent.
  */
 #ifndef TCFFT_GB300_H
 #define TCFFT_GB300_H
