@@ -127,6 +127,22 @@ tcfftStatus tcfftExecuteHost(tcfftPlan plan, const void* host_in, void* host_out
  * by bounded waits since the last check; clears the flag. */
 tcfftStatus tcfftCheckDevice(tcfftPlan plan, void* stream);
 
+/* Limit, in nanoseconds, of every bounded device-side wait of this plan's
+ * two-phase kernels (the cross-CTA completion counters and the shared-memory
+ * ring barriers); 0 restores the default of 2 s.  A wait that runs out stops
+ * its kernel early and raises the flag tcfftCheckDevice reports as
+ * TCFFT_TIMEOUT.  Applies to the plan's sub-plans too.  No counterpart in the
+ * reference, whose kernels never wait on one another. */
+tcfftStatus tcfftSetWaitLimit(tcfftPlan plan, int64_t limit_ns);
+
+/* Test hook for the timeout path: the next execute of this plan starts with
+ * one completion counter preset (on the host, before the launch) to a value
+ * that no number of completed tiles raises to its target, so the waits on it
+ * run out after the wait limit and tcfftCheckDevice returns TCFFT_TIMEOUT.
+ * Nothing faults; the output of that one execute is undefined, later executes
+ * are unaffected.  Two-phase schedules only (others: TCFFT_NOT_SUPPORTED). */
+tcfftStatus tcfftInjectWaitTimeout(tcfftPlan plan);
+
 tcfftStatus tcfftDestroy(tcfftPlan plan);
 
 const char* tcfftGetErrorString(tcfftStatus status);
@@ -177,9 +193,19 @@ const char* tcfftVersion(void);
  * calls ordered on one stream are independent, but calls that overlap on the
  * GPU (different streams or host threads) race and must not be issued
  * concurrently.  The first call on a device looks up the arrays' device
- * addresses (cudaGetSymbolAddress); make it before any stream capture. */
+ * addresses (cudaGetSymbolAddress); make it before any stream capture.
+ *
+ * A bounded device-side wait that runs out (2 s) stops the kernel early and
+ * sets a flag in the static arrays; tcfftCheckDeviceNoAlloc reads it. */
 tcfftStatus tcfftExecute1dNoAlloc(void* data, int64_t n, int64_t batch, int32_t precision, int32_t direction,
                                   void* stream);
+
+/* Status of the allocation-free entry point on the current device:
+ * synchronises `stream`, then returns TCFFT_TIMEOUT (and clears the flag) if a
+ * bounded wait of any tcfftExecute1dNoAlloc call since the last check ran out,
+ * else TCFFT_SUCCESS.  Allocates nothing (the flag is read with
+ * cudaMemcpyFromSymbol).  No counterpart in the reference. */
+tcfftStatus tcfftCheckDeviceNoAlloc(void* stream);
 
 #ifdef __cplusplus
 }

@@ -92,6 +92,9 @@ _SIGNATURES = {
     "tcfftVersion": ([], ctypes.c_char_p),
     "tcfftExecute1dNoAlloc": ([ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_int32, ctypes.c_int32,
                                ctypes.c_void_p], ctypes.c_int),
+    "tcfftCheckDeviceNoAlloc": ([ctypes.c_void_p], ctypes.c_int),
+    "tcfftSetWaitLimit": ([ctypes.c_void_p, ctypes.c_int64], ctypes.c_int),
+    "tcfftInjectWaitTimeout": ([ctypes.c_void_p], ctypes.c_int),
 }
 
 
@@ -265,6 +268,14 @@ class Plan:
         """Synchronise and raise TcfftError(TCFFT_TIMEOUT) if a bounded wait expired."""
         _check(lib().tcfftCheckDevice(self._handle, _stream_handle(stream)), "tcfftCheckDevice")
 
+    def set_wait_limit(self, limit_ns):
+        """Limit of the two-phase kernels' bounded device-side waits (ns; 0 = the 2 s default)."""
+        _check(lib().tcfftSetWaitLimit(self._handle, int(limit_ns)), "tcfftSetWaitLimit")
+
+    def inject_wait_timeout(self):
+        """Test hook: make the next execute's bounded waits run out (tcfftInjectWaitTimeout)."""
+        _check(lib().tcfftInjectWaitTimeout(self._handle), "tcfftInjectWaitTimeout")
+
     @property
     def info(self):
         inf = PlanInfo()
@@ -330,3 +341,9 @@ def execute_1d_noalloc(data, n, batch, precision="plain", adjoint=False, stream=
     _check(lib().tcfftExecute1dNoAlloc(ctypes.c_void_p(ptr), int(n), int(batch), prec, 1 if adjoint else 0,
                                        _stream_handle(stream)), "tcfftExecute1dNoAlloc")
     return data
+
+
+def check_device_noalloc(stream=None):
+    """Synchronise and raise TcfftError(TCFFT_TIMEOUT) if a bounded wait of an
+    allocation-free call ran out since the last check (tcfftCheckDeviceNoAlloc)."""
+    _check(lib().tcfftCheckDeviceNoAlloc(_stream_handle(stream)), "tcfftCheckDeviceNoAlloc")

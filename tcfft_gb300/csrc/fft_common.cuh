@@ -75,13 +75,14 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
       : "memory");
   return ok != 0;
 }
-// Bounded wait (wall clock, kTimeoutNs); on expiry records kDevTimeout in
-// *err and returns false.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* err) {
+// Bounded wait (wall clock, `limit_ns`, by default kTimeoutNs); on expiry
+// records kDevTimeout in *err and returns false.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* err,
+                                          unsigned long long limit_ns = kTimeoutNs) {
   if (mbar_try_wait(bar, parity)) return true;
   const unsigned long long t0 = global_ns();
   while (!mbar_try_wait(bar, parity)) {
-    if (global_ns() - t0 > kTimeoutNs) {
+    if (global_ns() - t0 > limit_ns) {
       if (err) atomicExch(err, kDevTimeout);
       return false;
     }

@@ -60,6 +60,7 @@ struct FusedParams {
   int* cnt1;           // [S] completed phase-1 tiles per slot
   int* err;
   float dsign;
+  unsigned long long wait_ns;  // limit of every bounded wait (0: kTimeoutNs)
 };
 
 // Column tiles: C columns x L rows of C*ES bytes (32, 64 or 128), moved by TMA
@@ -142,12 +143,12 @@ __device__ __forceinline__ int ld_acquire(const int* p) {
 __device__ __forceinline__ void red_release_add(int* p, int v) {
   asm volatile("red.release.gpu.global.add.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
-// Bounded spin until *p >= target.
-__device__ __forceinline__ bool wait_counter(const int* p, int target, int* err) {
+// Bounded spin until *p >= target (at most limit_ns).
+__device__ __forceinline__ bool wait_counter(const int* p, int target, int* err, unsigned long long limit_ns) {
   if (ld_acquire(p) >= target) return true;
   const unsigned long long t0 = global_ns();
   while (ld_acquire(p) < target) {
-    if (global_ns() - t0 > kTimeoutNs) {
+    if (global_ns() - t0 > limit_ns) {
       if (err) atomicExch(err, kDevTimeout);
       return false;
     }
@@ -339,13 +340,16 @@ __device__ __forceinline__ void plain_row_jobs(const JobConsts<false>& jc, uint3
   fft256r_jobs_fold<R, JN, false>(jc, fold, dsign, ld, st);
 }
 
-// Tiles per work item of a 1D row-transpose schedule: as many tiles as fill a
-// 64 KiB stage (at most 4); other schedules move one tile per item.
-__host__ __device__ constexpr int fused_sub_of(bool sub_ok, int tile_bytes) {
-  return !sub_ok || tile_bytes >= 65536 ? 1 : (65536 / tile_bytes > 4 ? 4 : 65536 / tile_bytes);
+// Tiles per work item of a 1D row-transpose schedule: as many tiles as fill an
+// item of `item_bytes` (at most 4); other schedules move one tile per item.
+__host__ __device__ constexpr int fused_sub_of(bool sub_ok, int tile_bytes, int item_bytes = 65536) {
+  return !sub_ok || tile_bytes >= item_bytes ? 1 : (item_bytes / tile_bytes > 4 ? 4 : item_bytes / tile_bytes);
 }
 
-template <int ROLE0, int R0, int C0, int ROLE1, int R1, int C1, bool SPLIT>
+// ITEM_KB: target bytes of one work item (KiB).  64 KiB items run a ring of at
+// most 4 stages; smaller items run deeper rings (up to 8 stages), which keeps
+// more loads in flight per SM for the same shared memory.
+template <int ROLE0, int R0, int C0, int ROLE1, int R1, int C1, bool SPLIT, int ITEM_KB = 64>
 struct FusedCfg {
   static constexpr int kES = SPLIT ? 8 : 4;
   static constexpr int kER = 128 / kES;
@@ -358,8 +362,8 @@ struct FusedCfg {
   // fewer per-item waits for tiles smaller than a stage (host T0/T1 count tiles;
   // the launcher passes items)
   static constexpr bool kSubOK = (k1D && ROLE1 == kRoleRowT) || (ROLE0 == kRoleRow && ROLE1 == kRoleCol);
-  static constexpr int kSub0 = fused_sub_of(kSubOK, kTile0 * kES);
-  static constexpr int kSub1 = fused_sub_of(kSubOK, kTile1 * kES);
+  static constexpr int kSub0 = fused_sub_of(kSubOK, kTile0 * kES, ITEM_KB * 1024);
+  static constexpr int kSub1 = fused_sub_of(kSubOK, kTile1 * kES, ITEM_KB * 1024);
   static constexpr int kItem0 = kSub0 * kTile0, kItem1 = kSub1 * kTile1;  // elements per work item
   static constexpr int kTileMax = kItem0 > kItem1 ? kItem0 : kItem1;
   static constexpr int kStageBytes = kTileMax * kES;
@@ -387,7 +391,8 @@ struct FusedCfg {
   static constexpr int kBH0 = kTile0 / kER < 256 ? kTile0 / kER : 256;
   static constexpr int kBH1 = kTile1 / kER < 256 ? kTile1 / kER : 256;
   static constexpr int kBudget = 225 * 1024 - kTabBytes - 1024 - 256;
-  static constexpr int kStages = kBudget / kStageBytes >= 4 ? 4 : kBudget / kStageBytes;
+  static constexpr int kMaxStages = ITEM_KB >= 64 ? 4 : 8;
+  static constexpr int kStages = kBudget / kStageBytes >= kMaxStages ? kMaxStages : kBudget / kStageBytes;
   static constexpr int kSmem = kStages * kStageBytes + kTabBytes + 1024 + 256;
   static_assert(kStages >= 2, "at least two tile stages");
   // 3 warpgroups: two of compute warps, one holding the producer and storer warps.
@@ -425,10 +430,10 @@ __device__ __forceinline__ Item decode_item(long long idx, const FusedParams& p)
   return it;
 }
 
-template <int ROLE0, int R0, int C0, int ROLE1, int R1, int C1, bool SPLIT>
+template <int ROLE0, int R0, int C0, int ROLE1, int R1, int C1, bool SPLIT, int ITEM_KB>
 __global__ void __launch_bounds__(384, 1)  // 12 warps at launch: 168 registers (3 warps per SM sub-partition)
     fft_fused_kernel(const __grid_constant__ FusedMaps maps, const FusedParams p) {
-  using Cfg = FusedCfg<ROLE0, R0, C0, ROLE1, R1, C1, SPLIT>;
+  using Cfg = FusedCfg<ROLE0, R0, C0, ROLE1, R1, C1, SPLIT, ITEM_KB>;
   constexpr int ES = Cfg::kES, ER = Cfg::kER, NST = Cfg::kStages;
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* smem =
@@ -445,6 +450,7 @@ __global__ void __launch_bounds__(384, 1)  // 12 warps at launch: 168 registers 
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const long long total = (long long)(p.batch + p.D) * (p.T0 + p.T1);
+  const unsigned long long lim = p.wait_ns ? p.wait_ns : kTimeoutNs;
 
   if (tid == 0) {
     for (int s = 0; s < NST; ++s) {
@@ -492,11 +498,11 @@ __global__ void __launch_bounds__(384, 1)  // 12 warps at launch: 168 registers 
         if (it.phase == 0) {
           // the previous occupant of this slot (transform b - S) must be finished, so that
           // the slot's scratch (1D) and completion counters (1D and 2D) are free
-          if (epoch > 0 && !wait_counter(&p.cnt1[slot], epoch * p.T1, p.err)) break;
+          if (epoch > 0 && !wait_counter(&p.cnt1[slot], epoch * p.T1, p.err, lim)) break;
         } else {
-          if (!wait_counter(&p.cnt0[slot], (epoch + 1) * p.T0, p.err)) break;
+          if (!wait_counter(&p.cnt0[slot], (epoch + 1) * p.T0, p.err, lim)) break;
         }
-        if (!mbar_wait(&empty[s], ((cnt / NST) + 1) & 1, p.err)) break;
+        if (!mbar_wait(&empty[s], ((cnt / NST) + 1) & 1, p.err, lim)) break;
         if (it.phase == 1) fence_proxy_async_global();
         unsigned char* dst = smem + s * Cfg::kStageBytes;
         if (it.phase == 0) {
@@ -571,7 +577,7 @@ __global__ void __launch_bounds__(384, 1)  // 12 warps at launch: 168 registers 
         const uint32_t cpar = (cnt / NST) & 1;
         if (!mbar_try_wait(&computed[s], cpar)) {
           release_all();
-          if (!mbar_wait(&computed[s], cpar, p.err)) {
+          if (!mbar_wait(&computed[s], cpar, p.err, lim)) {
             failed = true;
             break;
           }
@@ -655,7 +661,7 @@ __global__ void __launch_bounds__(384, 1)  // 12 warps at launch: 168 registers 
     if (!it.valid) continue;
     const int s = cnt % NST;
     // all compute warps agree on success before any of them enters a named barrier
-    const bool ok = named_bar_and(2, 256, mbar_wait(&full[s], (cnt / NST) & 1, p.err));
+    const bool ok = named_bar_and(2, 256, mbar_wait(&full[s], (cnt / NST) & 1, p.err, lim));
     const uint32_t base = smem_addr(smem + s * Cfg::kStageBytes);
     if constexpr (Cfg::k1D) {
       if (ok && it.phase == 1) {

@@ -240,6 +240,16 @@ void free_tables(tcfftPlanImpl* p) {
   p->host_fork = nullptr;
 }
 
+// SM count of the current device (152 on GB300 when it cannot be queried).
+int current_num_sms() {
+  int dev = 0, n = 0;
+  if (cudaGetDevice(&dev) == cudaSuccess && cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess &&
+      n > 0)
+    return n;
+  cudaGetLastError();
+  return 152;
+}
+
 int ilog2_exact(int64_t v) {
   int r = 0;
   while ((int64_t(1) << r) < v) ++r;
@@ -254,17 +264,19 @@ int ilog2_exact(int64_t v) {
 // Lag multiplier chosen by the autotuner while it times candidates (0: none).
 thread_local double g_lag_override = 0.0;
 
-// Items of several tiles (fused_sub_of) keep more tiles in flight per CTA: the
-// lag grows with the tiles per item (x 1.25, measured at N = 2^16 and 2^17).
-void fused_lag(int T0, int T1, int64_t batch, Schedule& s, const FusedKey* key = nullptr) {
+// Items of several tiles keep more tiles in flight per CTA: the lag grows with
+// the tiles per item (x 1.25, measured at N = 2^16 and 2^17).  Rings deeper than
+// four stages (32 KiB items) keep that many items in flight per CTA.
+void fused_lag(int T0, int T1, int64_t batch, Schedule& s, const FusedKey* key, int num_sms) {
   static const double env_scale = getenv("TCFFT_LAG_SCALE") ? atof(getenv("TCFFT_LAG_SCALE")) : 1.0;
   double scale = g_lag_override > 0.0 ? g_lag_override : env_scale;
-  if (key && (key->role1 == kRoleRowT || (key->role0 == kRoleRow && key->role1 == kRoleCol))) {
-    const int es = key->split ? 8 : 4;
-    const int s0 = fused_sub_of(true, key->C0 * 256 * key->R0 * es), s1 = fused_sub_of(true, key->C1 * 256 * key->R1 * es);
-    if (s0 > 1 || s1 > 1) scale *= 1.25 * (double)(T0 * s0 + T1 * s1) / (double)(T0 + T1);
+  int per_cta = 4;
+  FusedShape sh;
+  if (key && fused_shape(*key, &sh)) {
+    if (sh.stages > per_cta) per_cta = sh.stages;
+    if (sh.sub0 > 1 || sh.sub1 > 1) scale *= 1.25 * (double)(T0 * sh.sub0 + T1 * sh.sub1) / (double)(T0 + T1);
   }
-  const int in_flight = (int)(152 * 4 * scale);  // CTAs x tiles per CTA
+  const int in_flight = (int)(num_sms * per_cta * scale);  // CTAs x tiles per CTA
   int D = (in_flight + (T0 + T1) - 1) / (T0 + T1) + 1;
   if (D > batch) D = (int)batch;
   if (D < 1) D = 1;
@@ -272,8 +284,17 @@ void fused_lag(int T0, int T1, int64_t batch, Schedule& s, const FusedKey* key =
   s.S = 2 * D + 2;
 }
 
+// Work-item size of the 1D two-phase schedules (TCFFT_ITEM_KB overrides it, for measurements).
+int item_kb_1d(int lg, bool split) {
+  static const int env = getenv("TCFFT_ITEM_KB") ? atoi(getenv("TCFFT_ITEM_KB")) : 0;
+  if (env == 32 || env == 64) return env;
+  (void)lg;
+  (void)split;
+  return 64;
+}
+
 // Host-only schedule selection for a 1D size (no CUDA calls).
-tcfftStatus choose_1d(int64_t n, int64_t batch, int precision, Schedule& s) {
+tcfftStatus choose_1d(int64_t n, int64_t batch, int precision, Schedule& s, int num_sms = 152) {
   if (!is_pow2(n) || n < 16 || n > (int64_t(1) << 27)) return TCFFT_INVALID_SIZE;
   if (batch < 1 || batch > (int64_t(1) << 40) / n) return TCFFT_INVALID_SIZE;
   const bool split = precision == TCFFT_PRECISION_SPLIT;
@@ -341,7 +362,7 @@ tcfftStatus choose_1d(int64_t n, int64_t batch, int precision, Schedule& s) {
     s.key = k;
     s.T0 = (int)(s.N2 / k.C0 > 0 ? s.N2 / k.C0 : 1);
     s.T1 = (int)(s.N1 / k.C1);
-    fused_lag(s.T0, s.T1, batch, s);
+    fused_lag(s.T0, s.T1, batch, s, &k, num_sms);
     s.launches = 1;
     snprintf(buf, sizeof buf, "fused1d(%s): N=%lld x %lld, phase0 columns R=%d C=%d, phase1 16-row groups R=%d, lag %d, %d slots",
              split ? "split" : "plain", (long long)s.N1, (long long)s.N2, k.R0, k.C0, k.R1, s.D, s.S);
@@ -356,12 +377,16 @@ tcfftStatus choose_1d(int64_t n, int64_t batch, int precision, Schedule& s) {
     FusedKey k;
     k.role0 = kRoleCol;
     k.R0 = (int)(n1 / 256);
-    k.C0 = fused_cols(k.R0, split);
     k.role1 = kRoleRowT;
     k.R1 = (int)(n2 / 256);
-    k.C1 = fused_cols(k.R1, split);
-    if (getenv("TCFFT_FUSED_C")) k.C0 = k.C1 = atoi(getenv("TCFFT_FUSED_C"));
     k.split = split;
+    for (int ikb : {item_kb_1d(lg, split), 64}) {  // the preferred item size, else 64 KiB items
+      k.item_kb = ikb;
+      k.C0 = fused_cols(k.R0, split, ikb * 1024);
+      k.C1 = fused_cols(k.R1, split, ikb * 1024);
+      if (getenv("TCFFT_FUSED_C")) k.C0 = k.C1 = atoi(getenv("TCFFT_FUSED_C"));
+      if (k.C0 != 0 && k.C1 != 0 && fused_shape(k, nullptr)) break;
+    }
     if (k.C0 == 0 || k.C1 == 0) return TCFFT_NOT_SUPPORTED;
     s.kind = Schedule::kFused1d;
     s.N1 = n1;
@@ -369,11 +394,11 @@ tcfftStatus choose_1d(int64_t n, int64_t batch, int precision, Schedule& s) {
     s.key = k;
     s.T0 = (int)(n2 / k.C0);
     s.T1 = (int)(n1 / k.C1);
-    fused_lag(s.T0, s.T1, batch, s, &k);
+    fused_lag(s.T0, s.T1, batch, s, &k, num_sms);
     s.launches = 1;
     snprintf(buf, sizeof buf,
-             "fused1d(%s): N=%lld x %lld, phase0 columns R=%d C=%d, phase1 rows R=%d C=%d, lag %d, %d slots",
-             split ? "split" : "plain", (long long)n1, (long long)n2, k.R0, k.C0, k.R1, k.C1, s.D, s.S);
+             "fused1d(%s): N=%lld x %lld, phase0 columns R=%d C=%d, phase1 rows R=%d C=%d, %d KiB items, lag %d, %d slots",
+             split ? "split" : "plain", (long long)n1, (long long)n2, k.R0, k.C0, k.R1, k.C1, k.item_kb, s.D, s.S);
     s.text = buf;
     return TCFFT_SUCCESS;
   }
@@ -410,7 +435,7 @@ tcfftStatus choose_1d(int64_t n, int64_t batch, int precision, Schedule& s) {
 }
 
 // Host-only schedule selection for a 2D size.
-tcfftStatus choose_2d(int64_t nx, int64_t ny, int64_t batch, int precision, Schedule& s) {
+tcfftStatus choose_2d(int64_t nx, int64_t ny, int64_t batch, int precision, Schedule& s, int num_sms = 152) {
   if (!is_pow2(nx) || !is_pow2(ny) || nx < 256 || ny < 256 || nx > 2048 || ny > 2048) return TCFFT_INVALID_SIZE;
   if (batch < 1 || batch > (int64_t(1) << 40) / (nx * ny)) return TCFFT_INVALID_SIZE;
   const bool split = precision == TCFFT_PRECISION_SPLIT;
@@ -432,7 +457,7 @@ tcfftStatus choose_2d(int64_t nx, int64_t ny, int64_t batch, int precision, Sche
   s.key = k;
   s.T0 = (int)(nx / k.C0);
   s.T1 = (int)(ny / k.C1);
-  fused_lag(s.T0, s.T1, batch, s, &k);
+  fused_lag(s.T0, s.T1, batch, s, &k, num_sms);
   s.launches = 1;
   char buf[160];
   snprintf(buf, sizeof buf, "fused2d(%s): %lld x %lld, phase0 rows R=%d C=%d, phase1 columns R=%d C=%d, lag %d",
@@ -486,6 +511,15 @@ bool generic2d_tout(const tcfftPlanImpl* p, int axis) {
   if (p->precision != TCFFT_PRECISION_PLAIN || p->total_elems * 4 > kToutMaxBytes) return false;
   return axis == 0 ? p->ny == 4096 && resident_tout_supported(4096, p->nx * p->batch, p->nx)
                    : p->nx == 4096 && resident_tout_supported(4096, p->ny * p->batch, p->ny);
+}
+
+// Armed by tcfftInjectWaitTimeout: after the counter reset, phase-0 completion
+// counter 0 is set to 0x80808080 (a large negative count), which no number of
+// completed tiles raises to its target, so every wait on it runs out.
+bool inject_stall(tcfftPlanImpl* plan, cudaStream_t st) {
+  if (!plan->inject_timeout) return false;
+  plan->inject_timeout = false;
+  return cudaMemsetAsync(plan->counters, 0x80, sizeof(int), st) != cudaSuccess;
 }
 
 tcfftStatus exec_plan(tcfftPlan plan, void* data, void* stream, int dir) {
@@ -560,6 +594,7 @@ tcfftStatus exec_plan(tcfftPlan plan, void* data, void* stream, int dir) {
     fp.cnt1 = plan->counters + s.S;
     fp.err = plan->tables.err;
     fp.dsign = dsign;
+    fp.wait_ns = plan->wait_ns;
     if (cuda_status(cudaMemsetAsync(plan->counters, 0, sizeof(int) * 2 * s.S, st), "counter reset"))
       return TCFFT_CUDA_ERROR;
     int grid = 0;
@@ -672,7 +707,9 @@ tcfftStatus exec_plan(tcfftPlan plan, void* data, void* stream, int dir) {
     fp.cnt1 = plan->counters + s.S;
     fp.err = plan->tables.err;
     fp.dsign = dsign;
-    if (cuda_status(cudaMemsetAsync(plan->counters, 0, sizeof(int) * 2 * s.S, st), "counter reset"))
+    fp.wait_ns = plan->wait_ns;
+    if (cuda_status(cudaMemsetAsync(plan->counters, 0, sizeof(int) * 2 * s.S, st), "counter reset") ||
+        inject_stall(plan, st))
       return TCFFT_CUDA_ERROR;
     int grid = 0;
     return cuda_status(launch_fused(s.key, plan->fmaps, fp, plan->num_sms, st, &grid), "fused launch");
@@ -717,7 +754,9 @@ tcfftStatus exec_plan(tcfftPlan plan, void* data, void* stream, int dir) {
     fp.cnt1 = plan->counters + s.S;
     fp.err = plan->tables.err;
     fp.dsign = dsign;
-    if (cuda_status(cudaMemsetAsync(plan->counters, 0, sizeof(int) * 2 * s.S, st), "counter reset"))
+    fp.wait_ns = plan->wait_ns;
+    if (cuda_status(cudaMemsetAsync(plan->counters, 0, sizeof(int) * 2 * s.S, st), "counter reset") ||
+        inject_stall(plan, st))
       return TCFFT_CUDA_ERROR;
     int grid = 0;
     return cuda_status(launch_fused(s.key, plan->fmaps, fp, plan->num_sms, st, &grid), "fused2d launch");
@@ -879,8 +918,8 @@ void load_tune_file(const char* path) {
 
 tcfftStatus choose_again(tcfftPlanImpl* p, double scale, Schedule& s) {
   g_lag_override = scale;
-  tcfftStatus st = p->kind == 1 ? choose_1d(p->n, p->batch, p->precision, s)
-                                : choose_2d(p->nx, p->ny, p->batch, p->precision, s);
+  tcfftStatus st = p->kind == 1 ? choose_1d(p->n, p->batch, p->precision, s, p->num_sms)
+                                : choose_2d(p->nx, p->ny, p->batch, p->precision, s, p->num_sms);
   g_lag_override = 0.0;
   return st;
 }
@@ -1077,7 +1116,7 @@ tcfftStatus tcfftPlan1d(tcfftPlan* out, int64_t n, int64_t batch, const tcfftOpt
   tcfftOptionsDefault(&o);
   if (opts) o = *opts;
   Schedule s;
-  st = choose_1d(n, batch, o.precision, s);
+  st = choose_1d(n, batch, o.precision, s, current_num_sms());
   if (st != TCFFT_SUCCESS) return st;
   std::vector<int> chain = {(int)n};  // natural order reads as a single radix-N digit
   if (o.input_order == TCFFT_ORDER_REFERENCE_DIGIT_REVERSED) {
@@ -1139,7 +1178,7 @@ tcfftStatus tcfftPlan2d(tcfftPlan* out, int64_t nx, int64_t ny, int64_t batch, c
   tcfftOptionsDefault(&o);
   if (opts) o = *opts;
   Schedule s;
-  st = choose_2d(nx, ny, batch, o.precision, s);
+  st = choose_2d(nx, ny, batch, o.precision, s, current_num_sms());
   if (st != TCFFT_SUCCESS) {
     // shapes outside the fused 2D range: compose from 1D plans (both axes must be valid 1D sizes)
     Schedule sx, sy;
@@ -1401,6 +1440,23 @@ tcfftStatus tcfftCheckDevice(tcfftPlan plan, void* stream) {
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
   if (cudaStreamSynchronize(st) != cudaSuccess) return TCFFT_CUDA_ERROR;
   return check_errors(plan);
+}
+
+tcfftStatus tcfftSetWaitLimit(tcfftPlan plan, int64_t limit_ns) {
+  if (!plan || plan->magic != tcfftPlanImpl::kMagic) return TCFFT_INVALID_PLAN;
+  if (limit_ns < 0) return TCFFT_INVALID_VALUE;
+  plan->wait_ns = (unsigned long long)limit_ns;
+  for (tcfftPlanImpl* sp : plan->subs) tcfftSetWaitLimit(sp, limit_ns);
+  for (tcfftPlanImpl* sp : plan->host_sub)
+    if (sp) tcfftSetWaitLimit(sp, limit_ns);
+  return TCFFT_SUCCESS;
+}
+
+tcfftStatus tcfftInjectWaitTimeout(tcfftPlan plan) {
+  if (!plan || plan->magic != tcfftPlanImpl::kMagic) return TCFFT_INVALID_PLAN;
+  if (plan->sched.kind != Schedule::kFused1d && plan->sched.kind != Schedule::kFused2d) return TCFFT_NOT_SUPPORTED;
+  plan->inject_timeout = true;
+  return TCFFT_SUCCESS;
 }
 
 tcfftStatus tcfftDestroy(tcfftPlan plan) {

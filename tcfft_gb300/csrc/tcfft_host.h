@@ -30,10 +30,17 @@ struct FusedParams;
 struct FusedKey {
   int role0 = 0, R0 = 1, C0 = 16, role1 = 0, R1 = 1, C1 = 16;
   bool split = false;
+  int item_kb = 64;  // work-item size target (KiB): 64 (rings of <= 4 stages) or 32 (<= 8 stages)
 };
-int fused_cols(int R, bool split);
+// Ring shape of one instantiation: stages, tiles per work item in each phase, dynamic shared memory.
+struct FusedShape {
+  int stages = 0, sub0 = 1, sub1 = 1, smem = 0;
+};
+int fused_cols(int R, bool split, int max_tile_bytes = 64 * 1024);
 cudaError_t launch_fused(const FusedKey& k, const FusedMaps& maps, const FusedParams& p, int num_sms,
                          cudaStream_t st, int* grid_out);
+// false if `k` names no compiled instantiation
+bool fused_shape(const FusedKey& k, FusedShape* out);
 // Tensor maps of the 1D two-phase executor (N = n1 * n2; S scratch slots of N elements).
 CUresult encode_fused1d_maps(FusedMaps* maps, const FusedKey& k, void* data, void* scratch, int64_t n1, int64_t n2,
                              int64_t batch, int S);

@@ -27,6 +27,7 @@
 // Set-up: the first call on a device looks up the device addresses of the
 // arrays with cudaGetSymbolAddress (with that device current).  Make that
 // first call before any stream capture; later calls only enqueue work.
+#include <atomic>
 #include <cstdio>
 #include <cstdlib>
 #include <mutex>
@@ -49,7 +50,7 @@ static __device__ __align__(256) int g_counters[2 * kNoAllocMaxSlots];
 static __device__ int g_err;
 
 struct DevicePtrs {
-  bool ready = false;
+  std::atomic<bool> ready{false};  // set (release) after the fields below are filled
   unsigned char* scratch = nullptr;
   float2* tw2048 = nullptr;
   float2* twlo = nullptr;
@@ -85,7 +86,7 @@ __global__ void noalloc_tables_kernel(float2* tw2048, float2* twlo, float2* twhi
 
 cudaError_t setup_device(int dev, DevicePtrs& d) {
   std::lock_guard<std::mutex> lock(g_mu);
-  if (d.ready) return cudaSuccess;
+  if (d.ready.load(std::memory_order_acquire)) return cudaSuccess;
   cudaError_t e;
   if ((e = cudaGetSymbolAddress((void**)&d.scratch, g_scratch)) != cudaSuccess) return e;
   if ((e = cudaGetSymbolAddress((void**)&d.tw2048, g_tw2048)) != cudaSuccess) return e;
@@ -94,7 +95,7 @@ cudaError_t setup_device(int dev, DevicePtrs& d) {
   if ((e = cudaGetSymbolAddress((void**)&d.counters, g_counters)) != cudaSuccess) return e;
   if ((e = cudaGetSymbolAddress((void**)&d.err, g_err)) != cudaSuccess) return e;
   if ((e = cudaDeviceGetAttribute(&d.num_sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
-  d.ready = true;
+  d.ready.store(true, std::memory_order_release);
   return cudaSuccess;
 }
 
@@ -108,6 +109,19 @@ int ilog2_i64(int64_t v) {
 }  // namespace tcfft
 
 using namespace tcfft;
+
+extern "C" tcfftStatus tcfftCheckDeviceNoAlloc(void* stream) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kNoAllocMaxDevices) return TCFFT_CUDA_ERROR;
+  if (cudaStreamSynchronize(reinterpret_cast<cudaStream_t>(stream)) != cudaSuccess) return TCFFT_CUDA_ERROR;
+  if (!g_dev[dev].ready.load(std::memory_order_acquire)) return TCFFT_SUCCESS;  // nothing ran on this device
+  int e = 0;
+  if (cudaMemcpyFromSymbol(&e, g_err, sizeof(int)) != cudaSuccess) return TCFFT_CUDA_ERROR;
+  if (e == 0) return TCFFT_SUCCESS;
+  const int zero = 0;
+  if (cudaMemcpyToSymbol(g_err, &zero, sizeof(int)) != cudaSuccess) return TCFFT_CUDA_ERROR;
+  return TCFFT_TIMEOUT;
+}
 
 extern "C" tcfftStatus tcfftExecute1dNoAlloc(void* data, int64_t n, int64_t batch, int32_t precision,
                                              int32_t direction, void* stream) {
@@ -129,7 +143,7 @@ extern "C" tcfftStatus tcfftExecute1dNoAlloc(void* data, int64_t n, int64_t batc
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kNoAllocMaxDevices) return TCFFT_CUDA_ERROR;
   DevicePtrs& d = g_dev[dev];
-  if (!d.ready) {
+  if (!d.ready.load(std::memory_order_acquire)) {
     cudaError_t e = setup_device(dev, d);
     if (e != cudaSuccess) {
       if (debug) fprintf(stderr, "tcfftExecute1dNoAlloc: set-up failed: %s\n", cudaGetErrorString(e));
@@ -142,11 +156,13 @@ extern "C" tcfftStatus tcfftExecute1dNoAlloc(void* data, int64_t n, int64_t batc
   FusedKey k;
   int64_t n1, n2;
   if (lg <= 15) {
-    n1 = 256;
-    n2 = n / 256;
+    // 256 x (16..64) short rows; 2^15 as 512 x 64 (the plan's choice, and the split short-row
+    // phase's R <= 4 limit)
+    n1 = lg == 15 ? 512 : 256;
+    n2 = n / n1;
     k.role0 = kRoleCol;
-    k.R0 = 1;
-    k.C0 = 16;
+    k.R0 = (int)(n1 / 256);
+    k.C0 = lg == 15 ? (split ? 16 : 32) : 16;
     k.role1 = kRoleRow16T;
     k.R1 = (int)(n2 / 16);
     k.C1 = 128;
@@ -168,7 +184,7 @@ extern "C" tcfftStatus tcfftExecute1dNoAlloc(void* data, int64_t n, int64_t batc
   const int64_t slot_bytes = n * es;
   int max_slots = (int)(kNoAllocScratchBytes / slot_bytes);
   if (max_slots > kNoAllocMaxSlots) max_slots = kNoAllocMaxSlots;
-  int D = (152 * 4 + (T0 + T1) - 1) / (T0 + T1) + 1;
+  int D = (d.num_sms * 4 + (T0 + T1) - 1) / (T0 + T1) + 1;
   if (D > batch) D = (int)batch;
   if (D > (max_slots - 2) / 2) D = (max_slots - 2) / 2;
   if (D < 1) return TCFFT_INVALID_SIZE;
@@ -206,6 +222,7 @@ extern "C" tcfftStatus tcfftExecute1dNoAlloc(void* data, int64_t n, int64_t batc
   fp.cnt1 = d.counters + S;
   fp.err = d.err;
   fp.dsign = direction == 0 ? 1.f : -1.f;
+  fp.wait_ns = 0;  // the default limit
   int grid = 0;
   cudaError_t e = launch_fused(k, maps, fp, d.num_sms, st, &grid);
   if (e != cudaSuccess) {

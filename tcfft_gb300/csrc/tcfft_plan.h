@@ -91,6 +91,10 @@ struct tcfftPlanImpl {
   cudaEvent_t host_fork = nullptr, host_join[2] = {};
   // autotuner: chosen lag multiplier of the fused executor (1 = built-in)
   double lag_scale = 1.0;
+  // limit of the two-phase kernels' bounded waits (0: the default, 2 s) and the
+  // one-shot stall injection of tcfftInjectWaitTimeout
+  unsigned long long wait_ns = 0;
+  bool inject_timeout = false;
   // reference input order (TCFFT_ORDER_REFERENCE_DIGIT_REVERSED)
   std::vector<int> radices_x, radices_y;  // reported chains (x = the 1D chain)
   int* rev_x = nullptr;                   // device digit-reversal tables (nullptr: natural)

@@ -6,7 +6,7 @@ import pytest
 
 import oracle
 import tcfft_gb300 as tc
-from fftcheck import TOL_PLAIN, TOL_SPLIT, oracle_1d, quantize, run_gpu, uniform_input
+from fftcheck import oracle_1d, quantize, run_gpu, tol_plain, tol_split, uniform_input
 
 pytestmark = pytest.mark.gpu
 
@@ -23,11 +23,11 @@ def test_plain_small(cuda_device, n, batch):
     ref = oracle_1d(xq)
     err = oracle.rel_l2(y, ref)
     assert np.isfinite(y).all()
-    assert err < TOL_PLAIN, "n=%d batch=%d rel-L2 %.3e" % (n, batch, err)
+    assert err < tol_plain(n), "n=%d batch=%d rel-L2 %.3e" % (n, batch, err)
     # per-transform error stays uniform (no transform left untouched, cf. the
     # reference's integer grid division tcfft_half.cu:1206)
     per = np.linalg.norm(y - ref, axis=-1) / np.linalg.norm(ref, axis=-1)
-    assert per.max() < 3 * TOL_PLAIN
+    assert per.max() < 3 * tol_plain(n)
 
 
 @pytest.mark.parametrize("n", [256, 512, 1024])
@@ -38,7 +38,7 @@ def test_split_small(cuda_device, n, batch):
     with tc.Plan(n=n, batch=batch, precision="split") as p:
         y = run_gpu(p, xq, "split")
     err = oracle.rel_l2(y, oracle_1d(xq))
-    assert err < TOL_SPLIT, "n=%d batch=%d rel-L2 %.3e" % (n, batch, err)
+    assert err < tol_split(n), "n=%d batch=%d rel-L2 %.3e" % (n, batch, err)
 
 
 @pytest.mark.parametrize("n", SMALL)
@@ -49,7 +49,7 @@ def test_adjoint_small(cuda_device, n):
     with tc.Plan(n=n, batch=batch) as p:
         y = run_gpu(p, xq, "plain", adjoint=True)
     err = oracle.rel_l2(y, oracle_1d(xq, adjoint=True))
-    assert err < TOL_PLAIN
+    assert err < tol_plain(n)
 
 
 @pytest.mark.parametrize("n", SMALL)
@@ -102,7 +102,7 @@ def test_plain_large(cuda_device, n, batch):
     ref = oracle_1d(xq)
     assert np.isfinite(y).all()
     err = oracle.rel_l2(y, ref)
-    assert err < TOL_PLAIN, "n=%d batch=%d rel-L2 %.3e" % (n, batch, err)
+    assert err < tol_plain(n), "n=%d batch=%d rel-L2 %.3e" % (n, batch, err)
 
 
 @pytest.mark.parametrize("n", [1 << 12, 1 << 14, 1 << 16, 1 << 18, 1 << 20])
@@ -113,7 +113,7 @@ def test_split_large(cuda_device, n):
     with tc.Plan(n=n, batch=batch, precision="split") as p:
         y = run_gpu(p, xq, "split")
     err = oracle.rel_l2(y, oracle_1d(xq))
-    assert err < TOL_SPLIT, "n=%d rel-L2 %.3e" % (n, err)
+    assert err < tol_split(n), "n=%d rel-L2 %.3e" % (n, err)
 
 
 @pytest.mark.parametrize("n", [1 << 16, 1 << 20])
@@ -122,7 +122,7 @@ def test_adjoint_large(cuda_device, n):
     xq = quantize(uniform_input((batch, n), seed=5), "plain")
     with tc.Plan(n=n, batch=batch) as p:
         y = run_gpu(p, xq, "plain", adjoint=True)
-    assert oracle.rel_l2(y, oracle_1d(xq, adjoint=True)) < TOL_PLAIN
+    assert oracle.rel_l2(y, oracle_1d(xq, adjoint=True)) < tol_plain(n)
 
 
 def test_large_batch_many_waves(cuda_device):
@@ -133,7 +133,7 @@ def test_large_batch_many_waves(cuda_device):
         y = run_gpu(p, xq, "plain")
     ref = oracle_1d(xq)
     per = np.linalg.norm(y - ref, axis=-1) / np.linalg.norm(ref, axis=-1)
-    assert per.max() < TOL_PLAIN
+    assert per.max() < 1.5 * tol_plain(n)
 
 
 def test_config1_n4096_batch64(cuda_device):
@@ -143,6 +143,6 @@ def test_config1_n4096_batch64(cuda_device):
     xq = quantize(x, "plain")
     with tc.Plan(n=n, batch=batch) as p:
         y = run_gpu(p, xq, "plain")
-    assert oracle.rel_l2(y, oracle_1d(xq)) < TOL_PLAIN
+    assert oracle.rel_l2(y, oracle_1d(xq)) < tol_plain(n)
     # error against the unrounded FP64 inputs includes fp16 input quantisation
-    assert oracle.rel_l2(y, oracle_1d(x)) < TOL_PLAIN
+    assert oracle.rel_l2(y, oracle_1d(x)) < tol_plain(n)

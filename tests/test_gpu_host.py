@@ -7,7 +7,7 @@ import pytest
 
 import oracle
 import tcfft_gb300 as tc
-from fftcheck import TOL_PLAIN, TOL_SPLIT, oracle_1d, oracle_2d, quantize, to_complex, uniform_input
+from fftcheck import oracle_1d, oracle_2d, quantize, to_complex, tol, tol_plain, uniform_input
 
 pytestmark = pytest.mark.gpu
 
@@ -39,7 +39,7 @@ def test_execute_host_matches_device(cuda_device, shape, batch, precision):
     y = to_complex(h_out.double().numpy())
     ref = oracle_1d(xq) if len(shape) == 1 else oracle_2d(xq)
     sub = slice(0, min(batch, 16))
-    assert oracle.rel_l2(y[sub], ref[sub]) < (TOL_PLAIN if precision == "plain" else TOL_SPLIT)
+    assert oracle.rel_l2(y[sub], ref[sub]) < tol(precision, int(np.prod(shape)))
 
 
 def test_execute_host_in_place_host_buffer(cuda_device):
@@ -51,7 +51,7 @@ def test_execute_host_in_place_host_buffer(cuda_device):
         work = torch.empty_like(h, device="cuda")
         p.exec_host(h, h, work)
         torch.cuda.synchronize()
-    assert oracle.rel_l2(to_complex(h.double().numpy()), oracle_1d(xq)) < TOL_PLAIN
+    assert oracle.rel_l2(to_complex(h.double().numpy()), oracle_1d(xq)) < tol_plain(8192)
 
 
 def test_execute_host_many(cuda_device):

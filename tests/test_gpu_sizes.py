@@ -15,7 +15,7 @@ import pytest
 
 import oracle
 import tcfft_gb300 as tc
-from fftcheck import TOL_PLAIN, TOL_SPLIT, oracle_1d, oracle_2d, quantize, run_gpu, to_complex, uniform_input
+from fftcheck import oracle_1d, oracle_2d, quantize, run_gpu, to_complex, tol_plain, tol_split, uniform_input
 
 pytestmark = pytest.mark.gpu
 
@@ -27,8 +27,8 @@ def test_tiny_plain(cuda_device, n, batch):
     with tc.Plan(n=n, batch=batch) as p:
         y = run_gpu(p, xq, "plain")
         ya = run_gpu(p, xq, "plain", adjoint=True)
-    assert oracle.rel_l2(y, oracle_1d(xq)) < TOL_PLAIN
-    assert oracle.rel_l2(ya, oracle_1d(xq, adjoint=True)) < TOL_PLAIN
+    assert oracle.rel_l2(y, oracle_1d(xq)) < tol_plain(n)
+    assert oracle.rel_l2(ya, oracle_1d(xq, adjoint=True)) < tol_plain(n)
 
 
 @pytest.mark.parametrize("n", [16, 32, 64])
@@ -37,7 +37,7 @@ def test_tiny_split(cuda_device, n):
     xq = quantize(uniform_input((batch, n), seed=5 * n), "split")
     with tc.Plan(n=n, batch=batch, precision="split") as p:
         y = run_gpu(p, xq, "split")
-    assert oracle.rel_l2(y, oracle_1d(xq)) < TOL_SPLIT
+    assert oracle.rel_l2(y, oracle_1d(xq)) < tol_split(n)
 
 
 def test_tiny_split_128_reports_not_supported(cuda_device):
@@ -53,7 +53,7 @@ def test_large_plain(cuda_device, n, batch):
         y = run_gpu(p, xq, "plain")
     err = oracle.rel_l2(y, oracle_1d(xq))
     assert np.isfinite(y).all()
-    assert err < TOL_PLAIN, "n=%d rel-L2 %.3e" % (n, err)
+    assert err < tol_plain(n), "n=%d rel-L2 %.3e" % (n, err)
 
 
 @pytest.mark.parametrize("n", [1 << 21, 1 << 23])
@@ -62,8 +62,8 @@ def test_large_split_and_adjoint(cuda_device, n):
     with tc.Plan(n=n, batch=1, precision="split") as p:
         y = run_gpu(p, xq, "split")
         ya = run_gpu(p, xq, "split", adjoint=True)
-    assert oracle.rel_l2(y, oracle_1d(xq)) < TOL_SPLIT
-    assert oracle.rel_l2(ya, oracle_1d(xq, adjoint=True)) < TOL_SPLIT
+    assert oracle.rel_l2(y, oracle_1d(xq)) < tol_split(n)
+    assert oracle.rel_l2(ya, oracle_1d(xq, adjoint=True)) < tol_split(n)
 
 
 def test_largest_size_properties(cuda_device):
@@ -86,7 +86,7 @@ def test_largest_size_properties(cuda_device):
     ya, yb, ys = (to_complex(t.double().cpu().numpy()) for t in (fa, fb, fs))
     # linearity: F(a + b) vs F(a) + F(b) (the inputs of the sum rounded to fp16)
     lin = np.linalg.norm(ys - (ya + yb)) / np.linalg.norm(ys)
-    assert lin < 3 * TOL_PLAIN, lin
+    assert lin < 3 * tol_plain(n), lin
     # Parseval on a: sum |X|^2 = N sum |x|^2
     xc = to_complex(xa)
     par = abs(np.sum(np.abs(ya) ** 2) / (n * np.sum(np.abs(xc) ** 2)) - 1)
@@ -107,8 +107,8 @@ def test_generic_2d_plain(cuda_device, nx, ny, batch):
         assert "generic2d" in p.info["schedule"]
         y = run_gpu(p, xq, "plain")
         ya = run_gpu(p, xq, "plain", adjoint=True)
-    assert oracle.rel_l2(y, oracle_2d(xq)) < TOL_PLAIN
-    assert oracle.rel_l2(ya, oracle_2d(xq, adjoint=True)) < TOL_PLAIN
+    assert oracle.rel_l2(y, oracle_2d(xq)) < tol_plain(nx * ny)
+    assert oracle.rel_l2(ya, oracle_2d(xq, adjoint=True)) < tol_plain(nx * ny)
 
 
 def test_generic_2d_4096_square(cuda_device):
@@ -117,7 +117,7 @@ def test_generic_2d_4096_square(cuda_device):
     with tc.Plan(nx=4096, ny=4096, batch=1) as p:
         y = run_gpu(p, xq, "plain")
     err = oracle.rel_l2(y, oracle_2d(xq))
-    assert np.isfinite(y).all() and err < TOL_PLAIN, err
+    assert np.isfinite(y).all() and err < tol_plain(4096 * 4096), err
 
 
 @pytest.mark.parametrize("nx,ny", [(64, 256), (32, 64)])
@@ -125,7 +125,7 @@ def test_generic_2d_split(cuda_device, nx, ny):
     xq = quantize(uniform_input((2, nx, ny), seed=3), "split")
     with tc.Plan(nx=nx, ny=ny, batch=2, precision="split") as p:
         y = run_gpu(p, xq, "split")
-    assert oracle.rel_l2(y, oracle_2d(xq)) < TOL_SPLIT
+    assert oracle.rel_l2(y, oracle_2d(xq)) < tol_split(nx * ny)
 
 
 @pytest.mark.parametrize("n", [2048, 32768])
@@ -138,14 +138,14 @@ def test_split_fourstep(cuda_device, n):
         assert ("fourstep" if n == 2048 else "fused1d") in p.info["schedule"]
         y = run_gpu(p, xq, "split")
         ya = run_gpu(p, xq, "split", adjoint=True)
-    assert oracle.rel_l2(y, oracle_1d(xq)) < TOL_SPLIT
-    assert oracle.rel_l2(ya, oracle_1d(xq, adjoint=True)) < TOL_SPLIT
+    assert oracle.rel_l2(y, oracle_1d(xq)) < tol_split(n)
+    assert oracle.rel_l2(ya, oracle_1d(xq, adjoint=True)) < tol_split(n)
     if n != 2048:
         return
     x2 = quantize(uniform_input((1, 256, 2048), seed=22), "split")
     with tc.Plan(nx=256, ny=2048, batch=1, precision="split") as p:
         y2 = run_gpu(p, x2, "split")
-    assert oracle.rel_l2(y2, oracle_2d(x2)) < TOL_SPLIT
+    assert oracle.rel_l2(y2, oracle_2d(x2)) < tol_split(256 * 2048)
 
 
 @pytest.mark.parametrize("n", [1 << 15, 1 << 16, 1 << 17, 1 << 18])
@@ -162,5 +162,5 @@ def test_cluster_opt_in(cuda_device, monkeypatch, n):
         ya = run_gpu(p, xq, "plain", adjoint=True)
     if not sched.startswith("cluster"):
         pytest.skip("cluster of %d CTAs not schedulable here: %s" % (n >> 14, sched))
-    assert oracle.rel_l2(y, oracle_1d(xq)) < TOL_PLAIN
-    assert oracle.rel_l2(ya, oracle_1d(xq, adjoint=True)) < TOL_PLAIN
+    assert oracle.rel_l2(y, oracle_1d(xq)) < tol_plain(n)
+    assert oracle.rel_l2(ya, oracle_1d(xq, adjoint=True)) < tol_plain(n)
