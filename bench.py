@@ -17,8 +17,14 @@ Keys beyond the base contract: `roofline` (dominant kernel vs the measured
 HBM copy bandwidth), `cpu_baseline` (the FP64 CPU FFT of oracle/ on the host
 cores, bounded sample), `e2e` (host buffers through the public API, copies
 inside the timed region), `clocks` (nvidia-smi sampled during the timed
-region), `sweep` (N = 2^8 .. 2^22 at 2^28 elements per call) and `accuracy`
-(rel-L2 vs numpy's FP64 FFT on a sample, plain and split).
+region), `sweep` (N = 2^8 .. 2^24 at 2^28 elements per call, with rel-L2 vs
+FP64 per N on the timed plans, uniform inputs and the tone variant) and
+`accuracy` (rel-L2 vs numpy's FP64 FFT: a separate sample, plain and split, and
+the timed plan itself on sampled transforms).
+
+With --impl reference it times the reference's CPU path (FFTW in the
+reference, absent here: the oracle's FP64 port) for exactly the steps it
+reports, one bounded sample of the workload per step.
 """
 import argparse
 import json
@@ -162,27 +168,79 @@ def accuracy_sample(torch, tc, size_args, precision, seed=0, count=2):
     rng = np.random.default_rng(seed)
     x = rng.uniform(-1.0, 1.0, shape + (2,))
     dt = np.float16 if precision == "plain" else np.float32
-    xq = x.astype(dt).astype(np.float64)
     t = torch.from_numpy(x.astype(dt)).cuda()
     with tc.Plan(batch=count, precision=precision, **size_args) as p:
         p.exec(t)
         p.check_device()
-    y = t.double().cpu().numpy()
+    return compare_fp64(t.double().cpu().numpy(), x, precision, two_d=not n)
+
+
+def compare_fp64(y, x, precision, two_d=False):
+    """rel-L2 of the result y against numpy's FP64 FFT of the inputs x (float64
+    [..., 2]) as given (unrounded) and as the kernel saw them (rounded)."""
+    import numpy as np
+    dt = np.float16 if precision == "plain" else np.float32
+    xq = x.astype(dt).astype(np.float64)
     yc = y[..., 0] + 1j * y[..., 1]
-    xc = xq[..., 0] + 1j * xq[..., 1]
-    xu = x[..., 0] + 1j * x[..., 1]
-    if n:
-        ref, refu = np.fft.fft(xc, axis=-1), np.fft.fft(xu, axis=-1)
+    fft = np.fft.fft2 if two_d else (lambda a: np.fft.fft(a, axis=-1))
+    ref = fft(xq[..., 0] + 1j * xq[..., 1])
+    refu = fft(x[..., 0] + 1j * x[..., 1])
+    finite = np.isfinite(yc)
+    out = {"rel_l2_vs_fp64_on_rounded_inputs": rel_l2_numpy(np.where(finite, yc, 0), ref),
+           "rel_l2_vs_fp64_on_unrounded_inputs": rel_l2_numpy(np.where(finite, yc, 0), refu),
+           "nonfinite": int((~finite).sum()), "transforms": int(np.prod(y.shape[:-2 if not two_d else -3]))}
+    return out
+
+
+def tone_input(n, count, seed=0):
+    """Three unit-amplitude complex tones (bins and phases from default_rng(seed + 100))
+    over N(0, 1e-3) noise, float64 [count, n, 2]: |X_k| ~ n at the tone bins."""
+    import numpy as np
+    rng = np.random.default_rng(seed + 100)
+    bins = rng.integers(0, n, 3)
+    phases = rng.uniform(0, 2 * np.pi, 3)
+    idx = np.arange(n)
+    z = sum(np.exp(1j * (2 * np.pi * ((int(k) * idx) % n) / n + ph)) for k, ph in zip(bins, phases))
+    x = np.empty((count, n, 2))
+    noise = rng.normal(0.0, 1e-3, (count, n, 2))
+    x[..., 0] = z.real + noise[..., 0]
+    x[..., 1] = z.imag + noise[..., 1]
+    return x
+
+
+def sample_rows(batch, count):
+    """Transforms checked in a batch: the first two, two in the middle, the last two."""
+    rows = sorted({0, 1, batch // 2 - 1, batch // 2, batch - 2, batch - 1})
+    return [r for r in rows if 0 <= r < batch][:count]
+
+
+def plan_accuracy(torch, plan, x_dev, precision, n, batch, kind="uniform", seed=0):
+    """Run `plan` (the timed one) once on its own buffer after writing seeded inputs
+    into sampled transforms (first, middle, last); returns rel-L2 against FP64 on them."""
+    import numpy as np
+    rows = sample_rows(batch, 6)
+    max_elems = 1 << 22
+    while len(rows) > 1 and len(rows) * n > max_elems:
+        rows = rows[::2]
+    if kind == "tone":
+        x = tone_input(n, len(rows), seed)
     else:
-        ref, refu = np.fft.fft2(xc), np.fft.fft2(xu)
-    return {"rel_l2_vs_fp64_on_rounded_inputs": rel_l2_numpy(yc, ref),
-            "rel_l2_vs_fp64_on_unrounded_inputs": rel_l2_numpy(yc, refu),
-            "nonfinite": int((~np.isfinite(yc)).sum()), "transforms": count}
+        x = np.random.default_rng(seed).uniform(-1.0, 1.0, (len(rows), n, 2))
+    dt = np.float16 if precision == "plain" else np.float32
+    for i, r in enumerate(rows):
+        x_dev[r].copy_(torch.from_numpy(x[i].astype(dt)))
+    plan.exec(x_dev)
+    plan.check_device()
+    y = torch.stack([x_dev[r] for r in rows]).double().cpu().numpy()
+    out = compare_fp64(y, x, precision)
+    out["rows"] = rows
+    return out
 
 
 def cpu_baseline(size_args, budget_s=10.0):
     """The oracle's FP64 CPU FFT (oracle/fft64.c, OpenMP) on the host cores,
-    timed on a bounded sample of the workload's transforms."""
+    timed on a bounded sample of the workload's transforms; scipy.fft
+    (pocketfft, all host threads) on the same sample is reported beside it."""
     import numpy as np
     import oracle
     n = size_args.get("n")
@@ -205,13 +263,43 @@ def cpu_baseline(size_args, budget_s=10.0):
         if el > budget_s or done >= 4096:
             break
     gflops = flops_per_call(size, done) / el / 1e9
-    return {"value": gflops, "unit": "GFLOP/s", "cores": threads, "kind": "port",
-            "sample": "%d transforms of the workload size (FP64, oracle/fft64.c, %d OpenMP threads), %.1f s"
-                      % (done, threads, el)}
+    out = {"value": gflops, "unit": "GFLOP/s", "cores": threads, "kind": "port",
+           "sample": "%d transforms of the workload size (FP64, oracle/fft64.c, %d OpenMP threads), %.1f s"
+                     % (done, threads, el)}
+    try:
+        out["scipy"] = scipy_baseline(size_args, x, budget_s=min(budget_s, 5.0))
+    except Exception as e:  # noqa: BLE001 - informational
+        out["scipy_error"] = str(e)[:200]
+    return out
 
 
-def sweep(torch, tc, precision, lgs=range(8, 25), total=1 << 28):
-    """1D sizes at `total` elements per call (the size-sweep workload)."""
+def scipy_baseline(size_args, x, budget_s=5.0):
+    """scipy.fft (pocketfft) complex128 and complex64 with workers = all host threads."""
+    import numpy as np
+    import scipy.fft as sf
+    n = size_args.get("n")
+    size = x.shape[-1]
+    workers = os.cpu_count() or 1
+    res = {"cores": workers, "what": "scipy.fft %s, workers=%d" % ("fft" if n else "fft2", workers)}
+    for name, dt in (("complex128", np.complex128), ("complex64", np.complex64)):
+        xx = x.astype(dt) if n else x.astype(dt).reshape(x.shape[0], size_args["nx"], size_args["ny"])
+        f = (lambda a: sf.fft(a, axis=-1, workers=workers)) if n else (lambda a: sf.fft2(a, workers=workers))
+        f(xx)
+        done, t0 = 0, time.perf_counter()
+        while True:
+            f(xx)
+            done += x.shape[0]
+            el = time.perf_counter() - t0
+            if el > budget_s / 2 or done >= 4096:
+                break
+        res[name + "_gflops"] = round(flops_per_call(size, done) / el / 1e9, 2)
+    return res
+
+
+def sweep(torch, tc, precision, lgs=range(8, 25), total=1 << 28, accuracy=True):
+    """1D sizes at `total` elements per call (the size-sweep workload): time per
+    call, and -- on the timed plan, after timing -- rel-L2 against FP64 on sampled
+    transforms for uniform inputs and for the tone variant, with non-finite counts."""
     out = []
     peak, _ = measured_peak()
     es = 4 if precision == "plain" else 8
@@ -222,9 +310,18 @@ def sweep(torch, tc, precision, lgs=range(8, 25), total=1 << 28):
         x = torch.empty((batch, n, 2), dtype=dt, device="cuda").uniform_(-1, 1)
         with tc.Plan(n=n, batch=batch, precision=precision) as p:
             sec = time_device(torch, p, x, 5, 3) / 5
-        out.append({"n": n, "batch": batch, "us": round(sec * 1e6, 1),
-                    "gflops": round(flops_per_call(n, batch) / sec / 1e9, 1),
-                    "hbm_frac_of_measured": round(2 * es * n * batch / sec / 1e9 / peak, 3)})
+            row = {"n": n, "batch": batch, "us": round(sec * 1e6, 1),
+                   "gflops": round(flops_per_call(n, batch) / sec / 1e9, 1),
+                   "hbm_frac_of_measured": round(2 * es * n * batch / sec / 1e9 / peak, 3)}
+            if accuracy:
+                u = plan_accuracy(torch, p, x, precision, n, batch, "uniform", seed=lg)
+                tn = plan_accuracy(torch, p, x, precision, n, batch, "tone", seed=lg)
+                row["rel_l2"] = float("%.3e" % u["rel_l2_vs_fp64_on_rounded_inputs"])
+                row["rel_l2_unrounded"] = float("%.3e" % u["rel_l2_vs_fp64_on_unrounded_inputs"])
+                row["tone_rel_l2"] = float("%.3e" % tn["rel_l2_vs_fp64_on_unrounded_inputs"])
+                row["tone_nonfinite"] = tn["nonfinite"]
+                row["checked_transforms"] = len(u["rows"])
+        out.append(row)
         del x
         torch.cuda.empty_cache()
     return out
@@ -299,6 +396,69 @@ def cufft_fp16(torch, size_args, batch):
             "what": "torch.fft.fft on complex32 (cuFFT fp16), out of place"}
 
 
+def reference_arm(size_args, size, args, config, metric, world):
+    """The reference's CPU path is FFTW fp64 (accuracy.cpp:11-23), absent here; its
+    restatement in oracle/ (fft64.c, OpenMP over transforms) runs on the host cores
+    with all threads.  Every step is one bounded sample of the workload -- one
+    transform per host thread -- and exactly the W + K steps the line reports are
+    run, K of them timed."""
+    import numpy as np
+    import oracle
+    threads = oracle.num_threads()
+    per = max(1, threads)
+    n = size_args.get("n")
+    rng = np.random.default_rng(0)
+    x = rng.uniform(-1, 1, (per, size)) + 1j * rng.uniform(-1, 1, (per, size))
+    if n:
+        run = lambda: oracle.fft_1d(x)  # noqa: E731
+    else:
+        xx = x.reshape(per, size_args["nx"], size_args["ny"])
+        run = lambda: oracle.fft_2d(xx)  # noqa: E731
+    for _ in range(args.warmup):
+        run()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        run()
+    el = time.perf_counter() - t0
+    value = flops_per_call(size, per) * args.steps / el / 1e9
+    sample = ("%d transforms of the workload size per step (one per host thread; FP64, oracle/fft64.c, "
+              "%d OpenMP threads), %d timed steps in %.2f s" % (per, threads, args.steps, el))
+    return {"impl": "reference", "metric": metric, "value": round(value, 3), "unit": "GFLOP/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(el / args.steps * 1e3, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp64",
+            "data": "synthetic uniform[-1,1)", "config": config,
+            "cpu_baseline": {"value": round(value, 3), "unit": "GFLOP/s", "cores": threads, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": round(value, 3), "unit": "GFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def copy_ceiling(torch, host_in, host_out, dev_a, dev_b, reps=5):
+    """Pinned host<->device copies of one step's bytes: H2D alone, D2H alone, and
+    both at once on two streams (the bound of a pipelined host-buffer call)."""
+    s_in, s_out = torch.cuda.Stream(), torch.cuda.Stream()
+    out = {}
+    for name, what in (("h2d", "in"), ("d2h", "out"), ("both", "both")):
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        cur = torch.cuda.current_stream()
+        for _ in range(reps):
+            s_in.wait_stream(cur)
+            s_out.wait_stream(cur)
+            if what in ("in", "both"):
+                with torch.cuda.stream(s_in):
+                    dev_a.copy_(host_in, non_blocking=True)
+            if what in ("out", "both"):
+                with torch.cuda.stream(s_out):
+                    host_out.copy_(dev_b, non_blocking=True)
+            cur.wait_stream(s_in)
+            cur.wait_stream(s_out)
+        e1.record()
+        torch.cuda.synchronize()
+        out[name + "_ms"] = round(e0.elapsed_time(e1) / reps, 3)
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -341,19 +501,9 @@ def main():
               "parallelism": "replicas x%d" % world}
 
     if args.impl == "reference":
-        # The reference's CPU path is FFTW fp64 (accuracy.cpp:11-23), absent here;
-        # its restatement in oracle/ runs on the host cores with all threads.
         if rank != 0:
             return
-        base = cpu_baseline(size_args, budget_s=args.cpu_budget)
-        steps = args.steps
-        ms = flops_per_call(size, batch) / (base["value"] * 1e9) * 1e3
-        line = {"impl": "reference", "metric": metric, "value": base["value"], "unit": "GFLOP/s", "n_gpus": world,
-                "steps": steps, "warmup": args.warmup, "ms_per_step": round(ms, 3), "higher_is_better": True,
-                "scaling": "weak", "vs_baseline": None, "dtype": "fp64", "data": "synthetic uniform[-1,1)",
-                "config": config, "cpu_baseline": base,
-                "e2e": {"value": base["value"], "unit": "GFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-        print(json.dumps(line), flush=True)
+        print(json.dumps(reference_arm(size_args, size, args, config, metric, world)), flush=True)
         return
 
     import torch
@@ -420,7 +570,7 @@ def main():
         dist.barrier()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
-    e2e_steps = max(3, args.steps // 4)
+    e2e_steps = max(10, args.steps // 4)
     e0.record()
     for _ in range(e2e_steps):
         plan.exec_host(host_in, host_out, x, stream=stream)
@@ -431,12 +581,24 @@ def main():
     e2e = {"value": round(flops_per_call(size, batch) * world / e2e_s / 1e9, 1), "unit": "GFLOP/s",
            "h2d_bytes_per_step": host_in.numel() * host_in.element_size(),
            "d2h_bytes_per_step": host_out.numel() * host_out.element_size(),
-           "ms_per_step": round(e2e_s * 1e3, 3)}
+           "ms_per_step": round(e2e_s * 1e3, 3), "steps": e2e_steps}
+    try:  # the host-link bound of the same bytes
+        dev_b = torch.empty_like(x)
+        ceil = copy_ceiling(torch, host_in, host_out, x, dev_b)
+        del dev_b
+        ceil["e2e_frac_of_copy_bound"] = round(ceil["both_ms"] / (e2e_s * 1e3), 3)
+        e2e["copy_ceiling"] = ceil
+    except Exception as e:  # noqa: BLE001 - informational
+        e2e["copy_ceiling_error"] = str(e)[:200]
     del host_in, host_out
 
     extra = {}
     if rank == 0:
         extra["accuracy"] = {p: accuracy_sample(torch, tc, size_args, p) for p in ("plain", "split")}
+        if "n" in size_args:  # the timed plan itself, on its own buffer, after the timed loop
+            for kind in ("uniform", "tone"):
+                extra["accuracy"]["timed_plan" + ("" if kind == "uniform" else "_tone")] = plan_accuracy(
+                    torch, plan, x, args.precision, size, batch, kind)
         if not args.no_sweep and "n" in size_args:
             for key, fn in (("sweep", lambda: sweep(torch, tc, args.precision)),
                             ("sweep_split", lambda: sweep(torch, tc, "split", lgs=(10, 12, 14, 16, 18, 20, 22))),

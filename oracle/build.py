@@ -25,7 +25,8 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_build")
 REF_OUT = os.path.join(HERE, "_ref")
-REFERENCE = "/root/reference"
+# where the reference sources lie (only on the build container); TCFFT_REFERENCE_DIR overrides
+REFERENCE = os.environ.get("TCFFT_REFERENCE_DIR", "/root/reference")
 CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

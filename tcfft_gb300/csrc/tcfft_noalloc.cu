@@ -168,7 +168,8 @@ extern "C" tcfftStatus tcfftExecute1dNoAlloc(void* data, int64_t n, int64_t batc
     k.C1 = 128;
     if (split && k.R1 > 4) return TCFFT_NOT_SUPPORTED;
   } else {
-    n1 = int64_t(1) << ((lg + 1) / 2);
+    // the plan's decompositions: N1 >= N2, except 2^21 as 1024 x 2048
+    n1 = lg == 21 ? 1024 : int64_t(1) << ((lg + 1) / 2);
     n2 = n / n1;
     k.role0 = kRoleCol;
     k.R0 = (int)(n1 / 256);

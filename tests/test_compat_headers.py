@@ -18,7 +18,7 @@ import pytest
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 INC = os.path.join(ROOT, "include")
 CUDA_INC = "/usr/local/cuda/include"
-REFERENCE = "/root/reference"
+from oracle.build import REFERENCE  # noqa: E402 - the reference source directory (TCFFT_REFERENCE_DIR)
 
 
 def _gxx(args, cwd):
