@@ -72,17 +72,33 @@ typedef enum tcfftInputOrder {
   TCFFT_ORDER_REFERENCE_DIGIT_REVERSED = 1
 } tcfftInputOrder;
 
+typedef enum tcfftDirection {
+  /* sign -1: X[k] = sum_n x[n] exp(-2 pi i n k / N), the reference's transform
+   * (F = exp(-2 pi i jk/16), tcfft_half.cu:1339) */
+  TCFFT_FORWARD = 0,
+  /* sign +1: the conjugate direction */
+  TCFFT_INVERSE = 1
+} tcfftDirection;
+
+typedef enum tcfftNormalization {
+  TCFFT_NORM_NONE = 0,   /* unnormalised, as the reference */
+  TCFFT_NORM_BY_N = 1    /* every transform scaled by 1/N (N = n, or nx * ny in 2D) */
+} tcfftNormalization;
+
 typedef struct tcfftOptions {
   int32_t precision;   /* tcfftPrecision */
   int32_t input_order; /* tcfftInputOrder */
   int32_t autotune;    /* 0: built-in schedule; 1: time candidates at plan time */
-  int32_t reserved;
+  int32_t direction;   /* tcfftDirection of tcfftExecute (default TCFFT_FORWARD) */
   const char* tune_cache_path; /* optional file for autotune results (NULL: none) */
+  int32_t normalization; /* tcfftNormalization of tcfftExecute (default TCFFT_NORM_NONE) */
+  int32_t reserved;
 } tcfftOptions;
 
 typedef struct tcfftPlanImpl* tcfftPlan;
 
-/* Fill `opts` with defaults (plain, natural order, no autotune). */
+/* Fill `opts` with defaults (plain, natural order, no autotune, forward,
+ * unnormalised). */
 tcfftStatus tcfftOptionsDefault(tcfftOptions* opts);
 
 /* 1D batched plan: `batch` transforms of length n (power of two, 16 <= n <= 2^27;
@@ -103,13 +119,22 @@ tcfftStatus tcfftPlan2d(tcfftPlan* plan, int64_t nx, int64_t ny, int64_t batch, 
 tcfftStatus tcfftPlanMany(tcfftPlan* plan, int64_t count, const int32_t* ranks, const int64_t* nx,
                           const int64_t* ny, const int64_t* offsets, const tcfftOptions* opts);
 
-/* Forward transform in place on device memory `data` on `stream`
- * (a cudaStream_t; NULL = legacy default stream). */
+/* The plan's transform (by default forward, unnormalised) in place on device
+ * memory `data` on `stream` (a cudaStream_t; NULL = legacy default stream). */
 tcfftStatus tcfftExecute(tcfftPlan plan, void* data, void* stream);
 
-/* Adjoint transform (conjugate direction, unnormalised: the exact adjoint of
- * tcfftExecute, i.e. n * inverse DFT), same layout and schedule. */
+/* Adjoint of tcfftExecute: the conjugate direction with the same scale (for
+ * the default plan: unnormalised, i.e. N times the inverse DFT), same layout
+ * and schedule. */
 tcfftStatus tcfftExecuteAdjoint(tcfftPlan plan, void* data, void* stream);
+
+/* Inverse of tcfftExecute: the conjugate direction scaled so that
+ * tcfftExecuteInverse(tcfftExecute(x)) = x (for the default plan: the inverse
+ * DFT with its 1/N).  The 1/N is folded into a twiddle multiply the kernels
+ * already make, so it costs no extra pass over the data, and intermediate
+ * values stay within fp16 range.  The reference has no inverse (its kernels
+ * use only the exp(-2 pi i jk/N) twiddles). */
+tcfftStatus tcfftExecuteInverse(tcfftPlan plan, void* data, void* stream);
 
 /* Host-buffer execution: the batch is copied in from `host_in`, transformed
  * (forward) in the caller's device buffer `work` (the plan's size, 128-byte

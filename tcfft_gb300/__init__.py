@@ -29,6 +29,10 @@ PRECISION_PLAIN = 0
 PRECISION_SPLIT = 1
 ORDER_NATURAL = 0
 ORDER_REFERENCE_DIGIT_REVERSED = 1
+FORWARD = 0        # sign -1 (the reference's transform)
+INVERSE = 1        # sign +1
+NORM_NONE = 0
+NORM_BY_N = 1
 
 _STATUS = {
     0: "TCFFT_SUCCESS", 1: "TCFFT_INVALID_VALUE", 2: "TCFFT_INVALID_SIZE", 3: "TCFFT_MISALIGNED",
@@ -54,8 +58,9 @@ class TcfftError(RuntimeError):
 class Options(ctypes.Structure):
     """struct tcfftOptions (include/tcfft_gb300.h)."""
     _fields_ = [("precision", ctypes.c_int32), ("input_order", ctypes.c_int32),
-                ("autotune", ctypes.c_int32), ("reserved", ctypes.c_int32),
-                ("tune_cache_path", ctypes.c_char_p)]
+                ("autotune", ctypes.c_int32), ("direction", ctypes.c_int32),
+                ("tune_cache_path", ctypes.c_char_p), ("normalization", ctypes.c_int32),
+                ("reserved", ctypes.c_int32)]
 
 
 class PlanInfo(ctypes.Structure):
@@ -81,6 +86,7 @@ _SIGNATURES = {
                        ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(Options)], ctypes.c_int),
     "tcfftExecute": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
     "tcfftExecuteAdjoint": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
+    "tcfftExecuteInverse": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
     "tcfftExecuteHost": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p],
                          ctypes.c_int),
     "tcfftCheckDevice": ([ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
@@ -174,7 +180,8 @@ class Plan:
     """
 
     def __init__(self, n=None, batch=1, nx=None, ny=None, precision="plain", input_order=ORDER_NATURAL,
-                 autotune=False, tune_cache_path=None, _handle=None, _shapes=None):
+                 autotune=False, tune_cache_path=None, direction=FORWARD, normalize=False, _handle=None,
+                 _shapes=None):
         self._handle = ctypes.c_void_p(None)
         self.precision = _precision_of(precision)
         self.input_order = int(input_order)
@@ -190,6 +197,8 @@ class Plan:
         opts.input_order = self.input_order
         opts.autotune = 1 if autotune else 0
         opts.tune_cache_path = tune_cache_path.encode() if tune_cache_path else None
+        opts.direction = int(direction)
+        opts.normalization = NORM_BY_N if normalize else NORM_NONE
         self._opts = opts
         if n is not None:
             self.n, self.nx, self.ny, self.batch = int(n), None, None, int(batch)
@@ -203,7 +212,7 @@ class Plan:
             raise ValueError("give n (1D) or nx and ny (2D)")
 
     @classmethod
-    def many(cls, shapes, offsets=None, precision="plain", autotune=False):
+    def many(cls, shapes, offsets=None, precision="plain", autotune=False, direction=FORWARD, normalize=False):
         """Uneven batch: ``shapes`` is a list of ``(n,)`` or ``(nx, ny)`` tuples,
         transforms packed back to back (or at ``offsets``, in elements)."""
         count = len(shapes)
@@ -221,6 +230,8 @@ class Plan:
         lib().tcfftOptionsDefault(ctypes.byref(opts))
         opts.precision = _precision_of(precision)
         opts.autotune = 1 if autotune else 0
+        opts.direction = int(direction)
+        opts.normalization = NORM_BY_N if normalize else NORM_NONE
         h = ctypes.c_void_p(None)
         _check(lib().tcfftPlanMany(ctypes.byref(h), count, ranks, nxs, nys, offa, ctypes.byref(opts)),
                "tcfftPlanMany(count=%d)" % count)
@@ -232,13 +243,16 @@ class Plan:
     def _ptr(self, data):
         return _device_ptr(data, self.precision)
 
-    def exec(self, data, stream=None, adjoint=False):
-        """Transform ``data`` in place (forward, or the adjoint)."""
+    def exec(self, data, stream=None, adjoint=False, inverse=False):
+        """Transform ``data`` in place: the plan's transform, its adjoint
+        (``adjoint=True``) or its inverse (``inverse=True``, so that
+        ``exec(exec(x), inverse=True) == x`` up to rounding)."""
         if not self._handle:
             raise TcfftError(8, "exec on destroyed plan")
-        fn = lib().tcfftExecuteAdjoint if adjoint else lib().tcfftExecute
-        _check(fn(self._handle, ctypes.c_void_p(self._ptr(data)), _stream_handle(stream)),
-               "tcfftExecute%s" % ("Adjoint" if adjoint else ""))
+        if adjoint and inverse:
+            raise ValueError("adjoint and inverse are exclusive")
+        name = "tcfftExecuteAdjoint" if adjoint else ("tcfftExecuteInverse" if inverse else "tcfftExecute")
+        _check(getattr(lib(), name)(self._handle, ctypes.c_void_p(self._ptr(data)), _stream_handle(stream)), name)
         return data
 
     def exec_host(self, host_in, host_out, work, stream=None):

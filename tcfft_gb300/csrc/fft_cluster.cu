@@ -115,6 +115,7 @@ struct ClParams {
   long long batch;
   int* err;
   float dsign;
+  float oscale = 1.f;  // output scale (a power of two), carried by the phase-0 W_N factors
 };
 
 template <int CL>
@@ -257,7 +258,7 @@ __device__ __forceinline__ void compute_warps(unsigned char* smem, uint64_t* ful
 #pragma unroll 1
       for (int t = 0; t < 2; ++t)
         plain_col_tile<1, 32, true, PI, RHO>(jc, fold0, base + t * Cfg::kTileBytes, warp, p.dsign,
-                                             (int)(64 * rank + 32 * t), wn);
+                                             (int)(64 * rank + 32 * t), wn, p.oscale);
       __syncwarp();
       if (lane == 0)
         for (int q = 0; q < CL; ++q) arrive_remote(remote_p0[q]);
@@ -402,7 +403,7 @@ bool cluster_supported(int64_t n, bool split, int num_sms) {
 
 cudaError_t launch_cluster(int64_t n, void* data, int64_t batch, const float2* tw2048, const float2* twlo,
                            const float2* twhi, float dsign, int* err, int num_sms, cudaStream_t st, CUtensorMap* lm,
-                           CUtensorMap* sm, bool encode) {
+                           CUtensorMap* sm, bool encode, float oscale) {
   const int64_t n2 = n / 256;
   const int cl = (int)(n2 / 64), rpc = 256 / cl, w = rpc < 32 ? rpc : 32;
   const int bh = n2 < 256 ? (int)n2 : 256;
@@ -423,6 +424,7 @@ cudaError_t launch_cluster(int64_t n, void* data, int64_t batch, const float2* t
   p.batch = batch;
   p.err = err;
   p.dsign = dsign;
+  p.oscale = oscale;
   int active = 0;
   return dispatch_cluster(n, *lm, *sm, p, num_sms, st, &active);
 }

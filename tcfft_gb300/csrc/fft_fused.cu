@@ -19,6 +19,8 @@ cudaError_t launch_fused_1d(const FusedKey& k, const FusedMaps* maps, const Fuse
   TCFFT_FUSED_CASE(kRoleCol, 8, 8, kRoleRowT, 4, 16, false, 64)
   TCFFT_FUSED_CASE(kRoleCol, 8, 8, kRoleRowT, 8, 8, false, 64)
   TCFFT_FUSED_CASE(kRoleCol, 4, 16, kRoleRowT, 8, 8, false, 64)
+  TCFFT_FUSED_CASE(kRoleCol, 2, 32, kRoleRowT, 8, 8, false, 64)
+  TCFFT_FUSED_CASE(kRoleCol, 8, 8, kRoleRowT, 2, 32, false, 64)
   // 32 KiB work items (deeper rings, one tile per item)
   TCFFT_FUSED_CASE(kRoleCol, 1, 32, kRoleRowT, 1, 32, false, 32)
   TCFFT_FUSED_CASE(kRoleCol, 2, 16, kRoleRowT, 1, 32, false, 32)

@@ -61,6 +61,8 @@ struct FusedParams {
   int* err;
   float dsign;
   unsigned long long wait_ns;  // limit of every bounded wait (0: kTimeoutNs)
+  float oscale0, oscale1;      // output scale of each phase (powers of two; 0 reads as 1): 1D carries
+                               // the 1/N of a normalised transform in phase 0's W_N factors
 };
 
 // Column tiles: C columns x L rows of C*ES bytes (32, 64 or 128), moved by TMA
@@ -209,9 +211,10 @@ struct WnTable {
 // 0) the output k of column n2 = n2base + jn is multiplied by W_N^(n2 k).
 // JNW: columns per call (default C/8: the 8 warps share the tile in one call; 2 with
 // 32-column tiles: two calls per warp, `warp` and `warp + 8`, fewer live registers).
+// wscale (WN only) multiplies the W_N factors: the outputs come out scaled by it.
 template <int R, int C, bool WN, class PI, class RHO, int JNW = C / 8>
 __device__ __forceinline__ void plain_col_tile(const JobConsts<false>& jc, uint32_t fold, uint32_t base, int warp,
-                                               float dsign, int n2base, const WnTable& wn) {
+                                               float dsign, int n2base, const WnTable& wn, float wscale = 1.f) {
   constexpr int ES = 4, JN = JNW;
   static_assert(JN * 8 == C || (JN == 2 && C == 32), "columns per call");
   constexpr bool PAIR = JN % 2 == 0;
@@ -235,7 +238,9 @@ __device__ __forceinline__ void plain_col_tile(const JobConsts<false>& jc, uint3
 #pragma unroll
     for (int jn = 0; jn < JN; ++jn) {
       const int n2 = n2base + col0 + jn;
-      const float2 F = wn(n2 * R * kbase), u = wn(n2 * R), u32 = wn(32 * n2 * R);
+      float2 F = wn(n2 * R * kbase);
+      F = make_float2(F.x * wscale, F.y * wscale);
+      const float2 u = wn(n2 * R), u32 = wn(32 * n2 * R);
       const float2 u2 = cmul(u, u), u3 = cmul(u2, u);
       const float2 f0[4] = {F, cmul(F, u), cmul(F, u2), cmul(F, u3)};
       fu[jn] = u32;
@@ -467,11 +472,16 @@ __global__ void __launch_bounds__(384, 1)  // 12 warps at launch: 168 registers 
     for (int j = tid; j < (1 << Cfg::kTwShift); j += blockDim.x) s_twlo[j] = p.twlo[j];
     for (int j = tid; j < Cfg::kTwHi; j += blockDim.x) s_twhi[j] = p.twhi[j];
   }
+  // output scales: 1D puts phase 0's into its W_N factors; 2D into each phase's
+  // stage-1 twiddles (fold tables here, JobConsts::tw1 per item below)
+  const float os0 = p.oscale0 != 0.f ? p.oscale0 : 1.f, os1 = p.oscale1 != 0.f ? p.oscale1 : 1.f;
   if constexpr (Cfg::kFold) {
-    build_fold_table<R0, typename Cfg::PI, typename Cfg::RHO>(s_fold0, p.tw2048, tid, blockDim.x);
+    build_fold_table<R0, typename Cfg::PI, typename Cfg::RHO>(s_fold0, p.tw2048, tid, blockDim.x,
+                                                              Cfg::k1D ? 1.f : os0);
     if constexpr (Cfg::kFold1Own)
       build_fold_table<R1, typename Cfg::PI, typename Cfg::RHO, ROLE1 != kRoleRow16T>(s_fold1, p.tw2048, tid,
-                                                                                       blockDim.x);
+                                                                                       blockDim.x,
+                                                                                       Cfg::k1D ? 1.f : os1);
   }
   __syncthreads();
 
@@ -655,11 +665,19 @@ __global__ void __launch_bounds__(384, 1)  // 12 warps at launch: 168 registers 
   wn.global = p.wn_global != 0;
   wn.shift = wn.global ? p.tw_shift : Cfg::kTwShift;
   wn.nmask = (int)p.n_mask;
+  float tw1_scale = 1.f;  // 2D: the phase scale currently folded into jc.tw1
   int cnt = 0;
   for (long long idx = blockIdx.x; idx < total; idx += gridDim.x) {
     const Item it = decode_item(idx, p);
     if (!it.valid) continue;
     const int s = cnt % NST;
+    if constexpr (!Cfg::k1D) {
+      const float want = it.phase == 0 ? os0 : os1;
+      if (want != tw1_scale) {  // powers of two: the ratio is exact
+        scale_tw1(jc, want / tw1_scale);
+        tw1_scale = want;
+      }
+    }
     // all compute warps agree on success before any of them enters a named barrier
     const bool ok = named_bar_and(2, 256, mbar_wait(&full[s], (cnt / NST) & 1, p.err, lim));
     const uint32_t base = smem_addr(smem + s * Cfg::kStageBytes);
@@ -679,7 +697,7 @@ __global__ void __launch_bounds__(384, 1)  // 12 warps at launch: 168 registers 
 #pragma unroll 1
           for (int u = 0; u < Cfg::kSub0; ++u)
             plain_col_tile<R0, C0, Cfg::k1D, PI, RHO>(jc, fold0, base + u * (Cfg::kTile0 * ES), warp, p.dsign,
-                                                      ((it.tile * Cfg::kSub0 + u) % p.cols0) * C0, wn);
+                                                      ((it.tile * Cfg::kSub0 + u) % p.cols0) * C0, wn, os0);
         } else if constexpr (ROLE0 == kRoleCol) {
 #pragma unroll 1
          for (int u = 0; u < Cfg::kSub0; ++u) {
@@ -707,7 +725,10 @@ __global__ void __launch_bounds__(384, 1)  // 12 warps at launch: 168 registers 
             for (int jn = 0; jn < JN; ++jn) {
               const int n2 = cg * C0 + col0 + jn;
 #pragma unroll
-              for (int sl = 0; sl < 8; ++sl) fk[jn][sl] = wn(n2 * R0 * jc.kval[sl >> 2][(sl >> 1) & 1][sl & 1]);
+              for (int sl = 0; sl < 8; ++sl) {
+                const float2 f = wn(n2 * R0 * jc.kval[sl >> 2][(sl >> 1) & 1][sl & 1]);
+                fk[jn][sl] = make_float2(f.x * os0, f.y * os0);
+              }
 #pragma unroll
               for (int q = 0; q < R0; ++q) fq[jn][q] = wn(n2 * q);
             }

@@ -54,6 +54,18 @@ __device__ __forceinline__ void init_job_consts(JobConsts<SPLIT>& c, const float
         c.kval[h][e][hh] = RHO::apply(2 * t + e + 8 * h) + 16 * RHO::apply(g + 8 * hh);
 }
 
+// Multiply the stage-1 -> stage-2 twiddles by s (a power of two): every job
+// output then comes out scaled by s exactly, at no cost per element.
+template <bool SPLIT>
+__device__ __forceinline__ void scale_tw1(JobConsts<SPLIT>& c, float s) {
+#pragma unroll
+  for (int j = 0; j < 2; ++j)
+#pragma unroll
+    for (int h = 0; h < 2; ++h)
+#pragma unroll
+      for (int e = 0; e < 2; ++e) c.tw1[j][h][e] = make_float2(c.tw1[j][h][e].x * s, c.tw1[j][h][e].y * s);
+}
+
 // JN independent jobs computed in lockstep by one warp (JN = 1 or 2): their
 // instruction streams interleave, which hides MMA/shared-memory latency when
 // only two warps share a scheduler.
@@ -215,8 +227,12 @@ struct FoldTab {
 
 // Fill one fold table (all threads of the CTA take part; tw2048 = W_2048^j).
 // WITH_T = false: the A_q part only (16R-point row jobs have no second stage).
+// tscale multiplies the stage-1 twiddles T_q (a power of two: the jobs' outputs
+// come out scaled by it exactly; together with JobConsts::tw1 it carries the
+// 1/N of a normalised transform).
 template <int R, class PI, class RHO, bool WITH_T = true>
-__device__ void build_fold_table(unsigned char* tab, const float2* __restrict__ tw2048, int tid, int nthreads) {
+__device__ void build_fold_table(unsigned char* tab, const float2* __restrict__ tw2048, int tid, int nthreads,
+                                 float tscale = 1.f) {
   if constexpr (R > 1) {
     uint32_t* A = reinterpret_cast<uint32_t*>(tab);
     for (int idx = tid; idx < (R - 1) * 16 * 32; idx += nthreads) {
@@ -231,7 +247,8 @@ __device__ void build_fold_table(unsigned char* tab, const float2* __restrict__ 
       const int q = idx / 256 + 1, sl = (idx >> 5) & 7, lane = idx & 31, g = lane >> 2, t = lane & 3;
       const int j = sl >> 2, h = (sl >> 1) & 1, e = sl & 1;
       const int m0 = PI::apply(2 * t + e + 8 * j), k0 = RHO::apply(g + 8 * h);
-      T[idx] = tw2048[((m0 * (R * k0 + q)) & (256 * R - 1)) * (8 / R)];  // W_{256R}^(m0 (R k0 + q))
+      const float2 w = tw2048[((m0 * (R * k0 + q)) & (256 * R - 1)) * (8 / R)];  // W_{256R}^(m0 (R k0 + q))
+      T[idx] = make_float2(w.x * tscale, w.y * tscale);
     }
   }
 }

@@ -83,6 +83,7 @@ struct ResParams {
   long long rows;  // transposed output: transforms per matrix (the destination's row length)
   int* err;
   float dsign;
+  float oscale;  // output scale (a power of two), carried by the phase-0 W_N factors
 };
 
 // TOUT (N = 4096): the output is written transposed, as dst[m][k][r] for transform
@@ -204,10 +205,10 @@ __global__ void __launch_bounds__(384, 1) fft_resident_kernel(const __grid_const
 #pragma unroll 1
           for (int h = 0; h < 2; ++h)
             plain_col_tile<1, C, true, PI, RHO, 2>(jc, fold, base + tile * Cfg::kTileBytes, warp + 8 * h,
-                                                   p.dsign, (tile % CG) * C, wn);
+                                                   p.dsign, (tile % CG) * C, wn, p.oscale);
         } else {
           plain_col_tile<1, C, true, PI, RHO>(jc, fold, base + tile * Cfg::kTileBytes, warp, p.dsign,
-                                              (tile % CG) * C, wn);
+                                              (tile % CG) * C, wn, p.oscale);
         }
       }
       named_bar_sync(1, 256);
@@ -406,7 +407,10 @@ __global__ void __launch_bounds__(384, 1) fft_resident_split_kernel(const __grid
         for (int jn = 0; jn < JN; ++jn) {
           const int n2 = (tile % CG) * C + col0 + jn;
 #pragma unroll
-          for (int sl = 0; sl < 8; ++sl) fk[jn][sl] = wn(n2 * jc.kval[sl >> 2][(sl >> 1) & 1][sl & 1]);
+          for (int sl = 0; sl < 8; ++sl) {
+            const float2 f = wn(n2 * jc.kval[sl >> 2][(sl >> 1) & 1][sl & 1]);
+            fk[jn][sl] = make_float2(f.x * p.oscale, f.y * p.oscale);
+          }
         }
         auto ldp = [&](int jp, int n, float2& x0, float2& x1) {
           lds_pair<true>(tb + ctile_off<C, ES>(col_in_row_t<true>(n), col0 + jp), x0, x1);
@@ -497,7 +501,7 @@ bool resident_supported(int64_t n, bool split) {
 // k2 bits 0..L-1), L = log2(N2 / 16), matching the stage layout above.
 cudaError_t launch_resident_split(int64_t n, void* data, int64_t batch, const float2* tw2048, const float2* twlo,
                                   const float2* twhi, float dsign, int* err, int num_sms, cudaStream_t st,
-                                  CUtensorMap* lm, CUtensorMap* sm, bool encode) {
+                                  CUtensorMap* lm, CUtensorMap* sm, bool encode, float oscale) {
   const int64_t n2 = n / 256;
   if (encode) {
     if (encode_col_load(lm, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, data, n2, batch, 8, 16, 1) != CUDA_SUCCESS)
@@ -517,6 +521,7 @@ cudaError_t launch_resident_split(int64_t n, void* data, int64_t batch, const fl
   p.rows = 0;
   p.err = err;
   p.dsign = dsign;
+  p.oscale = oscale;
   switch (n) {
     case 4096: return launch_resident_split_t<1>(*lm, *sm, p, num_sms, st);
     case 8192: return launch_resident_split_t<2>(*lm, *sm, p, num_sms, st);
@@ -526,7 +531,7 @@ cudaError_t launch_resident_split(int64_t n, void* data, int64_t batch, const fl
 
 cudaError_t launch_resident(int64_t n, void* data, int64_t batch, const float2* tw2048, const float2* twlo,
                             const float2* twhi, float dsign, int* err, int num_sms, cudaStream_t st,
-                            CUtensorMap* lm, CUtensorMap* sm, bool encode) {
+                            CUtensorMap* lm, CUtensorMap* sm, bool encode, float oscale) {
   const int64_t n2 = n / 256;
   const int C = n2 < 32 ? (int)n2 : 32;
   if (encode) {
@@ -549,6 +554,7 @@ cudaError_t launch_resident(int64_t n, void* data, int64_t batch, const float2* 
   p.rows = 0;
   p.err = err;
   p.dsign = dsign;
+  p.oscale = oscale;
   switch (n) {
     case 4096: return launch_resident_t<1>(*lm, *sm, p, num_sms, st);
     case 8192: return launch_resident_t<2>(*lm, *sm, p, num_sms, st);
@@ -564,7 +570,8 @@ bool resident_tout_supported(int64_t n, int64_t batch, int64_t rows) {
 }
 cudaError_t launch_resident_tout(int64_t n, const void* in, void* out, int64_t batch, int64_t rows,
                                  const float2* tw2048, const float2* twlo, const float2* twhi, float dsign, int* err,
-                                 int num_sms, cudaStream_t st, CUtensorMap* lm, CUtensorMap* sm, bool encode) {
+                                 int num_sms, cudaStream_t st, CUtensorMap* lm, CUtensorMap* sm, bool encode,
+                                 float oscale) {
   if (!resident_tout_supported(n, batch, rows)) return cudaErrorInvalidValue;
   if (encode) {
     if (encode_col_load(lm, CU_TENSOR_MAP_DATA_TYPE_UINT32, const_cast<void*>(in), 16, batch, 4, 16, 1) !=
@@ -586,6 +593,7 @@ cudaError_t launch_resident_tout(int64_t n, const void* in, void* out, int64_t b
   p.rows = rows;
   p.err = err;
   p.dsign = dsign;
+  p.oscale = oscale;
   return launch_resident_t<1, true>(*lm, *sm, p, num_sms, st);
 }
 

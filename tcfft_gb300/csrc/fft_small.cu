@@ -10,7 +10,7 @@ namespace tcfft {
 namespace {
 template <int R, bool SPLIT>
 cudaError_t launch_one(const CUtensorMap& tmap, int64_t total_elems, const float2* tw, float dsign, int* err,
-                       int num_sms, cudaStream_t stream) {
+                       int num_sms, cudaStream_t stream, float oscale) {
   using C = SmallCfg<R, SPLIT>;
   static std::once_flag once;
   static int blocks_per_sm = 1;
@@ -27,6 +27,7 @@ cudaError_t launch_one(const CUtensorMap& tmap, int64_t total_elems, const float
   p.num_tiles = (int)((total_elems + C::kTE - 1) / C::kTE);
   p.dsign = dsign;
   p.err = err;
+  p.oscale = oscale;
   int grid = num_sms * blocks_per_sm;
   if (grid > p.num_tiles) grid = p.num_tiles;
   if (grid < 1) return cudaSuccess;
@@ -49,16 +50,16 @@ int small_tile_elems(int R, bool split) {
 }
 
 cudaError_t launch_small(int R, bool split, const CUtensorMap& tmap, int64_t total_elems, const float2* tw,
-                         float dsign, int* err, int num_sms, cudaStream_t stream, int* launches) {
+                         float dsign, int* err, int num_sms, cudaStream_t stream, int* launches, float oscale) {
   if (launches) *launches = 1;
   switch (R * 2 + (split ? 1 : 0)) {
-    case 2: return launch_one<1, false>(tmap, total_elems, tw, dsign, err, num_sms, stream);
-    case 3: return launch_one<1, true>(tmap, total_elems, tw, dsign, err, num_sms, stream);
-    case 4: return launch_one<2, false>(tmap, total_elems, tw, dsign, err, num_sms, stream);
-    case 5: return launch_one<2, true>(tmap, total_elems, tw, dsign, err, num_sms, stream);
-    case 8: return launch_one<4, false>(tmap, total_elems, tw, dsign, err, num_sms, stream);
-    case 9: return launch_one<4, true>(tmap, total_elems, tw, dsign, err, num_sms, stream);
-    case 16: return launch_one<8, false>(tmap, total_elems, tw, dsign, err, num_sms, stream);
+    case 2: return launch_one<1, false>(tmap, total_elems, tw, dsign, err, num_sms, stream, oscale);
+    case 3: return launch_one<1, true>(tmap, total_elems, tw, dsign, err, num_sms, stream, oscale);
+    case 4: return launch_one<2, false>(tmap, total_elems, tw, dsign, err, num_sms, stream, oscale);
+    case 5: return launch_one<2, true>(tmap, total_elems, tw, dsign, err, num_sms, stream, oscale);
+    case 8: return launch_one<4, false>(tmap, total_elems, tw, dsign, err, num_sms, stream, oscale);
+    case 9: return launch_one<4, true>(tmap, total_elems, tw, dsign, err, num_sms, stream, oscale);
+    case 16: return launch_one<8, false>(tmap, total_elems, tw, dsign, err, num_sms, stream, oscale);
     default: return cudaErrorInvalidValue;
   }
 }

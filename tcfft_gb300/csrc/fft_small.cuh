@@ -55,6 +55,8 @@ struct SmallParams {
   int num_tiles;
   float dsign;       // +1 forward, -1 adjoint (conjugate direction)
   int* err;
+  float oscale;      // output scale (a power of two; 1/N for a normalised transform), carried
+                     // by the stage-1 twiddles, so it costs nothing per element
 };
 
 template <int R, bool SPLIT>
@@ -78,7 +80,7 @@ __global__ void __launch_bounds__(256, SmallCfg<R, SPLIT>::kMinBlocks)
     fence_barrier_init();
   }
   if constexpr (C::kFold)
-    build_fold_table<R, PI, RHO>(reinterpret_cast<unsigned char*>(s_tw), p.tw, tid, blockDim.x);
+    build_fold_table<R, PI, RHO>(reinterpret_cast<unsigned char*>(s_tw), p.tw, tid, blockDim.x, p.oscale);
   else if constexpr (R > 1)
     for (int j = tid; j < C::kN; j += blockDim.x) s_tw[j] = p.tw[j * (2048 / C::kN)];
   __syncthreads();
@@ -97,7 +99,10 @@ __global__ void __launch_bounds__(256, SmallCfg<R, SPLIT>::kMinBlocks)
 
   // ---- per-thread constants
   JobConsts<false> jc;  // the fold path's fragments and stage-1 twiddles
-  if constexpr (C::kFold) init_job_consts<false, PI, RHO>(jc, p.tw);
+  if constexpr (C::kFold) {
+    init_job_consts<false, PI, RHO>(jc, p.tw);
+    scale_tw1(jc, p.oscale);
+  }
   uint32_t afr[2][2][4], afr_lo[2][2][4];
   build_dft_frags<PI, RHO>(p.tw, 128, afr, afr_lo, SPLIT);
   float2 tw1[2][2][2];  // W256^(m0 k0) for stage-1 output (j, h, e)
@@ -108,7 +113,8 @@ __global__ void __launch_bounds__(256, SmallCfg<R, SPLIT>::kMinBlocks)
 #pragma unroll
       for (int e = 0; e < 2; ++e) {
         const int m0 = PI::apply(2 * t + e + 8 * j), k0 = RHO::apply(g + 8 * h);
-        tw1[j][h][e] = p.tw[((m0 * k0) & 255) * 8];
+        const float2 w = p.tw[((m0 * k0) & 255) * 8];
+        tw1[j][h][e] = make_float2(w.x * p.oscale, w.y * p.oscale);
       }
   uint32_t in_off[2][2][2];   // physical element offset of load slot (kt, r, j) in tile a = 0
   int mval[2][2][2];          // m = 16 m1 + m0 of that slot

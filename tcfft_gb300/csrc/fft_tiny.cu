@@ -30,7 +30,7 @@ struct TinyCfg {
 
 template <int R, bool SPLIT>
 __global__ void __launch_bounds__(128) fft_tiny_kernel(unsigned char* data, long long batch,
-                                                       const float2* __restrict__ tw2048, float dsign) {
+                                                       const float2* __restrict__ tw2048, float dsign, float oscale) {
   using C = TinyCfg<R, SPLIT>;
   constexpr int N = C::kN, ES = C::kES, ROW = C::kRow;
   __shared__ __align__(16) unsigned char buf[C::kWarps][C::kWarpBytes];
@@ -62,6 +62,7 @@ __global__ void __launch_bounds__(128) fft_tiny_kernel(unsigned char* data, long
     };
     auto st = [&](int v, int k, int, int, float2 val) {
       const uint32_t a = wb + (uint32_t)((v * ROW + k) * ES);
+      val = make_float2(val.x * oscale, val.y * oscale);  // output scale (1 unless normalised)
       if constexpr (SPLIT) sts64f(a, val);
       else sts32(a, pack_h2(val.x, val.y));
     };
@@ -77,14 +78,15 @@ __global__ void __launch_bounds__(128) fft_tiny_kernel(unsigned char* data, long
 }
 
 template <int R, bool SPLIT>
-cudaError_t launch_tiny_t(void* data, int64_t batch, const float2* tw, float dsign, int num_sms, cudaStream_t st) {
+cudaError_t launch_tiny_t(void* data, int64_t batch, const float2* tw, float dsign, int num_sms, cudaStream_t st,
+                          float oscale) {
   using C = TinyCfg<R, SPLIT>;
   const long long groups = (batch + 15) / 16;
   long long blocks = (groups + C::kWarps - 1) / C::kWarps;
   if (blocks > (long long)num_sms * 12) blocks = (long long)num_sms * 12;
   if (blocks < 1) blocks = 1;
   fft_tiny_kernel<R, SPLIT><<<(unsigned)blocks, 32 * C::kWarps, 0, st>>>(static_cast<unsigned char*>(data), batch,
-                                                                        tw, dsign);
+                                                                        tw, dsign, oscale);
   return cudaGetLastError();
 }
 
@@ -93,15 +95,15 @@ cudaError_t launch_tiny_t(void* data, int64_t batch, const float2* tw, float dsi
 bool tiny_supported(int64_t n, bool split) { return n == 16 || n == 32 || n == 64 || (n == 128 && !split); }
 
 cudaError_t launch_tiny(int64_t n, bool split, void* data, int64_t batch, const float2* tw, float dsign, int num_sms,
-                        cudaStream_t st) {
+                        cudaStream_t st, float oscale) {
   switch (n * 2 + (split ? 1 : 0)) {
-    case 32: return launch_tiny_t<1, false>(data, batch, tw, dsign, num_sms, st);
-    case 33: return launch_tiny_t<1, true>(data, batch, tw, dsign, num_sms, st);
-    case 64: return launch_tiny_t<2, false>(data, batch, tw, dsign, num_sms, st);
-    case 65: return launch_tiny_t<2, true>(data, batch, tw, dsign, num_sms, st);
-    case 128: return launch_tiny_t<4, false>(data, batch, tw, dsign, num_sms, st);
-    case 129: return launch_tiny_t<4, true>(data, batch, tw, dsign, num_sms, st);
-    case 256: return launch_tiny_t<8, false>(data, batch, tw, dsign, num_sms, st);
+    case 32: return launch_tiny_t<1, false>(data, batch, tw, dsign, num_sms, st, oscale);
+    case 33: return launch_tiny_t<1, true>(data, batch, tw, dsign, num_sms, st, oscale);
+    case 64: return launch_tiny_t<2, false>(data, batch, tw, dsign, num_sms, st, oscale);
+    case 65: return launch_tiny_t<2, true>(data, batch, tw, dsign, num_sms, st, oscale);
+    case 128: return launch_tiny_t<4, false>(data, batch, tw, dsign, num_sms, st, oscale);
+    case 129: return launch_tiny_t<4, true>(data, batch, tw, dsign, num_sms, st, oscale);
+    case 256: return launch_tiny_t<8, false>(data, batch, tw, dsign, num_sms, st, oscale);
     default: return cudaErrorInvalidValue;
   }
 }

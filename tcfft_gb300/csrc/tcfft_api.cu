@@ -206,7 +206,7 @@ void free_tables(tcfftPlanImpl* p) {
     *q = nullptr;
   }
   p->mv_n = 0;
-  for (int d = 0; d < 2; ++d) {
+  for (int d = 0; d < 4; ++d) {
     if (p->graph_exec[d]) cudaGraphExecDestroy(p->graph_exec[d]);
     p->graph_exec[d] = nullptr;
     p->graph_ptr[d] = nullptr;
@@ -373,6 +373,8 @@ tcfftStatus choose_1d(int64_t n, int64_t batch, int precision, Schedule& s, int 
     // N1 >= N2 except 2^21: 1024 x 2048 (0.90 ms for 2^28 elements) against 2048 x 1024 (0.94 ms)
     int64_t n1 = int64_t(1) << ((lg + 1) / 2);
     if (lg == 21) n1 = 1024;
+    if (getenv("TCFFT_N1")) n1 = atoll(getenv("TCFFT_N1"));  // decomposition override (measurements)
+    if (n1 < 256 || n1 > 2048 || n / n1 < 256 || n / n1 > 2048) return TCFFT_NOT_SUPPORTED;
     const int64_t n2 = n / n1;
     FusedKey k;
     k.role0 = kRoleCol;
@@ -491,10 +493,12 @@ tcfftStatus validate_opts(const tcfftOptions* o) {
   if (o->precision != TCFFT_PRECISION_PLAIN && o->precision != TCFFT_PRECISION_SPLIT) return TCFFT_INVALID_VALUE;
   if (o->input_order != TCFFT_ORDER_NATURAL && o->input_order != TCFFT_ORDER_REFERENCE_DIGIT_REVERSED)
     return TCFFT_INVALID_VALUE;
+  if (o->direction != TCFFT_FORWARD && o->direction != TCFFT_INVERSE) return TCFFT_INVALID_VALUE;
+  if (o->normalization != TCFFT_NORM_NONE && o->normalization != TCFFT_NORM_BY_N) return TCFFT_INVALID_VALUE;
   return TCFFT_SUCCESS;
 }
 
-tcfftStatus exec_many(tcfftPlanImpl* plan, void* data, cudaStream_t st, int dir);
+tcfftStatus exec_many(tcfftPlanImpl* plan, void* data, cudaStream_t st, int dir, int norm);
 
 // Composite schedules whose 4096-point row pass writes its output transposed
 // (resident kernel, plain): 1D N1 x 4096 (no final transpose) and 2D axes of 4096.
@@ -522,12 +526,17 @@ bool inject_stall(tcfftPlanImpl* plan, cudaStream_t st) {
   return cudaMemsetAsync(plan->counters, 0x80, sizeof(int), st) != cudaSuccess;
 }
 
-tcfftStatus exec_plan(tcfftPlan plan, void* data, void* stream, int dir) {
+// dir: 0 = sign -1 (the reference's forward), 1 = sign +1 (conjugate direction);
+// norm: 1 = scale every transform by 1 / (its element count).  The scale is a
+// power of two, so it is exact; each kernel folds it into a twiddle it already
+// applies (no extra pass, no extra work per element except in the tiny kernel).
+tcfftStatus exec_plan(tcfftPlan plan, void* data, void* stream, int dir, int norm) {
   if (!plan || plan->magic != tcfftPlanImpl::kMagic) return TCFFT_INVALID_PLAN;
   if (!data) return TCFFT_INVALID_VALUE;
   if ((reinterpret_cast<uintptr_t>(data) & 127) != 0) return TCFFT_MISALIGNED;
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
-  if (plan->kind == 3) return exec_many(plan, data, st, dir);
+  if (plan->kind == 3) return exec_many(plan, data, st, dir, norm);
+  const float oscale = norm ? 1.f / (float)(plan->kind == 2 ? plan->nx * plan->ny : plan->n) : 1.f;
   const bool split = plan->precision == TCFFT_PRECISION_SPLIT;
   const float2* tw = plan->tables.tw2048[dir];
   const float dsign = dir == 0 ? 1.f : -1.f;
@@ -543,7 +552,8 @@ tcfftStatus exec_plan(tcfftPlan plan, void* data, void* stream, int dir) {
   if (s.kind == Schedule::kCluster) {
     const bool enc = plan->tmap_ptr != data;
     cudaError_t e = launch_cluster(plan->n, data, plan->batch, tw, plan->twlo[dir], plan->twhi[dir], dsign,
-                                   plan->tables.err, plan->num_sms, st, &plan->fmaps.load0, &plan->fmaps.store0, enc);
+                                   plan->tables.err, plan->num_sms, st, &plan->fmaps.load0, &plan->fmaps.store0, enc,
+                                   oscale);
     if (e == cudaSuccess) plan->tmap_ptr = data;
     return cuda_status(e, "cluster launch");
   }
@@ -551,14 +561,17 @@ tcfftStatus exec_plan(tcfftPlan plan, void* data, void* stream, int dir) {
     const bool enc = plan->tmap_ptr != data;
     cudaError_t e =
         split ? launch_resident_split(plan->n, data, plan->batch, tw, plan->twlo[dir], plan->twhi[dir], dsign,
-                                      plan->tables.err, plan->num_sms, st, &plan->fmaps.load0, &plan->fmaps.store0, enc)
+                                      plan->tables.err, plan->num_sms, st, &plan->fmaps.load0, &plan->fmaps.store0, enc,
+                                      oscale)
               : launch_resident(plan->n, data, plan->batch, tw, plan->twlo[dir], plan->twhi[dir], dsign,
-                                plan->tables.err, plan->num_sms, st, &plan->fmaps.load0, &plan->fmaps.store0, enc);
+                                plan->tables.err, plan->num_sms, st, &plan->fmaps.load0, &plan->fmaps.store0, enc,
+                                oscale);
     if (e == cudaSuccess) plan->tmap_ptr = data;
     return cuda_status(e, "resident launch");
   }
   if (s.kind == Schedule::kTiny)
-    return cuda_status(launch_tiny(plan->n, split, data, plan->batch, tw, dsign, plan->num_sms, st), "tiny launch");
+    return cuda_status(launch_tiny(plan->n, split, data, plan->batch, tw, dsign, plan->num_sms, st, oscale),
+                       "tiny launch");
   if (s.kind == Schedule::kLarge1d) {
     const FusedKey& k = s.key;
     const bool fresh = plan->tmap_ptr != data;
@@ -595,6 +608,8 @@ tcfftStatus exec_plan(tcfftPlan plan, void* data, void* stream, int dir) {
     fp.err = plan->tables.err;
     fp.dsign = dsign;
     fp.wait_ns = plan->wait_ns;
+    fp.oscale0 = oscale;  // the column pass's W_N factors carry the whole scale
+    fp.oscale1 = 1.f;
     if (cuda_status(cudaMemsetAsync(plan->counters, 0, sizeof(int) * 2 * s.S, st), "counter reset"))
       return TCFFT_CUDA_ERROR;
     int grid = 0;
@@ -607,7 +622,7 @@ tcfftStatus exec_plan(tcfftPlan plan, void* data, void* stream, int dir) {
                                               &plan->fmaps.load1, &plan->fmaps.store1, fresh),
                          "rows (transposed output)");
     }
-    tcfftStatus r = exec_plan(plan->subs[0], plan->big, stream, dir);  // rows of N2, natural order
+    tcfftStatus r = exec_plan(plan->subs[0], plan->big, stream, dir, 0);  // rows of N2, natural order
     if (r != TCFFT_SUCCESS) return r;
     // [B][N1 rows k1][N2 cols k2] -> X[k1 + N1 k2] = [B][N2][N1]
     return cuda_status(launch_transpose(plan->big, data, plan->batch, s.N1, s.N2, es, plan->num_sms, st), "transpose");
@@ -617,13 +632,13 @@ tcfftStatus exec_plan(tcfftPlan plan, void* data, void* stream, int dir) {
     // and transposed -> [B][N1][N2]; rows of N2 -> Z[k1][k2]; X[k1 + N1 k2] = [B][N2][N1]
     if (cuda_status(launch_transpose(data, plan->big, plan->batch, s.N1, s.N2, es, plan->num_sms, st), "transpose"))
       return TCFFT_CUDA_ERROR;
-    tcfftStatus r = exec_plan(plan->subs[0], plan->big, stream, dir);
+    tcfftStatus r = exec_plan(plan->subs[0], plan->big, stream, dir, norm);  // scaled by 1/N1
     if (r != TCFFT_SUCCESS) return r;
     if (cuda_status(launch_transpose_twiddle(plan->big, data, plan->batch, s.N2, s.N1, plan->n, dsign, split,
                                              plan->num_sms, st),
                     "transpose-twiddle"))
       return TCFFT_CUDA_ERROR;
-    r = exec_plan(plan->subs[1], data, stream, dir);
+    r = exec_plan(plan->subs[1], data, stream, dir, norm);  // scaled by 1/N2
     if (r != TCFFT_SUCCESS) return r;
     if (cuda_status(launch_transpose(data, plan->big, plan->batch, s.N1, s.N2, es, plan->num_sms, st), "transpose"))
       return TCFFT_CUDA_ERROR;
@@ -640,11 +655,11 @@ tcfftStatus exec_plan(tcfftPlan plan, void* data, void* stream, int dir) {
       const tcfftPlanImpl* rp = plan->subs[0];
       if (cuda_status(launch_resident_tout(4096, data, plan->big, nx * B, nx, tw, rp->twlo[dir], rp->twhi[dir], dsign,
                                            plan->tables.err, plan->num_sms, st, &plan->fmaps.load0,
-                                           &plan->fmaps.store0, fresh),
+                                           &plan->fmaps.store0, fresh, norm ? 1.f / 4096 : 1.f),
                       "rows (transposed output)"))
         return TCFFT_CUDA_ERROR;
     } else {
-      tcfftStatus r = exec_plan(plan->subs[0], data, stream, dir);  // rows of ny
+      tcfftStatus r = exec_plan(plan->subs[0], data, stream, dir, norm);  // rows of ny (scaled by 1/ny)
       if (r != TCFFT_SUCCESS) return r;
       if (cuda_status(launch_transpose(data, plan->big, B, nx, ny, es, plan->num_sms, st), "transpose"))
         return TCFFT_CUDA_ERROR;
@@ -653,10 +668,10 @@ tcfftStatus exec_plan(tcfftPlan plan, void* data, void* stream, int dir) {
       const tcfftPlanImpl* cp = plan->subs[1];
       return cuda_status(launch_resident_tout(4096, plan->big, data, ny * B, ny, tw, cp->twlo[dir], cp->twhi[dir],
                                               dsign, plan->tables.err, plan->num_sms, st, &plan->fmaps.load1,
-                                              &plan->fmaps.store1, fresh),
+                                              &plan->fmaps.store1, fresh, norm ? 1.f / 4096 : 1.f),
                          "columns (transposed output)");
     }
-    tcfftStatus r = exec_plan(plan->subs[1], plan->big, stream, dir);  // columns of nx, now rows
+    tcfftStatus r = exec_plan(plan->subs[1], plan->big, stream, dir, norm);  // columns of nx, now rows
     if (r != TCFFT_SUCCESS) return r;
     return cuda_status(launch_transpose(plan->big, data, B, ny, nx, es, plan->num_sms, st), "transpose");
   }
@@ -675,7 +690,7 @@ tcfftStatus exec_plan(tcfftPlan plan, void* data, void* stream, int dir) {
     }
     int launches = 0;
     return cuda_status(launch_small(s.R, split, plan->tmap0, plan->total_elems, tw, dsign, plan->tables.err,
-                                    plan->num_sms, st, &launches));
+                                    plan->num_sms, st, &launches, oscale));
   }
   if (s.kind == Schedule::kFused1d) {
     const int es = split ? 8 : 4, er = 128 / es;
@@ -708,6 +723,8 @@ tcfftStatus exec_plan(tcfftPlan plan, void* data, void* stream, int dir) {
     fp.err = plan->tables.err;
     fp.dsign = dsign;
     fp.wait_ns = plan->wait_ns;
+    fp.oscale0 = oscale;  // phase 0's W_N factors carry the whole scale
+    fp.oscale1 = 1.f;
     if (cuda_status(cudaMemsetAsync(plan->counters, 0, sizeof(int) * 2 * s.S, st), "counter reset") ||
         inject_stall(plan, st))
       return TCFFT_CUDA_ERROR;
@@ -755,6 +772,8 @@ tcfftStatus exec_plan(tcfftPlan plan, void* data, void* stream, int dir) {
     fp.err = plan->tables.err;
     fp.dsign = dsign;
     fp.wait_ns = plan->wait_ns;
+    fp.oscale0 = norm ? 1.f / (float)ny : 1.f;  // rows
+    fp.oscale1 = norm ? 1.f / (float)nx : 1.f;  // columns
     if (cuda_status(cudaMemsetAsync(plan->counters, 0, sizeof(int) * 2 * s.S, st), "counter reset") ||
         inject_stall(plan, st))
       return TCFFT_CUDA_ERROR;
@@ -963,9 +982,9 @@ tcfftStatus autotune_plan(tcfftPlanImpl* p, const tcfftOptions& o) {
       if (choose_again(p, c, s) != TCFFT_SUCCESS || seen_d.count(s.D)) continue;
       seen_d.insert(s.D);
       if (apply_lag(p, c) != TCFFT_SUCCESS) break;
-      if (exec_plan(p, tmp, nullptr, 0) != TCFFT_SUCCESS) break;
+      if (exec_plan(p, tmp, nullptr, 0, 0) != TCFFT_SUCCESS) break;
       cudaEventRecord(e0, nullptr);
-      for (int r = 0; r < 3; ++r) exec_plan(p, tmp, nullptr, 0);
+      for (int r = 0; r < 3; ++r) exec_plan(p, tmp, nullptr, 0, 0);
       cudaEventRecord(e1, nullptr);
       if (cudaEventSynchronize(e1) != cudaSuccess) break;
       float ms = 0;
@@ -1015,12 +1034,13 @@ tcfftStatus check_errors(tcfftPlanImpl* p) {
   return r;
 }
 
-tcfftStatus exec_many(tcfftPlanImpl* plan, void* data, cudaStream_t st, int dir) {
+tcfftStatus exec_many(tcfftPlanImpl* plan, void* data, cudaStream_t st, int dir, int norm) {
   const int es = plan->precision == TCFFT_PRECISION_SPLIT ? 8 : 4;
-  if (!plan->graph_exec[dir] || plan->graph_ptr[dir] != data) {
-    if (plan->graph_exec[dir]) cudaGraphExecDestroy(plan->graph_exec[dir]);
-    plan->graph_exec[dir] = nullptr;
-    plan->graph_ptr[dir] = nullptr;
+  const int g = 2 * dir + norm;  // one captured graph per direction and normalisation
+  if (!plan->graph_exec[g] || plan->graph_ptr[g] != data) {
+    if (plan->graph_exec[g]) cudaGraphExecDestroy(plan->graph_exec[g]);
+    plan->graph_exec[g] = nullptr;
+    plan->graph_ptr[g] = nullptr;
     if (cuda_status(cudaStreamBeginCapture(plan->cap_stream, cudaStreamCaptureModeThreadLocal), "graph capture"))
       return TCFFT_CUDA_ERROR;
     tcfftStatus r = TCFFT_SUCCESS;
@@ -1045,7 +1065,7 @@ tcfftStatus exec_many(tcfftPlanImpl* plan, void* data, cudaStream_t st, int dir)
         }
       }
       unsigned char* base = static_cast<unsigned char*>(run.in_big ? plan->big : data);
-      r = exec_plan(run.sub, base + run.offset * es, plan->branch[b], dir);
+      r = exec_plan(run.sub, base + run.offset * es, plan->branch[b], dir, norm);
     }
     for (int b = 0; b < tcfftPlanImpl::kBranches; ++b)  // join every forked branch (also after a failure)
       if (used[b] && (cudaEventRecord(plan->join_ev[b], plan->branch[b]) != cudaSuccess ||
@@ -1055,18 +1075,18 @@ tcfftStatus exec_many(tcfftPlanImpl* plan, void* data, cudaStream_t st, int dir)
       r = cuda_status(launch_move_blocks(plan->big, data, plan->mv_big, plan->mv_user, plan->mv_cum, plan->mv_n,
                                          plan->mv_chunks, plan->num_sms, plan->cap_stream),
                       "scatter");
-    cudaGraph_t g = nullptr;
-    cudaError_t ce = cudaStreamEndCapture(plan->cap_stream, &g);
+    cudaGraph_t gr = nullptr;
+    cudaError_t ce = cudaStreamEndCapture(plan->cap_stream, &gr);
     if (r != TCFFT_SUCCESS || ce != cudaSuccess) {
-      if (g) cudaGraphDestroy(g);
+      if (gr) cudaGraphDestroy(gr);
       return r != TCFFT_SUCCESS ? r : cuda_status(ce, "graph capture");
     }
-    ce = cudaGraphInstantiate(&plan->graph_exec[dir], g, 0);
-    cudaGraphDestroy(g);
+    ce = cudaGraphInstantiate(&plan->graph_exec[g], gr, 0);
+    cudaGraphDestroy(gr);
     if (cuda_status(ce, "graph instantiate")) return TCFFT_CUDA_ERROR;
-    plan->graph_ptr[dir] = data;
+    plan->graph_ptr[g] = data;
   }
-  return cuda_status(cudaGraphLaunch(plan->graph_exec[dir], st), "graph launch");
+  return cuda_status(cudaGraphLaunch(plan->graph_exec[g], st), "graph launch");
 }
 
 }  // namespace
@@ -1132,6 +1152,8 @@ tcfftStatus tcfftPlan1d(tcfftPlan* out, int64_t n, int64_t batch, const tcfftOpt
   p->batch = batch;
   p->precision = o.precision;
   p->input_order = o.input_order;
+  p->direction = o.direction;
+  p->normalize = o.normalization;
   p->total_elems = n * batch;
   p->sched = s;
   p->radices_x = chain;
@@ -1210,6 +1232,8 @@ tcfftStatus tcfftPlan2d(tcfftPlan* out, int64_t nx, int64_t ny, int64_t batch, c
   p->batch = batch;
   p->precision = o.precision;
   p->input_order = o.input_order;
+  p->direction = o.direction;
+  p->normalize = o.normalization;
   p->total_elems = nx * ny * batch;
   p->sched = s;
   p->radices_x = cx;
@@ -1257,6 +1281,8 @@ tcfftStatus tcfftPlanMany(tcfftPlan* out, int64_t count, const int32_t* ranks, c
   if (!p) return TCFFT_ALLOC_FAILED;
   p->kind = 3;
   p->precision = o.precision;
+  p->direction = o.direction;
+  p->normalize = o.normalization;
   p->batch = count;
   st = alloc_tables(p);
   tcfftOptions os = o;
@@ -1350,7 +1376,10 @@ tcfftStatus tcfftPlanMany(tcfftPlan* out, int64_t count, const int32_t* ranks, c
   return TCFFT_SUCCESS;
 }
 
-tcfftStatus tcfftExecute(tcfftPlan plan, void* data, void* stream) { return exec_plan(plan, data, stream, 0); }
+tcfftStatus tcfftExecute(tcfftPlan plan, void* data, void* stream) {
+  if (!plan || plan->magic != tcfftPlanImpl::kMagic) return TCFFT_INVALID_PLAN;
+  return exec_plan(plan, data, stream, plan->direction, plan->normalize);
+}
 
 tcfftStatus tcfftExecuteHost(tcfftPlan plan, const void* host_in, void* host_out, void* work, void* stream) {
   if (!plan || plan->magic != tcfftPlanImpl::kMagic) return TCFFT_INVALID_PLAN;
@@ -1364,7 +1393,7 @@ tcfftStatus tcfftExecuteHost(tcfftPlan plan, const void* host_in, void* host_out
   if (K <= 1) {  // unchunked
     if (cuda_status(cudaMemcpyAsync(work, host_in, total, cudaMemcpyHostToDevice, st), "copy in"))
       return TCFFT_CUDA_ERROR;
-    tcfftStatus r = exec_plan(plan, work, stream, 0);
+    tcfftStatus r = exec_plan(plan, work, stream, plan->direction, plan->normalize);
     if (r != TCFFT_SUCCESS) return r;
     return cuda_status(cudaMemcpyAsync(host_out, work, total, cudaMemcpyDeviceToHost, st), "copy out");
   }
@@ -1412,7 +1441,7 @@ tcfftStatus tcfftExecuteHost(tcfftPlan plan, const void* host_in, void* host_out
         cuda_status(cudaEventRecord(plan->host_ev_in[c], sin), "copy in") ||
         cuda_status(cudaStreamWaitEvent(sfft, plan->host_ev_in[c], 0), "copy in"))
       return TCFFT_CUDA_ERROR;
-    const tcfftStatus r = exec_plan(plan->host_sub[b == b0 ? 0 : 1], dev, sfft, 0);
+    const tcfftStatus r = exec_plan(plan->host_sub[b == b0 ? 0 : 1], dev, sfft, plan->direction, plan->normalize);
     if (r != TCFFT_SUCCESS) return r;
     if (cuda_status(cudaEventRecord(plan->host_ev_fft[c], sfft), "transform") ||
         cuda_status(cudaStreamWaitEvent(sout, plan->host_ev_fft[c], 0), "transform") ||
@@ -1432,7 +1461,13 @@ tcfftStatus tcfftExecuteHost(tcfftPlan plan, const void* host_in, void* host_out
 }
 
 tcfftStatus tcfftExecuteAdjoint(tcfftPlan plan, void* data, void* stream) {
-  return exec_plan(plan, data, stream, 1);
+  if (!plan || plan->magic != tcfftPlanImpl::kMagic) return TCFFT_INVALID_PLAN;
+  return exec_plan(plan, data, stream, 1 - plan->direction, plan->normalize);
+}
+
+tcfftStatus tcfftExecuteInverse(tcfftPlan plan, void* data, void* stream) {
+  if (!plan || plan->magic != tcfftPlanImpl::kMagic) return TCFFT_INVALID_PLAN;
+  return exec_plan(plan, data, stream, 1 - plan->direction, 1 - plan->normalize);
 }
 
 tcfftStatus tcfftCheckDevice(tcfftPlan plan, void* stream) {

@@ -47,8 +47,9 @@ CUresult encode_fused1d_maps(FusedMaps* maps, const FusedKey& k, void* data, voi
 
 // Short 1D transforms N = 16..128 (fft_tiny.cu); N = 128 is plain only.
 bool tiny_supported(int64_t n, bool split);
+// oscale: output scale of a launch (a power of two; 1/N for a normalised transform).
 cudaError_t launch_tiny(int64_t n, bool split, void* data, int64_t batch, const float2* tw, float dsign, int num_sms,
-                        cudaStream_t st);
+                        cudaStream_t st, float oscale = 1.f);
 // Batched out-of-place transpose [B][R][C] -> [B][C][R] of es-byte elements (tcfft_transpose.cu).
 cudaError_t launch_transpose(const void* in, void* out, int64_t B, int64_t R, int64_t C, int es, int num_sms,
                              cudaStream_t st);
@@ -71,25 +72,26 @@ CUresult encode_col_store(CUtensorMap* m, CUtensorMapDataType dt, void* base, in
 bool resident_supported(int64_t n, bool split);
 cudaError_t launch_resident(int64_t n, void* data, int64_t batch, const float2* tw2048, const float2* twlo,
                             const float2* twhi, float dsign, int* err, int num_sms, cudaStream_t st,
-                            CUtensorMap* lm, CUtensorMap* sm, bool encode);
+                            CUtensorMap* lm, CUtensorMap* sm, bool encode, float oscale = 1.f);
 cudaError_t launch_resident_split(int64_t n, void* data, int64_t batch, const float2* tw2048, const float2* twlo,
                                   const float2* twhi, float dsign, int* err, int num_sms, cudaStream_t st,
-                                  CUtensorMap* lm, CUtensorMap* sm, bool encode);
+                                  CUtensorMap* lm, CUtensorMap* sm, bool encode, float oscale = 1.f);
 bool resident_tout_supported(int64_t n, int64_t batch, int64_t rows);
 cudaError_t launch_resident_tout(int64_t n, const void* in, void* out, int64_t batch, int64_t rows,
                                  const float2* tw2048, const float2* twlo, const float2* twhi, float dsign, int* err,
-                                 int num_sms, cudaStream_t st, CUtensorMap* lm, CUtensorMap* sm, bool encode);
+                                 int num_sms, cudaStream_t st, CUtensorMap* lm, CUtensorMap* sm, bool encode,
+                                 float oscale = 1.f);
 
 // One transform per thread-block cluster, N = 2^15..2^18 plain (fft_cluster.cu).
 bool cluster_supported(int64_t n, bool split, int num_sms);
 cudaError_t launch_cluster(int64_t n, void* data, int64_t batch, const float2* tw2048, const float2* twlo,
                            const float2* twhi, float dsign, int* err, int num_sms, cudaStream_t st, CUtensorMap* lm,
-                           CUtensorMap* sm, bool encode);
+                           CUtensorMap* sm, bool encode, float oscale = 1.f);
 
 // Launch entry points implemented in the kernel translation units. Each
 // returns cudaSuccess or the launch error.
 cudaError_t launch_small(int R, bool split, const CUtensorMap& tmap, int64_t total_elems, const float2* tw,
-                         float dsign, int* err, int num_sms, cudaStream_t stream, int* launches);
+                         float dsign, int* err, int num_sms, cudaStream_t stream, int* launches, float oscale = 1.f);
 int small_tile_elems(int R, bool split);
 
 // Reference input-order contract (tcfft_permute.cu).

@@ -224,6 +224,7 @@ extern "C" tcfftStatus tcfftExecute1dNoAlloc(void* data, int64_t n, int64_t batc
   fp.err = d.err;
   fp.dsign = direction == 0 ? 1.f : -1.f;
   fp.wait_ns = 0;  // the default limit
+  fp.oscale0 = fp.oscale1 = 1.f;  // unnormalised
   int grid = 0;
   cudaError_t e = launch_fused(k, maps, fp, d.num_sms, st, &grid);
   if (e != cudaSuccess) {

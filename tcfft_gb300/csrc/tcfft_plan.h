@@ -38,6 +38,7 @@ struct tcfftPlanImpl {
   int kind = 0;  // 1: 1D, 2: 2D, 3: many
   int64_t n = 0, nx = 0, ny = 0, batch = 0;
   int precision = 0, input_order = 0;
+  int direction = 0, normalize = 0;  // of tcfftExecute (tcfftOptions)
   int device = -1, num_sms = 0;
   int64_t total_elems = 0;
   int64_t span_elems = 0;  // elements from the buffer start to the end of the last transform
@@ -79,8 +80,8 @@ struct tcfftPlanImpl {
   cudaStream_t branch[kBranches] = {};
   cudaEvent_t fork_ev = nullptr;
   cudaEvent_t join_ev[kBranches] = {};
-  void* graph_ptr[2] = {nullptr, nullptr};
-  cudaGraphExec_t graph_exec[2] = {nullptr, nullptr};
+  void* graph_ptr[4] = {};  // per (direction, normalisation)
+  cudaGraphExec_t graph_exec[4] = {};
   // tcfftExecuteHost: sub-plans for the chunk batches (created on first use), copy-in,
   // compute and copy-out streams, per-chunk events
   static constexpr int kHostChunks = 16;

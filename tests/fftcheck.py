@@ -66,13 +66,13 @@ def quantize(x, precision):
     return np.asarray(x).astype(dt).astype(np.float64)
 
 
-def run_gpu(plan, x, precision, adjoint=False, device="cuda:0"):
+def run_gpu(plan, x, precision, adjoint=False, device="cuda:0", inverse=False):
     """Copy float64 [..., 2] input to the device in the plan's precision, run
     in place through the C ABI, return complex128 result."""
     import torch
     dt = torch.float16 if precision == "plain" else torch.float32
     t = torch.from_numpy(np.ascontiguousarray(x)).to(dtype=dt).to(device)
-    plan.exec(t, adjoint=adjoint)
+    plan.exec(t, adjoint=adjoint, inverse=inverse)
     plan.check_device()
     return to_complex(t.float().cpu().numpy())
 

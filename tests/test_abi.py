@@ -108,3 +108,23 @@ def test_plan_many_rejects_bad_layouts():
     assert call([(256,)], [3]) == 3                       # TCFFT_MISALIGNED: 12-byte offset
     assert call([(256,), (256,)], [0, 128]) == 1          # overlapping transforms
     assert call([(100,)], [0]) == 2                       # TCFFT_INVALID_SIZE
+
+
+@pytest.mark.parametrize("field,value", [("direction", 2), ("direction", -1), ("normalization", 3),
+                                         ("precision", 5), ("input_order", 7)])
+def test_plan_rejects_bad_options_before_touching_the_gpu(field, value):
+    """Option validation is host logic: bad values return TCFFT_INVALID_VALUE."""
+    lib = tc.lib()
+    opts = tc.Options()
+    assert lib.tcfftOptionsDefault(ctypes.byref(opts)) == 0
+    assert opts.direction == tc.FORWARD and opts.normalization == tc.NORM_NONE
+    setattr(opts, field, value)
+    h = ctypes.c_void_p(None)
+    assert lib.tcfftPlan1d(ctypes.byref(h), 1024, 4, ctypes.byref(opts)) == 1
+    assert lib.tcfftPlan2d(ctypes.byref(h), 256, 256, 4, ctypes.byref(opts)) == 1
+    assert not h.value
+
+
+def test_options_struct_layout_matches_header():
+    """The ctypes mirror of tcfftOptions has the header's size (pointer-aligned)."""
+    assert ctypes.sizeof(tc.Options) == 32
