@@ -136,6 +136,34 @@ tcfftStatus tcfftExecuteAdjoint(tcfftPlan plan, void* data, void* stream);
  * use only the exp(-2 pi i jk/N) twiddles). */
 tcfftStatus tcfftExecuteInverse(tcfftPlan plan, void* data, void* stream);
 
+/* tcfftExecute with a separate input: `in` (not modified) is transformed into
+ * `out`; both device memory of the plan's size and layout, 128-byte aligned,
+ * not overlapping (in == out is tcfftExecute).  The 1D schedules of up to
+ * 2^22 points (and the composite 1D ones) read `in` directly, so the
+ * out-of-place call moves no more data than the in-place one; 2D, uneven-batch
+ * and reference-order plans copy `in` to `out` first.  The reference's
+ * tcfftExec is in place only (tcfft_half.h:20). */
+tcfftStatus tcfftExecuteOutOfPlace(tcfftPlan plan, const void* in, void* out, void* stream);
+
+/* Real 1D transforms (no counterpart in the reference): `batch` sequences of n
+ * real values (power of two, 32 <= n <= 2^27), fp16 (TCFFT_PRECISION_PLAIN) or
+ * fp32 (TCFFT_PRECISION_SPLIT), contiguous [batch][n], and their Hermitian
+ * halves, n/2 + 1 complex values each, [batch][n/2 + 1] (interleaved, half2 /
+ * float2).  Computed as complex transforms of n/2 points plus one pass that
+ * splits (or, for C2R, merges) the even and odd spectra.  C2R is the inverse of
+ * R2C (c2r(r2c(x)) = x): with TCFFT_NORM_NONE (default) R2C is unnormalised and
+ * C2R carries the 1/n (numpy's rfft / irfft), with TCFFT_NORM_BY_N R2C carries
+ * it and C2R is unnormalised.  Options: precision, normalization, autotune;
+ * direction must be TCFFT_FORWARD and input order natural. */
+tcfftStatus tcfftPlanReal1d(tcfftPlan* plan, int64_t n, int64_t batch, const tcfftOptions* opts);
+/* X = DFT(x) (sign -1; times 1/n with TCFFT_NORM_BY_N), the n/2 + 1
+ * non-redundant values; `in` is not modified. */
+tcfftStatus tcfftExecuteR2C(tcfftPlan plan, const void* in, void* out, void* stream);
+/* x[j] = c * sum over the full Hermitian spectrum of X[k] exp(+2 pi i jk/n),
+ * c = 1/n (TCFFT_NORM_NONE) or 1 (TCFFT_NORM_BY_N); the imaginary parts of
+ * X[0] and X[n/2] are ignored; `in` is not modified. */
+tcfftStatus tcfftExecuteC2R(tcfftPlan plan, const void* in, void* out, void* stream);
+
 /* Host-buffer execution: the batch is copied in from `host_in`, transformed
  * (forward) in the caller's device buffer `work` (the plan's size, 128-byte
  * aligned) and copied out to `host_out`, pipelined over chunks of the batch on

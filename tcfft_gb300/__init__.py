@@ -87,6 +87,11 @@ _SIGNATURES = {
     "tcfftExecute": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
     "tcfftExecuteAdjoint": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
     "tcfftExecuteInverse": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
+    "tcfftExecuteOutOfPlace": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
+    "tcfftPlanReal1d": ([ctypes.POINTER(ctypes.c_void_p), ctypes.c_int64, ctypes.c_int64, ctypes.POINTER(Options)],
+                        ctypes.c_int),
+    "tcfftExecuteR2C": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
+    "tcfftExecuteC2R": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
     "tcfftExecuteHost": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p],
                          ctypes.c_int),
     "tcfftCheckDevice": ([ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
@@ -255,6 +260,15 @@ class Plan:
         _check(getattr(lib(), name)(self._handle, ctypes.c_void_p(self._ptr(data)), _stream_handle(stream)), name)
         return data
 
+    def exec_out(self, data, out, stream=None):
+        """The plan's transform of ``data`` written to ``out`` (``data`` is not modified)."""
+        if not self._handle:
+            raise TcfftError(8, "exec on destroyed plan")
+        _check(lib().tcfftExecuteOutOfPlace(self._handle, ctypes.c_void_p(self._ptr(data)),
+                                            ctypes.c_void_p(self._ptr(out)), _stream_handle(stream)),
+               "tcfftExecuteOutOfPlace")
+        return out
+
     def exec_host(self, host_in, host_out, work, stream=None):
         """Forward transform of a host batch: ``host_in`` is copied into the device
         buffer ``work``, transformed and copied to ``host_out`` (pinned CPU tensors of
@@ -319,6 +333,43 @@ class Plan:
                 self._handle = ctypes.c_void_p(None)
         except Exception:  # noqa: BLE001 - interpreter shutdown
             pass
+
+
+class RealPlan(Plan):
+    """Real 1D transforms of ``n`` points (tcfftPlanReal1d): ``r2c(x, out)`` maps
+    real ``[batch, n]`` (fp16 plain / fp32 split) to the Hermitian half
+    ``[batch, n // 2 + 1, 2]``; ``c2r(X, out)`` is its inverse (c2r(r2c(x)) = x:
+    the 1/n on c2r, or on r2c with ``normalize=True``)."""
+
+    def __init__(self, n, batch=1, precision="plain", normalize=False, autotune=False):
+        self._handle = ctypes.c_void_p(None)
+        self.precision = _precision_of(precision)
+        self.n, self.batch = int(n), int(batch)
+        self.nx = self.ny = None
+        opts = Options()
+        lib().tcfftOptionsDefault(ctypes.byref(opts))
+        opts.precision = self.precision
+        opts.normalization = NORM_BY_N if normalize else NORM_NONE
+        opts.autotune = 1 if autotune else 0
+        _check(lib().tcfftPlanReal1d(ctypes.byref(self._handle), self.n, self.batch, ctypes.byref(opts)),
+               "tcfftPlanReal1d(n=%d, batch=%d)" % (self.n, self.batch))
+
+    def _real_ptr(self, t):
+        import torch
+        want = torch.float16 if self.precision == PRECISION_PLAIN else torch.float32
+        if not isinstance(t, torch.Tensor) or not t.is_cuda or not t.is_contiguous() or t.dtype != want:
+            raise TypeError("expected a contiguous CUDA %s tensor" % want)
+        return t.data_ptr()
+
+    def r2c(self, x, out, stream=None):
+        _check(lib().tcfftExecuteR2C(self._handle, ctypes.c_void_p(self._real_ptr(x)),
+                                     ctypes.c_void_p(self._real_ptr(out)), _stream_handle(stream)), "tcfftExecuteR2C")
+        return out
+
+    def c2r(self, spec, out, stream=None):
+        _check(lib().tcfftExecuteC2R(self._handle, ctypes.c_void_p(self._real_ptr(spec)),
+                                     ctypes.c_void_p(self._real_ptr(out)), _stream_handle(stream)), "tcfftExecuteC2R")
+        return out
 
 
 # ---------------------------------------------------------------- reference-named API

@@ -403,12 +403,13 @@ bool cluster_supported(int64_t n, bool split, int num_sms) {
 
 cudaError_t launch_cluster(int64_t n, void* data, int64_t batch, const float2* tw2048, const float2* twlo,
                            const float2* twhi, float dsign, int* err, int num_sms, cudaStream_t st, CUtensorMap* lm,
-                           CUtensorMap* sm, bool encode, float oscale) {
+                           CUtensorMap* sm, bool encode, float oscale, const void* in) {
   const int64_t n2 = n / 256;
   const int cl = (int)(n2 / 64), rpc = 256 / cl, w = rpc < 32 ? rpc : 32;
   const int bh = n2 < 256 ? (int)n2 : 256;
   if (encode) {
-    if (encode_col_load(lm, CU_TENSOR_MAP_DATA_TYPE_UINT32, data, n2, batch, 4, 32, 1) != CUDA_SUCCESS)
+    void* src = const_cast<void*>(in ? in : data);  // loads from the input, stores to data
+    if (encode_col_load(lm, CU_TENSOR_MAP_DATA_TYPE_UINT32, src, n2, batch, 4, 32, 1) != CUDA_SUCCESS)
       return cudaErrorInvalidValue;
     uint64_t dims[2] = {256, (uint64_t)(n2 * batch)};  // X[b][k1 + 256 k2] as rows k2 of 256 k1
     uint64_t str[1] = {1024};

@@ -501,10 +501,11 @@ bool resident_supported(int64_t n, bool split) {
 // k2 bits 0..L-1), L = log2(N2 / 16), matching the stage layout above.
 cudaError_t launch_resident_split(int64_t n, void* data, int64_t batch, const float2* tw2048, const float2* twlo,
                                   const float2* twhi, float dsign, int* err, int num_sms, cudaStream_t st,
-                                  CUtensorMap* lm, CUtensorMap* sm, bool encode, float oscale) {
+                                  CUtensorMap* lm, CUtensorMap* sm, bool encode, float oscale, const void* in) {
   const int64_t n2 = n / 256;
   if (encode) {
-    if (encode_col_load(lm, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, data, n2, batch, 8, 16, 1) != CUDA_SUCCESS)
+    void* src = const_cast<void*>(in ? in : data);  // loads from the input, stores to data
+    if (encode_col_load(lm, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, src, n2, batch, 8, 16, 1) != CUDA_SUCCESS)
       return cudaErrorInvalidValue;
     uint64_t dims[2] = {16, (uint64_t)(n * batch / 16)};
     uint64_t str[1] = {128};
@@ -531,11 +532,12 @@ cudaError_t launch_resident_split(int64_t n, void* data, int64_t batch, const fl
 
 cudaError_t launch_resident(int64_t n, void* data, int64_t batch, const float2* tw2048, const float2* twlo,
                             const float2* twhi, float dsign, int* err, int num_sms, cudaStream_t st,
-                            CUtensorMap* lm, CUtensorMap* sm, bool encode, float oscale) {
+                            CUtensorMap* lm, CUtensorMap* sm, bool encode, float oscale, const void* in) {
   const int64_t n2 = n / 256;
   const int C = n2 < 32 ? (int)n2 : 32;
   if (encode) {
-    if (encode_col_load(lm, CU_TENSOR_MAP_DATA_TYPE_UINT32, data, n2, batch, 4, C, 1) != CUDA_SUCCESS)
+    void* src = const_cast<void*>(in ? in : data);  // loads from the input, stores to data
+    if (encode_col_load(lm, CU_TENSOR_MAP_DATA_TYPE_UINT32, src, n2, batch, 4, C, 1) != CUDA_SUCCESS)
       return cudaErrorInvalidValue;
     const uint64_t r1 = (uint64_t)(n2 / 16), row = 256 * 4;  // R1; bytes per k2 step
     const uint32_t T = (uint32_t)(4 / r1);                    // transforms per stage

@@ -9,8 +9,8 @@ namespace tcfft {
 
 namespace {
 template <int R, bool SPLIT>
-cudaError_t launch_one(const CUtensorMap& tmap, int64_t total_elems, const float2* tw, float dsign, int* err,
-                       int num_sms, cudaStream_t stream, float oscale) {
+cudaError_t launch_one(const CUtensorMap& tmap, const CUtensorMap& omap, int64_t total_elems, const float2* tw,
+                       float dsign, int* err, int num_sms, cudaStream_t stream, float oscale) {
   using C = SmallCfg<R, SPLIT>;
   static std::once_flag once;
   static int blocks_per_sm = 1;
@@ -31,7 +31,7 @@ cudaError_t launch_one(const CUtensorMap& tmap, int64_t total_elems, const float
   int grid = num_sms * blocks_per_sm;
   if (grid > p.num_tiles) grid = p.num_tiles;
   if (grid < 1) return cudaSuccess;
-  fft_small_kernel<R, SPLIT><<<grid, 256, C::kSmem, stream>>>(tmap, p);
+  fft_small_kernel<R, SPLIT><<<grid, 256, C::kSmem, stream>>>(tmap, omap, p);
   return cudaGetLastError();
 }
 }  // namespace
@@ -49,17 +49,18 @@ int small_tile_elems(int R, bool split) {
   }
 }
 
-cudaError_t launch_small(int R, bool split, const CUtensorMap& tmap, int64_t total_elems, const float2* tw,
-                         float dsign, int* err, int num_sms, cudaStream_t stream, int* launches, float oscale) {
+cudaError_t launch_small(int R, bool split, const CUtensorMap& tmap, const CUtensorMap& omap, int64_t total_elems,
+                         const float2* tw, float dsign, int* err, int num_sms, cudaStream_t stream, int* launches,
+                         float oscale) {
   if (launches) *launches = 1;
   switch (R * 2 + (split ? 1 : 0)) {
-    case 2: return launch_one<1, false>(tmap, total_elems, tw, dsign, err, num_sms, stream, oscale);
-    case 3: return launch_one<1, true>(tmap, total_elems, tw, dsign, err, num_sms, stream, oscale);
-    case 4: return launch_one<2, false>(tmap, total_elems, tw, dsign, err, num_sms, stream, oscale);
-    case 5: return launch_one<2, true>(tmap, total_elems, tw, dsign, err, num_sms, stream, oscale);
-    case 8: return launch_one<4, false>(tmap, total_elems, tw, dsign, err, num_sms, stream, oscale);
-    case 9: return launch_one<4, true>(tmap, total_elems, tw, dsign, err, num_sms, stream, oscale);
-    case 16: return launch_one<8, false>(tmap, total_elems, tw, dsign, err, num_sms, stream, oscale);
+    case 2: return launch_one<1, false>(tmap, omap, total_elems, tw, dsign, err, num_sms, stream, oscale);
+    case 3: return launch_one<1, true>(tmap, omap, total_elems, tw, dsign, err, num_sms, stream, oscale);
+    case 4: return launch_one<2, false>(tmap, omap, total_elems, tw, dsign, err, num_sms, stream, oscale);
+    case 5: return launch_one<2, true>(tmap, omap, total_elems, tw, dsign, err, num_sms, stream, oscale);
+    case 8: return launch_one<4, false>(tmap, omap, total_elems, tw, dsign, err, num_sms, stream, oscale);
+    case 9: return launch_one<4, true>(tmap, omap, total_elems, tw, dsign, err, num_sms, stream, oscale);
+    case 16: return launch_one<8, false>(tmap, omap, total_elems, tw, dsign, err, num_sms, stream, oscale);
     default: return cudaErrorInvalidValue;
   }
 }

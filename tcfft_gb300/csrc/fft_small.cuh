@@ -14,9 +14,9 @@
 // in registers.
 //
 // CTA structure: persistent CTAs, 8 warps, a ring of NSTAGE shared-memory
-// tiles filled by 2D TMA loads (128B swizzle) and drained by TMA stores; the
-// transform is in place (each tile is loaded, transformed and stored back to
-// the same global rows).
+// tiles filled by 2D TMA loads (128B swizzle) and drained by TMA stores; tiles
+// are loaded through one tensor map and stored to the same rows through another
+// (the same map in place, the output buffer's map out of place).
 #pragma once
 #include "fft_common.cuh"
 #include "fft_job.cuh"
@@ -61,7 +61,8 @@ struct SmallParams {
 
 template <int R, bool SPLIT>
 __global__ void __launch_bounds__(256, SmallCfg<R, SPLIT>::kMinBlocks)
-    fft_small_kernel(const __grid_constant__ CUtensorMap tmap, const SmallParams p) {
+    fft_small_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ CUtensorMap omap,
+                     const SmallParams p) {
   using C = SmallCfg<R, SPLIT>;
   using PI = typename C::PI;
   using RHO = typename C::RHO;
@@ -76,6 +77,7 @@ __global__ void __launch_bounds__(256, SmallCfg<R, SPLIT>::kMinBlocks)
 
   if (tid == 0) {
     prefetch_tmap(&tmap);
+    prefetch_tmap(&omap);
     for (int s = 0; s < C::kStages; ++s) mbar_init(&full[s], 1);
     fence_barrier_init();
   }
@@ -307,7 +309,7 @@ __global__ void __launch_bounds__(256, SmallCfg<R, SPLIT>::kMinBlocks)
       const int tile = blockIdx.x + i * gridDim.x;
 #pragma unroll
       for (int b = 0; b < C::kBoxes; ++b)
-        tma_store_2d(&tmap, 0, tile * (C::kTE / C::kER) + b * 256, tile_base + b * C::kBoxElems * C::kES);
+        tma_store_2d(&omap, 0, tile * (C::kTE / C::kER) + b * 256, tile_base + b * C::kBoxElems * C::kES);
       bulk_commit();
       // the store issued in iteration i-1 has finished reading its stage -> reuse it
       if (i >= 1 && i - 1 + C::kStages < ntile_cta) {

@@ -29,7 +29,7 @@ struct TinyCfg {
 };
 
 template <int R, bool SPLIT>
-__global__ void __launch_bounds__(128) fft_tiny_kernel(unsigned char* data, long long batch,
+__global__ void __launch_bounds__(128) fft_tiny_kernel(const unsigned char* in, unsigned char* data, long long batch,
                                                        const float2* __restrict__ tw2048, float dsign, float oscale) {
   using C = TinyCfg<R, SPLIT>;
   constexpr int N = C::kN, ES = C::kES, ROW = C::kRow;
@@ -47,7 +47,7 @@ __global__ void __launch_bounds__(128) fft_tiny_kernel(unsigned char* data, long
   for (long long gi = (long long)blockIdx.x * C::kWarps + warp; gi < groups; gi += (long long)gridDim.x * C::kWarps) {
     const long long v0 = gi * 16;
     const int nv = batch - v0 < 16 ? (int)(batch - v0) : 16;
-    const uint4* src = reinterpret_cast<const uint4*>(data + v0 * N * ES);
+    const uint4* src = reinterpret_cast<const uint4*>(in + v0 * N * ES);
     // global -> shared (padded rows); missing transforms of the last group read as zero
     for (int i = lane; i < 16 * kVecPerRow; i += 32) {
       const int v = i / kVecPerRow, c = i - v * kVecPerRow;
@@ -78,15 +78,15 @@ __global__ void __launch_bounds__(128) fft_tiny_kernel(unsigned char* data, long
 }
 
 template <int R, bool SPLIT>
-cudaError_t launch_tiny_t(void* data, int64_t batch, const float2* tw, float dsign, int num_sms, cudaStream_t st,
-                          float oscale) {
+cudaError_t launch_tiny_t(const void* in, void* data, int64_t batch, const float2* tw, float dsign, int num_sms,
+                          cudaStream_t st, float oscale) {
   using C = TinyCfg<R, SPLIT>;
   const long long groups = (batch + 15) / 16;
   long long blocks = (groups + C::kWarps - 1) / C::kWarps;
   if (blocks > (long long)num_sms * 12) blocks = (long long)num_sms * 12;
   if (blocks < 1) blocks = 1;
-  fft_tiny_kernel<R, SPLIT><<<(unsigned)blocks, 32 * C::kWarps, 0, st>>>(static_cast<unsigned char*>(data), batch,
-                                                                        tw, dsign, oscale);
+  fft_tiny_kernel<R, SPLIT><<<(unsigned)blocks, 32 * C::kWarps, 0, st>>>(
+      static_cast<const unsigned char*>(in), static_cast<unsigned char*>(data), batch, tw, dsign, oscale);
   return cudaGetLastError();
 }
 
@@ -95,15 +95,16 @@ cudaError_t launch_tiny_t(void* data, int64_t batch, const float2* tw, float dsi
 bool tiny_supported(int64_t n, bool split) { return n == 16 || n == 32 || n == 64 || (n == 128 && !split); }
 
 cudaError_t launch_tiny(int64_t n, bool split, void* data, int64_t batch, const float2* tw, float dsign, int num_sms,
-                        cudaStream_t st, float oscale) {
+                        cudaStream_t st, float oscale, const void* in) {
+  if (!in) in = data;
   switch (n * 2 + (split ? 1 : 0)) {
-    case 32: return launch_tiny_t<1, false>(data, batch, tw, dsign, num_sms, st, oscale);
-    case 33: return launch_tiny_t<1, true>(data, batch, tw, dsign, num_sms, st, oscale);
-    case 64: return launch_tiny_t<2, false>(data, batch, tw, dsign, num_sms, st, oscale);
-    case 65: return launch_tiny_t<2, true>(data, batch, tw, dsign, num_sms, st, oscale);
-    case 128: return launch_tiny_t<4, false>(data, batch, tw, dsign, num_sms, st, oscale);
-    case 129: return launch_tiny_t<4, true>(data, batch, tw, dsign, num_sms, st, oscale);
-    case 256: return launch_tiny_t<8, false>(data, batch, tw, dsign, num_sms, st, oscale);
+    case 32: return launch_tiny_t<1, false>(in, data, batch, tw, dsign, num_sms, st, oscale);
+    case 33: return launch_tiny_t<1, true>(in, data, batch, tw, dsign, num_sms, st, oscale);
+    case 64: return launch_tiny_t<2, false>(in, data, batch, tw, dsign, num_sms, st, oscale);
+    case 65: return launch_tiny_t<2, true>(in, data, batch, tw, dsign, num_sms, st, oscale);
+    case 128: return launch_tiny_t<4, false>(in, data, batch, tw, dsign, num_sms, st, oscale);
+    case 129: return launch_tiny_t<4, true>(in, data, batch, tw, dsign, num_sms, st, oscale);
+    case 256: return launch_tiny_t<8, false>(in, data, batch, tw, dsign, num_sms, st, oscale);
     default: return cudaErrorInvalidValue;
   }
 }

@@ -98,10 +98,10 @@ CUresult encode_col_store(CUtensorMap* m, CUtensorMapDataType dt, void* base, in
 // scratch slots [S][N1 rows][N2 cols]; phase 1 reads scratch rows and writes
 // `data` transposed (X[k1 + N1 k2]).
 CUresult encode_fused1d_maps(FusedMaps* maps, const FusedKey& k, void* data, void* scratch, int64_t n1, int64_t n2,
-                             int64_t batch, int S) {
+                             int64_t batch, int S, const void* in) {
   const int es = k.split ? 8 : 4, er = 128 / es;
   const CUtensorMapDataType dt = k.split ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_UINT32;
-  CUresult r = encode_col_load(&maps->load0, dt, data, n2, batch, es, k.C0, k.R0);
+  CUresult r = encode_col_load(&maps->load0, dt, const_cast<void*>(in ? in : data), n2, batch, es, k.C0, k.R0);
   if (r != CUDA_SUCCESS) return r;
   r = encode_col_store(&maps->store0, dt, scratch, n2, S, es, k.C0, k.R0);
   if (r != CUDA_SUCCESS) return r;
@@ -530,17 +530,39 @@ bool inject_stall(tcfftPlanImpl* plan, cudaStream_t st) {
 // norm: 1 = scale every transform by 1 / (its element count).  The scale is a
 // power of two, so it is exact; each kernel folds it into a twiddle it already
 // applies (no extra pass, no extra work per element except in the tiny kernel).
-tcfftStatus exec_plan(tcfftPlan plan, void* data, void* stream, int dir, int norm) {
+// in: out of place, the input (not modified; `data` receives the output);
+// nullptr or data: in place.  The single-pass, tiny, resident, cluster,
+// two-phase 1D and composite 1D schedules read `in` directly; the others copy
+// it to `data` first.
+tcfftStatus exec_plan(tcfftPlan plan, void* data, void* stream, int dir, int norm, const void* in = nullptr) {
   if (!plan || plan->magic != tcfftPlanImpl::kMagic) return TCFFT_INVALID_PLAN;
   if (!data) return TCFFT_INVALID_VALUE;
-  if ((reinterpret_cast<uintptr_t>(data) & 127) != 0) return TCFFT_MISALIGNED;
+  if ((reinterpret_cast<uintptr_t>(data) & 127) != 0 || (reinterpret_cast<uintptr_t>(in) & 127) != 0)
+    return TCFFT_MISALIGNED;
+  if (plan->kind == 4) return TCFFT_INVALID_VALUE;  // real plans run through tcfftExecuteR2C / C2R
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  const bool split = plan->precision == TCFFT_PRECISION_SPLIT;
+  const int es = split ? 8 : 4;
+  const Schedule& s = plan->sched;
+  const void* src = in ? in : data;
+  const bool direct = plan->kind != 3 && !plan->perm_tmp &&
+                      (s.kind == Schedule::kSmall || s.kind == Schedule::kTiny || s.kind == Schedule::kResident ||
+                       s.kind == Schedule::kCluster || s.kind == Schedule::kFused1d || s.kind == Schedule::kLarge1d);
+  if (src != data && !direct) {  // schedules without a separate input: copy, then in place
+    const int64_t bytes = (plan->kind == 3 ? plan->span_elems : plan->total_elems) * es;
+    if (cuda_status(cudaMemcpyAsync(data, src, bytes, cudaMemcpyDeviceToDevice, st), "copy input")) return TCFFT_CUDA_ERROR;
+    src = data;
+  }
   if (plan->kind == 3) return exec_many(plan, data, st, dir, norm);
   const float oscale = norm ? 1.f / (float)(plan->kind == 2 ? plan->nx * plan->ny : plan->n) : 1.f;
-  const bool split = plan->precision == TCFFT_PRECISION_SPLIT;
   const float2* tw = plan->tables.tw2048[dir];
   const float dsign = dir == 0 ? 1.f : -1.f;
-  const Schedule& s = plan->sched;
+  // tensor maps name the buffers: re-encode when the (input, output) pair changes
+  const bool fresh_maps = plan->tmap_ptr != data || plan->tmap_in != src;
+  auto maps_done = [&]() {
+    plan->tmap_ptr = data;
+    plan->tmap_in = src;
+  };
   if (plan->perm_tmp) {  // reference input order: move the input to natural order first
     const int64_t nx = plan->kind == 1 ? 1 : plan->nx, ny = plan->kind == 1 ? plan->n : plan->ny;
     if (cuda_status(to_natural_order(data, plan->perm_tmp, plan->rev_x, plan->rev_y, nx, ny, plan->batch,
@@ -548,42 +570,41 @@ tcfftStatus exec_plan(tcfftPlan plan, void* data, void* stream, int dir, int nor
                     "input reorder"))
       return TCFFT_CUDA_ERROR;
   }
-  const int es = split ? 8 : 4;
   if (s.kind == Schedule::kCluster) {
-    const bool enc = plan->tmap_ptr != data;
     cudaError_t e = launch_cluster(plan->n, data, plan->batch, tw, plan->twlo[dir], plan->twhi[dir], dsign,
-                                   plan->tables.err, plan->num_sms, st, &plan->fmaps.load0, &plan->fmaps.store0, enc,
-                                   oscale);
-    if (e == cudaSuccess) plan->tmap_ptr = data;
+                                   plan->tables.err, plan->num_sms, st, &plan->fmaps.load0, &plan->fmaps.store0,
+                                   fresh_maps, oscale, src);
+    if (e == cudaSuccess) maps_done();
     return cuda_status(e, "cluster launch");
   }
   if (s.kind == Schedule::kResident) {
-    const bool enc = plan->tmap_ptr != data;
     cudaError_t e =
         split ? launch_resident_split(plan->n, data, plan->batch, tw, plan->twlo[dir], plan->twhi[dir], dsign,
-                                      plan->tables.err, plan->num_sms, st, &plan->fmaps.load0, &plan->fmaps.store0, enc,
-                                      oscale)
+                                      plan->tables.err, plan->num_sms, st, &plan->fmaps.load0, &plan->fmaps.store0,
+                                      fresh_maps, oscale, src)
               : launch_resident(plan->n, data, plan->batch, tw, plan->twlo[dir], plan->twhi[dir], dsign,
-                                plan->tables.err, plan->num_sms, st, &plan->fmaps.load0, &plan->fmaps.store0, enc,
-                                oscale);
-    if (e == cudaSuccess) plan->tmap_ptr = data;
+                                plan->tables.err, plan->num_sms, st, &plan->fmaps.load0, &plan->fmaps.store0,
+                                fresh_maps, oscale, src);
+    if (e == cudaSuccess) maps_done();
     return cuda_status(e, "resident launch");
   }
   if (s.kind == Schedule::kTiny)
-    return cuda_status(launch_tiny(plan->n, split, data, plan->batch, tw, dsign, plan->num_sms, st, oscale),
+    return cuda_status(launch_tiny(plan->n, split, data, plan->batch, tw, dsign, plan->num_sms, st, oscale, src),
                        "tiny launch");
   if (s.kind == Schedule::kLarge1d) {
     const FusedKey& k = s.key;
-    const bool fresh = plan->tmap_ptr != data;
+    const bool fresh = fresh_maps;
     if (fresh) {
       const CUtensorMapDataType dt = split ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_UINT32;
-      if (cu_status(encode_col_load(&plan->fmaps.load0, dt, data, s.N2, plan->batch, es, k.C0, k.R0), "tmap load0") ||
+      if (cu_status(encode_col_load(&plan->fmaps.load0, dt, const_cast<void*>(src), s.N2, plan->batch, es, k.C0,
+                                    k.R0),
+                    "tmap load0") ||
           cu_status(encode_col_store(&plan->fmaps.store0, dt, plan->big, s.N2, plan->batch, es, k.C0, k.R0),
                     "tmap store0"))
         return TCFFT_CUDA_ERROR;
       plan->fmaps.load1 = plan->fmaps.load0;  // phase 1 has no work items
       plan->fmaps.store1 = plan->fmaps.store0;
-      plan->tmap_ptr = data;
+      maps_done();
     }
     FusedParams fp;
     memset(&fp, 0, sizeof fp);
@@ -648,8 +669,8 @@ tcfftStatus exec_plan(tcfftPlan plan, void* data, void* stream, int dir, int nor
   if (s.kind == Schedule::kGeneric2d) {
     // an axis of 4096 runs as the resident kernel with transposed output, which
     // replaces that axis' transpose
-    const bool fresh = plan->tmap_ptr != data;
-    plan->tmap_ptr = data;
+    const bool fresh = fresh_maps;
+    maps_done();
     const int64_t nx = plan->nx, ny = plan->ny, B = plan->batch;
     if (generic2d_tout(plan, 0)) {  // rows of ny -> big = [B][ny][nx]
       const tcfftPlanImpl* rp = plan->subs[0];
@@ -677,30 +698,32 @@ tcfftStatus exec_plan(tcfftPlan plan, void* data, void* stream, int dir, int nor
   }
   if (s.kind == Schedule::kSmall) {
     // 2D view of the whole batch: rows of 128 bytes
-    const int es = split ? 8 : 4, er = 128 / es;
+    const int er = 128 / es;
     const uint64_t rows = (uint64_t)plan->total_elems / er;
-    if (plan->tmap_ptr != data) {
+    if (fresh_maps) {  // loads through tmap0 (the input), stores through tmap1 (the output)
       uint64_t dims[2] = {(uint64_t)er, rows};
       uint64_t strides[1] = {128};
       uint32_t box[2] = {(uint32_t)er, 256};
-      CUresult r = encode_tmap(&plan->tmap0, split ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_UINT32,
-                               2, data, dims, strides, box, CU_TENSOR_MAP_SWIZZLE_128B);
-      if (cu_status(r, "tmap small")) return TCFFT_CUDA_ERROR;
-      plan->tmap_ptr = data;
+      const CUtensorMapDataType dt = split ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_UINT32;
+      if (cu_status(encode_tmap(&plan->tmap0, dt, 2, const_cast<void*>(src), dims, strides, box,
+                                CU_TENSOR_MAP_SWIZZLE_128B),
+                    "tmap small") ||
+          cu_status(encode_tmap(&plan->tmap1, dt, 2, data, dims, strides, box, CU_TENSOR_MAP_SWIZZLE_128B),
+                    "tmap small"))
+        return TCFFT_CUDA_ERROR;
+      maps_done();
     }
     int launches = 0;
-    return cuda_status(launch_small(s.R, split, plan->tmap0, plan->total_elems, tw, dsign, plan->tables.err,
-                                    plan->num_sms, st, &launches, oscale));
+    return cuda_status(launch_small(s.R, split, plan->tmap0, plan->tmap1, plan->total_elems, tw, dsign,
+                                    plan->tables.err, plan->num_sms, st, &launches, oscale));
   }
   if (s.kind == Schedule::kFused1d) {
-    const int es = split ? 8 : 4, er = 128 / es;
-    const CUtensorMapDataType dt = split ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_UINT32;
-    if (plan->tmap_ptr != data) {
+    if (fresh_maps) {
       const FusedKey& k = s.key;
-      if (cu_status(encode_fused1d_maps(&plan->fmaps, k, data, plan->scratch, s.N1, s.N2, plan->batch, s.S),
+      if (cu_status(encode_fused1d_maps(&plan->fmaps, k, data, plan->scratch, s.N1, s.N2, plan->batch, s.S, src),
                     "tmap fused1d"))
         return TCFFT_CUDA_ERROR;
-      plan->tmap_ptr = data;
+      maps_done();
     }
     FusedParams fp;
     fp.tw2048 = tw;
@@ -732,11 +755,11 @@ tcfftStatus exec_plan(tcfftPlan plan, void* data, void* stream, int dir, int nor
     return cuda_status(launch_fused(s.key, plan->fmaps, fp, plan->num_sms, st, &grid), "fused launch");
   }
   if (s.kind == Schedule::kFused2d) {
-    const int es = split ? 8 : 4, er = 128 / es;
+    const int er = 128 / es;
     const CUtensorMapDataType dt = split ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_UINT32;
     const FusedKey& k = s.key;
     const int64_t nx = s.N1, ny = s.N2;
-    if (plan->tmap_ptr != data) {
+    if (fresh_maps) {
       {  // phase 0 (rows, in place): contiguous 128-byte rows, one tile per box group
         const int64_t tile_rows = (int64_t)k.C0 * ny / er;
         uint64_t dims[2] = {(uint64_t)er, (uint64_t)(plan->batch * nx * ny / er)};
@@ -753,7 +776,7 @@ tcfftStatus exec_plan(tcfftPlan plan, void* data, void* stream, int dir, int nor
       if (cu_status(encode_col_store(&plan->fmaps.store1, dt, data, ny, plan->batch, es, k.C1, k.R1),
                     "tmap2d store1"))
         return TCFFT_CUDA_ERROR;
-      plan->tmap_ptr = data;
+      maps_done();
     }
     FusedParams fp;
     memset(&fp, 0, sizeof fp);
@@ -1379,6 +1402,94 @@ tcfftStatus tcfftPlanMany(tcfftPlan* out, int64_t count, const int32_t* ranks, c
 tcfftStatus tcfftExecute(tcfftPlan plan, void* data, void* stream) {
   if (!plan || plan->magic != tcfftPlanImpl::kMagic) return TCFFT_INVALID_PLAN;
   return exec_plan(plan, data, stream, plan->direction, plan->normalize);
+}
+
+tcfftStatus tcfftExecuteOutOfPlace(tcfftPlan plan, const void* in, void* out, void* stream) {
+  if (!plan || plan->magic != tcfftPlanImpl::kMagic) return TCFFT_INVALID_PLAN;
+  if (!in || !out) return TCFFT_INVALID_VALUE;
+  return exec_plan(plan, out, stream, plan->direction, plan->normalize, in);
+}
+
+tcfftStatus tcfftPlanReal1d(tcfftPlan* out, int64_t n, int64_t batch, const tcfftOptions* opts) {
+  if (!out) return TCFFT_INVALID_VALUE;
+  *out = nullptr;
+  tcfftStatus st = validate_opts(opts);
+  if (st != TCFFT_SUCCESS) return st;
+  tcfftOptions o;
+  tcfftOptionsDefault(&o);
+  if (opts) o = *opts;
+  if (o.input_order != TCFFT_ORDER_NATURAL || o.direction != TCFFT_FORWARD) return TCFFT_INVALID_VALUE;
+  if (!is_pow2(n) || n < 32 || n > (int64_t(1) << 27) || batch < 1 || batch > (int64_t(1) << 40) / n)
+    return TCFFT_INVALID_SIZE;
+  Schedule s;
+  st = choose_1d(n / 2, batch, o.precision, s, current_num_sms());  // the half-length complex schedule
+  if (st != TCFFT_SUCCESS) return st;
+  tcfftPlanImpl* p = new (std::nothrow) tcfftPlanImpl();
+  if (!p) return TCFFT_ALLOC_FAILED;
+  p->kind = 4;
+  p->n = n;
+  p->nx = n;
+  p->ny = 1;
+  p->batch = batch;
+  p->precision = o.precision;
+  p->normalize = o.normalization;
+  p->total_elems = (n / 2) * batch;  // complex elements of the half-length transforms
+  p->sched.kind = Schedule::kNone;
+  st = alloc_tables(p);
+  if (st == TCFFT_SUCCESS) st = alloc_wn_tables(p, n);
+  tcfftOptions so;
+  tcfftOptionsDefault(&so);
+  so.precision = o.precision;
+  so.autotune = o.autotune;
+  so.tune_cache_path = o.tune_cache_path;
+  tcfftPlan sub = nullptr;
+  if (st == TCFFT_SUCCESS) st = tcfftPlan1d(&sub, n / 2, batch, &so);
+  if (st == TCFFT_SUCCESS) p->subs.push_back(sub);
+  const int es = o.precision == TCFFT_PRECISION_SPLIT ? 8 : 4;
+  if (st == TCFFT_SUCCESS) {
+    p->scratch_bytes = (n / 2) * batch * es + sub->scratch_bytes;
+    if (cudaMalloc(&p->big, (n / 2) * batch * es) != cudaSuccess) st = TCFFT_ALLOC_FAILED;
+  }
+  if (st != TCFFT_SUCCESS) {
+    free_tables(p);
+    delete p;
+    return st;
+  }
+  p->sched.launches = sub->sched.launches + 1;
+  p->sched.text = "real(" + std::string(o.precision == TCFFT_PRECISION_SPLIT ? "split" : "plain") + "): N=" +
+                  std::to_string(n) + " as complex " + sub->sched.text.substr(0, 60) + " + Hermitian split pass";
+  *out = p;
+  return TCFFT_SUCCESS;
+}
+
+tcfftStatus tcfftExecuteR2C(tcfftPlan plan, const void* in, void* out, void* stream) {
+  if (!plan || plan->magic != tcfftPlanImpl::kMagic) return TCFFT_INVALID_PLAN;
+  if (plan->kind != 4 || !in || !out) return TCFFT_INVALID_VALUE;
+  if ((reinterpret_cast<uintptr_t>(in) & 127) != 0) return TCFFT_MISALIGNED;
+  const int64_t h = plan->n / 2;
+  // the real input is the complex sequence x[2m] + i x[2m+1]: its h-point transform into the plan's buffer
+  tcfftStatus r = exec_plan(plan->subs[0], plan->big, stream, 0, 0, in);
+  if (r != TCFFT_SUCCESS) return r;
+  return cuda_status(launch_r2c_post(plan->big, out, plan->batch, h, plan->twlo[0], plan->twhi[0], plan->tw_shift,
+                                     plan->normalize ? 1.f / (float)plan->n : 1.f,
+                                     plan->precision == TCFFT_PRECISION_SPLIT, plan->num_sms,
+                                     reinterpret_cast<cudaStream_t>(stream)),
+                     "r2c split pass");
+}
+
+tcfftStatus tcfftExecuteC2R(tcfftPlan plan, const void* in, void* out, void* stream) {
+  if (!plan || plan->magic != tcfftPlanImpl::kMagic) return TCFFT_INVALID_PLAN;
+  if (plan->kind != 4 || !in || !out) return TCFFT_INVALID_VALUE;
+  if ((reinterpret_cast<uintptr_t>(out) & 127) != 0) return TCFFT_MISALIGNED;
+  const int64_t h = plan->n / 2;
+  // C2R is the inverse of R2C: it carries the 1/n unless R2C does (TCFFT_NORM_BY_N)
+  if (cuda_status(launch_c2r_pre(in, out, plan->batch, h, plan->twlo[1], plan->twhi[1], plan->tw_shift,
+                                 plan->normalize ? 1.f : 1.f / (float)plan->n,
+                                 plan->precision == TCFFT_PRECISION_SPLIT, plan->num_sms,
+                                 reinterpret_cast<cudaStream_t>(stream)),
+                  "c2r split pass"))
+    return TCFFT_CUDA_ERROR;
+  return exec_plan(plan->subs[0], out, stream, 1, 0);  // unnormalised inverse of h points
 }
 
 tcfftStatus tcfftExecuteHost(tcfftPlan plan, const void* host_in, void* host_out, void* work, void* stream) {

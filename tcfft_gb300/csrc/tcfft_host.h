@@ -41,15 +41,17 @@ cudaError_t launch_fused(const FusedKey& k, const FusedMaps& maps, const FusedPa
                          cudaStream_t st, int* grid_out);
 // false if `k` names no compiled instantiation
 bool fused_shape(const FusedKey& k, FusedShape* out);
-// Tensor maps of the 1D two-phase executor (N = n1 * n2; S scratch slots of N elements).
+// Tensor maps of the 1D two-phase executor (N = n1 * n2; S scratch slots of N elements);
+// phase 0 loads from `in` (nullptr: data), phase 1 stores to data.
 CUresult encode_fused1d_maps(FusedMaps* maps, const FusedKey& k, void* data, void* scratch, int64_t n1, int64_t n2,
-                             int64_t batch, int S);
+                             int64_t batch, int S, const void* in = nullptr);
 
 // Short 1D transforms N = 16..128 (fft_tiny.cu); N = 128 is plain only.
 bool tiny_supported(int64_t n, bool split);
 // oscale: output scale of a launch (a power of two; 1/N for a normalised transform).
+// in: the input when out of place (nullptr: in place on data)
 cudaError_t launch_tiny(int64_t n, bool split, void* data, int64_t batch, const float2* tw, float dsign, int num_sms,
-                        cudaStream_t st, float oscale = 1.f);
+                        cudaStream_t st, float oscale = 1.f, const void* in = nullptr);
 // Batched out-of-place transpose [B][R][C] -> [B][C][R] of es-byte elements (tcfft_transpose.cu).
 cudaError_t launch_transpose(const void* in, void* out, int64_t B, int64_t R, int64_t C, int es, int num_sms,
                              cudaStream_t st);
@@ -72,10 +74,12 @@ CUresult encode_col_store(CUtensorMap* m, CUtensorMapDataType dt, void* base, in
 bool resident_supported(int64_t n, bool split);
 cudaError_t launch_resident(int64_t n, void* data, int64_t batch, const float2* tw2048, const float2* twlo,
                             const float2* twhi, float dsign, int* err, int num_sms, cudaStream_t st,
-                            CUtensorMap* lm, CUtensorMap* sm, bool encode, float oscale = 1.f);
+                            CUtensorMap* lm, CUtensorMap* sm, bool encode, float oscale = 1.f,
+                            const void* in = nullptr);
 cudaError_t launch_resident_split(int64_t n, void* data, int64_t batch, const float2* tw2048, const float2* twlo,
                                   const float2* twhi, float dsign, int* err, int num_sms, cudaStream_t st,
-                                  CUtensorMap* lm, CUtensorMap* sm, bool encode, float oscale = 1.f);
+                                  CUtensorMap* lm, CUtensorMap* sm, bool encode, float oscale = 1.f,
+                                  const void* in = nullptr);
 bool resident_tout_supported(int64_t n, int64_t batch, int64_t rows);
 cudaError_t launch_resident_tout(int64_t n, const void* in, void* out, int64_t batch, int64_t rows,
                                  const float2* tw2048, const float2* twlo, const float2* twhi, float dsign, int* err,
@@ -86,13 +90,22 @@ cudaError_t launch_resident_tout(int64_t n, const void* in, void* out, int64_t b
 bool cluster_supported(int64_t n, bool split, int num_sms);
 cudaError_t launch_cluster(int64_t n, void* data, int64_t batch, const float2* tw2048, const float2* twlo,
                            const float2* twhi, float dsign, int* err, int num_sms, cudaStream_t st, CUtensorMap* lm,
-                           CUtensorMap* sm, bool encode, float oscale = 1.f);
+                           CUtensorMap* sm, bool encode, float oscale = 1.f, const void* in = nullptr);
 
 // Launch entry points implemented in the kernel translation units. Each
 // returns cudaSuccess or the launch error.
-cudaError_t launch_small(int R, bool split, const CUtensorMap& tmap, int64_t total_elems, const float2* tw,
-                         float dsign, int* err, int num_sms, cudaStream_t stream, int* launches, float oscale = 1.f);
+// tmap: tiles loaded; omap: tiles stored (the same map for an in-place transform)
+cudaError_t launch_small(int R, bool split, const CUtensorMap& tmap, const CUtensorMap& omap, int64_t total_elems,
+                         const float2* tw, float dsign, int* err, int num_sms, cudaStream_t stream, int* launches,
+                         float oscale = 1.f);
 int small_tile_elems(int R, bool split);
+
+// Real transforms of N = 2h points through complex transforms of h points (tcfft_real.cu):
+// Z [batch][h] -> Hermitian half X [batch][h + 1], and back; lo/hi: two-level W_N tables.
+cudaError_t launch_r2c_post(const void* z, void* x, int64_t batch, int64_t h, const float2* lo, const float2* hi,
+                            int shift, float scale, bool split, int num_sms, cudaStream_t st);
+cudaError_t launch_c2r_pre(const void* x, void* z, int64_t batch, int64_t h, const float2* lo, const float2* hi,
+                           int shift, float scale, bool split, int num_sms, cudaStream_t st);
 
 // Reference input-order contract (tcfft_permute.cu).
 std::vector<int> reference_radices_1d(int64_t n);

@@ -35,7 +35,7 @@ struct Schedule {
 struct tcfftPlanImpl {
   static constexpr uint32_t kMagic = 0x7cff7600u;
   uint32_t magic = kMagic;
-  int kind = 0;  // 1: 1D, 2: 2D, 3: many
+  int kind = 0;  // 1: 1D, 2: 2D, 3: many, 4: real 1D (R2C / C2R through subs[0], a complex plan of n / 2)
   int64_t n = 0, nx = 0, ny = 0, batch = 0;
   int precision = 0, input_order = 0;
   int direction = 0, normalize = 0;  // of tcfftExecute (tcfftOptions)
@@ -102,7 +102,8 @@ struct tcfftPlanImpl {
   int* rev_y = nullptr;
   void* perm_tmp = nullptr;               // natural-order staging buffer
   // tensor maps encoded for the last data pointer
-  void* tmap_ptr = nullptr;
-  CUtensorMap tmap0;
+  void* tmap_ptr = nullptr;        // output buffer the maps were encoded for
+  const void* tmap_in = nullptr;   // input buffer (== tmap_ptr in place)
+  CUtensorMap tmap0, tmap1;        // single-pass schedule: loads, stores
   tcfft::FusedMaps fmaps;
 };
