@@ -602,6 +602,7 @@ def main():
         if not args.no_sweep and "n" in size_args:
             for key, fn in (("sweep", lambda: sweep(torch, tc, args.precision)),
                             ("sweep_split", lambda: sweep(torch, tc, "split", lgs=(10, 12, 14, 16, 18, 20, 22))),
+                            ("sweep_fp32io", lambda: sweep(torch, tc, "fp32io", lgs=(10, 12, 14, 16, 18, 20, 22))),
                             ("sweep_2d", lambda: sweep_2d(torch, tc)),
                             ("uneven_batch", lambda: uneven_batch(torch, tc)),
                             ("cufft_fp16", lambda: cufft_fp16(torch, size_args, batch))):

@@ -61,7 +61,14 @@ typedef enum tcfftPrecision {
   /* fp32 complex in/out (8 bytes per element); every tensor-core product is
    * split into hi+lo fp16 pairs (hi*hi + hi*lo + lo*hi, fp32 accumulation),
    * fp32 twiddles and fp32 storage between passes. */
-  TCFFT_PRECISION_SPLIT = 1
+  TCFFT_PRECISION_SPLIT = 1,
+  /* fp32 complex in/out (8 bytes per element, e.g. complex64 tensors), fp16
+   * tensor-core operands with fp32 accumulation: the fp32 -> fp16 conversion
+   * is fused into the kernels' shared-memory reads and the results are stored
+   * from the fp32 accumulators (fp32 between passes).  Plain arithmetic on
+   * fp32 data: the schedules and HBM traffic of TCFFT_PRECISION_SPLIT, one
+   * tensor-core product per stage instead of three. */
+  TCFFT_PRECISION_FP32_IO = 2
 } tcfftPrecision;
 
 typedef enum tcfftInputOrder {

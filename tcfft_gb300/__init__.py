@@ -27,6 +27,7 @@ LIB_PATH = os.path.join(HERE, "libtcfft_gb300.so")
 
 PRECISION_PLAIN = 0
 PRECISION_SPLIT = 1
+PRECISION_FP32_IO = 2
 ORDER_NATURAL = 0
 ORDER_REFERENCE_DIGIT_REVERSED = 1
 FORWARD = 0        # sign -1 (the reference's transform)
@@ -147,7 +148,9 @@ def _precision_of(p):
         return PRECISION_PLAIN
     if p in (PRECISION_SPLIT, "split"):
         return PRECISION_SPLIT
-    raise ValueError("precision must be 'plain' or 'split', got %r" % (p,))
+    if p in (PRECISION_FP32_IO, "fp32io"):
+        return PRECISION_FP32_IO
+    raise ValueError("precision must be 'plain', 'split' or 'fp32io', got %r" % (p,))
 
 
 def _stream_handle(stream):
@@ -173,7 +176,7 @@ def _device_ptr(data, precision):
     want = (torch.float16, torch.complex32) if precision == PRECISION_PLAIN else (torch.float32, torch.complex64)
     if data.dtype not in want:
         raise TypeError("precision %s expects %s, got %s" % (
-            "plain" if precision == PRECISION_PLAIN else "split", want, data.dtype))
+            {0: "plain", 1: "split", 2: "fp32io"}[precision], want, data.dtype))
     return data.data_ptr()
 
 

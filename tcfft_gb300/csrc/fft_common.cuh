@@ -28,6 +28,9 @@ namespace tcfft {
 
 // ---------------------------------------------------------------- constants
 constexpr unsigned long long kTimeoutNs = 2000000000ull;  // every device-side wait gives up after 2 s
+// Precision modes of the kernels: fp16 data and arithmetic; fp32 data with
+// hi/lo split products; fp32 data with fp16 operands (one product per stage).
+enum KernelMode : int { kModePlain = 0, kModeSplit = 1, kModeIo32 = 2 };
 enum DeviceError : int { kDevOk = 0, kDevTimeout = 1 };
 
 __device__ __forceinline__ unsigned long long global_ns() {

@@ -354,9 +354,11 @@ __host__ __device__ constexpr int fused_sub_of(bool sub_ok, int tile_bytes, int 
 // ITEM_KB: target bytes of one work item (KiB).  64 KiB items run a ring of at
 // most 4 stages; smaller items run deeper rings (up to 8 stages), which keeps
 // more loads in flight per SM for the same shared memory.
-template <int ROLE0, int R0, int C0, int ROLE1, int R1, int C1, bool SPLIT, int ITEM_KB = 64>
+template <int ROLE0, int R0, int C0, int ROLE1, int R1, int C1, int MODE, int ITEM_KB = 64>
 struct FusedCfg {
-  static constexpr int kES = SPLIT ? 8 : 4;
+  static constexpr bool kWide = MODE != kModePlain;   // 8-byte (float2) elements
+  static constexpr bool kSplit = MODE == kModeSplit;  // three products per stage
+  static constexpr int kES = kWide ? 8 : 4;
   static constexpr int kER = 128 / kES;
   static constexpr bool k1D = ROLE1 == kRoleRowT || ROLE1 == kRoleRow16T;
   static constexpr int kLen0 = role_len(ROLE0, R0), kLen1 = role_len(ROLE1, R1);  // FFT lengths
@@ -379,11 +381,11 @@ struct FusedCfg {
   static constexpr int kLog2N = ilog2c(kLen0) + ilog2c(kLen1);
   static constexpr int kTwShift = (kLog2N + 1) / 2;          // log2 of the low table length
   static constexpr int kTwHi = 1 << (kLog2N - kTwShift);     // N >> shift
-  static constexpr bool kFold = !SPLIT;                       // plain 256R-point jobs use fft256r_jobs_fold
+  static constexpr bool kFold = !kWide;                       // plain 256R-point jobs use fft256r_jobs_fold
   // (short-row phases use the A_q part only; with R1 == R0 they share the phase-0 table,
   // whose A part comes first)
   static constexpr bool kFold1Own = kFold && R1 != R0 && R1 > 1;
-  static constexpr int kTwRBytes = (SPLIT || ROLE1 == kRoleRow16T) ? kLmax * 8 : 0;
+  static constexpr int kTwRBytes = (kWide || ROLE1 == kRoleRow16T) ? kLmax * 8 : 0;
   static constexpr int kWnBytes = k1D ? ((1 << kTwShift) + kTwHi) * 8 : 0;
   static constexpr int kFold0Bytes = kFold ? FoldTab<R0>::kBytes : 0;
   static constexpr int kFold1Bytes =
@@ -407,7 +409,7 @@ struct FusedCfg {
   static constexpr int kComputeRegs = 224;
   static constexpr int kAuxRegs = 56;
   static_assert(256 * kComputeRegs + 128 * kAuxRegs == 384 * 168, "register split must match the launch");
-  using PI = typename std::conditional<SPLIT, BitPerm<0, 1, 2, 3>, BitPerm<0, 1, 3, 2>>::type;
+  using PI = typename std::conditional<kWide, BitPerm<0, 1, 2, 3>, BitPerm<0, 1, 3, 2>>::type;
   using RHO = BitPerm<0, 2, 3, 1>;
 };
 
@@ -435,10 +437,11 @@ __device__ __forceinline__ Item decode_item(long long idx, const FusedParams& p)
   return it;
 }
 
-template <int ROLE0, int R0, int C0, int ROLE1, int R1, int C1, bool SPLIT, int ITEM_KB>
+template <int ROLE0, int R0, int C0, int ROLE1, int R1, int C1, int MODE, int ITEM_KB>
 __global__ void __launch_bounds__(384, 1)  // 12 warps at launch: 168 registers (3 warps per SM sub-partition)
     fft_fused_kernel(const __grid_constant__ FusedMaps maps, const FusedParams p) {
-  using Cfg = FusedCfg<ROLE0, R0, C0, ROLE1, R1, C1, SPLIT, ITEM_KB>;
+  using Cfg = FusedCfg<ROLE0, R0, C0, ROLE1, R1, C1, MODE, ITEM_KB>;
+  constexpr bool WIDE = Cfg::kWide, SPLIT = Cfg::kSplit;  // element width; split arithmetic
   constexpr int ES = Cfg::kES, ER = Cfg::kER, NST = Cfg::kStages;
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* smem =
@@ -472,16 +475,20 @@ __global__ void __launch_bounds__(384, 1)  // 12 warps at launch: 168 registers 
     for (int j = tid; j < (1 << Cfg::kTwShift); j += blockDim.x) s_twlo[j] = p.twlo[j];
     for (int j = tid; j < Cfg::kTwHi; j += blockDim.x) s_twhi[j] = p.twhi[j];
   }
-  // output scales: 1D puts phase 0's into its W_N factors; 2D into each phase's
-  // stage-1 twiddles (fold tables here, JobConsts::tw1 per item below)
+  // Output scales (powers of two; a normalised transform splits its 1/N between the
+  // phases, so the intermediate keeps its magnitude and never drifts into fp16's
+  // subnormal range).  2D: each phase's stage-1 twiddles (fold tables here,
+  // JobConsts::tw1 per item below).  1D: the stage-1 twiddles of both phases carry
+  // phase 1's scale and phase 0's W_N factors the ratio os0 / os1 (the short-row
+  // phase has no stage-1 twiddle: its plans pass os1 = 1).
   const float os0 = p.oscale0 != 0.f ? p.oscale0 : 1.f, os1 = p.oscale1 != 0.f ? p.oscale1 : 1.f;
+  const float wscale0 = Cfg::k1D ? os0 / os1 : 1.f;  // phase 0's W_N factors (1D)
   if constexpr (Cfg::kFold) {
     build_fold_table<R0, typename Cfg::PI, typename Cfg::RHO>(s_fold0, p.tw2048, tid, blockDim.x,
-                                                              Cfg::k1D ? 1.f : os0);
+                                                              Cfg::k1D ? os1 : os0);
     if constexpr (Cfg::kFold1Own)
       build_fold_table<R1, typename Cfg::PI, typename Cfg::RHO, ROLE1 != kRoleRow16T>(s_fold1, p.tw2048, tid,
-                                                                                       blockDim.x,
-                                                                                       Cfg::k1D ? 1.f : os1);
+                                                                                       blockDim.x, os1);
   }
   __syncthreads();
 
@@ -521,7 +528,7 @@ __global__ void __launch_bounds__(384, 1)  // 12 warps at launch: 168 registers 
 #pragma unroll 1
             for (int u = 0; u < Cfg::kSub0; ++u) {
               const int cg = (it.tile * Cfg::kSub0 + u) % p.cols0;
-              tma_load_5d(dst + u * (Cfg::kTile0 * ES), &maps.load0, cg * C0, 0, 0, 0, col_blk<SPLIT>(it.b, R0),
+              tma_load_5d(dst + u * (Cfg::kTile0 * ES), &maps.load0, cg * C0, 0, 0, 0, col_blk<WIDE>(it.b, R0),
                           &full[s]);
             }
           } else {  // contiguous rows (the item's tiles are consecutive row groups)
@@ -537,7 +544,7 @@ __global__ void __launch_bounds__(384, 1)  // 12 warps at launch: 168 registers 
 #pragma unroll 1
             for (int u = 0; u < Cfg::kSub1; ++u) {
               const int cg = (it.tile * Cfg::kSub1 + u) % p.cols1;
-              tma_load_5d(dst + u * (Cfg::kTile1 * ES), &maps.load1, cg * C1, 0, 0, 0, col_blk<SPLIT>(it.b, R1),
+              tma_load_5d(dst + u * (Cfg::kTile1 * ES), &maps.load1, cg * C1, 0, 0, 0, col_blk<WIDE>(it.b, R1),
                           &full[s]);
             }
           } else {
@@ -652,7 +659,7 @@ __global__ void __launch_bounds__(384, 1)  // 12 warps at launch: 168 registers 
   asm volatile("setmaxnreg.inc.sync.aligned.u32 %0;" ::"n"(Cfg::kComputeRegs));
   using PI = typename Cfg::PI;
   using RHO = typename Cfg::RHO;
-  using Hold = typename std::conditional<SPLIT, float2, uint32_t>::type;
+  using Hold = typename std::conditional<WIDE, float2, uint32_t>::type;
   JobConsts<SPLIT> jc;
   init_job_consts<SPLIT, PI, RHO>(jc, p.tw2048);
   const uint32_t twR = smem_addr(s_twR);
@@ -665,7 +672,11 @@ __global__ void __launch_bounds__(384, 1)  // 12 warps at launch: 168 registers 
   wn.global = p.wn_global != 0;
   wn.shift = wn.global ? p.tw_shift : Cfg::kTwShift;
   wn.nmask = (int)p.n_mask;
-  float tw1_scale = 1.f;  // 2D: the phase scale currently folded into jc.tw1
+  float tw1_scale = 1.f;  // the scale currently folded into jc.tw1
+  if constexpr (Cfg::k1D) {
+    scale_tw1(jc, os1);
+    tw1_scale = os1;
+  }
   int cnt = 0;
   for (long long idx = blockIdx.x; idx < total; idx += gridDim.x) {
     const Item it = decode_item(idx, p);
@@ -693,11 +704,11 @@ __global__ void __launch_bounds__(384, 1)  // 12 warps at launch: 168 registers 
     }
     if (ok) {
       if (it.phase == 0) {
-        if constexpr (ROLE0 == kRoleCol && !SPLIT) {
+        if constexpr (ROLE0 == kRoleCol && !WIDE) {
 #pragma unroll 1
           for (int u = 0; u < Cfg::kSub0; ++u)
             plain_col_tile<R0, C0, Cfg::k1D, PI, RHO>(jc, fold0, base + u * (Cfg::kTile0 * ES), warp, p.dsign,
-                                                      ((it.tile * Cfg::kSub0 + u) % p.cols0) * C0, wn, os0);
+                                                      ((it.tile * Cfg::kSub0 + u) % p.cols0) * C0, wn, wscale0);
         } else if constexpr (ROLE0 == kRoleCol) {
 #pragma unroll 1
          for (int u = 0; u < Cfg::kSub0; ++u) {
@@ -710,10 +721,10 @@ __global__ void __launch_bounds__(384, 1)  // 12 warps at launch: 168 registers 
           const int cg = (it.tile * Cfg::kSub0 + u) % p.cols0;
           const int col0 = JN * warp;
           auto ld = [&](int jn, int n) {
-            return lds_elem<SPLIT>(base + ctile_off<C0, ES>(col_in_row_t<SPLIT>(n), col0 + jn));
+            return lds_elem<WIDE>(base + ctile_off<C0, ES>(col_in_row_t<WIDE>(n), col0 + jn));
           };
           auto ldp = [&](int jp, int n, float2& x0, float2& x1) {
-            lds_pair<SPLIT>(base + ctile_off<C0, ES>(col_in_row_t<SPLIT>(n), col0 + jp), x0, x1);
+            lds_pair<WIDE>(base + ctile_off<C0, ES>(col_in_row_t<WIDE>(n), col0 + jp), x0, x1);
           };
           auto oaddr = [&](int jn, int k, int q) {
             return base + ctile_off<C0, ES>(col_out_row((k - q) / R0, q), col0 + jn);
@@ -727,7 +738,7 @@ __global__ void __launch_bounds__(384, 1)  // 12 warps at launch: 168 registers 
 #pragma unroll
               for (int sl = 0; sl < 8; ++sl) {
                 const float2 f = wn(n2 * R0 * jc.kval[sl >> 2][(sl >> 1) & 1][sl & 1]);
-                fk[jn][sl] = make_float2(f.x * os0, f.y * os0);
+                fk[jn][sl] = make_float2(f.x * wscale0, f.y * wscale0);
               }
 #pragma unroll
               for (int q = 0; q < R0; ++q) fq[jn][q] = wn(n2 * q);
@@ -736,23 +747,23 @@ __global__ void __launch_bounds__(384, 1)  // 12 warps at launch: 168 registers 
               auto st = [&](int jp, int k, int q, int sl, float2 v0, float2 v1) {
                 v0 = cmul(v0, cmul(fk[jp][sl], fq[jp][q]));
                 v1 = cmul(v1, cmul(fk[jp + 1][sl], fq[jp + 1][q]));
-                sts_pair<SPLIT>(oaddr(jp, k, q), v0, v1);
+                sts_pair<WIDE>(oaddr(jp, k, q), v0, v1);
               };
               fft256r_jobs<R0, SPLIT, TWS, JN, true>(jc, twR, p.dsign, ldp, st);
             } else {
               auto st = [&](int jn, int k, int q, int sl, float2 v) {
-                sts_elem<SPLIT>(oaddr(jn, k, q), cmul(v, cmul(fk[jn][sl], fq[jn][q])));
+                sts_elem<WIDE>(oaddr(jn, k, q), cmul(v, cmul(fk[jn][sl], fq[jn][q])));
               };
               fft256r_jobs<R0, SPLIT, TWS, JN>(jc, twR, p.dsign, ld, st);
             }
           } else {
             if constexpr (PAIR) {
               auto st = [&](int jp, int k, int q, int, float2 v0, float2 v1) {
-                sts_pair<SPLIT>(oaddr(jp, k, q), v0, v1);
+                sts_pair<WIDE>(oaddr(jp, k, q), v0, v1);
               };
               fft256r_jobs<R0, SPLIT, TWS, JN, true>(jc, twR, p.dsign, ldp, st);
             } else {
-              auto st = [&](int jn, int k, int q, int, float2 v) { sts_elem<SPLIT>(oaddr(jn, k, q), v); };
+              auto st = [&](int jn, int k, int q, int, float2 v) { sts_elem<WIDE>(oaddr(jn, k, q), v); };
               fft256r_jobs<R0, SPLIT, TWS, JN>(jc, twR, p.dsign, ld, st);
             }
           }
@@ -763,11 +774,11 @@ __global__ void __launch_bounds__(384, 1)  // 12 warps at launch: 168 registers 
           const uint32_t base = smem_addr(smem + s * Cfg::kStageBytes) + u * (Cfg::kTile0 * ES);
           constexpr int JN = C0 / 8;
           auto rowb = [&](int jn) { return base + (uint32_t)((warp + 8 * jn) * 256 * R0 * ES); };
-          auto ld = [&](int jn, int n) { return lds_elem<SPLIT>(rowb(jn) + swz_w<ES>(n) * ES); };
+          auto ld = [&](int jn, int n) { return lds_elem<WIDE>(rowb(jn) + swz_w<ES>(n) * ES); };
           // outputs k = q + R0 k' of one slot are R0 consecutive elements: hold all q, then
           // store each slot's run with vector stores (conflict-free, like the single-pass kernel)
           Hold out[JN][R0][8];
-          if constexpr (!SPLIT) {
+          if constexpr (!WIDE) {
             plain_row_jobs<R0, JN, PI, RHO>(jc, fold0, rowb(0), 8 * 256 * R0 * ES, p.dsign, out);
           } else {
             auto st = [&](int jn, int k, int q, int sl, float2 v) { out[jn][q][sl] = v; };
@@ -779,7 +790,7 @@ __global__ void __launch_bounds__(384, 1)  // 12 warps at launch: 168 registers 
             for (int sl = 0; sl < 8; ++sl) {
               const uint32_t rb = rowb(jn);
               const int k0 = R0 * jc.kval[sl >> 2][(sl >> 1) & 1][sl & 1];
-              if constexpr (!SPLIT) {
+              if constexpr (!WIDE) {
                 if constexpr (R0 == 1) sts32(rb + swz_w<4>(k0) * 4, out[jn][0][sl]);
                 else if constexpr (R0 == 2) sts64(rb + swz_w<4>(k0) * 4, out[jn][0][sl], out[jn][1][sl]);
                 else {
@@ -800,7 +811,7 @@ __global__ void __launch_bounds__(384, 1)  // 12 warps at launch: 168 registers 
          }
         }
       } else {
-        if constexpr (ROLE1 == kRoleCol && !SPLIT) {
+        if constexpr (ROLE1 == kRoleCol && !WIDE) {
 #pragma unroll 1
           for (int u = 0; u < Cfg::kSub1; ++u)
             plain_col_tile<R1, C1, false, PI, RHO>(jc, fold1, base + u * (Cfg::kTile1 * ES), warp, p.dsign, 0, wn);
@@ -816,17 +827,17 @@ __global__ void __launch_bounds__(384, 1)  // 12 warps at launch: 168 registers 
           };
           if constexpr (JN % 2 == 0) {
             auto ldp = [&](int jp, int n, float2& x0, float2& x1) {
-              lds_pair<SPLIT>(base + ctile_off<C1, ES>(col_in_row_t<SPLIT>(n), col0 + jp), x0, x1);
+              lds_pair<WIDE>(base + ctile_off<C1, ES>(col_in_row_t<WIDE>(n), col0 + jp), x0, x1);
             };
             auto st = [&](int jp, int k, int q, int, float2 v0, float2 v1) {
-              sts_pair<SPLIT>(oaddr(jp, k, q), v0, v1);
+              sts_pair<WIDE>(oaddr(jp, k, q), v0, v1);
             };
             fft256r_jobs<R1, SPLIT, TWS, JN, true>(jc, twR, p.dsign, ldp, st);
           } else {
             auto ld = [&](int jn, int n) {
-              return lds_elem<SPLIT>(base + ctile_off<C1, ES>(col_in_row_t<SPLIT>(n), col0 + jn));
+              return lds_elem<WIDE>(base + ctile_off<C1, ES>(col_in_row_t<WIDE>(n), col0 + jn));
             };
-            auto st = [&](int jn, int k, int q, int, float2 v) { sts_elem<SPLIT>(oaddr(jn, k, q), v); };
+            auto st = [&](int jn, int k, int q, int, float2 v) { sts_elem<WIDE>(oaddr(jn, k, q), v); };
             fft256r_jobs<R1, SPLIT, TWS, JN>(jc, twR, p.dsign, ld, st);
           }
          }
@@ -837,12 +848,12 @@ __global__ void __launch_bounds__(384, 1)  // 12 warps at launch: 168 registers 
           Hold out[8 * R1];
           {
             const uint32_t rb = base + (uint32_t)(warp * 16 * Cfg::kLen1 * ES);
-            auto ld = [&](int v, int n) { return lds_elem<SPLIT>(rb + swz_w<ES>(v * Cfg::kLen1 + n) * ES); };
+            auto ld = [&](int v, int n) { return lds_elem<WIDE>(rb + swz_w<ES>(v * Cfg::kLen1 + n) * ES); };
             auto st = [&](int v, int k, int q, int sl, float2 val) {
-              if constexpr (SPLIT) out[8 * q + sl] = val;
+              if constexpr (WIDE) out[8 * q + sl] = val;
               else out[8 * q + sl] = pack_h2(val.x, val.y);
             };
-            if constexpr (SPLIT) {
+            if constexpr (WIDE) {
               fft16r_job<R1, SPLIT, Cfg::kLmax / (16 * R1), PI, RHO>(jc, twR, p.dsign, ld, st);
             } else {
               auto ldr = [&](int v, int n) { return lds32(rb + swz_w<4>(v * Cfg::kLen1 + n) * 4); };
@@ -861,7 +872,7 @@ __global__ void __launch_bounds__(384, 1)  // 12 warps at launch: 168 registers 
                 const int row = RHO::apply(lane_g + 8 * h) + 16 * q;
                 const uint32_t addr = base + (uint32_t)((col / Cfg::kBW) * (Cfg::kBW * Cfg::kLen1 * ES)) +
                                       ctile_off<Cfg::kBW, ES>(row, col % Cfg::kBW);
-                if constexpr (SPLIT) sts64f(addr, out[8 * q + sl]);
+                if constexpr (WIDE) sts64f(addr, out[8 * q + sl]);
                 else sts32(addr, out[8 * q + sl]);
               }
           }
@@ -875,10 +886,10 @@ __global__ void __launch_bounds__(384, 1)  // 12 warps at launch: 168 registers 
          for (int u = 0; u < Cfg::kSub1; ++u) {       // the item's tiles, one after the other
           const uint32_t base = smem_addr(smem + s * Cfg::kStageBytes) + u * (Cfg::kTile1 * ES);
           Hold out[JN][R1][8];
-          if constexpr (!SPLIT) {
+          if constexpr (!WIDE) {
             plain_row_jobs<R1, JN, PI, RHO>(jc, fold1, base + row0 * kRow, kRow, p.dsign, out);
           } else {
-            auto ld = [&](int jn, int n) { return lds_elem<SPLIT>(base + (row0 + jn) * kRow + swz_w<ES>(n) * ES); };
+            auto ld = [&](int jn, int n) { return lds_elem<WIDE>(base + (row0 + jn) * kRow + swz_w<ES>(n) * ES); };
             auto st = [&](int jn, int k, int q, int sl, float2 v) { out[jn][q][sl] = v; };
             fft256r_jobs<R1, SPLIT, Cfg::kLmax / (256 * R1), JN>(jc, twR, p.dsign, ld, st);
           }
@@ -888,20 +899,20 @@ __global__ void __launch_bounds__(384, 1)  // 12 warps at launch: 168 registers 
             const uint32_t so = base + ctile_off<C1, ES>(col_out_row(slot_kval<PI, RHO>(sl), 0), row0);
 #pragma unroll
             for (int q = 0; q < R1; ++q) {
-              if constexpr (!SPLIT && JN == 4) {  // 128-byte rows: one 16-byte store per slot
+              if constexpr (!WIDE && JN == 4) {  // 128-byte rows: one 16-byte store per slot
                 sts128(so + q * kStep, out[0][q][sl], out[1][q][sl], out[2][q][sl], out[3][q][sl]);
               } else if constexpr (JN % 2 == 0) {
 #pragma unroll
                 for (int jp = 0; jp < JN; jp += 2) {
                   const uint32_t addr = so + jp * ES + q * kStep;
-                  if constexpr (SPLIT) sts128f(addr, out[jp][q][sl], out[jp + 1][q][sl]);
+                  if constexpr (WIDE) sts128f(addr, out[jp][q][sl], out[jp + 1][q][sl]);
                   else sts64(addr, out[jp][q][sl], out[jp + 1][q][sl]);
                 }
               } else {
 #pragma unroll
                 for (int jn = 0; jn < JN; ++jn) {
                   const uint32_t addr = so + jn * ES + q * kStep;
-                  if constexpr (SPLIT) sts64f(addr, out[jn][q][sl]);
+                  if constexpr (WIDE) sts64f(addr, out[jn][q][sl]);
                   else sts32(addr, out[jn][q][sl]);
                 }
               }

@@ -10,11 +10,17 @@ cudaError_t launch_fused_2d_plain(const FusedKey&, const FusedMaps*, const Fused
                                   FusedShape*, bool*);
 cudaError_t launch_fused_2d_split(const FusedKey&, const FusedMaps*, const FusedParams*, int, cudaStream_t, int*,
                                   FusedShape*, bool*);
+cudaError_t launch_fused_io32(const FusedKey&, const FusedMaps*, const FusedParams*, int, cudaStream_t, int*,
+                              FusedShape*, bool*);
 
 namespace {
 // Routes `k` to its translation unit: launches, or with `shape` set only reports the ring shape.
 cudaError_t route(const FusedKey& k, const FusedMaps* maps, const FusedParams* p, int num_sms, cudaStream_t st,
                   int* grid_out, FusedShape* shape, bool* handled) {
+  if (k.split && k.io32) {
+    cudaError_t e = launch_fused_io32(k, maps, p, num_sms, st, grid_out, shape, handled);
+    return *handled ? e : cudaErrorNotSupported;
+  }
   cudaError_t e = launch_fused_1d(k, maps, p, num_sms, st, grid_out, shape, handled);
   if (*handled) return e;
   e = k.split ? launch_fused_2d_split(k, maps, p, num_sms, st, grid_out, shape, handled)

@@ -10,10 +10,10 @@
 
 namespace tcfft {
 
-template <int ROLE0, int R0, int C0, int ROLE1, int R1, int C1, bool SPLIT, int ITEM_KB>
+template <int ROLE0, int R0, int C0, int ROLE1, int R1, int C1, int MODE, int ITEM_KB>
 cudaError_t fused_launch_or_query(const FusedMaps* maps, const FusedParams* p, int num_sms, cudaStream_t st,
                                   int* grid_out, FusedShape* shape) {
-  using Cfg = FusedCfg<ROLE0, R0, C0, ROLE1, R1, C1, SPLIT, ITEM_KB>;
+  using Cfg = FusedCfg<ROLE0, R0, C0, ROLE1, R1, C1, MODE, ITEM_KB>;
   if (shape) {
     shape->stages = Cfg::kStages;
     shape->sub0 = Cfg::kSub0;
@@ -21,7 +21,7 @@ cudaError_t fused_launch_or_query(const FusedMaps* maps, const FusedParams* p, i
     shape->smem = Cfg::kSmem;
     return cudaSuccess;
   }
-  auto kern = fft_fused_kernel<ROLE0, R0, C0, ROLE1, R1, C1, SPLIT, ITEM_KB>;
+  auto kern = fft_fused_kernel<ROLE0, R0, C0, ROLE1, R1, C1, MODE, ITEM_KB>;
   static std::once_flag once;
   static cudaError_t init_err = cudaSuccess;
   std::call_once(once, [&] {
@@ -43,11 +43,13 @@ cudaError_t fused_launch_or_query(const FusedMaps* maps, const FusedParams* p, i
 
 }  // namespace tcfft
 
-// One instantiation: roles, radices and tile widths of both phases, precision,
-// work-item size in KiB.
+// One instantiation: roles, radices and tile widths of both phases, precision
+// (false: plain, true: split; kModeIo32 in fft_fused_io32.cu), work-item size in KiB.
 #define TCFFT_FUSED_CASE(RO0, RR0, CC0, RO1, RR1, CC1, SP, KB)                                                  \
+  TCFFT_FUSED_CASE_MODE(RO0, RR0, CC0, RO1, RR1, CC1, ((SP) ? kModeSplit : kModePlain), KB)
+#define TCFFT_FUSED_CASE_MODE(RO0, RR0, CC0, RO1, RR1, CC1, MM, KB)                                             \
   if (k.role0 == RO0 && k.R0 == RR0 && k.C0 == CC0 && k.role1 == RO1 && k.R1 == RR1 && k.C1 == CC1 &&        \
-      k.split == SP && k.item_kb == KB) {                                                                    \
+      fused_mode(k) == (MM) && k.item_kb == KB) {                                                            \
     *handled = true;                                                                                          \
-    return fused_launch_or_query<RO0, RR0, CC0, RO1, RR1, CC1, SP, KB>(maps, p, num_sms, st, grid_out, shape); \
+    return fused_launch_or_query<RO0, RR0, CC0, RO1, RR1, CC1, (MM), KB>(maps, p, num_sms, st, grid_out, shape); \
   }

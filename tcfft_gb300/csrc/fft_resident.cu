@@ -299,7 +299,7 @@ struct ResSplitCfg {
   static_assert(kT >= 1 && kT * kN * kES == kStageBytes, "a stage holds whole transforms");
 };
 
-template <int R1>
+template <int R1, bool SPLIT>  // SPLIT: three products per stage; else fp16 operands (fp32-I/O mode)
 __global__ void __launch_bounds__(384, 1) fft_resident_split_kernel(const __grid_constant__ CUtensorMap load_map,
                                                                      const __grid_constant__ CUtensorMap store_map,
                                                                      const ResParams p) {
@@ -378,8 +378,8 @@ __global__ void __launch_bounds__(384, 1) fft_resident_split_kernel(const __grid
 
   // ------------------------------------------------------------------ compute warps
   asm volatile("setmaxnreg.inc.sync.aligned.u32 %0;" ::"n"(224));
-  JobConsts<true> jc;
-  init_job_consts<true, PI, RHO>(jc, p.tw2048);
+  JobConsts<SPLIT> jc;
+  init_job_consts<SPLIT, PI, RHO>(jc, p.tw2048);
   const uint32_t tw16 = smem_addr(s_tw16);
   WnTable wn;
   wn.hi = smem_addr(s_twhi);
@@ -419,7 +419,7 @@ __global__ void __launch_bounds__(384, 1) fft_resident_split_kernel(const __grid
           sts_pair<true>(tb + ctile_off<C, ES>(col_out_row(k, 0), col0 + jp), cmul(v0, fk[jp][sl]),
                          cmul(v1, fk[jp + 1][sl]));
         };
-        fft256r_jobs<1, true, 1, JN, true>(jc, tw16, p.dsign, ldp, st);
+        fft256r_jobs<1, SPLIT, 1, JN, true>(jc, tw16, p.dsign, ldp, st);
       }
       named_bar_sync(1, 256);
       // phase 1: 16 rows k1 per job, FFT over n2 (length 16 R1); jobs j = warp + 8 i
@@ -434,7 +434,7 @@ __global__ void __launch_bounds__(384, 1) fft_resident_split_kernel(const __grid
                                 ctile_off<C, ES>(col_out_row(k1base + v, 0), n % C));
         };
         auto st = [&](int, int, int q, int slot, float2 val) { out[i][8 * q + slot] = val; };
-        fft16r_job<R1, true, 1, PI, RHO>(jc, tw16, p.dsign, ld, st);
+        fft16r_job<R1, SPLIT, 1, PI, RHO>(jc, tw16, p.dsign, ld, st);
       }
       named_bar_sync(1, 256);  // every warp has read the stage
       // natural order X[k1 + 256 k2] of transform t at element t N + k1 + 256 k2 (128B-swizzled rows)
@@ -459,11 +459,11 @@ __global__ void __launch_bounds__(384, 1) fft_resident_split_kernel(const __grid
   }
 }
 
-template <int R1>
+template <int R1, bool SPLIT>
 cudaError_t launch_resident_split_t(const CUtensorMap& lm, const CUtensorMap& sm, const ResParams& p, int num_sms,
                                     cudaStream_t st) {
   using Cfg = ResSplitCfg<R1>;
-  auto kern = fft_resident_split_kernel<R1>;
+  auto kern = fft_resident_split_kernel<R1, SPLIT>;
   static std::once_flag once;
   static cudaError_t init_err = cudaSuccess;
   std::call_once(once, [&] { init_err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg::kSmem); });
@@ -501,7 +501,8 @@ bool resident_supported(int64_t n, bool split) {
 // k2 bits 0..L-1), L = log2(N2 / 16), matching the stage layout above.
 cudaError_t launch_resident_split(int64_t n, void* data, int64_t batch, const float2* tw2048, const float2* twlo,
                                   const float2* twhi, float dsign, int* err, int num_sms, cudaStream_t st,
-                                  CUtensorMap* lm, CUtensorMap* sm, bool encode, float oscale, const void* in) {
+                                  CUtensorMap* lm, CUtensorMap* sm, bool encode, float oscale, const void* in,
+                                  bool io32) {
   const int64_t n2 = n / 256;
   if (encode) {
     void* src = const_cast<void*>(in ? in : data);  // loads from the input, stores to data
@@ -524,8 +525,10 @@ cudaError_t launch_resident_split(int64_t n, void* data, int64_t batch, const fl
   p.dsign = dsign;
   p.oscale = oscale;
   switch (n) {
-    case 4096: return launch_resident_split_t<1>(*lm, *sm, p, num_sms, st);
-    case 8192: return launch_resident_split_t<2>(*lm, *sm, p, num_sms, st);
+    case 4096: return io32 ? launch_resident_split_t<1, false>(*lm, *sm, p, num_sms, st)
+                           : launch_resident_split_t<1, true>(*lm, *sm, p, num_sms, st);
+    case 8192: return io32 ? launch_resident_split_t<2, false>(*lm, *sm, p, num_sms, st)
+                           : launch_resident_split_t<2, true>(*lm, *sm, p, num_sms, st);
     default: return cudaErrorInvalidValue;
   }
 }

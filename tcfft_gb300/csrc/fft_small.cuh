@@ -23,28 +23,33 @@
 
 namespace tcfft {
 
-template <int R, bool SPLIT>
+// MODE: kModePlain (fp16 data and arithmetic), kModeSplit (fp32 data, hi/lo
+// split products), kModeIo32 (fp32 data converted to fp16 operands as they are
+// read from shared memory, fp32 results stored: one product per stage).
+template <int R, int MODE>
 struct SmallCfg {
+  static constexpr bool kWide = MODE != kModePlain;      // 8-byte (float2) elements
+  static constexpr bool kSplit = MODE == kModeSplit;     // three products per stage
   static constexpr int kN = 256 * R;
-  static constexpr int kES = SPLIT ? 8 : 4;              // bytes per complex element
+  static constexpr int kES = kWide ? 8 : 4;              // bytes per complex element
   static constexpr int kER = 128 / kES;                  // elements per 128-byte row
   static constexpr int kBoxElems = kER * 256;            // one TMA box: 256 rows
-  static constexpr int kJPW = SPLIT ? (R >= 2 ? 1 : 2) : (R >= 4 ? 1 : 4 / R);  // jobs per warp
+  static constexpr int kJPW = kWide ? (R >= 2 ? 1 : 2) : (R >= 4 ? 1 : 4 / R);  // jobs per warp
   static constexpr int kTE = 8 * kJPW * kN;              // elements per tile
   static constexpr int kBoxes = kTE / kBoxElems;
   static constexpr int kTileBytes = kTE * kES;
   static constexpr int kStages = 3;
   // split: W_N^j table (radix-R twiddles); plain: the folded radix-R tables (per-q DFT
   // matrices and stage-1 twiddles, fft256r_jobs_fold) in place of it
-  static constexpr bool kFold = !SPLIT && R > 1;
+  static constexpr bool kFold = !kWide && R > 1;
   static constexpr int kTabBytes = kFold ? FoldTab<R>::kBytes : (R > 1 ? kN * 8 : 0);
   static constexpr int kSmem = kStages * kTileBytes + kTabBytes + 1024 + 64;
   static constexpr int kMinBlocks = (kSmem <= 112 * 1024) ? 2 : 1;
   static_assert(kTE % kBoxElems == 0, "tile must be whole TMA boxes");
   // bank-conflict-free slot permutations (see fft_common.cuh)
-  using PI = typename std::conditional<SPLIT, BitPerm<0, 1, 2, 3>, BitPerm<0, 1, 3, 2>>::type;
+  using PI = typename std::conditional<kWide, BitPerm<0, 1, 2, 3>, BitPerm<0, 1, 3, 2>>::type;
   using RHO = typename std::conditional<
-      SPLIT,
+      kWide,
       typename std::conditional<R == 1, BitPerm<1, 0, 3, 2>, BitPerm<0, 2, 3, 1>>::type,
       typename std::conditional<R == 1, BitPerm<2, 0, 1, 3>,
                                 typename std::conditional<R == 2, BitPerm<1, 0, 3, 2>, BitPerm<0, 2, 3, 1>>::type>::type>::type;
@@ -59,11 +64,12 @@ struct SmallParams {
                      // by the stage-1 twiddles, so it costs nothing per element
 };
 
-template <int R, bool SPLIT>
-__global__ void __launch_bounds__(256, SmallCfg<R, SPLIT>::kMinBlocks)
+template <int R, int MODE>
+__global__ void __launch_bounds__(256, SmallCfg<R, MODE>::kMinBlocks)
     fft_small_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ CUtensorMap omap,
                      const SmallParams p) {
-  using C = SmallCfg<R, SPLIT>;
+  using C = SmallCfg<R, MODE>;
+  constexpr bool WIDE = C::kWide, SPLIT = C::kSplit;
   using PI = typename C::PI;
   using RHO = typename C::RHO;
   extern __shared__ __align__(1024) unsigned char smem_raw[];
@@ -185,14 +191,14 @@ __global__ void __launch_bounds__(256, SmallCfg<R, SPLIT>::kMinBlocks)
         for (int r = 0; r < 2; ++r)
 #pragma unroll
           for (int j = 0; j < 2; ++j) {
-            if constexpr (!SPLIT && R == 1) {
+            if constexpr (!WIDE && R == 1) {
               bhi[0][kt][r][j] = lds32(job + in_off[kt][r][j] * 4);
             } else {
               float2 x[R];
 #pragma unroll
               for (int a = 0; a < R; ++a) {
                 const uint32_t addr = job + (uint32_t)(a * 256 + in_off[kt][r][j]) * C::kES;
-                if constexpr (SPLIT) x[a] = lds64f(addr);
+                if constexpr (WIDE) x[a] = lds64f(addr);
                 else x[a] = unpack_h2(lds32(addr));
               }
               if constexpr (R > 1) {
@@ -236,7 +242,7 @@ __global__ void __launch_bounds__(256, SmallCfg<R, SPLIT>::kMinBlocks)
       __syncwarp();  // all lanes finished reading this job's region (in-place)
 
       // ---------------- two radix-16 tensor-core stages per tile q
-      float2 res[R][2][2][2];  // SPLIT: fp32 results; PLAIN: packed half2 in .x bits
+      float2 res[R][2][2][2];  // wide: fp32 results; plain: packed half2 in .x bits
 #pragma unroll
       for (int q = 0; q < R; ++q) {
         float acc[2][2][4];
@@ -263,6 +269,7 @@ __global__ void __launch_bounds__(256, SmallCfg<R, SPLIT>::kMinBlocks)
             for (int hh = 0; hh < 2; ++hh) {
               const float2 v = acc_get(acc, h, hh, e);
               if constexpr (SPLIT) res[q][h][e][hh] = make_float2(v.x * inv, v.y * inv);
+              else if constexpr (WIDE) res[q][h][e][hh] = v;
               else res[q][h][e][hh].x = __uint_as_float(pack_h2(v.x, v.y));
             }
       }
@@ -274,7 +281,7 @@ __global__ void __launch_bounds__(256, SmallCfg<R, SPLIT>::kMinBlocks)
 #pragma unroll
           for (int hh = 0; hh < 2; ++hh) {
             const uint32_t base = job + out_off[h][e][hh] * C::kES;
-            if constexpr (!SPLIT) {
+            if constexpr (!WIDE) {
               if constexpr (R == 1) sts32(base, __float_as_uint(res[0][h][e][hh].x));
               else if constexpr (R == 2)
                 sts64(base, __float_as_uint(res[0][h][e][hh].x), __float_as_uint(res[1][h][e][hh].x));

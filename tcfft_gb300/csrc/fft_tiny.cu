@@ -16,22 +16,24 @@
 namespace tcfft {
 namespace {
 
-template <int R, bool SPLIT>
+template <int R, int MODE>
 struct TinyCfg {
+  static constexpr bool kWide = MODE != kModePlain, kSplit = MODE == kModeSplit;
   static constexpr int kN = 16 * R;
-  static constexpr int kES = SPLIT ? 8 : 4;
+  static constexpr int kES = kWide ? 8 : 4;
   static constexpr int kPad = 16 / kES;      // elements of padding per row
   static constexpr int kRow = kN + kPad;     // padded row length (elements)
   static constexpr int kWarps = 4;
   static constexpr int kWarpBytes = 16 * kRow * kES;
-  using PI = typename std::conditional<SPLIT, BitPerm<0, 1, 2, 3>, BitPerm<0, 1, 3, 2>>::type;
+  using PI = typename std::conditional<kWide, BitPerm<0, 1, 2, 3>, BitPerm<0, 1, 3, 2>>::type;
   using RHO = BitPerm<0, 2, 3, 1>;
 };
 
-template <int R, bool SPLIT>
+template <int R, int MODE>
 __global__ void __launch_bounds__(128) fft_tiny_kernel(const unsigned char* in, unsigned char* data, long long batch,
                                                        const float2* __restrict__ tw2048, float dsign, float oscale) {
-  using C = TinyCfg<R, SPLIT>;
+  using C = TinyCfg<R, MODE>;
+  constexpr bool WIDE = C::kWide, SPLIT = C::kSplit;
   constexpr int N = C::kN, ES = C::kES, ROW = C::kRow;
   __shared__ __align__(16) unsigned char buf[C::kWarps][C::kWarpBytes];
   __shared__ float2 tw[N];  // W_N^j
@@ -57,13 +59,13 @@ __global__ void __launch_bounds__(128) fft_tiny_kernel(const unsigned char* in, 
     __syncwarp();
     auto ld = [&](int v, int n) {
       const uint32_t a = wb + (uint32_t)((v * ROW + n) * ES);
-      if constexpr (SPLIT) return lds64f(a);
+      if constexpr (WIDE) return lds64f(a);
       else return unpack_h2(lds32(a));
     };
     auto st = [&](int v, int k, int, int, float2 val) {
       const uint32_t a = wb + (uint32_t)((v * ROW + k) * ES);
       val = make_float2(val.x * oscale, val.y * oscale);  // output scale (1 unless normalised)
-      if constexpr (SPLIT) sts64f(a, val);
+      if constexpr (WIDE) sts64f(a, val);
       else sts32(a, pack_h2(val.x, val.y));
     };
     fft16r_job<R, SPLIT, 1, typename C::PI, typename C::RHO>(jc, tw_addr, dsign, ld, st);
@@ -77,36 +79,42 @@ __global__ void __launch_bounds__(128) fft_tiny_kernel(const unsigned char* in, 
   }
 }
 
-template <int R, bool SPLIT>
+template <int R, int MODE>
 cudaError_t launch_tiny_t(const void* in, void* data, int64_t batch, const float2* tw, float dsign, int num_sms,
                           cudaStream_t st, float oscale) {
-  using C = TinyCfg<R, SPLIT>;
+  using C = TinyCfg<R, MODE>;
   const long long groups = (batch + 15) / 16;
   long long blocks = (groups + C::kWarps - 1) / C::kWarps;
   if (blocks > (long long)num_sms * 12) blocks = (long long)num_sms * 12;
   if (blocks < 1) blocks = 1;
-  fft_tiny_kernel<R, SPLIT><<<(unsigned)blocks, 32 * C::kWarps, 0, st>>>(
+  fft_tiny_kernel<R, MODE><<<(unsigned)blocks, 32 * C::kWarps, 0, st>>>(
       static_cast<const unsigned char*>(in), static_cast<unsigned char*>(data), batch, tw, dsign, oscale);
   return cudaGetLastError();
 }
 
 }  // namespace
 
-bool tiny_supported(int64_t n, bool split) { return n == 16 || n == 32 || n == 64 || (n == 128 && !split); }
+bool tiny_supported(int64_t n, int mode) { return n == 16 || n == 32 || n == 64 || (n == 128 && mode == kModePlain); }
 
-cudaError_t launch_tiny(int64_t n, bool split, void* data, int64_t batch, const float2* tw, float dsign, int num_sms,
+cudaError_t launch_tiny(int64_t n, int mode, void* data, int64_t batch, const float2* tw, float dsign, int num_sms,
                         cudaStream_t st, float oscale, const void* in) {
   if (!in) in = data;
-  switch (n * 2 + (split ? 1 : 0)) {
-    case 32: return launch_tiny_t<1, false>(in, data, batch, tw, dsign, num_sms, st, oscale);
-    case 33: return launch_tiny_t<1, true>(in, data, batch, tw, dsign, num_sms, st, oscale);
-    case 64: return launch_tiny_t<2, false>(in, data, batch, tw, dsign, num_sms, st, oscale);
-    case 65: return launch_tiny_t<2, true>(in, data, batch, tw, dsign, num_sms, st, oscale);
-    case 128: return launch_tiny_t<4, false>(in, data, batch, tw, dsign, num_sms, st, oscale);
-    case 129: return launch_tiny_t<4, true>(in, data, batch, tw, dsign, num_sms, st, oscale);
-    case 256: return launch_tiny_t<8, false>(in, data, batch, tw, dsign, num_sms, st, oscale);
+#define TCFFT_TINY(NN, RR, MM) \
+  case NN * 4 + MM: return launch_tiny_t<RR, MM>(in, data, batch, tw, dsign, num_sms, st, oscale);
+  switch (n * 4 + mode) {
+    TCFFT_TINY(16, 1, kModePlain)
+    TCFFT_TINY(16, 1, kModeSplit)
+    TCFFT_TINY(16, 1, kModeIo32)
+    TCFFT_TINY(32, 2, kModePlain)
+    TCFFT_TINY(32, 2, kModeSplit)
+    TCFFT_TINY(32, 2, kModeIo32)
+    TCFFT_TINY(64, 4, kModePlain)
+    TCFFT_TINY(64, 4, kModeSplit)
+    TCFFT_TINY(64, 4, kModeIo32)
+    TCFFT_TINY(128, 8, kModePlain)
     default: return cudaErrorInvalidValue;
   }
+#undef TCFFT_TINY
 }
 
 }  // namespace tcfft

@@ -240,6 +240,11 @@ void free_tables(tcfftPlanImpl* p) {
   p->host_fork = nullptr;
 }
 
+// Name of a precision in schedule descriptions.
+const char* prec_name(int precision) {
+  return precision == TCFFT_PRECISION_SPLIT ? "split" : (precision == TCFFT_PRECISION_FP32_IO ? "fp32io" : "plain");
+}
+
 // SM count of the current device (152 on GB300 when it cannot be queried).
 int current_num_sms() {
   int dev = 0, n = 0;
@@ -297,16 +302,19 @@ int item_kb_1d(int lg, bool split) {
 tcfftStatus choose_1d(int64_t n, int64_t batch, int precision, Schedule& s, int num_sms = 152) {
   if (!is_pow2(n) || n < 16 || n > (int64_t(1) << 27)) return TCFFT_INVALID_SIZE;
   if (batch < 1 || batch > (int64_t(1) << 40) / n) return TCFFT_INVALID_SIZE;
-  const bool split = precision == TCFFT_PRECISION_SPLIT;
+  // split and fp32-I/O share the 8-byte-element schedules; they differ in arithmetic only
+  const bool split = precision != TCFFT_PRECISION_PLAIN;
+  const bool io32 = precision == TCFFT_PRECISION_FP32_IO;
+  const char* pname = prec_name(precision);
   s = Schedule();
   char buf[160];
   if (n < 256) {
-    if (!tiny_supported(n, split)) return TCFFT_NOT_SUPPORTED;
+    if (!tiny_supported(n, precision)) return TCFFT_NOT_SUPPORTED;
     s.kind = Schedule::kTiny;
     s.R = (int)(n / 16);
     s.launches = 1;
     snprintf(buf, sizeof buf, "tiny(N=%lld,%s): 16 transforms per warp, 1 mma stage + radix-%d", (long long)n,
-             split ? "split" : "plain", s.R);
+             pname, s.R);
     s.text = buf;
     return TCFFT_SUCCESS;
   }
@@ -314,7 +322,7 @@ tcfftStatus choose_1d(int64_t n, int64_t batch, int precision, Schedule& s, int 
     s.kind = Schedule::kSmall;
     s.R = (int)(n / 256);
     s.launches = 1;
-    snprintf(buf, sizeof buf, "small(R=%d,%s): 1 pass, 2 mma stages + radix-%d", s.R, split ? "split" : "plain", s.R);
+    snprintf(buf, sizeof buf, "small(R=%d,%s): 1 pass, 2 mma stages + radix-%d", s.R, pname, s.R);
     s.text = buf;
     return TCFFT_SUCCESS;
   }
@@ -326,7 +334,7 @@ tcfftStatus choose_1d(int64_t n, int64_t batch, int precision, Schedule& s, int 
     s.N1 = n / 64;
     s.N2 = 64;
     s.launches = 5;
-    snprintf(buf, sizeof buf, "fourstep(split): N=%lld x 64, two sub-plans, 3 transposes (one with the twiddle)",
+    snprintf(buf, sizeof buf, "fourstep(%s): N=%lld x 64, two sub-plans, 3 transposes (one with the twiddle)", pname,
              (long long)s.N1);
     s.text = buf;
     return TCFFT_SUCCESS;
@@ -337,7 +345,7 @@ tcfftStatus choose_1d(int64_t n, int64_t batch, int precision, Schedule& s, int 
     s.N2 = n / 256;
     s.launches = 1;
     snprintf(buf, sizeof buf, "resident(%s): N=256 x %lld, whole transforms in shared memory, one HBM pass",
-             split ? "split" : "plain", (long long)s.N2);
+             pname, (long long)s.N2);
     s.text = buf;
     return TCFFT_SUCCESS;
   }
@@ -355,6 +363,7 @@ tcfftStatus choose_1d(int64_t n, int64_t batch, int precision, Schedule& s, int 
     k.R1 = (int)(n / n1 / 16);
     k.C1 = 128;
     k.split = split;
+    k.io32 = io32;
     if (split && k.R1 > 4) return TCFFT_NOT_SUPPORTED;
     s.kind = Schedule::kFused1d;
     s.N1 = n1;
@@ -365,7 +374,7 @@ tcfftStatus choose_1d(int64_t n, int64_t batch, int precision, Schedule& s, int 
     fused_lag(s.T0, s.T1, batch, s, &k, num_sms);
     s.launches = 1;
     snprintf(buf, sizeof buf, "fused1d(%s): N=%lld x %lld, phase0 columns R=%d C=%d, phase1 16-row groups R=%d, lag %d, %d slots",
-             split ? "split" : "plain", (long long)s.N1, (long long)s.N2, k.R0, k.C0, k.R1, s.D, s.S);
+             pname, (long long)s.N1, (long long)s.N2, k.R0, k.C0, k.R1, s.D, s.S);
     s.text = buf;
     return TCFFT_SUCCESS;
   }
@@ -382,6 +391,7 @@ tcfftStatus choose_1d(int64_t n, int64_t batch, int precision, Schedule& s, int 
     k.role1 = kRoleRowT;
     k.R1 = (int)(n2 / 256);
     k.split = split;
+    k.io32 = io32;
     for (int ikb : {item_kb_1d(lg, split), 64}) {  // the preferred item size, else 64 KiB items
       k.item_kb = ikb;
       k.C0 = fused_cols(k.R0, split, ikb * 1024);
@@ -400,7 +410,7 @@ tcfftStatus choose_1d(int64_t n, int64_t batch, int precision, Schedule& s, int 
     s.launches = 1;
     snprintf(buf, sizeof buf,
              "fused1d(%s): N=%lld x %lld, phase0 columns R=%d C=%d, phase1 rows R=%d C=%d, %d KiB items, lag %d, %d slots",
-             split ? "split" : "plain", (long long)n1, (long long)n2, k.R0, k.C0, k.R1, k.C1, k.item_kb, s.D, s.S);
+             pname, (long long)n1, (long long)n2, k.R0, k.C0, k.R1, k.C1, k.item_kb, s.D, s.S);
     s.text = buf;
     return TCFFT_SUCCESS;
   }
@@ -419,6 +429,7 @@ tcfftStatus choose_1d(int64_t n, int64_t batch, int precision, Schedule& s, int 
     k.R1 = k.R0;
     k.C1 = k.C0;
     k.split = split;
+    k.io32 = io32;
     s.kind = Schedule::kLarge1d;
     s.N1 = n1;
     s.N2 = n2;
@@ -429,7 +440,7 @@ tcfftStatus choose_1d(int64_t n, int64_t batch, int precision, Schedule& s, int 
     s.S = (int)batch;
     s.launches = 3;  // updated with the sub-plan's count at plan time
     snprintf(buf, sizeof buf, "large1d(%s): N=%lld x %lld, column pass R=%d C=%d -> rows of %lld (sub-plan) -> transpose",
-             split ? "split" : "plain", (long long)n1, (long long)n2, k.R0, k.C0, (long long)n2);
+             pname, (long long)n1, (long long)n2, k.R0, k.C0, (long long)n2);
     s.text = buf;
     return TCFFT_SUCCESS;
   }
@@ -440,7 +451,8 @@ tcfftStatus choose_1d(int64_t n, int64_t batch, int precision, Schedule& s, int 
 tcfftStatus choose_2d(int64_t nx, int64_t ny, int64_t batch, int precision, Schedule& s, int num_sms = 152) {
   if (!is_pow2(nx) || !is_pow2(ny) || nx < 256 || ny < 256 || nx > 2048 || ny > 2048) return TCFFT_INVALID_SIZE;
   if (batch < 1 || batch > (int64_t(1) << 40) / (nx * ny)) return TCFFT_INVALID_SIZE;
-  const bool split = precision == TCFFT_PRECISION_SPLIT;
+  const bool split = precision != TCFFT_PRECISION_PLAIN;  // 8-byte elements
+  const char* pname = prec_name(precision);
   const int es = split ? 8 : 4;
   s = Schedule();
   FusedKey k;
@@ -452,6 +464,7 @@ tcfftStatus choose_2d(int64_t nx, int64_t ny, int64_t batch, int precision, Sche
   k.C1 = fused_cols(k.R1, split);
   if (getenv("TCFFT_FUSED_C")) k.C0 = k.C1 = atoi(getenv("TCFFT_FUSED_C"));
   k.split = split;
+  k.io32 = precision == TCFFT_PRECISION_FP32_IO;
   if (k.C1 == 0 || k.C0 * 256 * k.R0 * es > 64 * 1024 || (split && (k.R0 > 4 || k.R1 > 4))) return TCFFT_NOT_SUPPORTED;
   s.kind = Schedule::kFused2d;
   s.N1 = nx;
@@ -463,14 +476,14 @@ tcfftStatus choose_2d(int64_t nx, int64_t ny, int64_t batch, int precision, Sche
   s.launches = 1;
   char buf[160];
   snprintf(buf, sizeof buf, "fused2d(%s): %lld x %lld, phase0 rows R=%d C=%d, phase1 columns R=%d C=%d, lag %d",
-           split ? "split" : "plain", (long long)nx, (long long)ny, k.R0, k.C0, k.R1, k.C1, s.D);
+           pname, (long long)nx, (long long)ny, k.R0, k.C0, k.R1, k.C1, s.D);
   s.text = buf;
   return TCFFT_SUCCESS;
 }
 
 // Device tables for the reference input order; chains must be supported by the reference.
 tcfftStatus setup_reference_order(tcfftPlanImpl* p) {
-  const int es = p->precision == TCFFT_PRECISION_SPLIT ? 8 : 4;
+  const int es = p->precision != TCFFT_PRECISION_PLAIN ? 8 : 4;
   auto upload = [&](const std::vector<int>& h, int** d) -> tcfftStatus {
     if (cudaMalloc(d, h.size() * sizeof(int)) != cudaSuccess) return TCFFT_ALLOC_FAILED;
     if (cudaMemcpy(*d, h.data(), h.size() * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess)
@@ -490,7 +503,9 @@ tcfftStatus setup_reference_order(tcfftPlanImpl* p) {
 
 tcfftStatus validate_opts(const tcfftOptions* o) {
   if (!o) return TCFFT_SUCCESS;
-  if (o->precision != TCFFT_PRECISION_PLAIN && o->precision != TCFFT_PRECISION_SPLIT) return TCFFT_INVALID_VALUE;
+  if (o->precision != TCFFT_PRECISION_PLAIN && o->precision != TCFFT_PRECISION_SPLIT &&
+      o->precision != TCFFT_PRECISION_FP32_IO)
+    return TCFFT_INVALID_VALUE;
   if (o->input_order != TCFFT_ORDER_NATURAL && o->input_order != TCFFT_ORDER_REFERENCE_DIGIT_REVERSED)
     return TCFFT_INVALID_VALUE;
   if (o->direction != TCFFT_FORWARD && o->direction != TCFFT_INVERSE) return TCFFT_INVALID_VALUE;
@@ -541,7 +556,8 @@ tcfftStatus exec_plan(tcfftPlan plan, void* data, void* stream, int dir, int nor
     return TCFFT_MISALIGNED;
   if (plan->kind == 4) return TCFFT_INVALID_VALUE;  // real plans run through tcfftExecuteR2C / C2R
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
-  const bool split = plan->precision == TCFFT_PRECISION_SPLIT;
+  const bool split = plan->precision != TCFFT_PRECISION_PLAIN;  // 8-byte elements (split or fp32 I/O)
+  const int mode = plan->precision;                             // kernel mode: kModePlain/Split/Io32
   const int es = split ? 8 : 4;
   const Schedule& s = plan->sched;
   const void* src = in ? in : data;
@@ -581,7 +597,7 @@ tcfftStatus exec_plan(tcfftPlan plan, void* data, void* stream, int dir, int nor
     cudaError_t e =
         split ? launch_resident_split(plan->n, data, plan->batch, tw, plan->twlo[dir], plan->twhi[dir], dsign,
                                       plan->tables.err, plan->num_sms, st, &plan->fmaps.load0, &plan->fmaps.store0,
-                                      fresh_maps, oscale, src)
+                                      fresh_maps, oscale, src, mode == TCFFT_PRECISION_FP32_IO)
               : launch_resident(plan->n, data, plan->batch, tw, plan->twlo[dir], plan->twhi[dir], dsign,
                                 plan->tables.err, plan->num_sms, st, &plan->fmaps.load0, &plan->fmaps.store0,
                                 fresh_maps, oscale, src);
@@ -589,7 +605,7 @@ tcfftStatus exec_plan(tcfftPlan plan, void* data, void* stream, int dir, int nor
     return cuda_status(e, "resident launch");
   }
   if (s.kind == Schedule::kTiny)
-    return cuda_status(launch_tiny(plan->n, split, data, plan->batch, tw, dsign, plan->num_sms, st, oscale, src),
+    return cuda_status(launch_tiny(plan->n, mode, data, plan->batch, tw, dsign, plan->num_sms, st, oscale, src),
                        "tiny launch");
   if (s.kind == Schedule::kLarge1d) {
     const FusedKey& k = s.key;
@@ -629,7 +645,7 @@ tcfftStatus exec_plan(tcfftPlan plan, void* data, void* stream, int dir, int nor
     fp.err = plan->tables.err;
     fp.dsign = dsign;
     fp.wait_ns = plan->wait_ns;
-    fp.oscale0 = oscale;  // the column pass's W_N factors carry the whole scale
+    fp.oscale0 = norm ? 1.f / (float)s.N1 : 1.f;  // the column pass scales by 1/N1, the rows by 1/N2
     fp.oscale1 = 1.f;
     if (cuda_status(cudaMemsetAsync(plan->counters, 0, sizeof(int) * 2 * s.S, st), "counter reset"))
       return TCFFT_CUDA_ERROR;
@@ -640,10 +656,11 @@ tcfftStatus exec_plan(tcfftPlan plan, void* data, void* stream, int dir, int nor
       const tcfftPlanImpl* rp = plan->subs[0];
       return cuda_status(launch_resident_tout(4096, plan->big, data, s.N1 * plan->batch, s.N1, tw, rp->twlo[dir],
                                               rp->twhi[dir], dsign, plan->tables.err, plan->num_sms, st,
-                                              &plan->fmaps.load1, &plan->fmaps.store1, fresh),
+                                              &plan->fmaps.load1, &plan->fmaps.store1, fresh,
+                                              norm ? 1.f / 4096 : 1.f),
                          "rows (transposed output)");
     }
-    tcfftStatus r = exec_plan(plan->subs[0], plan->big, stream, dir, 0);  // rows of N2, natural order
+    tcfftStatus r = exec_plan(plan->subs[0], plan->big, stream, dir, norm);  // rows of N2 (scaled by 1/N2)
     if (r != TCFFT_SUCCESS) return r;
     // [B][N1 rows k1][N2 cols k2] -> X[k1 + N1 k2] = [B][N2][N1]
     return cuda_status(launch_transpose(plan->big, data, plan->batch, s.N1, s.N2, es, plan->num_sms, st), "transpose");
@@ -714,7 +731,7 @@ tcfftStatus exec_plan(tcfftPlan plan, void* data, void* stream, int dir, int nor
       maps_done();
     }
     int launches = 0;
-    return cuda_status(launch_small(s.R, split, plan->tmap0, plan->tmap1, plan->total_elems, tw, dsign,
+    return cuda_status(launch_small(s.R, mode, plan->tmap0, plan->tmap1, plan->total_elems, tw, dsign,
                                     plan->tables.err, plan->num_sms, st, &launches, oscale));
   }
   if (s.kind == Schedule::kFused1d) {
@@ -746,8 +763,10 @@ tcfftStatus exec_plan(tcfftPlan plan, void* data, void* stream, int dir, int nor
     fp.err = plan->tables.err;
     fp.dsign = dsign;
     fp.wait_ns = plan->wait_ns;
-    fp.oscale0 = oscale;  // phase 0's W_N factors carry the whole scale
-    fp.oscale1 = 1.f;
+    // 1/N split as 1/N1 (columns) and 1/N2 (rows); the short-row phase takes no scale
+    const bool short_rows = s.key.role1 == kRoleRow16T;
+    fp.oscale0 = norm ? (short_rows ? oscale : 1.f / (float)s.N1) : 1.f;
+    fp.oscale1 = norm && !short_rows ? 1.f / (float)s.N2 : 1.f;
     if (cuda_status(cudaMemsetAsync(plan->counters, 0, sizeof(int) * 2 * s.S, st), "counter reset") ||
         inject_stall(plan, st))
       return TCFFT_CUDA_ERROR;
@@ -835,7 +854,7 @@ tcfftStatus alloc_wn_tables(tcfftPlanImpl* p, int64_t n) {
 // Counters and (1D) scratch ring for the current schedule's slot count.
 tcfftStatus alloc_ring(tcfftPlanImpl* p) {
   const Schedule& s = p->sched;
-  const int es = p->precision == TCFFT_PRECISION_SPLIT ? 8 : 4;
+  const int es = p->precision != TCFFT_PRECISION_PLAIN ? 8 : 4;
   if (p->counters) cudaFree(p->counters);
   if (p->scratch) cudaFree(p->scratch);
   p->counters = nullptr;
@@ -862,7 +881,7 @@ tcfftStatus alloc_fused(tcfftPlanImpl* p) {
 // tables for N (read from global memory by the column pass) and the row plan.
 tcfftStatus setup_large1d(tcfftPlanImpl* p) {
   const Schedule& s = p->sched;
-  const int es = p->precision == TCFFT_PRECISION_SPLIT ? 8 : 4;
+  const int es = p->precision != TCFFT_PRECISION_PLAIN ? 8 : 4;
   if (cudaMalloc(&p->counters, sizeof(int) * 2 * s.S) != cudaSuccess) return TCFFT_ALLOC_FAILED;
   tcfftStatus st = alloc_wn_tables(p, p->n);
   if (st != TCFFT_SUCCESS) return st;
@@ -888,7 +907,7 @@ tcfftStatus setup_large1d(tcfftPlanImpl* p) {
 // intermediate.
 tcfftStatus setup_fourstep(tcfftPlanImpl* p) {
   const Schedule& s = p->sched;
-  const int es = p->precision == TCFFT_PRECISION_SPLIT ? 8 : 4;
+  const int es = p->precision != TCFFT_PRECISION_PLAIN ? 8 : 4;
   p->scratch_bytes = p->n * p->batch * es;
   if (cudaMalloc(&p->big, p->scratch_bytes) != cudaSuccess) return TCFFT_ALLOC_FAILED;
   tcfftOptions o;
@@ -908,7 +927,7 @@ tcfftStatus setup_fourstep(tcfftPlanImpl* p) {
 // Generic 2D: row plan over ny, column plan over nx (run on the transpose), one
 // full-size intermediate.
 tcfftStatus setup_generic2d(tcfftPlanImpl* p) {
-  const int es = p->precision == TCFFT_PRECISION_SPLIT ? 8 : 4;
+  const int es = p->precision != TCFFT_PRECISION_PLAIN ? 8 : 4;
   p->scratch_bytes = p->nx * p->ny * p->batch * es;
   if (cudaMalloc(&p->big, p->scratch_bytes) != cudaSuccess) return TCFFT_ALLOC_FAILED;
   tcfftOptions o;
@@ -988,7 +1007,7 @@ tcfftStatus autotune_plan(tcfftPlanImpl* p, const tcfftOptions& o) {
   if (it != g_tune_cache.end()) {
     best = it->second;
   } else {
-    const int es = p->precision == TCFFT_PRECISION_SPLIT ? 8 : 4;
+    const int es = p->precision != TCFFT_PRECISION_PLAIN ? 8 : 4;
     void* tmp = nullptr;
     if (cudaMalloc(&tmp, p->total_elems * es) != cudaSuccess) {
       cudaGetLastError();
@@ -1058,7 +1077,7 @@ tcfftStatus check_errors(tcfftPlanImpl* p) {
 }
 
 tcfftStatus exec_many(tcfftPlanImpl* plan, void* data, cudaStream_t st, int dir, int norm) {
-  const int es = plan->precision == TCFFT_PRECISION_SPLIT ? 8 : 4;
+  const int es = plan->precision != TCFFT_PRECISION_PLAIN ? 8 : 4;
   const int g = 2 * dir + norm;  // one captured graph per direction and normalisation
   if (!plan->graph_exec[g] || plan->graph_ptr[g] != data) {
     if (plan->graph_exec[g]) cudaGraphExecDestroy(plan->graph_exec[g]);
@@ -1142,7 +1161,9 @@ tcfftStatus tcfftOptionsDefault(tcfftOptions* o) {
 
 tcfftStatus tcfftDescribe1d(int64_t n, int64_t batch, int32_t precision, char* buf, size_t len) {
   if (!buf || len == 0) return TCFFT_INVALID_VALUE;
-  if (precision != TCFFT_PRECISION_PLAIN && precision != TCFFT_PRECISION_SPLIT) return TCFFT_INVALID_VALUE;
+  if (precision != TCFFT_PRECISION_PLAIN && precision != TCFFT_PRECISION_SPLIT &&
+      precision != TCFFT_PRECISION_FP32_IO)
+    return TCFFT_INVALID_VALUE;
   Schedule s;
   tcfftStatus st = choose_1d(n, batch, precision, s);
   if (st != TCFFT_SUCCESS) return st;
@@ -1183,7 +1204,7 @@ tcfftStatus tcfftPlan1d(tcfftPlan* out, int64_t n, int64_t batch, const tcfftOpt
   st = alloc_tables(p);
   const char* cl_env = getenv("TCFFT_CLUSTER");
   if (st == TCFFT_SUCCESS && s.kind == Schedule::kFused1d && cl_env && atoi(cl_env) != 0 &&
-      cluster_supported(n, o.precision == TCFFT_PRECISION_SPLIT, p->num_sms)) {
+      cluster_supported(n, o.precision != TCFFT_PRECISION_PLAIN, p->num_sms)) {
     // opt-in: clusters of N / 2^14 CTAs, one transform per cluster, no L2 round trip.  Correct at
     // N = 2^15..2^18 but slower than the two-phase kernel above 2^15 (remote shared-memory loads
     // and the cluster-wide barrier between the phases), so the planner does not pick it by itself.
@@ -1237,7 +1258,7 @@ tcfftStatus tcfftPlan2d(tcfftPlan* out, int64_t nx, int64_t ny, int64_t batch, c
     s.N2 = ny;
     char buf[160];
     snprintf(buf, sizeof buf, "generic2d(%s): rows of %lld, transpose, rows of %lld, transpose",
-             o.precision == TCFFT_PRECISION_SPLIT ? "split" : "plain", (long long)ny, (long long)nx);
+             prec_name(o.precision), (long long)ny, (long long)nx);
     s.text = buf;
   }
   std::vector<int> cx = {(int)nx}, cy = {(int)ny};
@@ -1285,7 +1306,7 @@ tcfftStatus tcfftPlanMany(tcfftPlan* out, int64_t count, const int32_t* ranks, c
   tcfftOptionsDefault(&o);
   if (opts) o = *opts;
   if (o.input_order != TCFFT_ORDER_NATURAL) return TCFFT_INVALID_VALUE;
-  const int es = o.precision == TCFFT_PRECISION_SPLIT ? 8 : 4;
+  const int es = o.precision != TCFFT_PRECISION_PLAIN ? 8 : 4;
   std::vector<int64_t> size(count);
   for (int64_t i = 0; i < count; ++i) {
     if (ranks[i] != 1 && ranks[i] != 2) return TCFFT_INVALID_VALUE;
@@ -1392,7 +1413,7 @@ tcfftStatus tcfftPlanMany(tcfftPlan* out, int64_t count, const int32_t* ranks, c
   p->sched.launches = launches;
   char buf[160];
   snprintf(buf, sizeof buf, "many(%s): %lld transforms in %d runs (%d gathered), %d sub-plans, %d launches per graph replay",
-           o.precision == TCFFT_PRECISION_SPLIT ? "split" : "plain", (long long)count, (int)p->runs.size(), p->mv_n,
+           prec_name(o.precision), (long long)count, (int)p->runs.size(), p->mv_n,
            nsub, launches);
   p->sched.text = buf;
   *out = p;
@@ -1445,7 +1466,7 @@ tcfftStatus tcfftPlanReal1d(tcfftPlan* out, int64_t n, int64_t batch, const tcff
   tcfftPlan sub = nullptr;
   if (st == TCFFT_SUCCESS) st = tcfftPlan1d(&sub, n / 2, batch, &so);
   if (st == TCFFT_SUCCESS) p->subs.push_back(sub);
-  const int es = o.precision == TCFFT_PRECISION_SPLIT ? 8 : 4;
+  const int es = o.precision != TCFFT_PRECISION_PLAIN ? 8 : 4;
   if (st == TCFFT_SUCCESS) {
     p->scratch_bytes = (n / 2) * batch * es + sub->scratch_bytes;
     if (cudaMalloc(&p->big, (n / 2) * batch * es) != cudaSuccess) st = TCFFT_ALLOC_FAILED;
@@ -1456,7 +1477,7 @@ tcfftStatus tcfftPlanReal1d(tcfftPlan* out, int64_t n, int64_t batch, const tcff
     return st;
   }
   p->sched.launches = sub->sched.launches + 1;
-  p->sched.text = "real(" + std::string(o.precision == TCFFT_PRECISION_SPLIT ? "split" : "plain") + "): N=" +
+  p->sched.text = "real(" + std::string(prec_name(o.precision)) + "): N=" +
                   std::to_string(n) + " as complex " + sub->sched.text.substr(0, 60) + " + Hermitian split pass";
   *out = p;
   return TCFFT_SUCCESS;
@@ -1472,7 +1493,7 @@ tcfftStatus tcfftExecuteR2C(tcfftPlan plan, const void* in, void* out, void* str
   if (r != TCFFT_SUCCESS) return r;
   return cuda_status(launch_r2c_post(plan->big, out, plan->batch, h, plan->twlo[0], plan->twhi[0], plan->tw_shift,
                                      plan->normalize ? 1.f / (float)plan->n : 1.f,
-                                     plan->precision == TCFFT_PRECISION_SPLIT, plan->num_sms,
+                                     plan->precision != TCFFT_PRECISION_PLAIN, plan->num_sms,
                                      reinterpret_cast<cudaStream_t>(stream)),
                      "r2c split pass");
 }
@@ -1485,7 +1506,7 @@ tcfftStatus tcfftExecuteC2R(tcfftPlan plan, const void* in, void* out, void* str
   // C2R is the inverse of R2C: it carries the 1/n unless R2C does (TCFFT_NORM_BY_N)
   if (cuda_status(launch_c2r_pre(in, out, plan->batch, h, plan->twlo[1], plan->twhi[1], plan->tw_shift,
                                  plan->normalize ? 1.f : 1.f / (float)plan->n,
-                                 plan->precision == TCFFT_PRECISION_SPLIT, plan->num_sms,
+                                 plan->precision != TCFFT_PRECISION_PLAIN, plan->num_sms,
                                  reinterpret_cast<cudaStream_t>(stream)),
                   "c2r split pass"))
     return TCFFT_CUDA_ERROR;
@@ -1497,7 +1518,7 @@ tcfftStatus tcfftExecuteHost(tcfftPlan plan, const void* host_in, void* host_out
   if (!host_in || !host_out || !work) return TCFFT_INVALID_VALUE;
   if ((reinterpret_cast<uintptr_t>(work) & 127) != 0) return TCFFT_MISALIGNED;
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
-  const int64_t es = plan->precision == TCFFT_PRECISION_SPLIT ? 8 : 4;
+  const int64_t es = plan->precision != TCFFT_PRECISION_PLAIN ? 8 : 4;
   const int64_t per = plan->kind == 2 ? plan->nx * plan->ny : plan->n;  // elements per transform
   const int64_t total = (plan->kind == 3 ? plan->span_elems : plan->total_elems) * es;
   const int K = plan->kind == 3 ? 1 : (int)std::min<int64_t>(tcfftPlanImpl::kHostChunks, plan->batch);
@@ -1618,7 +1639,7 @@ tcfftStatus tcfftGetPlanInfo(tcfftPlan plan, tcfftPlanInfo* info) {
   if (!info) return TCFFT_INVALID_VALUE;
   memset(info, 0, sizeof(*info));
   info->total_elements = plan->total_elems;
-  info->element_bytes = plan->precision == TCFFT_PRECISION_SPLIT ? 8 : 4;
+  info->element_bytes = plan->precision != TCFFT_PRECISION_PLAIN ? 8 : 4;
   info->launches_per_exec = plan->sched.launches;
   info->scratch_bytes = plan->scratch_bytes;
   info->n_radices = (int)plan->radices_x.size();

@@ -29,9 +29,12 @@ struct FusedParams;
 // Identifies one instantiation of the two-phase executor (fft_fused.cuh).
 struct FusedKey {
   int role0 = 0, R0 = 1, C0 = 16, role1 = 0, R1 = 1, C1 = 16;
-  bool split = false;
-  int item_kb = 64;  // work-item size target (KiB): 64 (rings of <= 4 stages) or 32 (<= 8 stages)
+  bool split = false;  // 8-byte (float2) elements
+  bool io32 = false;   // with split: one fp16 product per stage (fp32 I/O mode) instead of three
+  int item_kb = 64;    // work-item size target (KiB): 64 (rings of <= 4 stages) or 32 (<= 8 stages)
 };
+// kModePlain / kModeSplit / kModeIo32 of a key (fft_common.cuh)
+inline int fused_mode(const FusedKey& k) { return k.split ? (k.io32 ? 2 : 1) : 0; }
 // Ring shape of one instantiation: stages, tiles per work item in each phase, dynamic shared memory.
 struct FusedShape {
   int stages = 0, sub0 = 1, sub1 = 1, smem = 0;
@@ -46,11 +49,12 @@ bool fused_shape(const FusedKey& k, FusedShape* out);
 CUresult encode_fused1d_maps(FusedMaps* maps, const FusedKey& k, void* data, void* scratch, int64_t n1, int64_t n2,
                              int64_t batch, int S, const void* in = nullptr);
 
-// Short 1D transforms N = 16..128 (fft_tiny.cu); N = 128 is plain only.
-bool tiny_supported(int64_t n, bool split);
+// Short 1D transforms N = 16..128 (fft_tiny.cu); N = 128 is plain only.  mode: kModePlain,
+// kModeSplit, kModeIo32 (fft_common.cuh).
+bool tiny_supported(int64_t n, int mode);
 // oscale: output scale of a launch (a power of two; 1/N for a normalised transform).
 // in: the input when out of place (nullptr: in place on data)
-cudaError_t launch_tiny(int64_t n, bool split, void* data, int64_t batch, const float2* tw, float dsign, int num_sms,
+cudaError_t launch_tiny(int64_t n, int mode, void* data, int64_t batch, const float2* tw, float dsign, int num_sms,
                         cudaStream_t st, float oscale = 1.f, const void* in = nullptr);
 // Batched out-of-place transpose [B][R][C] -> [B][C][R] of es-byte elements (tcfft_transpose.cu).
 cudaError_t launch_transpose(const void* in, void* out, int64_t B, int64_t R, int64_t C, int es, int num_sms,
@@ -76,10 +80,11 @@ cudaError_t launch_resident(int64_t n, void* data, int64_t batch, const float2* 
                             const float2* twhi, float dsign, int* err, int num_sms, cudaStream_t st,
                             CUtensorMap* lm, CUtensorMap* sm, bool encode, float oscale = 1.f,
                             const void* in = nullptr);
+// fp32 data (8-byte elements): split products, or with io32 one fp16 product per stage
 cudaError_t launch_resident_split(int64_t n, void* data, int64_t batch, const float2* tw2048, const float2* twlo,
                                   const float2* twhi, float dsign, int* err, int num_sms, cudaStream_t st,
                                   CUtensorMap* lm, CUtensorMap* sm, bool encode, float oscale = 1.f,
-                                  const void* in = nullptr);
+                                  const void* in = nullptr, bool io32 = false);
 bool resident_tout_supported(int64_t n, int64_t batch, int64_t rows);
 cudaError_t launch_resident_tout(int64_t n, const void* in, void* out, int64_t batch, int64_t rows,
                                  const float2* tw2048, const float2* twlo, const float2* twhi, float dsign, int* err,
@@ -95,10 +100,10 @@ cudaError_t launch_cluster(int64_t n, void* data, int64_t batch, const float2* t
 // Launch entry points implemented in the kernel translation units. Each
 // returns cudaSuccess or the launch error.
 // tmap: tiles loaded; omap: tiles stored (the same map for an in-place transform)
-cudaError_t launch_small(int R, bool split, const CUtensorMap& tmap, const CUtensorMap& omap, int64_t total_elems,
+cudaError_t launch_small(int R, int mode, const CUtensorMap& tmap, const CUtensorMap& omap, int64_t total_elems,
                          const float2* tw, float dsign, int* err, int num_sms, cudaStream_t stream, int* launches,
                          float oscale = 1.f);
-int small_tile_elems(int R, bool split);
+int small_tile_elems(int R, int mode);
 
 // Real transforms of N = 2h points through complex transforms of h points (tcfft_real.cu):
 // Z [batch][h] -> Hermitian half X [batch][h + 1], and back; lo/hi: two-level W_N tables.
