@@ -352,9 +352,10 @@ def sweep_2d(torch, tc):
     return out
 
 
-def uneven_batch(torch, tc):
+def uneven_batch(torch, tc, graph=False):
     """The uneven-batch workload: 512 1D transforms of 2^8..2^16 and 64 2D transforms
-    of 2^7..2^10 per axis (seed 2), back to back in one buffer, one plan, graph-replayed."""
+    of 2^7..2^10 per axis (seed 2), back to back in one buffer, one plan: the persistent
+    many-shape passes, or (graph=True) the per-shape sub-plans replayed as one CUDA graph."""
     import numpy as np
     rng = np.random.default_rng(2)
     shapes = [(1 << int(e),) for e in rng.integers(8, 17, size=512)]
@@ -364,9 +365,14 @@ def uneven_batch(torch, tc):
     flops = sum(5.0 * int(np.prod(sh)) * math.log2(int(np.prod(sh))) for sh in shapes)
     x = torch.empty((elems, 2), dtype=torch.float16, device="cuda").uniform_(-1, 1)
     peak, _ = measured_peak()
-    with tc.Plan.many(shapes) as p:
-        sec = time_device(torch, p, x, 20, 3) / 20
-        info = p.info
+    if graph:
+        os.environ["TCFFT_MANY_GRAPH"] = "1"
+    try:
+        with tc.Plan.many(shapes) as p:
+            sec = time_device(torch, p, x, 20, 3) / 20
+            info = p.info
+    finally:
+        os.environ.pop("TCFFT_MANY_GRAPH", None)
     return {"transforms": len(shapes), "elements": elems, "us": round(sec * 1e6, 1),
             "gflops": round(flops / sec / 1e9, 1), "hbm_frac_of_measured": round(8 * elems / sec / 1e9 / peak, 3),
             "launches_per_replay": info["launches_per_exec"], "schedule": info["schedule"]}
@@ -421,6 +427,10 @@ def reference_arm(size_args, size, args, config, metric, world):
         run()
     el = time.perf_counter() - t0
     value = flops_per_call(size, per) * args.steps / el / 1e9
+    try:  # informational, outside the timed CPU steps
+        ref_gpu = reference_gpu_timings()
+    except Exception as e:  # noqa: BLE001
+        ref_gpu = {"error": str(e)[:200]}
     sample = ("%d transforms of the workload size per step (one per host thread; FP64, oracle/fft64.c, "
               "%d OpenMP threads), %d timed steps in %.2f s" % (per, threads, args.steps, el))
     return {"impl": "reference", "metric": metric, "value": round(value, 3), "unit": "GFLOP/s", "n_gpus": world,
@@ -429,7 +439,49 @@ def reference_arm(size_args, size, args, config, metric, world):
             "data": "synthetic uniform[-1,1)", "config": config,
             "cpu_baseline": {"value": round(value, 3), "unit": "GFLOP/s", "cores": threads, "kind": "port",
                              "sample": sample},
-            "e2e": {"value": round(value, 3), "unit": "GFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+            "e2e": {"value": round(value, 3), "unit": "GFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "reference_gpu": ref_gpu}
+
+
+def reference_gpu_timings(total=1 << 28, reps=5):
+    """Informational: the reference's own GPU kernels (compiled from its sources for sm_103a,
+    driven by oracle/ref_runner.cpp, which restates tcfftExec's launch sequence) timed with
+    CUDA events at its supported sizes, 2^28 elements per call.  "a100" are the kernels that
+    compute the DFT on this GPU; "volta" the ones tcfftCreate binds (wrong output on sm_103a)."""
+    import torch
+    import oracle
+    if not torch.cuda.is_available() or not oracle.reference_gpu_available():
+        return {"unavailable": "no GPU or reference kernels not built"}
+    peak, _ = measured_peak()
+    out = []
+    buf = torch.zeros((total, 2), dtype=torch.float16, device="cuda")
+    cases = [((n,), total // n) for n in (256, 512, 1024, 1 << 17, 1 << 18, 1 << 19, 1 << 24)]
+    cases += [((256, 256), total // 65536), ((512, 512), total // 262144), ((256, 1024), total // 262144)]
+    for shape, batch in cases:
+        for fam in ("a100", "volta"):
+            run = ((lambda: oracle.reference_gpu_fft_1d(buf.data_ptr(), shape[0], batch, fam, sync=False))
+                   if len(shape) == 1 else
+                   (lambda: oracle.reference_gpu_fft_2d(buf.data_ptr(), shape[0], shape[1], batch, fam, sync=False)))
+            try:
+                for _ in range(2):
+                    run()
+                torch.cuda.synchronize()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record()
+                for _ in range(reps):
+                    run()
+                e1.record()
+                torch.cuda.synchronize()
+                sec = e0.elapsed_time(e1) / 1000.0 / reps
+                size = int(math.prod(shape))
+                out.append({"shape": list(shape), "batch": batch, "family": fam, "us": round(sec * 1e6, 1),
+                            "gflops": round(flops_per_call(size, batch) / sec / 1e9, 1),
+                            "hbm_frac_of_measured": round(8 * total / sec / 1e9 / peak, 3)})
+            except Exception as e:  # noqa: BLE001 - informational
+                out.append({"shape": list(shape), "family": fam, "error": str(e)[:120]})
+    del buf
+    torch.cuda.empty_cache()
+    return out
 
 
 def copy_ceiling(torch, host_in, host_out, dev_a, dev_b, reps=5):
@@ -605,6 +657,7 @@ def main():
                             ("sweep_fp32io", lambda: sweep(torch, tc, "fp32io", lgs=(10, 12, 14, 16, 18, 20, 22))),
                             ("sweep_2d", lambda: sweep_2d(torch, tc)),
                             ("uneven_batch", lambda: uneven_batch(torch, tc)),
+                            ("uneven_batch_graph", lambda: uneven_batch(torch, tc, graph=True)),
                             ("cufft_fp16", lambda: cufft_fp16(torch, size_args, batch))):
                 try:  # informational
                     extra[key] = fn()

@@ -12,8 +12,9 @@
  *     6-29) the identity, so its host-side permutation becomes a no-op;
  *     define TCFFT_REFERENCE_INPUT_ORDER before including this header to get
  *     the reference's digit-reversed contract and radix chain instead;
- *   - every power of two 256 <= n <= 2^22 works (the reference supports ten
- *     sizes and leaves others undefined); failures print a message;
+ *   - every power of two 16 <= n <= 2^27 works, with batch x n up to 2^40
+ *     elements (the reference supports ten sizes from 256 to 2^27 and leaves
+ *     others undefined); failures print a message;
  *   - tcfftDestroy releases the plan (the reference leaks it).
  * Like the reference, this header and tcfft_half_2d.h define the same
  * `tcfftHandle` name and cannot be included in one translation unit.

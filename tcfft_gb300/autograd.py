@@ -17,44 +17,58 @@ import threading
 
 import torch
 
-from . import Plan
+from . import FORWARD, INVERSE, Plan
 
 _CACHE = {}
 _LOCK = threading.Lock()
 
 
 class TcfftFunction(torch.autograd.Function):
-    """y = FFT(x) with backward grad_x = FFT^H(grad_y) (adjoint kernel)."""
+    """y = FFT(x) with backward grad_x = FFT^H(grad_y) (adjoint kernel).
+
+    Both passes run out of place (tcfftExecuteOutOfPlace): the kernels read the
+    input through their own tensor maps and write a fresh output, so neither
+    pass needs a copy of its input."""
 
     @staticmethod
-    def forward(ctx, x, plan):
-        y = x.detach().clone().contiguous()
-        plan.exec(y)
-        ctx.plan = plan
+    def forward(ctx, x, ndim, precision):
+        src = x.detach().contiguous()
+        y = torch.empty_like(src)
+        _get_plan(src, ndim, precision, FORWARD).exec_out(src, y)
+        ctx.ndim, ctx.precision = ndim, precision
         return y
 
     @staticmethod
     def backward(ctx, gy):
-        gx = gy.detach().clone().contiguous()
-        ctx.plan.exec(gx, adjoint=True)
-        return gx, None
+        src = gy.detach().contiguous()
+        gx = torch.empty_like(src)
+        # the unnormalised sign +1 transform is F^H
+        _get_plan(src, ctx.ndim, ctx.precision, INVERSE).exec_out(src, gx)
+        return gx, None, None
 
 
-def _get_plan(x, ndim, precision):
+def _get_plan(x, ndim, precision, direction):
+    """One plan per (shape, precision, direction, device, thread, stream): a plan's
+    scratch ring and counters must not be shared by transforms that may run
+    concurrently, and two host threads or two streams may differentiate the same
+    shape at once."""
+    stream = torch.cuda.current_stream(x.device).cuda_stream
+    ident = (direction, precision, x.device.index, threading.get_ident(), stream)
     if ndim == 1:
         n = x.shape[-2]
         batch = x.numel() // (2 * n)
-        key = ("1d", n, batch, precision, x.device.index)
+        key = ("1d", n, batch) + ident
         kw = {"n": n, "batch": batch}
     else:
         nx, ny = x.shape[-3], x.shape[-2]
         batch = x.numel() // (2 * nx * ny)
-        key = ("2d", nx, ny, batch, precision, x.device.index)
+        key = ("2d", nx, ny, batch) + ident
         kw = {"nx": nx, "ny": ny, "batch": batch}
     with _LOCK:
         p = _CACHE.get(key)
         if p is None:
-            p = Plan(precision=precision, **kw)
+            with torch.cuda.device(x.device):
+                p = Plan(precision=precision, direction=direction, **kw)
             _CACHE[key] = p
     return p
 
@@ -62,13 +76,13 @@ def _get_plan(x, ndim, precision):
 def fft(x, precision=None):
     """Differentiable batched 1D FFT over dim -2 of a real view ``[..., n, 2]``."""
     precision = precision or ("plain" if x.dtype == torch.float16 else "split")
-    return TcfftFunction.apply(x, _get_plan(x, 1, precision))
+    return TcfftFunction.apply(x, 1, precision)
 
 
 def fft2(x, precision=None):
     """Differentiable batched 2D FFT over dims (-3, -2) of ``[..., nx, ny, 2]``."""
     precision = precision or ("plain" if x.dtype == torch.float16 else "split")
-    return TcfftFunction.apply(x, _get_plan(x, 2, precision))
+    return TcfftFunction.apply(x, 2, precision)
 
 
 def clear_plan_cache():

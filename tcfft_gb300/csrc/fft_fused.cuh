@@ -230,10 +230,11 @@ __device__ __forceinline__ void plain_col_tile(const JobConsts<false>& jc, uint3
   if constexpr (WN) {
     // W_N^(n2 (q + R k')), k' = kbase + e + 2h + 32hh (RHO digit structure):
     // fk[osl] = W^(n2 R kbase) u^(e + 2h) u32^hh with u = W^(n2 R); fq[q] = W^(n2 q)
-    // (four jobs: only the even-slot factors and u32 are held, 40 registers instead of 64,
-    // the odd slots cost one product at the store)
+    // Only the even-slot factors and u32 are held; an odd slot costs one product at the store
+    // (four jobs: 40 registers instead of 64; two jobs at 2^20: no spills instead of 8/40 bytes,
+    // 1 % faster at 2^19..2^22).
     const int kbase = slot_kval<PI, RHO>(0);
-    constexpr int NK = QUAD ? 4 : 8;
+    constexpr int NK = 4;
     float2 fk[JN][NK], fu[JN], fq[JN][R];
 #pragma unroll
     for (int jn = 0; jn < JN; ++jn) {
@@ -245,14 +246,7 @@ __device__ __forceinline__ void plain_col_tile(const JobConsts<false>& jc, uint3
       const float2 f0[4] = {F, cmul(F, u), cmul(F, u2), cmul(F, u3)};
       fu[jn] = u32;
 #pragma unroll
-      for (int osl = 0; osl < NK; ++osl) {
-        if constexpr (QUAD) {
-          fk[jn][osl] = f0[osl];
-        } else {
-          const float2 f = f0[((osl >> 1) & 1) + 2 * (osl >> 2)];
-          fk[jn][osl] = (osl & 1) ? cmul(f, u32) : f;
-        }
-      }
+      for (int osl = 0; osl < NK; ++osl) fk[jn][osl] = f0[osl];
       fq[jn][0] = make_float2(1.f, 0.f);
       if constexpr (R > 1) fq[jn][1] = wn(n2);
 #pragma unroll
@@ -261,13 +255,8 @@ __device__ __forceinline__ void plain_col_tile(const JobConsts<false>& jc, uint3
     // W_N^(n2 (q + R k')) of job jn, output slot osl (osl and q are compile-time constants
     // after unrolling: q = 0 needs no product)
     auto wfac = [&](int jn, int osl, int q) {
-      float2 f;
-      if constexpr (QUAD) {
-        f = fk[jn][((osl >> 1) & 1) + 2 * (osl >> 2)];
-        if (osl & 1) f = cmul(f, fu[jn]);
-      } else {
-        f = fk[jn][osl];
-      }
+      float2 f = fk[jn][((osl >> 1) & 1) + 2 * (osl >> 2)];
+      if (osl & 1) f = cmul(f, fu[jn]);
       return q == 0 ? f : cmul(f, fq[jn][q]);
     };
     if constexpr (QUAD) {

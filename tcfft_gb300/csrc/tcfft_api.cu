@@ -213,6 +213,19 @@ void free_tables(tcfftPlanImpl* p) {
   }
   if (p->cap_stream) cudaStreamDestroy(p->cap_stream);
   p->cap_stream = nullptr;
+  if (p->many_items) cudaFree(p->many_items);
+  if (p->many_rows) cudaFree(p->many_rows);
+  if (p->many_maps) cudaFree(p->many_maps);
+  if (p->many_hmaps) cudaFreeHost(p->many_hmaps);
+  if (p->many_scratch) cudaFree(p->many_scratch);
+  if (p->many_wn_buf) cudaFree(p->many_wn_buf);
+  p->many_items = nullptr;
+  p->many_rows = nullptr;
+  p->many_maps = nullptr;
+  p->many_hmaps = nullptr;
+  p->many_scratch = nullptr;
+  p->many_wn_buf = nullptr;
+  p->many_ok = false;
   for (int b = 0; b < tcfftPlanImpl::kBranches; ++b) {
     if (p->branch[b]) cudaStreamDestroy(p->branch[b]);
     if (p->join_ev[b]) cudaEventDestroy(p->join_ev[b]);
@@ -266,8 +279,11 @@ int ilog2_exact(int64_t v) {
 // Tiles in flight span about (CTAs x stages) items; a transform's phase 1 is
 // placed D blocks after its phase 0, and a slot is reused S blocks later, so
 // both D and S - D must exceed the blocks in flight.
-// Lag multiplier chosen by the autotuner while it times candidates (0: none).
+// Lag multiplier, 1D column length N1 and work-item size chosen by the autotuner
+// while it times candidates (0: none).
 thread_local double g_lag_override = 0.0;
+thread_local int64_t g_n1_override = 0;
+thread_local int g_item_kb_override = 0;
 
 // Items of several tiles keep more tiles in flight per CTA: the lag grows with
 // the tiles per item (x 1.25, measured at N = 2^16 and 2^17).  Rings deeper than
@@ -292,6 +308,7 @@ void fused_lag(int T0, int T1, int64_t batch, Schedule& s, const FusedKey* key, 
 // Work-item size of the 1D two-phase schedules (TCFFT_ITEM_KB overrides it, for measurements).
 int item_kb_1d(int lg, bool split) {
   static const int env = getenv("TCFFT_ITEM_KB") ? atoi(getenv("TCFFT_ITEM_KB")) : 0;
+  if (g_item_kb_override == 32 || g_item_kb_override == 64) return g_item_kb_override;
   if (env == 32 || env == 64) return env;
   (void)lg;
   (void)split;
@@ -383,6 +400,7 @@ tcfftStatus choose_1d(int64_t n, int64_t batch, int precision, Schedule& s, int 
     int64_t n1 = int64_t(1) << ((lg + 1) / 2);
     if (lg == 21) n1 = 1024;
     if (getenv("TCFFT_N1")) n1 = atoll(getenv("TCFFT_N1"));  // decomposition override (measurements)
+    if (g_n1_override) n1 = g_n1_override;                     // the autotuner's candidate
     if (n1 < 256 || n1 > 2048 || n / n1 < 256 || n / n1 > 2048) return TCFFT_NOT_SUPPORTED;
     const int64_t n2 = n / n1;
     FusedKey k;
@@ -952,15 +970,23 @@ tcfftStatus setup_generic2d(tcfftPlanImpl* p) {
 }
 
 // ------------------------------------------------------------------ autotuner
-// For the fused executor the free parameter with the largest measured effect
-// is the lag (how many transforms are between their first and second phase,
-// which sets the L2 footprint of the intermediate and the slack of the
-// cross-CTA dependency).  At plan time, with tcfftOptions.autotune = 1, the
-// plan times a few lag multipliers on a scratch buffer of its own size and
-// keeps the fastest; results are cached per (shape, batch, precision) in the
-// process and, if tune_cache_path is set, in that text file ("key scale" lines).
+// For the two-phase executor the free parameters with measured effect are the
+// lag (how many transforms are between their first and second phase, which
+// sets the L2 footprint of the intermediate and the slack of the cross-CTA
+// dependency) and, for 1D sizes N = N1 x N2, the decomposition N1 and the
+// work-item size (64 or 32 KiB).  At plan time, with tcfftOptions.autotune = 1,
+// the plan times each decomposition / item-size candidate at the built-in lag,
+// then a few lag multipliers for the fastest, on a scratch buffer of its own
+// size, and keeps the fastest; results are cached per (shape, batch,
+// precision) in the process and, if tune_cache_path is set, in that text file
+// ("key|lag|N1|item KiB" lines; "key|lag" lines of older files still load).
+struct TuneChoice {
+  double lag = 1.0;
+  int64_t n1 = 0;  // 0: the built-in decomposition
+  int item_kb = 0; // 0: the built-in item size
+};
 std::mutex g_tune_mu;
-std::map<std::string, double> g_tune_cache;
+std::map<std::string, TuneChoice> g_tune_cache;
 std::set<std::string> g_tune_files_read;
 
 void load_tune_file(const char* path) {
@@ -971,27 +997,62 @@ void load_tune_file(const char* path) {
   char line[256];
   while (fgets(line, sizeof line, f)) {
     char key[200];
-    double v = 0;
-    if (sscanf(line, "%199[^|]|%lf", key, &v) == 2 && v > 0) g_tune_cache[key] = v;
+    TuneChoice c;
+    long long n1 = 0;
+    int kb = 0;
+    const int got = sscanf(line, "%199[^|]|%lf|%lld|%d", key, &c.lag, &n1, &kb);
+    if (got < 2 || !(c.lag > 0)) continue;
+    if (got == 4) {
+      c.n1 = n1;
+      c.item_kb = kb;
+    }
+    g_tune_cache[key] = c;
   }
   fclose(f);
 }
 
-tcfftStatus choose_again(tcfftPlanImpl* p, double scale, Schedule& s) {
-  g_lag_override = scale;
+tcfftStatus choose_again(tcfftPlanImpl* p, const TuneChoice& c, Schedule& s) {
+  g_lag_override = c.lag;
+  g_n1_override = c.n1;
+  g_item_kb_override = c.item_kb;
   tcfftStatus st = p->kind == 1 ? choose_1d(p->n, p->batch, p->precision, s, p->num_sms)
                                 : choose_2d(p->nx, p->ny, p->batch, p->precision, s, p->num_sms);
   g_lag_override = 0.0;
+  g_n1_override = 0;
+  g_item_kb_override = 0;
   return st;
 }
 
-tcfftStatus apply_lag(tcfftPlanImpl* p, double scale) {
+tcfftStatus apply_choice(tcfftPlanImpl* p, const TuneChoice& c) {
   Schedule s;
-  tcfftStatus st = choose_again(p, scale, s);
+  tcfftStatus st = choose_again(p, c, s);
   if (st != TCFFT_SUCCESS) return st;
+  if (s.kind != p->sched.kind) return TCFFT_NOT_SUPPORTED;  // candidates never change the schedule kind
   p->sched = s;
-  p->lag_scale = scale;
+  p->lag_scale = c.lag;
   return alloc_ring(p);
+}
+
+// 1D decomposition / item-size candidates for the tuner: N1 = 2^ceil(lg/2) and
+// 2^floor(lg/2) (the schedule's bounds keep N1, N2 in 256..2048), each with
+// 64 and 32 KiB items; choose_1d falls back to 64 KiB where 32 is not built.
+std::vector<TuneChoice> shape_candidates(const tcfftPlanImpl* p) {
+  std::vector<TuneChoice> out;
+  out.push_back(TuneChoice());
+  if (p->kind != 1) return out;
+  const int lg = ilog2_exact(p->n);
+  if (lg < 16 || lg > 22) return out;
+  for (int e : {(lg + 1) / 2, lg / 2, (lg + 1) / 2 + 1, lg / 2 - 1}) {
+    const int64_t n1 = int64_t(1) << e;
+    if (n1 < 256 || n1 > 2048 || p->n / n1 < 256 || p->n / n1 > 2048) continue;
+    for (int kb : {64, 32}) {
+      TuneChoice c;
+      c.n1 = n1;
+      c.item_kb = kb;
+      out.push_back(c);
+    }
+  }
+  return out;
 }
 
 tcfftStatus autotune_plan(tcfftPlanImpl* p, const tcfftOptions& o) {
@@ -1002,7 +1063,7 @@ tcfftStatus autotune_plan(tcfftPlanImpl* p, const tcfftOptions& o) {
   const std::string key = kb;
   std::lock_guard<std::mutex> lock(g_tune_mu);
   load_tune_file(o.tune_cache_path);
-  double best = 1.0;
+  TuneChoice best;
   auto it = g_tune_cache.find(key);
   if (it != g_tune_cache.end()) {
     best = it->second;
@@ -1011,26 +1072,60 @@ tcfftStatus autotune_plan(tcfftPlanImpl* p, const tcfftOptions& o) {
     void* tmp = nullptr;
     if (cudaMalloc(&tmp, p->total_elems * es) != cudaSuccess) {
       cudaGetLastError();
-      return TCFFT_SUCCESS;  // not enough memory to time: keep the built-in lag
+      return TCFFT_SUCCESS;  // not enough memory to time: keep the built-in schedule
     }
     cudaMemset(tmp, 0, p->total_elems * es);
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     float best_ms = 1e30f;
-    std::set<int> seen_d;
-    for (double c : {1.0, 0.6, 1.6, 2.5}) {
-      Schedule s;
-      if (choose_again(p, c, s) != TCFFT_SUCCESS || seen_d.count(s.D)) continue;
-      seen_d.insert(s.D);
-      if (apply_lag(p, c) != TCFFT_SUCCESS) break;
-      if (exec_plan(p, tmp, nullptr, 0, 0) != TCFFT_SUCCESS) break;
+    bool failed = false;
+    // one timing: a warm-up execute, then three timed ones
+    auto time_choice = [&](const TuneChoice& c, float* ms) {
+      if (apply_choice(p, c) != TCFFT_SUCCESS) return false;
+      if (exec_plan(p, tmp, nullptr, 0, 0) != TCFFT_SUCCESS) return false;
       cudaEventRecord(e0, nullptr);
       for (int r = 0; r < 3; ++r) exec_plan(p, tmp, nullptr, 0, 0);
       cudaEventRecord(e1, nullptr);
-      if (cudaEventSynchronize(e1) != cudaSuccess) break;
+      if (cudaEventSynchronize(e1) != cudaSuccess) return false;
+      cudaEventElapsedTime(ms, e0, e1);
+      return true;
+    };
+    // stage 1: decomposition and item size at the built-in lag (distinct schedules only)
+    std::set<std::string> seen;
+    for (const TuneChoice& c : shape_candidates(p)) {
+      Schedule s;
+      if (choose_again(p, c, s) != TCFFT_SUCCESS || s.kind != p->sched.kind) continue;
+      char sig[64];
+      snprintf(sig, sizeof sig, "%lld %d %d %d", (long long)s.N1, s.key.item_kb, s.key.C0, s.key.C1);
+      if (!seen.insert(sig).second) continue;
       float ms = 0;
-      cudaEventElapsedTime(&ms, e0, e1);
+      if (!time_choice(c, &ms)) {
+        failed = true;
+        break;
+      }
+      if (ms < best_ms) {
+        best_ms = ms;
+        best = c;
+      }
+    }
+    // stage 2: the lag for the chosen shape
+    std::set<int> seen_d;
+    {
+      Schedule s;
+      if (!failed && choose_again(p, best, s) == TCFFT_SUCCESS) seen_d.insert(s.D);
+    }
+    for (double lag : {0.6, 1.6, 2.5}) {
+      if (failed) break;
+      TuneChoice c = best;
+      c.lag = lag;
+      Schedule s;
+      if (choose_again(p, c, s) != TCFFT_SUCCESS || !seen_d.insert(s.D).second) continue;
+      float ms = 0;
+      if (!time_choice(c, &ms)) {
+        failed = true;
+        break;
+      }
       if (ms < best_ms) {
         best_ms = ms;
         best = c;
@@ -1039,20 +1134,34 @@ tcfftStatus autotune_plan(tcfftPlanImpl* p, const tcfftOptions& o) {
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     cudaFree(tmp);
-    g_tune_cache[key] = best;
-    if (o.tune_cache_path) {
-      FILE* f = fopen(o.tune_cache_path, "a");
-      if (f) {
-        fprintf(f, "%s|%.3f\n", key.c_str(), best);
-        fclose(f);
+    if (failed) {
+      cudaGetLastError();
+      best = TuneChoice();  // a candidate failed to run: keep the built-in schedule, cache nothing
+    } else {
+      g_tune_cache[key] = best;
+      if (o.tune_cache_path) {
+        FILE* f = fopen(o.tune_cache_path, "a");
+        if (f) {
+          fprintf(f, "%s|%.3f|%lld|%d\n", key.c_str(), best.lag, (long long)best.n1, best.item_kb);
+          fclose(f);
+        }
       }
     }
   }
-  tcfftStatus st = apply_lag(p, best);
-  if (st != TCFFT_SUCCESS) return st;
-  char buf[48];
-  snprintf(buf, sizeof buf, " [tuned: lag x%.2g]", best);
-  p->sched.text += buf;
+  tcfftStatus st = apply_choice(p, best);
+  if (st != TCFFT_SUCCESS) {
+    st = apply_choice(p, TuneChoice());  // e.g. a cache line for another build's instantiations
+    if (st != TCFFT_SUCCESS) return st;
+    best = TuneChoice();
+  }
+  // in front: the plan-info string is 128 characters
+  char buf[96];
+  if (p->kind == 1 && p->sched.kind == Schedule::kFused1d)
+    snprintf(buf, sizeof buf, "[tuned: N1=%lld, %d KiB items, lag x%.2g] ", (long long)p->sched.N1,
+             p->sched.key.item_kb, best.lag);
+  else
+    snprintf(buf, sizeof buf, "[tuned: lag x%.2g] ", best.lag);
+  p->sched.text = buf + p->sched.text;
   return TCFFT_SUCCESS;
 }
 
@@ -1076,7 +1185,268 @@ tcfftStatus check_errors(tcfftPlanImpl* p) {
   return r;
 }
 
+// ------------------------------------------------------------------ many-shape executor (plain)
+// Pass A / pass B kinds of a transform (kMkKinds: not supported by the executor).
+int many_kind_a(int rank, int64_t nx, int64_t ny) {
+  if (rank == 1) {
+    switch (nx) {
+      case 256: return kMkRow1 | kMkList;
+      case 512: return kMkRow2 | kMkList;
+      case 1024: return kMkRow4 | kMkList;
+      case 2048: return kMkRow8 | kMkList;
+      case 4096: case 8192: case 16384: return kMkColWn1x16;
+      case 32768: return kMkColWn2x32;
+      case 65536: return kMkColWn1x32;
+      default: return kMkKinds;
+    }
+  }
+  switch (ny) {
+    case 128: return kMkRow128;
+    case 256: return kMkRow1;
+    case 512: return kMkRow2;
+    case 1024: return kMkRow4;
+    case 2048: return kMkRow8;
+    default: return kMkKinds;
+  }
+}
+int many_kind_b(int rank, int64_t nx, int64_t ny) {
+  if (rank == 1) {
+    switch (nx) {
+      case 4096: return kMkRow16T1;
+      case 8192: return kMkRow16T2;
+      case 16384: case 32768: return kMkRow16T4;
+      case 65536: return kMkRowT1;
+      default: return nx <= 2048 ? -1 : kMkKinds;  // -1: no pass B
+    }
+  }
+  switch (nx) {
+    case 128: return kMkCol128;
+    case 256: return kMkCol1;
+    case 512: return kMkCol2;
+    case 1024: return kMkCol4;
+    case 2048: return kMkCol8;
+    default: return kMkKinds;
+  }
+}
+// 1D N >= 4096 = N1 x N2 in the executor (N1 = 256, 2^15: 512)
+int64_t many_n1(int64_t n) { return n == 32768 ? 512 : 256; }
+
+// Tiles of a transform's pass for a (non-listed) kind.
+int64_t many_tiles(int kind, int rank, int64_t nx, int64_t ny) {
+  const int C = many_c(kind);
+  switch (kind) {
+    case kMkRow1: case kMkRow2: case kMkRow4: case kMkRow8: return nx / C;
+    case kMkRow128: return nx / 128;
+    case kMkColWn1x16: case kMkColWn1x32: case kMkColWn2x32: return (nx / many_n1(nx)) / C;
+    case kMkRowT1: return many_n1(nx) / C;
+    case kMkRow16T1: case kMkRow16T2: case kMkRow16T4: return many_n1(nx) / 128;
+    case kMkCol1: case kMkCol2: case kMkCol4: case kMkCol8: return ny / C;
+    case kMkCol128: return ny / 128;
+    default: (void)rank; return 0;
+  }
+}
+
+// Builds the executor's items, row list, scratch and W_N tables; false (nothing
+// allocated that the plan does not free) when a shape is not supported.
+bool setup_many_pass(tcfftPlanImpl* p, int64_t count, const int32_t* ranks, const int64_t* nx, const int64_t* ny,
+                     const int64_t* offsets) {
+  if (p->precision != TCFFT_PRECISION_PLAIN || getenv("TCFFT_MANY_GRAPH")) return false;
+  if (count > (int64_t)1 << 24) return false;
+  std::vector<tcfftPlanImpl::ManyXf> xf((size_t)count);
+  std::vector<int64_t> wn_sizes;
+  int64_t soff = 0;
+  for (int64_t i = 0; i < count; ++i) {
+    const int r = ranks[i];
+    const int64_t x = nx[i], y = r == 2 ? ny[i] : 1;
+    if (many_kind_a(r, x, y) == kMkKinds || many_kind_b(r, x, y) == kMkKinds) return false;
+    xf[i] = {r, x, y, offsets[i], 0};
+    if (r == 1 && x >= 4096) {
+      xf[i].soff = soff;
+      soff += x;
+      if (std::find(wn_sizes.begin(), wn_sizes.end(), x) == wn_sizes.end()) wn_sizes.push_back(x);
+    }
+  }
+  if ((int)wn_sizes.size() > kManyMaxWn) return false;
+  // items: pass A then pass B, each ordered by kind (larger tiles first within a kind)
+  std::vector<ManyItem> items[2];
+  std::vector<int> rows;
+  for (int pass = 0; pass < 2; ++pass) {
+    for (int kind = 0; kind < kMkKinds; ++kind) {
+      std::vector<int64_t> listed;  // 1D transforms whose pass A is kind as listed rows
+      for (int64_t i = 0; i < count; ++i) {
+        const auto& t = xf[i];
+        const int k = pass == 0 ? many_kind_a(t.rank, t.nx, t.ny) : many_kind_b(t.rank, t.nx, t.ny);
+        if (k < 0 || (k & 0xff) != kind) continue;
+        if (k & kMkList) {
+          listed.push_back(i);
+          continue;
+        }
+        const int64_t tiles = many_tiles(kind, t.rank, t.nx, t.ny);
+        int wn = 0;
+        if (kind == kMkColWn1x16 || kind == kMkColWn1x32 || kind == kMkColWn2x32)
+          wn = (int)(std::find(wn_sizes.begin(), wn_sizes.end(), t.nx) - wn_sizes.begin());
+        for (int64_t tile = 0; tile < tiles; ++tile) items[pass].push_back({kind, (int)i, (int)tile, wn});
+      }
+      const int C = many_c(kind);
+      for (size_t j = 0; j < listed.size(); j += C) {
+        const int cnt = (int)std::min<size_t>(C, listed.size() - j);
+        items[pass].push_back({kind | kMkList, (int)rows.size(), 0, cnt});
+        for (int q = 0; q < cnt; ++q) rows.push_back((int)listed[j + q]);
+      }
+    }
+  }
+  // device arrays
+  const size_t nit = items[0].size() + items[1].size();
+  if (cudaMalloc(&p->many_items, std::max<size_t>(nit, 1) * sizeof(ManyItem)) != cudaSuccess ||
+      cudaMalloc(&p->many_rows, std::max<size_t>(rows.size(), 1) * sizeof(int)) != cudaSuccess ||
+      cudaMalloc(&p->many_maps, (size_t)count * 4 * sizeof(CUtensorMap)) != cudaSuccess ||
+      cudaMallocHost(&p->many_hmaps, (size_t)count * 4 * sizeof(CUtensorMap)) != cudaSuccess ||
+      (soff > 0 && cudaMalloc(&p->many_scratch, soff * 4) != cudaSuccess)) {
+    cudaGetLastError();
+    return false;
+  }
+  std::vector<ManyItem> all(items[0]);
+  all.insert(all.end(), items[1].begin(), items[1].end());
+  if ((nit && cudaMemcpy(p->many_items, all.data(), nit * sizeof(ManyItem), cudaMemcpyHostToDevice) != cudaSuccess) ||
+      (!rows.empty() &&
+       cudaMemcpy(p->many_rows, rows.data(), rows.size() * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess))
+    return false;
+  // W_N tables of each 1D size >= 4096, both directions: lo then hi
+  int64_t wn_elems = 0;
+  for (int64_t n : wn_sizes) {
+    const int lg = ilog2_exact(n), shift = (lg + 1) / 2;
+    wn_elems += 2 * ((int64_t(1) << shift) + (n >> shift));
+  }
+  if (wn_elems > 0) {
+    std::vector<float2> h((size_t)wn_elems);
+    if (cudaMalloc(&p->many_wn_buf, wn_elems * sizeof(float2)) != cudaSuccess) return false;
+    int64_t at = 0;
+    for (size_t w = 0; w < wn_sizes.size(); ++w) {
+      const int64_t n = wn_sizes[w];
+      const int lg = ilog2_exact(n), shift = (lg + 1) / 2;
+      const int64_t nlo = int64_t(1) << shift, nhi = n >> shift;
+      p->many_wn[w].shift = shift;
+      p->many_wn[w].nmask = (int)(n - 1);
+      for (int d = 0; d < 2; ++d) {
+        const long double sgn = d == 0 ? -1.0L : 1.0L;
+        const long double twopi = 2.0L * 3.141592653589793238462643383279502884L;
+        p->many_wn[w].lo[d] = p->many_wn_buf + at;
+        for (int64_t j = 0; j < nlo; ++j, ++at) {
+          const long double th = twopi * (long double)j / (long double)n;
+          h[at] = make_float2((float)cosl(th), (float)(sgn * sinl(th)));
+        }
+        p->many_wn[w].hi[d] = p->many_wn_buf + at;
+        for (int64_t j = 0; j < nhi; ++j, ++at) {
+          const long double th = twopi * (long double)(j << shift) / (long double)n;
+          h[at] = make_float2((float)cosl(th), (float)(sgn * sinl(th)));
+        }
+      }
+    }
+    if (cudaMemcpy(p->many_wn_buf, h.data(), wn_elems * sizeof(float2), cudaMemcpyHostToDevice) != cudaSuccess)
+      return false;
+  }
+  p->many_xf = std::move(xf);
+  p->many_n[0] = (int)items[0].size();
+  p->many_n[1] = (int)items[1].size();
+  p->scratch_bytes += soff * 4;
+  p->many_ok = true;
+  return true;
+}
+
+// The transforms' tensor maps for data buffer `data` (into the pinned staging copy).
+CUresult encode_many_maps(tcfftPlanImpl* p, void* data) {
+  const CUtensorMapDataType dt = CU_TENSOR_MAP_DATA_TYPE_UINT32;
+  unsigned char* d = static_cast<unsigned char*>(data);
+  unsigned char* sc = static_cast<unsigned char*>(p->many_scratch);
+  for (size_t i = 0; i < p->many_xf.size(); ++i) {
+    const auto& t = p->many_xf[i];
+    CUtensorMap* m = p->many_hmaps + 4 * i;
+    memset(m, 0, 4 * sizeof(CUtensorMap));
+    void* base = d + t.off * 4;
+    CUresult r = CUDA_SUCCESS;
+    auto rows_map = [&](CUtensorMap* mm, void* b, int64_t elems, int64_t box_rows) {
+      uint64_t dims[2] = {32, (uint64_t)(elems / 32)};
+      uint64_t str[1] = {128};
+      uint32_t box[2] = {32, (uint32_t)box_rows};
+      return encode_tmap(mm, dt, 2, b, dims, str, box, CU_TENSOR_MAP_SWIZZLE_128B);
+    };
+    if (t.rank == 1 && t.nx <= 2048) {
+      r = rows_map(&m[0], base, t.nx, t.nx / 32);
+    } else if (t.rank == 1) {
+      const int64_t n1 = many_n1(t.nx), n2 = t.nx / n1;
+      const int ka = many_kind_a(1, t.nx, 1), kb = many_kind_b(1, t.nx, 1);
+      void* sbase = sc + t.soff * 4;
+      r = encode_col_load(&m[0], dt, base, n2, 1, 4, many_c(ka), many_r(ka));
+      if (r == CUDA_SUCCESS) r = encode_col_store(&m[1], dt, sbase, n2, 1, 4, many_c(ka), many_r(ka));
+      if (kb == kMkRowT1) {
+        if (r == CUDA_SUCCESS) r = rows_map(&m[2], sbase, t.nx, 256);
+        if (r == CUDA_SUCCESS) r = encode_col_store(&m[3], dt, base, n1, 1, 4, many_c(kb), many_r(kb));
+      } else {  // 128 rows of 16 R per item; store [N1][k0][q][1] in boxes of 32 columns
+        const int R1 = many_r(kb);
+        if (r == CUDA_SUCCESS) r = rows_map(&m[2], sbase, t.nx, 64 * R1);
+        const uint64_t rowb = (uint64_t)n1 * 4;
+        uint64_t dims[4] = {(uint64_t)n1, 16, (uint64_t)R1, 1};
+        uint64_t str[3] = {rowb * R1, rowb, rowb * n2};
+        uint32_t box[4] = {32, 16, (uint32_t)R1, 1};
+        if (r == CUDA_SUCCESS) r = encode_tmap(&m[3], dt, 4, base, dims, str, box, CU_TENSOR_MAP_SWIZZLE_128B);
+      }
+    } else {
+      const int ka = many_kind_a(2, t.nx, t.ny), kb = many_kind_b(2, t.nx, t.ny);
+      const int64_t elems = t.nx * t.ny;
+      if (ka == kMkRow128) {
+        r = rows_map(&m[0], base, elems, 256);
+      } else {
+        const int64_t rows = (int64_t)many_c(ka) * t.ny / 32;
+        r = rows_map(&m[0], base, elems, rows < 256 ? rows : 256);
+      }
+      if (kb == kMkCol128) {  // [128 rows][ny cols], boxes of 32 columns x 128 rows
+        uint64_t dims[2] = {(uint64_t)t.ny, 128};
+        uint64_t str[1] = {(uint64_t)t.ny * 4};
+        uint32_t box[2] = {32, 128};
+        if (r == CUDA_SUCCESS) r = encode_tmap(&m[2], dt, 2, base, dims, str, box, CU_TENSOR_MAP_SWIZZLE_128B);
+        m[3] = m[2];
+      } else {
+        if (r == CUDA_SUCCESS) r = encode_col_load(&m[2], dt, base, t.ny, 1, 4, many_c(kb), many_r(kb));
+        if (r == CUDA_SUCCESS) r = encode_col_store(&m[3], dt, base, t.ny, 1, 4, many_c(kb), many_r(kb));
+      }
+    }
+    if (r != CUDA_SUCCESS) return r;
+  }
+  return CUDA_SUCCESS;
+}
+
+tcfftStatus exec_many_pass(tcfftPlanImpl* plan, void* data, cudaStream_t st, int dir) {
+  if (plan->many_maps_ptr != data) {
+    // the staging copy may still be read by an earlier execute's copy: let it finish first
+    if (cuda_status(cudaStreamSynchronize(st), "many maps")) return TCFFT_CUDA_ERROR;
+    if (cu_status(encode_many_maps(plan, data), "many maps")) return TCFFT_CUDA_ERROR;
+    const size_t bytes = plan->many_xf.size() * 4 * sizeof(CUtensorMap);
+    if (cuda_status(cudaMemcpyAsync(plan->many_maps, plan->many_hmaps, bytes, cudaMemcpyHostToDevice, st),
+                    "many maps"))
+      return TCFFT_CUDA_ERROR;
+    plan->many_maps_ptr = data;
+  }
+  ManyParams mp;
+  memset(&mp, 0, sizeof mp);
+  mp.maps = plan->many_maps;
+  mp.row_list = plan->many_rows;
+  mp.tw2048 = plan->tables.tw2048[dir];
+  for (int w = 0; w < kManyMaxWn; ++w) mp.wn[w] = plan->many_wn[w];
+  mp.dir = dir;
+  mp.dsign = dir == 0 ? 1.f : -1.f;
+  mp.err = plan->tables.err;
+  mp.wait_ns = plan->wait_ns;
+  for (int pass = 0; pass < 2; ++pass) {
+    mp.items = plan->many_items + (pass == 0 ? 0 : plan->many_n[0]);
+    mp.n_items = plan->many_n[pass];
+    if (mp.n_items == 0) continue;
+    if (cuda_status(launch_many(mp, plan->num_sms, st), "many pass")) return TCFFT_CUDA_ERROR;
+  }
+  return TCFFT_SUCCESS;
+}
+
 tcfftStatus exec_many(tcfftPlanImpl* plan, void* data, cudaStream_t st, int dir, int norm) {
+  if (plan->many_ok && !norm) return exec_many_pass(plan, data, st, dir);
   const int es = plan->precision != TCFFT_PRECISION_PLAIN ? 8 : 4;
   const int g = 2 * dir + norm;  // one captured graph per direction and normalisation
   if (!plan->graph_exec[g] || plan->graph_ptr[g] != data) {
@@ -1411,11 +1781,20 @@ tcfftStatus tcfftPlanMany(tcfftPlan* out, int64_t count, const int32_t* ranks, c
     return st;
   }
   p->sched.launches = launches;
-  char buf[160];
+  char buf[200];
   snprintf(buf, sizeof buf, "many(%s): %lld transforms in %d runs (%d gathered), %d sub-plans, %d launches per graph replay",
            prec_name(o.precision), (long long)count, (int)p->runs.size(), p->mv_n,
            nsub, launches);
   p->sched.text = buf;
+  if (setup_many_pass(p, count, ranks, nx, ny, offsets)) {
+    // the graph stays for normalised executes
+    p->sched.launches = (p->many_n[0] > 0) + (p->many_n[1] > 0);
+    snprintf(buf, sizeof buf,
+             "many(%s): %lld transforms, persistent many-shape passes: %d + %d work items, %d launches "
+             "(normalised: %d sub-plans in a graph)",
+             prec_name(o.precision), (long long)count, p->many_n[0], p->many_n[1], p->sched.launches, nsub);
+    p->sched.text = buf;
+  }
   *out = p;
   return TCFFT_SUCCESS;
 }

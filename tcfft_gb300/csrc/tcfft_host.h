@@ -112,6 +112,75 @@ cudaError_t launch_r2c_post(const void* z, void* x, int64_t batch, int64_t h, co
 cudaError_t launch_c2r_pre(const void* x, void* z, int64_t batch, int64_t h, const float2* lo, const float2* hi,
                            int shift, float scale, bool split, int num_sms, cudaStream_t st);
 
+// ---------------------------------------------------------------- many-shape executor (fft_many.cu)
+// Kinds of work item of the plain-precision executor of tcfftPlanMany: each is one
+// tile of one transform's pass (or, for kMkRow* with kMkList, up to C whole 1D
+// transforms of 256R points listed in the row list).  Pass A: rows / 1D column
+// phase; pass B: 1D row phase / 2D columns.  Per transform, four tensor maps:
+// [0] pass-A load (and in-place store), [1] pass-A store to scratch (1D),
+// [2] pass-B load, [3] pass-B store.
+enum ManyKind : int {
+  kMkRow1 = 0, kMkRow2, kMkRow4, kMkRow8,    // rows of 256R in place, C = 32, 32, 16, 8 rows per item
+  kMkColWn1x16, kMkColWn1x32, kMkColWn2x32,  // 1D phase 0: columns of 256R times W_N, to scratch
+  kMkRowT1,                                  // 1D phase 1: 32 rows of 256 from scratch, written transposed
+  kMkRow16T1, kMkRow16T2, kMkRow16T4,        // 1D phase 1: 128 rows of 16R from scratch, written transposed
+  kMkCol1, kMkCol2, kMkCol4, kMkCol8,        // 2D columns of 256R in place, C = 32, 32, 16, 8
+  kMkRow128, kMkCol128,                      // 2D axes of 128: 128 rows / 128 columns per item, in place
+  kMkKinds
+};
+constexpr int kMkList = 0x100;  // kind flag: the item's rows are whole transforms from the row list
+// kind -> R (points / 256, or / 16 for the 16R kinds), C (rows or columns per item)
+__host__ __device__ constexpr int many_r(int kind) {
+  return kind == kMkRow1 || kind == kMkColWn1x16 || kind == kMkColWn1x32 || kind == kMkRowT1 ||
+                 kind == kMkRow16T1 || kind == kMkCol1
+             ? 1
+             : kind == kMkRow2 || kind == kMkColWn2x32 || kind == kMkRow16T2 || kind == kMkCol2
+                   ? 2
+                   : kind == kMkRow4 || kind == kMkRow16T4 || kind == kMkCol4 ? 4 : 8;
+}
+__host__ __device__ constexpr int many_c(int kind) {
+  return kind == kMkRow1 || kind == kMkRow2 || kind == kMkColWn1x32 || kind == kMkColWn2x32 || kind == kMkRowT1 ||
+                 kind == kMkCol1 || kind == kMkCol2
+             ? 32
+             : kind == kMkRow4 || kind == kMkColWn1x16 || kind == kMkCol4
+                   ? 16
+                   : kind == kMkRow8 || kind == kMkCol8 ? 8 : 128;
+}
+// elements one item moves
+__host__ __device__ constexpr int many_item_elems(int kind) {
+  return kind == kMkRow16T1 || kind == kMkRow16T2 || kind == kMkRow16T4 ? 128 * 16 * many_r(kind)
+         : kind == kMkRow128 || kind == kMkCol128                       ? 128 * 128
+                                                                        : many_c(kind) * 256 * many_r(kind);
+}
+struct ManyItem {
+  int kind;   // ManyKind, | kMkList for listed rows
+  int xf;     // transform (maps at 4 xf); listed rows: first row-list entry
+  int tile;   // tile of the transform's pass
+  int count;  // listed rows: transforms in the item; kMkColWn*: W_N table index
+};
+// Two-level W_N tables of one 1D size (W_N^e = hi[e >> shift] lo[e & mask]), per direction.
+struct ManyWn {
+  const float2* lo[2];
+  const float2* hi[2];
+  int shift;
+  int nmask;
+};
+constexpr int kManyMaxWn = 8;
+struct ManyParams {
+  const CUtensorMap* maps;  // [4 per transform], 64-byte aligned, global memory
+  const ManyItem* items;
+  int n_items;
+  const int* row_list;      // transform indices of listed-row items
+  const float2* tw2048;     // W_2048^j of the direction
+  ManyWn wn[kManyMaxWn];
+  int dir;
+  float dsign;
+  int* err;
+  unsigned long long wait_ns;
+};
+// One pass over `n_items` work items (grid: one CTA per SM at most).
+cudaError_t launch_many(const ManyParams& p, int num_sms, cudaStream_t st);
+
 // Reference input-order contract (tcfft_permute.cu).
 std::vector<int> reference_radices_1d(int64_t n);
 std::vector<int> reference_radices_2d_axis(int64_t n);

@@ -82,6 +82,26 @@ struct tcfftPlanImpl {
   cudaEvent_t join_ev[kBranches] = {};
   void* graph_ptr[4] = {};  // per (direction, normalisation)
   cudaGraphExec_t graph_exec[4] = {};
+  // tcfftPlanMany, plain precision, every shape supported: the two-pass many-shape
+  // executor (fft_many.cu) in place of the graph.  Per transform its element offset,
+  // shape and scratch offset (1D N >= 4096); device item lists of both passes, the
+  // row list, the transforms' tensor maps (re-encoded when the data pointer changes,
+  // through a pinned staging copy) and the W_N tables of the 1D sizes >= 4096.
+  struct ManyXf {
+    int rank;
+    int64_t nx, ny, off, soff;
+  };
+  bool many_ok = false;
+  std::vector<ManyXf> many_xf;
+  tcfft::ManyItem* many_items = nullptr;  // pass A items, then pass B items
+  int many_n[2] = {0, 0};
+  int* many_rows = nullptr;
+  CUtensorMap* many_maps = nullptr;
+  CUtensorMap* many_hmaps = nullptr;      // pinned
+  void* many_maps_ptr = nullptr;
+  void* many_scratch = nullptr;
+  float2* many_wn_buf = nullptr;
+  tcfft::ManyWn many_wn[tcfft::kManyMaxWn] = {};
   // tcfftExecuteHost: sub-plans for the chunk batches (created on first use), copy-in,
   // compute and copy-out streams, per-chunk events
   static constexpr int kHostChunks = 16;

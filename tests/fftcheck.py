@@ -83,3 +83,19 @@ def oracle_1d(xq, adjoint=False):
 
 def oracle_2d(xq, adjoint=False):
     return oracle.fft_2d(to_complex(xq), sign=+1 if adjoint else -1)
+
+
+def tone_input(n, count, seed=0):
+    """Three unit-amplitude complex tones (bins and phases from default_rng(seed + 100)) over
+    N(0, 1e-3) noise, float64 [count, n, 2]: the size sweep's tone variant; |X_k| ~ n at the
+    tone bins, so fp16 output overflows from n ~ 2^16."""
+    rng = np.random.default_rng(seed + 100)
+    bins = rng.integers(0, n, 3)
+    phases = rng.uniform(0, 2 * np.pi, 3)
+    idx = np.arange(n)
+    z = sum(np.exp(1j * (2 * np.pi * ((int(k) * idx) % n) / n + ph)) for k, ph in zip(bins, phases))
+    x = np.empty((count, n, 2))
+    noise = rng.normal(0.0, 1e-3, (count, n, 2))
+    x[..., 0] = z.real + noise[..., 0]
+    x[..., 1] = z.imag + noise[..., 1]
+    return x

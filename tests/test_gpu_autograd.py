@@ -91,3 +91,28 @@ def test_grad_vs_finite_differences(cuda_device):
             lm = (wt.double() * (ym[..., 0] ** 2 + ym[..., 1] ** 2)).sum().item()
         fd = (lp - lm) / (2 * h)
         assert abs(fd - g[b, i, c]) <= 2e-3 * max(1.0, abs(g[b, i, c])) + 0.5, (b, i, c, fd, g[b, i, c])
+
+
+def test_grad_on_two_streams_and_input_untouched(cuda_device):
+    """Two streams differentiating the same shape at once get plans of their own
+    (the scratch ring of a plan is not shared by concurrent transforms), and the
+    out-of-place passes leave x unmodified."""
+    batch, n = 16, 1 << 16
+    xs = [quantize(uniform_input((batch, n), seed=20 + k), "plain") for k in range(2)]
+    w = np.random.default_rng(3).uniform(0, 1, (batch, n)) / n
+    wt = torch.from_numpy(w).float().to(cuda_device)
+    streams = [torch.cuda.Stream(), torch.cuda.Stream()]
+    xt = [torch.from_numpy(x).half().to(cuda_device).requires_grad_(True) for x in xs]
+    keep = [t.detach().clone() for t in xt]
+    torch.cuda.synchronize()
+    for s, t in zip(streams, xt):
+        with torch.cuda.stream(s):
+            loss_fn(ag.fft(t, "plain"), wt).backward()
+    torch.cuda.synchronize()
+    for t, k, x in zip(xt, keep, xs):
+        assert torch.equal(t.detach(), k), "the forward pass modified its input"
+        g = t.grad.double().cpu().numpy()
+        ref = fp64_grad(x, w, 1)
+        assert np.linalg.norm(g - ref) / np.linalg.norm(ref) < 3e-3
+    keys = [k for k in ag._CACHE if k[1] == n]
+    assert len({k[-1] for k in keys}) >= 2, "both streams used one plan"

@@ -122,3 +122,107 @@ def test_autotune(cuda_device, tmp_path):
     assert err < tol_plain(n)
     with open(cache) as f:
         assert "|" in f.read()
+
+
+def test_autotune_decomposition(cuda_device, tmp_path):
+    """The tuner times the 1D decompositions N1 x N2 and item sizes, then the lag; the
+    choice is cached as "key|lag|N1|item KiB" and reused by a later plan."""
+    cache = str(tmp_path / "tune.txt")
+    n, batch = 1 << 20, 6
+    rng = np.random.default_rng(5)
+    xq = quantize(rng.uniform(-1, 1, (batch, n, 2)), "plain")
+    with tc.Plan(n=n, batch=batch, autotune=True, tune_cache_path=cache) as p:
+        text = p.info["schedule"]
+        assert "tuned: N1=" in text, text
+        t = torch.from_numpy(xq).half().cuda()
+        p.exec(t)
+        p.check_device()
+    err = oracle.rel_l2(to_complex(t.double().cpu().numpy()), oracle.fft_1d(to_complex(xq)))
+    assert err < tol_plain(n)
+    with open(cache) as f:
+        fields = f.read().strip().split("|")
+    assert len(fields) == 4 and int(fields[2]) in (512, 1024, 2048) and int(fields[3]) in (32, 64), fields
+    with tc.Plan(n=n, batch=batch, autotune=True, tune_cache_path=cache) as p2:
+        assert p2.info["schedule"] == text  # served from the cache
+
+
+def test_autotune_cache_file_forms(cuda_device, tmp_path):
+    """Older "key|lag" lines still load; a cached decomposition the build cannot run
+    (N1 = 4096 leaves N2 = 128) falls back to the built-in schedule."""
+    n = 1 << 19
+    cache = tmp_path / "tune.txt"
+    cache.write_text("1 %d 1 3 0|1.600\n1 %d 1 5 0|1.000|4096|64\n" % (n, n))
+    rng = np.random.default_rng(9)
+    for batch, expect in ((3, "lag x1.6"), (5, "lag x1]")):
+        xq = quantize(rng.uniform(-1, 1, (batch, n, 2)), "plain")
+        with tc.Plan(n=n, batch=batch, autotune=True, tune_cache_path=str(cache)) as p:
+            assert expect in p.info["schedule"], p.info["schedule"]
+            t = torch.from_numpy(xq).half().cuda()
+            p.exec(t)
+            p.check_device()
+        err = oracle.rel_l2(to_complex(t.double().cpu().numpy()), oracle.fft_1d(to_complex(xq)))
+        assert err < tol_plain(n)
+
+
+# Shapes of every work-item kind of the persistent many-shape passes (fft_many.cu):
+# 1D 256..2048 listed rows, 4096..16384 / 2^15 / 2^16 column + row phases, 2D rows and
+# columns of 128..2048 (128: the 16-per-warp kinds).
+PASS_SHAPES = [(256,), (512,), (1024,), (2048,), (4096,), (8192,), (16384,), (1 << 15,), (1 << 16,),
+               (128, 128), (128, 256), (256, 128), (512, 1024), (1024, 512), (2048, 256), (256, 2048),
+               (128, 2048), (2048, 128), (256,), (2048,), (4096,), (1 << 16,)]
+
+
+@pytest.mark.parametrize("adjoint", [False, True])
+def test_many_pass_every_kind(cuda_device, adjoint):
+    """One plan over every kind, at gapped offsets (gaps untouched), forward and
+    adjoint, each transform against FP64; at most two launches per execute."""
+    shapes = PASS_SHAPES
+    parts, _ = pack(shapes, 21, "plain")
+    offsets, at = [], 0
+    for s in shapes:
+        offsets.append(at)
+        at += int(np.prod(s)) + 96  # a 384-byte gap after every transform
+    buf = torch.full((at, 2), 5.0, dtype=torch.float16, device="cuda")
+    for x, o in zip(parts, offsets):
+        buf[o:o + x.reshape(-1, 2).shape[0]] = torch.from_numpy(x.reshape(-1, 2)).half()
+    with tc.Plan.many(shapes, offsets=offsets) as p:
+        assert "persistent" in p.info["schedule"], p.info["schedule"]
+        assert p.info["launches_per_exec"] <= 2
+        p.exec(buf, adjoint=adjoint)
+        p.check_device()
+    got = buf.double().cpu().numpy()
+    ys = [got[o:o + int(np.prod(s))].reshape(tuple(s) + (2,)) for s, o in zip(shapes, offsets)]
+    check(parts, ys, "plain", adjoint=adjoint)
+    for s, o in zip(shapes, offsets):
+        e = o + int(np.prod(s))
+        assert (got[e:e + 96] == 5.0).all(), "gap after %s written" % (s,)
+
+
+def test_many_pass_agrees_with_graph(cuda_device, monkeypatch):
+    """The persistent passes and the per-shape graph (TCFFT_MANY_GRAPH=1) both meet
+    each transform's bound on the uneven-batch workload; the normalised execute of a
+    pass plan takes the graph."""
+    shapes = mixed_shapes()
+    parts, flat = pack(shapes, 7, "plain")
+    base = torch.from_numpy(flat).half().cuda()
+    outs = {}
+    for mode in ("pass", "graph"):
+        if mode == "graph":
+            monkeypatch.setenv("TCFFT_MANY_GRAPH", "1")
+        with tc.Plan.many(shapes) as p:
+            assert ("persistent" in p.info["schedule"]) == (mode == "pass"), p.info["schedule"]
+            buf = base.clone()
+            p.exec(buf)
+            p.check_device()
+            outs[mode] = buf.double().cpu().numpy()
+            check(parts, unpack(outs[mode], shapes), "plain")
+    monkeypatch.delenv("TCFFT_MANY_GRAPH")
+    with tc.Plan.many(shapes, normalize=True) as p:
+        buf = base.clone()
+        p.exec(buf)
+        p.check_device()
+        ys = unpack(buf.double().cpu().numpy(), shapes)
+    for x, y in zip(parts, ys):
+        n = int(np.prod(x.shape[:-1]))
+        ref = (oracle.fft_1d(to_complex(x)) if x.ndim == 2 else oracle.fft_2d(to_complex(x))) / n
+        assert oracle.rel_l2(to_complex(y), ref) < tol_plain(n)
