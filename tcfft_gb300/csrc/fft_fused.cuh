@@ -212,9 +212,11 @@ struct WnTable {
 // JNW: columns per call (default C/8: the 8 warps share the tile in one call; 2 with
 // 32-column tiles: two calls per warp, `warp` and `warp + 8`, fewer live registers).
 // wscale (WN only) multiplies the W_N factors: the outputs come out scaled by it.
-template <int R, int C, bool WN, class PI, class RHO, int JNW = C / 8>
+// WnT: the W_N lookup (WnTable, or any functor int e -> W_N^e).
+template <int R, int C, bool WN, class PI, class RHO, int JNW = C / 8, class WnT = WnTable>
 __device__ __forceinline__ void plain_col_tile(const JobConsts<false>& jc, uint32_t fold, uint32_t base, int warp,
-                                               float dsign, int n2base, const WnTable& wn, float wscale = 1.f) {
+                                               float dsign, int n2base, const WnT& wn, float wscale = 1.f,
+                                               const float2* tglob = nullptr) {
   constexpr int ES = 4, JN = JNW;
   static_assert(JN * 8 == C || (JN == 2 && C == 32), "columns per call");
   constexpr bool PAIR = JN % 2 == 0;
@@ -276,7 +278,7 @@ __device__ __forceinline__ void plain_col_tile(const JobConsts<false>& jc, uint3
         sts128(so[osl] + q * kStep, pack_h2(v0.x, v0.y), pack_h2(v1.x, v1.y), pack_h2(v2.x, v2.y),
                pack_h2(v3.x, v3.y));
       };
-      fft256r_jobs_fold_quad<R>(jc, fold, dsign, ld, st);
+      fft256r_jobs_fold_quad<R>(jc, fold, dsign, ld, st, tglob);
     } else if constexpr (PAIR) {
       auto ld = [&](int jp, int sl, int a, uint32_t& x0, uint32_t& x1) { lds64(lo[sl] + jp * ES + a * kStep, x0, x1); };
       auto st = [&](int jp, int osl, int q, float2 v0, float2 v1) {
@@ -284,13 +286,13 @@ __device__ __forceinline__ void plain_col_tile(const JobConsts<false>& jc, uint3
         v1 = cmul(v1, wfac(jp + 1, osl, q));
         sts_pair<false>(so[osl] + jp * ES + q * kStep, v0, v1);
       };
-      fft256r_jobs_fold<R, JN, true>(jc, fold, dsign, ld, st);
+      fft256r_jobs_fold<R, JN, true>(jc, fold, dsign, ld, st, tglob);
     } else {
       auto ld = [&](int jn, int sl, int a) { return lds32(lo[sl] + jn * ES + a * kStep); };
       auto st = [&](int jn, int osl, int q, float2 v) {
         sts_elem<false>(so[osl] + jn * ES + q * kStep, cmul(v, wfac(jn, osl, q)));
       };
-      fft256r_jobs_fold<R, JN, false>(jc, fold, dsign, ld, st);
+      fft256r_jobs_fold<R, JN, false>(jc, fold, dsign, ld, st, tglob);
     }
   } else {
     if constexpr (QUAD) {
@@ -306,17 +308,17 @@ __device__ __forceinline__ void plain_col_tile(const JobConsts<false>& jc, uint3
         sts128(so[osl] + q * kStep, pack_h2(v0.x, v0.y), pack_h2(v1.x, v1.y), pack_h2(v2.x, v2.y),
                pack_h2(v3.x, v3.y));
       };
-      fft256r_jobs_fold_quad<R>(jc, fold, dsign, ld, st);
+      fft256r_jobs_fold_quad<R>(jc, fold, dsign, ld, st, tglob);
     } else if constexpr (PAIR) {
       auto ld = [&](int jp, int sl, int a, uint32_t& x0, uint32_t& x1) { lds64(lo[sl] + jp * ES + a * kStep, x0, x1); };
       auto st = [&](int jp, int osl, int q, float2 v0, float2 v1) {
         sts_pair<false>(so[osl] + jp * ES + q * kStep, v0, v1);
       };
-      fft256r_jobs_fold<R, JN, true>(jc, fold, dsign, ld, st);
+      fft256r_jobs_fold<R, JN, true>(jc, fold, dsign, ld, st, tglob);
     } else {
       auto ld = [&](int jn, int sl, int a) { return lds32(lo[sl] + jn * ES + a * kStep); };
       auto st = [&](int jn, int osl, int q, float2 v) { sts_elem<false>(so[osl] + jn * ES + q * kStep, v); };
-      fft256r_jobs_fold<R, JN, false>(jc, fold, dsign, ld, st);
+      fft256r_jobs_fold<R, JN, false>(jc, fold, dsign, ld, st, tglob);
     }
   }
 }
@@ -325,13 +327,14 @@ __device__ __forceinline__ void plain_col_tile(const JobConsts<false>& jc, uint3
 // (out[jn][q][osl], packed half2) for the caller to store.
 template <int R, int JN, class PI, class RHO>
 __device__ __forceinline__ void plain_row_jobs(const JobConsts<false>& jc, uint32_t fold, uint32_t row_addr0,
-                                               uint32_t row_stride, float dsign, uint32_t (&out)[JN][R][8]) {
+                                               uint32_t row_stride, float dsign, uint32_t (&out)[JN][R][8],
+                                               const float2* tglob = nullptr) {
   uint32_t lo[8];
 #pragma unroll
   for (int sl = 0; sl < 8; ++sl) lo[sl] = row_addr0 + swz_w<4>(slot_m<PI, RHO>(sl)) * 4;
   auto ld = [&](int jn, int sl, int a) { return lds32(lo[sl] + jn * row_stride + a * 1024); };
   auto st = [&](int jn, int osl, int q, float2 v) { out[jn][q][osl] = pack_h2(v.x, v.y); };
-  fft256r_jobs_fold<R, JN, false>(jc, fold, dsign, ld, st);
+  fft256r_jobs_fold<R, JN, false>(jc, fold, dsign, ld, st, tglob);
 }
 
 // Tiles per work item of a 1D row-transpose schedule: as many tiles as fill an

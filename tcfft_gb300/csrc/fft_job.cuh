@@ -266,7 +266,7 @@ __device__ void build_fold_table(unsigned char* tab, const float2* __restrict__ 
 // LOAD(0, slot, a, x0, x1, x2, x3) and STORE(0, osl, q, v0, v1, v2, v3).
 template <int R, int JN, bool PAIR, class LoadF, class StoreF, bool QUAD = false>
 __device__ __forceinline__ void fft256r_jobs_fold_impl(const JobConsts<false>& c, uint32_t tab, float dsign,
-                                                       LoadF&& load, StoreF&& store) {
+                                                       LoadF&& load, StoreF&& store, const float2* tglob) {
   static_assert(!PAIR || JN % 2 == 0, "paired jobs come in twos");
   static_assert(!QUAD || (PAIR && JN == 4), "quads are four paired jobs");
   const uint32_t lane4 = (threadIdx.x & 31) * 4;
@@ -321,9 +321,12 @@ __device__ __forceinline__ void fft256r_jobs_fold_impl(const JobConsts<false>& c
       for (int h = 0; h < 2; ++h)
 #pragma unroll
         for (int r = 0; r < 2; ++r) {
+          // T_q from the table's T part in shared memory or, with tglob, from a copy of it in
+          // global memory (same [q - 1][slot][lane] layout)
+          const int ti = ((q - 1) * 8 + 4 * kt + 2 * h + r) * 32;
           const float2 w = q == 0 ? c.tw1[kt][h][r]
-                                  : lds64f(tab + FoldTab<R>::kABytes + ((q - 1) * 8 + 4 * kt + 2 * h + r) * 256 +
-                                           lane4 * 2);
+                           : tglob ? __ldg(tglob + ti + (threadIdx.x & 31))
+                                   : lds64f(tab + FoldTab<R>::kABytes + ti * 8 + lane4 * 2);
 #pragma unroll
           for (int jn = 0; jn < JN; ++jn) {
             const float2 v = cmul(acc_get(acc[jn], kt, h, r), w);
@@ -354,17 +357,18 @@ __device__ __forceinline__ void fft256r_jobs_fold_impl(const JobConsts<false>& c
   }
 }
 
+// tglob: the fold table's T part in global memory (nullptr: in shared memory after the A part).
 template <int R, int JN, bool PAIR, class LoadF, class StoreF>
 __device__ __forceinline__ void fft256r_jobs_fold(const JobConsts<false>& c, uint32_t tab, float dsign, LoadF&& load,
-                                                  StoreF&& store) {
+                                                  StoreF&& store, const float2* tglob = nullptr) {
   fft256r_jobs_fold_impl<R, JN, PAIR, LoadF, StoreF, false>(c, tab, dsign, static_cast<LoadF&&>(load),
-                                                            static_cast<StoreF&&>(store));
+                                                            static_cast<StoreF&&>(store), tglob);
 }
 template <int R, class LoadF, class StoreF>
 __device__ __forceinline__ void fft256r_jobs_fold_quad(const JobConsts<false>& c, uint32_t tab, float dsign,
-                                                       LoadF&& load, StoreF&& store) {
+                                                       LoadF&& load, StoreF&& store, const float2* tglob = nullptr) {
   fft256r_jobs_fold_impl<R, 4, true, LoadF, StoreF, true>(c, tab, dsign, static_cast<LoadF&&>(load),
-                                                          static_cast<StoreF&&>(store));
+                                                          static_cast<StoreF&&>(store), tglob);
 }
 
 }  // namespace tcfft

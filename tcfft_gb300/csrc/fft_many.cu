@@ -3,7 +3,7 @@
 //
 // An uneven batch (1D transforms of 256..65536 points and 2D transforms with
 // axes of 128..2048, at arbitrary 128-byte-aligned offsets of one buffer) runs
-// as two launches of this kernel:
+// as one launch of this kernel over two passes per transform:
 //   pass A: 1D N <= 2048 whole (rows of 256R, several transforms per item),
 //           1D N >= 4096 phase 0 (columns of N1, times W_N, into a scratch
 //           region of the transform), 2D rows;
@@ -15,9 +15,16 @@
 // two-phase executor (fft_fused.cuh) and of the 16R-point jobs (fft_job.cuh).
 //
 // CTA = 8 compute warps + 1 TMA-load warp + 1 TMA-store warp (the two-phase
-// executor's structure, without cross-CTA counters: the pass boundary is the
-// kernel boundary).  Items are taken round-robin (item CTA + k * grid); the host
-// orders them by kind, so that the CTAs run one kind at a time.
+// executor's structure).  The items form one sequence in which a transform's
+// pass-B items follow its pass-A items a few hundred items later, so that its
+// intermediate is read back from L2.  Each CTA's producer claims the next item
+// from a global counter when a stage is free and hands its descriptor to the
+// compute and store warps with the stage (kind -1 ends the CTA's work); a pass-B
+// item is loaded once its transform's completion counter shows every pass-A item
+// stored (release by the storer after the stores complete, acquire by the
+// producer; bounded waits).  Pass-A items wait for nothing and are loaded as soon
+// as they are claimed, so every wait ends.
+
 #include <mutex>
 
 #include "fft_fused.cuh"
@@ -30,17 +37,34 @@ using MPI = BitPerm<0, 1, 3, 2>;  // the plain two-phase executor's slot permuta
 using MRHO = BitPerm<0, 2, 3, 1>;
 
 constexpr int kManyStage = 64 * 1024;  // bytes of one ring stage (the largest item)
-// shared-memory tables: the plain fold tables of R = 2, 4, 8 (A and T parts)
+// shared-memory tables: the plain fold tables of R = 2 and 4 and the A part of R = 8's;
+// the T part of R = 8's is read from global memory (ManyParams::fold8_t), which leaves
+// room for three stages
 constexpr int kFold2 = 0, kFold4 = kFold2 + FoldTab<2>::kBytes, kFold8 = kFold4 + FoldTab<4>::kBytes;
-constexpr int kManyTab = kFold8 + FoldTab<8>::kBytes;
+constexpr int kWn3 = kFold8 + FoldTab<8>::kABytes;  // W_65536 in three levels: hi[64], mid[32], lo[32]
+constexpr int kManyTab = kWn3 + 128 * 8;
 constexpr int kManyBudget = 225 * 1024 - kManyTab - 1024 - 256;
 constexpr int kManyStages = kManyBudget / kManyStage >= 3 ? 3 : kManyBudget / kManyStage;
 static_assert(kManyStages >= 2, "at least two ring stages");
 constexpr int kManySmem = kManyStages * kManyStage + kManyTab + 1024 + 256;
+static_assert(3 * 8 * kManyStages + 16 * kManyStages <= 256, "barriers and descriptors fit the tail");
 
 __device__ __forceinline__ uint32_t fold_of(uint32_t tab, int R) {
   return tab + (R == 2 ? kFold2 : R == 4 ? kFold4 : kFold8);
 }
+
+// W_N^e for any N dividing 65536, from W_65536 in three shared-memory levels:
+// W_65536^x = hi[x >> 10] mid[(x >> 5) & 31] lo[x & 31], x = e (65536 / N) mod 65536.
+struct Wn3 {
+  uint32_t tab;  // hi at tab, mid at tab + 512, lo at tab + 768
+  int scale;     // log2(65536 / N)
+  int nmask;     // N - 1
+  __device__ __forceinline__ float2 operator()(int e) const {
+    const int x = (e & nmask) << scale;
+    return cmul(cmul(lds64f(tab + (x >> 10) * 8), lds64f(tab + 512 + ((x >> 5) & 31) * 8)),
+                lds64f(tab + 768 + (x & 31) * 8));
+  }
+};
 
 // ---------------------------------------------------------------- job bodies (compute warps)
 
@@ -48,11 +72,11 @@ __device__ __forceinline__ uint32_t fold_of(uint32_t tab, int R) {
 // executor's row role).
 template <int R, int C>
 __device__ __forceinline__ void many_rows(const JobConsts<false>& jc, uint32_t fold, uint32_t base, int warp,
-                                          float dsign) {
+                                          float dsign, const float2* tglob = nullptr) {
   constexpr int JN = C / 8;
   const uint32_t rb0 = base + (uint32_t)(warp * 256 * R * 4);
   uint32_t out[JN][R][8];
-  plain_row_jobs<R, JN, MPI, MRHO>(jc, fold, rb0, 8 * 256 * R * 4, dsign, out);
+  plain_row_jobs<R, JN, MPI, MRHO>(jc, fold, rb0, 8 * 256 * R * 4, dsign, out, tglob);
 #pragma unroll
   for (int jn = 0; jn < JN; ++jn)
 #pragma unroll
@@ -155,40 +179,45 @@ __device__ __forceinline__ const CUtensorMap* tmap_acquire(const CUtensorMap* m,
   return m;
 }
 
+__device__ __forceinline__ int ilog2_small(int v) { return v >= 8 ? 3 : v >= 4 ? 2 : v >= 2 ? 1 : 0; }
+// Bytes of one tile of a (non-listed) kind.
+__device__ __forceinline__ uint32_t tile_bytes(int kind) { return (uint32_t)many_item_elems(kind) * 4u; }
+
 // Bytes an item moves (listed rows: `count` transforms of 256R points).
 __device__ __forceinline__ uint32_t item_bytes(const ManyItem& it) {
   const int kind = it.kind & 0xff;
   if (it.kind & kMkList) return (uint32_t)it.count * 256u * (uint32_t)many_r(kind) * 4u;
-  return (uint32_t)many_item_elems(kind) * 4u;
+  return (uint32_t)it.nsub * tile_bytes(kind);
 }
 
 __device__ __forceinline__ void many_load(const ManyParams& p, const ManyItem& it, unsigned char* dst, uint64_t* bar) {
   const int kind = it.kind & 0xff;
-  const CUtensorMap* m = p.maps + 4 * (size_t)it.xf;
   const int R = many_r(kind), C = many_c(kind);
-  if (it.kind & kMkList) {  // whole transforms of 256R points (<= 64 rows of 128 bytes: one box each)
-    for (int j = 0; j < it.count; ++j)
-      tma_load_2d(dst + j * (256 * R * 4), tmap_acquire(p.maps + 4 * (size_t)p.row_list[it.xf + j], 1), 0, 0, bar);
+  if (it.kind & kMkList) {  // whole transforms of 256R points, one box each, through the buffer-wide map
+    const CUtensorMap* bm = tmap_acquire(p.maps + 4 * (size_t)p.n_xf + ilog2_small(R), 1);
+    for (int j = 0; j < it.count; ++j) tma_load_2d(dst + j * (256 * R * 4), bm, 0, p.row_list[it.xf + j], bar);
     return;
   }
-  tmap_acquire(m, 4);
+  const CUtensorMap* m = tmap_acquire(p.maps + 4 * (size_t)it.xf, 4);
+  const uint32_t tb = tile_bytes(kind);
   switch (kind) {
     case kMkRow1: case kMkRow2: case kMkRow4: case kMkRow8: {  // consecutive rows of one transform
       const int rows = C * 256 * R / 32, bh = rows < 256 ? rows : 256;
-      for (int i = 0; i < rows / bh; ++i) tma_load_2d(dst + i * bh * 128, m, 0, it.tile * rows + i * bh, bar);
+      for (int i = 0; i < it.nsub * rows / bh; ++i)
+        tma_load_2d(dst + i * bh * 128, m, 0, it.tile * rows + i * bh, bar);
       break;
     }
     case kMkColWn1x16: case kMkColWn1x32: case kMkColWn2x32:
-      tma_load_5d(dst, m, it.tile * C, 0, 0, 0, 0, bar);
+      for (int u = 0; u < it.nsub; ++u) tma_load_5d(dst + u * tb, m, (it.tile + u) * C, 0, 0, 0, 0, bar);
       break;
-    case kMkRowT1:  // 32 rows of 256 from the scratch: 256 rows of 128 bytes
-      tma_load_2d(dst, m + 2, 0, it.tile * 256, bar);
+    case kMkRowT1:  // 32 rows of 256 from the scratch: 256 rows of 128 bytes per tile
+      for (int u = 0; u < it.nsub; ++u) tma_load_2d(dst + u * tb, m + 2, 0, (it.tile + u) * 256, bar);
       break;
-    case kMkRow16T1: case kMkRow16T2: case kMkRow16T4:  // 128 rows of 16R: 64R rows of 128 bytes
-      tma_load_2d(dst, m + 2, 0, it.tile * 64 * R, bar);
+    case kMkRow16T1: case kMkRow16T2: case kMkRow16T4:  // 128 rows of 16R: 64R rows of 128 bytes per tile
+      for (int u = 0; u < it.nsub; ++u) tma_load_2d(dst + u * tb, m + 2, 0, (it.tile + u) * 64 * R, bar);
       break;
     case kMkCol1: case kMkCol2: case kMkCol4: case kMkCol8:
-      tma_load_5d(dst, m + 2, it.tile * C, 0, 0, 0, 0, bar);
+      for (int u = 0; u < it.nsub; ++u) tma_load_5d(dst + u * tb, m + 2, (it.tile + u) * C, 0, 0, 0, 0, bar);
       break;
     case kMkRow128:  // 128 rows of 128 points: 512 rows of 128 bytes, two boxes
       tma_load_2d(dst, m, 0, it.tile * 512, bar);
@@ -204,31 +233,34 @@ __device__ __forceinline__ void many_load(const ManyParams& p, const ManyItem& i
 
 __device__ __forceinline__ void many_store(const ManyParams& p, const ManyItem& it, const unsigned char* src) {
   const int kind = it.kind & 0xff;
-  const CUtensorMap* m = p.maps + 4 * (size_t)it.xf;
   const int R = many_r(kind), C = many_c(kind);
   if (it.kind & kMkList) {
-    for (int j = 0; j < it.count; ++j)
-      tma_store_2d(tmap_acquire(p.maps + 4 * (size_t)p.row_list[it.xf + j], 1), 0, 0, src + j * (256 * R * 4));
+    const CUtensorMap* bm = tmap_acquire(p.maps + 4 * (size_t)p.n_xf + ilog2_small(R), 1);
+    for (int j = 0; j < it.count; ++j) tma_store_2d(bm, 0, p.row_list[it.xf + j], src + j * (256 * R * 4));
     return;
   }
-  tmap_acquire(m, 4);
+  const CUtensorMap* m = tmap_acquire(p.maps + 4 * (size_t)it.xf, 4);
+  const uint32_t tb = tile_bytes(kind);
   switch (kind) {
     case kMkRow1: case kMkRow2: case kMkRow4: case kMkRow8: {
       const int rows = C * 256 * R / 32, bh = rows < 256 ? rows : 256;
-      for (int i = 0; i < rows / bh; ++i) tma_store_2d(m, 0, it.tile * rows + i * bh, src + i * bh * 128);
+      for (int i = 0; i < it.nsub * rows / bh; ++i)
+        tma_store_2d(m, 0, it.tile * rows + i * bh, src + i * bh * 128);
       break;
     }
     case kMkColWn1x16: case kMkColWn1x32: case kMkColWn2x32:  // into the transform's scratch
-      tma_store_5d(m + 1, it.tile * C, 0, 0, 0, 0, src);
+      for (int u = 0; u < it.nsub; ++u) tma_store_5d(m + 1, (it.tile + u) * C, 0, 0, 0, 0, src + u * tb);
       break;
     case kMkRowT1:  // output columns k1 of [N2 rows k2][N1 cols k1]
-      tma_store_5d(m + 3, it.tile * C, 0, 0, 0, 0, src);
+      for (int u = 0; u < it.nsub; ++u) tma_store_5d(m + 3, (it.tile + u) * C, 0, 0, 0, 0, src + u * tb);
       break;
     case kMkRow16T1: case kMkRow16T2: case kMkRow16T4:  // 4D [N1][k0][q][1], boxes of 32 columns
-      for (int bx = 0; bx < 4; ++bx) tma_store_4d(m + 3, it.tile * 128 + bx * 32, 0, 0, 0, src + bx * (32 * 16 * R * 4));
+      for (int u = 0; u < it.nsub; ++u)
+        for (int bx = 0; bx < 4; ++bx)
+          tma_store_4d(m + 3, (it.tile + u) * 128 + bx * 32, 0, 0, 0, src + u * tb + bx * (32 * 16 * R * 4));
       break;
     case kMkCol1: case kMkCol2: case kMkCol4: case kMkCol8:
-      tma_store_5d(m + 3, it.tile * C, 0, 0, 0, 0, src);
+      for (int u = 0; u < it.nsub; ++u) tma_store_5d(m + 3, (it.tile + u) * C, 0, 0, 0, 0, src + u * tb);
       break;
     case kMkRow128:
       tma_store_2d(m, 0, it.tile * 512, src);
@@ -251,6 +283,7 @@ __global__ void __launch_bounds__(384, 1) fft_many_kernel(const __grid_constant_
   uint64_t* full = reinterpret_cast<uint64_t*>(s_tab + kManyTab);
   uint64_t* computed = full + NST;
   uint64_t* empty = computed + NST;
+  ManyItem* s_meta = reinterpret_cast<ManyItem*>(empty + NST);  // descriptor of each stage's item
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const unsigned long long lim = p.wait_ns ? p.wait_ns : kTimeoutNs;
 
@@ -264,7 +297,8 @@ __global__ void __launch_bounds__(384, 1) fft_many_kernel(const __grid_constant_
   }
   build_fold_table<2, MPI, MRHO>(s_tab + kFold2, p.tw2048, tid, blockDim.x);
   build_fold_table<4, MPI, MRHO>(s_tab + kFold4, p.tw2048, tid, blockDim.x);
-  build_fold_table<8, MPI, MRHO>(s_tab + kFold8, p.tw2048, tid, blockDim.x);
+  build_fold_table<8, MPI, MRHO, false>(s_tab + kFold8, p.tw2048, tid, blockDim.x);
+  if (tid < 128) reinterpret_cast<float2*>(s_tab + kWn3)[tid] = p.wn3[p.dir][tid];
   __syncthreads();
 
   if (warp >= 8) asm volatile("setmaxnreg.dec.sync.aligned.u32 %0;" ::"n"(56));
@@ -273,34 +307,103 @@ __global__ void __launch_bounds__(384, 1) fft_many_kernel(const __grid_constant_
     // ------------------------------------------------------------ TMA producer
     if (lane == 0) {
       int cnt = 0;
-      for (int idx = blockIdx.x; idx < p.n_items; idx += gridDim.x) {
-        const ManyItem it = p.items[idx];
+      bool failed = false;
+      // the next item is claimed, read and its maps prefetched before the wait for a free
+      // stage, so that their latency overlaps the work already in flight
+      auto claim = [&](ManyItem& it) {
+        const int idx = atomicAdd(p.claim, 1);
+        if (idx >= p.n_items) {
+          it.kind = -1;
+          return;
+        }
+        it = p.items[idx];
+        if (!(it.kind & kMkList)) {
+          const CUtensorMap* m = p.maps + 4 * (size_t)it.xf;
+          for (int i = 0; i < 4; ++i) prefetch_tmap(m + i);
+        }
+      };
+      ManyItem it;
+      claim(it);
+      while (true) {
         const int s = cnt % NST;
-        if (!mbar_wait(&empty[s], ((cnt / NST) + 1) & 1, p.err, lim)) break;
+        if (!mbar_wait(&empty[s], ((cnt / NST) + 1) & 1, p.err, lim)) {
+          failed = true;
+          break;
+        }
+        if (it.kind < 0) {  // the end of the work: a descriptor of kind -1, no bytes
+          s_meta[s].kind = -1;
+          mbar_arrive(&full[s]);
+          break;
+        }
+        if (it.kind & kMkB) {  // every pass-A item of the transform stored
+          if (!wait_counter(&p.done[it.xf], it.count, p.err, lim)) {
+            failed = true;
+            break;
+          }
+          fence_proxy_async_global();
+        }
         unsigned char* dst = smem + s * kManyStage;
+        s_meta[s] = it;  // published to the other warps by the arrive below
         mbar_arrive_expect_tx(&full[s], item_bytes(it));
         many_load(p, it, dst, &full[s]);
         ++cnt;
+        claim(it);
       }
-      // on an early exit let the loads still in flight land before the CTA ends (bounded)
-      for (int i = (cnt > NST ? cnt - NST : 0); i < cnt; ++i) mbar_wait(&full[i % NST], (i / NST) & 1, nullptr);
+      // on an early exit let the loads still in flight land before the CTA ends (bounded); on the
+      // normal exit the compute warps have waited for every load
+      if (failed)
+        for (int i = (cnt > NST ? cnt - NST : 0); i < cnt; ++i) mbar_wait(&full[i % NST], (i / NST) & 1, nullptr);
     }
     return;
   }
   if (warp == 9) {
     // ------------------------------------------------------------ TMA storer
+    // A pass-A item's completion is released (done[xf] += 1) once its stores are
+    // complete: up to kMaxPending stay in flight, and before the storer blocks it
+    // releases every pending one, so a producer waiting on this CTA's output never
+    // waits behind this CTA's own pipeline.
     if (lane == 0) {
+      constexpr int kMaxPending = 2;
+      int* pend[kMaxPending + 1];
+      int npend = 0;
+      auto release_all = [&]() {
+        if (npend == 0) return;
+        bulk_wait<0>();
+        fence_proxy_async_global();
+        for (int i = 0; i < npend; ++i)
+          if (pend[i]) red_release_add(pend[i], 1);
+        npend = 0;
+      };
+      auto wait_stage = [&](uint64_t* bar, uint32_t par) {
+        if (mbar_try_wait(bar, par)) return true;
+        release_all();
+        return mbar_wait(bar, par, p.err, lim);
+      };
       int cnt = 0;
-      for (int idx = blockIdx.x; idx < p.n_items; idx += gridDim.x) {
-        const ManyItem it = p.items[idx];
+      while (true) {
         const int s = cnt % NST;
-        if (!mbar_wait(&computed[s], (cnt / NST) & 1, p.err, lim)) break;
+        // the stage's descriptor first (the end of the work has no computed phase)
+        if (!wait_stage(&full[s], (cnt / NST) & 1)) break;
+        const ManyItem it = s_meta[s];
+        if (it.kind < 0) break;
+        if (!wait_stage(&computed[s], (cnt / NST) & 1)) break;
         many_store(p, it, smem + s * kManyStage);
         bulk_commit();
+        if (it.kind & kMkRelease) pend[npend++] = &p.done[it.xf];
+        else if (npend > 0) pend[npend++] = nullptr;  // keeps the groups and entries in step
         bulk_wait_read<0>();  // the stage has been read: the producer may refill it
         mbar_arrive(&empty[s]);
+        if (npend > kMaxPending) {
+          // the oldest group is complete once at most kMaxPending remain
+          bulk_wait<kMaxPending>();
+          fence_proxy_async_global();
+          if (pend[0]) red_release_add(pend[0], 1);
+          for (int i = 1; i < npend; ++i) pend[i - 1] = pend[i];
+          --npend;
+        }
         ++cnt;
       }
+      release_all();
       bulk_wait<0>();
     }
     return;
@@ -312,33 +415,34 @@ __global__ void __launch_bounds__(384, 1) fft_many_kernel(const __grid_constant_
   init_job_consts<false, MPI, MRHO>(jc, p.tw2048);
   const uint32_t tab = smem_addr(s_tab);
   int cnt = 0;
-  for (int idx = blockIdx.x; idx < p.n_items; idx += gridDim.x) {
-    const ManyItem it = p.items[idx];
+  while (true) {
     const int s = cnt % NST;
     const bool ok = named_bar_and(2, 256, mbar_wait(&full[s], (cnt / NST) & 1, p.err, lim));
-    const uint32_t base = smem_addr(smem + s * kManyStage);
-    if (ok) {
-      const int kind = it.kind & 0xff;
+    const ManyItem it = s_meta[s];
+    if (ok && it.kind < 0) break;  // end of the pass (every compute warp sees the same descriptor)
+    const uint32_t stage = smem_addr(smem + s * kManyStage);
+    const int kind = it.kind & 0xff;
+    const int nsub = (it.kind & kMkList) ? 1 : it.nsub;
+#pragma unroll 1
+    for (int u = 0; ok && u < nsub; ++u) {
+      const uint32_t base = stage + u * tile_bytes(kind);
+      const int tile = it.tile + u;
       switch (kind) {
         case kMkRow1: many_rows<1, 32>(jc, tab, base, warp, p.dsign); break;
         case kMkRow2: many_rows<2, 32>(jc, fold_of(tab, 2), base, warp, p.dsign); break;
         case kMkRow4: many_rows<4, 16>(jc, fold_of(tab, 4), base, warp, p.dsign); break;
-        case kMkRow8: many_rows<8, 8>(jc, fold_of(tab, 8), base, warp, p.dsign); break;
+        case kMkRow8: many_rows<8, 8>(jc, fold_of(tab, 8), base, warp, p.dsign, p.fold8_t[p.dir]); break;
         case kMkColWn1x16: case kMkColWn1x32: case kMkColWn2x32: {
-          const ManyWn& w = p.wn[it.count];
-          WnTable wn;
-          wn.hi = wn.lo = 0;
-          wn.ghi = w.hi[p.dir];
-          wn.glo = w.lo[p.dir];
-          wn.global = true;
-          wn.shift = w.shift;
-          wn.nmask = w.nmask;
+          Wn3 wn;
+          wn.tab = tab + kWn3;
+          wn.nmask = p.wn[it.wn].nmask;
+          wn.scale = 16 - (31 - __clz(wn.nmask + 1));
           if (kind == kMkColWn1x16)
-            plain_col_tile<1, 16, true, MPI, MRHO>(jc, tab, base, warp, p.dsign, it.tile * 16, wn);
+            plain_col_tile<1, 16, true, MPI, MRHO, 2, Wn3>(jc, tab, base, warp, p.dsign, tile * 16, wn);
           else if (kind == kMkColWn1x32)
-            plain_col_tile<1, 32, true, MPI, MRHO>(jc, tab, base, warp, p.dsign, it.tile * 32, wn);
+            plain_col_tile<1, 32, true, MPI, MRHO, 4, Wn3>(jc, tab, base, warp, p.dsign, tile * 32, wn);
           else
-            plain_col_tile<2, 32, true, MPI, MRHO>(jc, fold_of(tab, 2), base, warp, p.dsign, it.tile * 32, wn);
+            plain_col_tile<2, 32, true, MPI, MRHO, 4, Wn3>(jc, fold_of(tab, 2), base, warp, p.dsign, tile * 32, wn);
           break;
         }
         case kMkRowT1: many_rows_t<1, 32>(jc, tab, base, warp, p.dsign); break;
@@ -358,7 +462,8 @@ __global__ void __launch_bounds__(384, 1) fft_many_kernel(const __grid_constant_
           else if (kind == kMkCol4)
             plain_col_tile<4, 16, false, MPI, MRHO>(jc, fold_of(tab, 4), base, warp, p.dsign, 0, wn);
           else
-            plain_col_tile<8, 8, false, MPI, MRHO>(jc, fold_of(tab, 8), base, warp, p.dsign, 0, wn);
+            plain_col_tile<8, 8, false, MPI, MRHO>(jc, fold_of(tab, 8), base, warp, p.dsign, 0, wn, 1.f,
+                                                   p.fold8_t[p.dir]);
           break;
         }
         case kMkRow128: many_rows128(jc, fold_of(tab, 8), base, warp, p.dsign); break;
@@ -374,7 +479,19 @@ __global__ void __launch_bounds__(384, 1) fft_many_kernel(const __grid_constant_
   }
 }
 
+__global__ void __launch_bounds__(256) many_fold8_kernel(unsigned char* out, const float2* tw2048) {
+  build_fold_table<8, MPI, MRHO>(out, tw2048, threadIdx.x, blockDim.x);
+}
+
 }  // namespace
+
+int many_stages() { return kManyStages; }
+int many_fold8_bytes() { return FoldTab<8>::kBytes; }
+int many_fold8_t_offset() { return FoldTab<8>::kABytes; }
+cudaError_t many_fold8_init(unsigned char* out, const float2* tw2048, cudaStream_t st) {
+  many_fold8_kernel<<<1, 256, 0, st>>>(out, tw2048);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_many(const ManyParams& p, int num_sms, cudaStream_t st) {
   static std::once_flag once;

@@ -215,6 +215,12 @@ void free_tables(tcfftPlanImpl* p) {
   p->cap_stream = nullptr;
   if (p->many_items) cudaFree(p->many_items);
   if (p->many_rows) cudaFree(p->many_rows);
+  if (p->many_claim) cudaFree(p->many_claim);
+  p->many_claim = nullptr;
+  if (p->many_fold8) cudaFree(p->many_fold8);
+  p->many_fold8 = nullptr;
+  if (p->many_wn3) cudaFree(p->many_wn3);
+  p->many_wn3 = nullptr;
   if (p->many_maps) cudaFree(p->many_maps);
   if (p->many_hmaps) cudaFreeHost(p->many_hmaps);
   if (p->many_scratch) cudaFree(p->many_scratch);
@@ -1267,46 +1273,110 @@ bool setup_many_pass(tcfftPlanImpl* p, int64_t count, const int32_t* ranks, cons
     }
   }
   if ((int)wn_sizes.size() > kManyMaxWn) return false;
-  // items: pass A then pass B, each ordered by kind (larger tiles first within a kind)
-  std::vector<ManyItem> items[2];
+  // Items: the listed 1D transforms (no pass B) first, then per transform its pass-A
+  // items, with its pass-B items following lag items later (its intermediate is still in
+  // L2 then and its pass A complete).  Transforms are taken in order of their kinds, so
+  // that the CTAs run at most a few kinds at a time.
+  std::vector<ManyItem> seq;
   std::vector<int> rows;
-  for (int pass = 0; pass < 2; ++pass) {
+  {
+    std::vector<int64_t> listed[kMkKinds];
+    std::vector<int64_t> order;
+    for (int64_t i = 0; i < count; ++i) {
+      const auto& t = xf[i];
+      const int k = many_kind_a(t.rank, t.nx, t.ny);
+      if (k & kMkList) listed[k & 0xff].push_back(i);
+      else order.push_back(i);
+    }
     for (int kind = 0; kind < kMkKinds; ++kind) {
-      std::vector<int64_t> listed;  // 1D transforms whose pass A is kind as listed rows
-      for (int64_t i = 0; i < count; ++i) {
-        const auto& t = xf[i];
-        const int k = pass == 0 ? many_kind_a(t.rank, t.nx, t.ny) : many_kind_b(t.rank, t.nx, t.ny);
-        if (k < 0 || (k & 0xff) != kind) continue;
-        if (k & kMkList) {
-          listed.push_back(i);
-          continue;
-        }
-        const int64_t tiles = many_tiles(kind, t.rank, t.nx, t.ny);
-        int wn = 0;
-        if (kind == kMkColWn1x16 || kind == kMkColWn1x32 || kind == kMkColWn2x32)
-          wn = (int)(std::find(wn_sizes.begin(), wn_sizes.end(), t.nx) - wn_sizes.begin());
-        for (int64_t tile = 0; tile < tiles; ++tile) items[pass].push_back({kind, (int)i, (int)tile, wn});
-      }
       const int C = many_c(kind);
-      for (size_t j = 0; j < listed.size(); j += C) {
-        const int cnt = (int)std::min<size_t>(C, listed.size() - j);
-        items[pass].push_back({kind | kMkList, (int)rows.size(), 0, cnt});
-        for (int q = 0; q < cnt; ++q) rows.push_back((int)listed[j + q]);
+      for (size_t j = 0; j < listed[kind].size(); j += C) {
+        const int cnt = (int)std::min<size_t>(C, listed[kind].size() - j);
+        seq.push_back({kind | kMkList, (int)rows.size(), 0, cnt, 1, 0, {0, 0}});
+        // the transform's offset in rows of 128 bytes (a coordinate of the buffer-wide maps)
+        for (int q = 0; q < cnt; ++q) rows.push_back((int)(xf[listed[kind][j + q]].off / 32));
       }
     }
+    auto kinds_of = [&](int64_t i) {
+      const auto& t = xf[i];
+      return std::make_pair(many_kind_a(t.rank, t.nx, t.ny), many_kind_b(t.rank, t.nx, t.ny));
+    };
+    std::stable_sort(order.begin(), order.end(), [&](int64_t a, int64_t b) { return kinds_of(a) < kinds_of(b); });
+    // lag (in items) between a transform's pass A and its pass B, in multiples of the SM
+    // count (TCFFT_MANY_LAG overrides it): on the uneven-batch workload 4 x gave 139 us, 6 x 130,
+    // 8 x 134 and 12 x 123 (a pass-B item that waits stalls its CTA's producer)
+    static const double lag_env = getenv("TCFFT_MANY_LAG") ? atof(getenv("TCFFT_MANY_LAG")) : 0.0;
+    const double lag_mult = lag_env > 0.0 ? lag_env : 10.0;
+    const size_t lag = (size_t)(lag_mult * (double)p->num_sms);
+    std::vector<std::pair<int64_t, size_t>> waiting;  // (transform, sequence length after its pass A)
+    size_t head = 0;
+    // consecutive tiles of a transform share an item up to one 64 KiB stage
+    auto sub_of = [](int kind) {
+      const int per = (64 * 1024) / (many_item_elems(kind) * 4);
+      return per < 1 ? 1 : per;
+    };
+    auto items_of = [&](int kind, int64_t tiles) { return (tiles + sub_of(kind) - 1) / sub_of(kind); };
+    auto emit_b = [&](int64_t i) {
+      const auto& t = xf[i];
+      const auto k = kinds_of(i);
+      const int na = (int)items_of(k.first, many_tiles(k.first, t.rank, t.nx, t.ny));
+      const int64_t tiles = many_tiles(k.second, t.rank, t.nx, t.ny);
+      for (int64_t tile = 0; tile < tiles; tile += sub_of(k.second)) {
+        const int nsub = (int)std::min<int64_t>(sub_of(k.second), tiles - tile);
+        seq.push_back({k.second | kMkB, (int)i, (int)tile, na, nsub, 0, {0, 0}});
+      }
+    };
+    for (int64_t i : order) {
+      const auto& t = xf[i];
+      const auto k = kinds_of(i);
+      int wn = 0;
+      if (k.first == kMkColWn1x16 || k.first == kMkColWn1x32 || k.first == kMkColWn2x32)
+        wn = (int)(std::find(wn_sizes.begin(), wn_sizes.end(), t.nx) - wn_sizes.begin());
+      const int64_t tiles = many_tiles(k.first, t.rank, t.nx, t.ny);
+      for (int64_t tile = 0; tile < tiles; tile += sub_of(k.first)) {
+        const int nsub = (int)std::min<int64_t>(sub_of(k.first), tiles - tile);
+        seq.push_back({k.first | kMkRelease, (int)i, (int)tile, 0, nsub, wn, {0, 0}});
+      }
+      waiting.push_back({i, seq.size()});
+      while (head < waiting.size() && waiting[head].second + lag <= seq.size()) emit_b(waiting[head++].first);
+    }
+    while (head < waiting.size()) emit_b(waiting[head++].first);
   }
   // device arrays
-  const size_t nit = items[0].size() + items[1].size();
+  const size_t nit = seq.size();
   if (cudaMalloc(&p->many_items, std::max<size_t>(nit, 1) * sizeof(ManyItem)) != cudaSuccess ||
       cudaMalloc(&p->many_rows, std::max<size_t>(rows.size(), 1) * sizeof(int)) != cudaSuccess ||
-      cudaMalloc(&p->many_maps, (size_t)count * 4 * sizeof(CUtensorMap)) != cudaSuccess ||
-      cudaMallocHost(&p->many_hmaps, (size_t)count * 4 * sizeof(CUtensorMap)) != cudaSuccess ||
+      cudaMalloc(&p->many_maps, (size_t)(count + 1) * 4 * sizeof(CUtensorMap)) != cudaSuccess ||
+      cudaMallocHost(&p->many_hmaps, (size_t)(count + 1) * 4 * sizeof(CUtensorMap)) != cudaSuccess ||
       (soff > 0 && cudaMalloc(&p->many_scratch, soff * 4) != cudaSuccess)) {
     cudaGetLastError();
     return false;
   }
-  std::vector<ManyItem> all(items[0]);
-  all.insert(all.end(), items[1].begin(), items[1].end());
+  const std::vector<ManyItem>& all = seq;
+  {  // W_65536 in three levels, both directions (fp32 from long double)
+    std::vector<float2> w3(256);
+    const long double twopi = 2.0L * 3.141592653589793238462643383279502884L;
+    for (int d = 0; d < 2; ++d)
+      for (int i = 0; i < 128; ++i) {
+        const int e = i < 64 ? i * 1024 : i < 96 ? (i - 64) * 32 : i - 96;
+        const long double th = twopi * (long double)e / 65536.0L;
+        w3[d * 128 + i] = make_float2((float)cosl(th), (float)((d == 0 ? -1.0L : 1.0L) * sinl(th)));
+      }
+    if (cudaMalloc(&p->many_wn3, 256 * sizeof(float2)) != cudaSuccess ||
+        cudaMemcpy(p->many_wn3, w3.data(), 256 * sizeof(float2), cudaMemcpyHostToDevice) != cudaSuccess) {
+      cudaGetLastError();
+      return false;
+    }
+  }
+  if (cudaMalloc(&p->many_claim, (size_t)(count + 1) * sizeof(int)) != cudaSuccess ||
+      cudaMalloc(&p->many_fold8, 2 * (size_t)many_fold8_bytes()) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  for (int d = 0; d < 2; ++d)
+    if (many_fold8_init(p->many_fold8 + d * many_fold8_bytes(), p->tables.tw2048[d], nullptr) != cudaSuccess)
+      return false;
+  if (cudaDeviceSynchronize() != cudaSuccess) return false;
   if ((nit && cudaMemcpy(p->many_items, all.data(), nit * sizeof(ManyItem), cudaMemcpyHostToDevice) != cudaSuccess) ||
       (!rows.empty() &&
        cudaMemcpy(p->many_rows, rows.data(), rows.size() * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess))
@@ -1346,8 +1416,8 @@ bool setup_many_pass(tcfftPlanImpl* p, int64_t count, const int32_t* ranks, cons
       return false;
   }
   p->many_xf = std::move(xf);
-  p->many_n[0] = (int)items[0].size();
-  p->many_n[1] = (int)items[1].size();
+  p->many_n[0] = (int)seq.size();
+  p->many_n[1] = 0;
   p->scratch_bytes += soff * 4;
   p->many_ok = true;
   return true;
@@ -1371,7 +1441,7 @@ CUresult encode_many_maps(tcfftPlanImpl* p, void* data) {
       return encode_tmap(mm, dt, 2, b, dims, str, box, CU_TENSOR_MAP_SWIZZLE_128B);
     };
     if (t.rank == 1 && t.nx <= 2048) {
-      r = rows_map(&m[0], base, t.nx, t.nx / 32);
+      continue;  // listed: the buffer-wide maps below
     } else if (t.rank == 1) {
       const int64_t n1 = many_n1(t.nx), n2 = t.nx / n1;
       const int ka = many_kind_a(1, t.nx, 1), kb = many_kind_b(1, t.nx, 1);
@@ -1412,6 +1482,15 @@ CUresult encode_many_maps(tcfftPlanImpl* p, void* data) {
     }
     if (r != CUDA_SUCCESS) return r;
   }
+  // the whole buffer as rows of 128 bytes, boxes of one listed transform of 256 << i points
+  CUtensorMap* bm = p->many_hmaps + 4 * p->many_xf.size();
+  for (int i = 0; i < 4; ++i) {
+    uint64_t dims[2] = {32, (uint64_t)((p->span_elems + 31) / 32)};
+    uint64_t str[1] = {128};
+    uint32_t box[2] = {32, (uint32_t)(8 << i)};
+    const CUresult r = encode_tmap(&bm[i], dt, 2, d, dims, str, box, CU_TENSOR_MAP_SWIZZLE_128B);
+    if (r != CUDA_SUCCESS) return r;
+  }
   return CUDA_SUCCESS;
 }
 
@@ -1420,7 +1499,7 @@ tcfftStatus exec_many_pass(tcfftPlanImpl* plan, void* data, cudaStream_t st, int
     // the staging copy may still be read by an earlier execute's copy: let it finish first
     if (cuda_status(cudaStreamSynchronize(st), "many maps")) return TCFFT_CUDA_ERROR;
     if (cu_status(encode_many_maps(plan, data), "many maps")) return TCFFT_CUDA_ERROR;
-    const size_t bytes = plan->many_xf.size() * 4 * sizeof(CUtensorMap);
+    const size_t bytes = (plan->many_xf.size() + 1) * 4 * sizeof(CUtensorMap);
     if (cuda_status(cudaMemcpyAsync(plan->many_maps, plan->many_hmaps, bytes, cudaMemcpyHostToDevice, st),
                     "many maps"))
       return TCFFT_CUDA_ERROR;
@@ -1430,18 +1509,26 @@ tcfftStatus exec_many_pass(tcfftPlanImpl* plan, void* data, cudaStream_t st, int
   memset(&mp, 0, sizeof mp);
   mp.maps = plan->many_maps;
   mp.row_list = plan->many_rows;
+  mp.n_xf = (int)plan->many_xf.size();
   mp.tw2048 = plan->tables.tw2048[dir];
   for (int w = 0; w < kManyMaxWn; ++w) mp.wn[w] = plan->many_wn[w];
+  for (int d = 0; d < 2; ++d) {
+    mp.fold8_t[d] = reinterpret_cast<const float2*>(plan->many_fold8 + d * many_fold8_bytes() + many_fold8_t_offset());
+    mp.wn3[d] = plan->many_wn3 + 128 * d;
+  }
   mp.dir = dir;
   mp.dsign = dir == 0 ? 1.f : -1.f;
   mp.err = plan->tables.err;
   mp.wait_ns = plan->wait_ns;
-  for (int pass = 0; pass < 2; ++pass) {
-    mp.items = plan->many_items + (pass == 0 ? 0 : plan->many_n[0]);
-    mp.n_items = plan->many_n[pass];
-    if (mp.n_items == 0) continue;
-    if (cuda_status(launch_many(mp, plan->num_sms, st), "many pass")) return TCFFT_CUDA_ERROR;
-  }
+  // the claim counter and the per-transform completion counters start at zero
+  const int64_t ntf = (int64_t)plan->many_xf.size();
+  if (cuda_status(cudaMemsetAsync(plan->many_claim, 0, (size_t)(ntf + 1) * sizeof(int), st), "many counters"))
+    return TCFFT_CUDA_ERROR;
+  mp.items = plan->many_items;
+  mp.n_items = plan->many_n[0];
+  mp.claim = plan->many_claim + ntf;
+  mp.done = plan->many_claim;
+  if (cuda_status(launch_many(mp, plan->num_sms, st), "many launch")) return TCFFT_CUDA_ERROR;
   return TCFFT_SUCCESS;
 }
 
@@ -1788,11 +1875,11 @@ tcfftStatus tcfftPlanMany(tcfftPlan* out, int64_t count, const int32_t* ranks, c
   p->sched.text = buf;
   if (setup_many_pass(p, count, ranks, nx, ny, offsets)) {
     // the graph stays for normalised executes
-    p->sched.launches = (p->many_n[0] > 0) + (p->many_n[1] > 0);
+    p->sched.launches = 1;
     snprintf(buf, sizeof buf,
-             "many(%s): %lld transforms, persistent many-shape passes: %d + %d work items, %d launches "
+             "many(%s): %lld transforms, one persistent many-shape launch of %d work items "
              "(normalised: %d sub-plans in a graph)",
-             prec_name(o.precision), (long long)count, p->many_n[0], p->many_n[1], p->sched.launches, nsub);
+             prec_name(o.precision), (long long)count, p->many_n[0], nsub);
     p->sched.text = buf;
   }
   *out = p;

@@ -116,7 +116,8 @@ cudaError_t launch_c2r_pre(const void* x, void* z, int64_t batch, int64_t h, con
 // Kinds of work item of the plain-precision executor of tcfftPlanMany: each is one
 // tile of one transform's pass (or, for kMkRow* with kMkList, up to C whole 1D
 // transforms of 256R points listed in the row list).  Pass A: rows / 1D column
-// phase; pass B: 1D row phase / 2D columns.  Per transform, four tensor maps:
+// phase; pass B: 1D row phase / 2D columns, started once the transform's pass-A
+// items are complete (one launch, per-transform counters).  Per transform, four tensor maps:
 // [0] pass-A load (and in-place store), [1] pass-A store to scratch (1D),
 // [2] pass-B load, [3] pass-B store.
 enum ManyKind : int {
@@ -129,6 +130,8 @@ enum ManyKind : int {
   kMkKinds
 };
 constexpr int kMkList = 0x100;  // kind flag: the item's rows are whole transforms from the row list
+constexpr int kMkB = 0x200;     // kind flag: a pass-B item; waits until done[xf] reaches `count`
+constexpr int kMkRelease = 0x400;  // kind flag: a pass-A item of a transform with a pass B (adds 1 to done[xf])
 // kind -> R (points / 256, or / 16 for the 16R kinds), C (rows or columns per item)
 __host__ __device__ constexpr int many_r(int kind) {
   return kind == kMkRow1 || kind == kMkColWn1x16 || kind == kMkColWn1x32 || kind == kMkRowT1 ||
@@ -153,10 +156,13 @@ __host__ __device__ constexpr int many_item_elems(int kind) {
                                                                         : many_c(kind) * 256 * many_r(kind);
 }
 struct ManyItem {
-  int kind;   // ManyKind, | kMkList for listed rows
+  int kind;   // ManyKind | kMkList / kMkB / kMkRelease
   int xf;     // transform (maps at 4 xf); listed rows: first row-list entry
-  int tile;   // tile of the transform's pass
-  int count;  // listed rows: transforms in the item; kMkColWn*: W_N table index
+  int tile;   // first tile of the transform's pass
+  int count;  // listed rows: transforms in the item; kMkB: pass-A items of xf
+  int nsub;   // consecutive tiles in the item (one stage holds them side by side)
+  int wn;     // kMkColWn*: W_N table index
+  int pad[2];
 };
 // Two-level W_N tables of one 1D size (W_N^e = hi[e >> shift] lo[e & mask]), per direction.
 struct ManyWn {
@@ -170,16 +176,29 @@ struct ManyParams {
   const CUtensorMap* maps;  // [4 per transform], 64-byte aligned, global memory
   const ManyItem* items;
   int n_items;
-  const int* row_list;      // transform indices of listed-row items
+  int* claim;               // items are claimed in order from this counter (zero at launch)
+  int* done;                // per transform: completed pass-A items (zero at launch)
+  const int* row_list;      // listed rows: each transform's offset in 128-byte rows of the buffer
+  int n_xf;                 // transforms; maps[4 n_xf + i] view the whole buffer as rows of 8 << i rows
+                            // of 128 bytes (the listed transforms of 256 << i points)
   const float2* tw2048;     // W_2048^j of the direction
+  const float2* fold8_t[2]; // T part of the R = 8 fold table, per direction (many_fold8_init)
+  const float2* wn3[2];     // per direction: W_65536^(1024 i) (i < 64), W_65536^(32 i), W_65536^i (i < 32)
   ManyWn wn[kManyMaxWn];
   int dir;
   float dsign;
   int* err;
   unsigned long long wait_ns;
 };
-// One pass over `n_items` work items (grid: one CTA per SM at most).
+// One launch over `n_items` work items (grid: one CTA per SM at most).
 cudaError_t launch_many(const ManyParams& p, int num_sms, cudaStream_t st);
+// Stages of the executor's ring (the host's lag between a transform's two passes).
+int many_stages();
+// The R = 8 fold table (A and T parts, many_fold8_bytes()) of W_2048 table `tw2048` into
+// global memory `out`; the T part starts many_fold8_t_offset() bytes in.
+int many_fold8_bytes();
+int many_fold8_t_offset();
+cudaError_t many_fold8_init(unsigned char* out, const float2* tw2048, cudaStream_t st);
 
 // Reference input-order contract (tcfft_permute.cu).
 std::vector<int> reference_radices_1d(int64_t n);

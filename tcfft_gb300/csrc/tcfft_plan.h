@@ -93,14 +93,17 @@ struct tcfftPlanImpl {
   };
   bool many_ok = false;
   std::vector<ManyXf> many_xf;
-  tcfft::ManyItem* many_items = nullptr;  // pass A items, then pass B items
-  int many_n[2] = {0, 0};
+  tcfft::ManyItem* many_items = nullptr;  // the item sequence of the one launch
+  int many_n[2] = {0, 0};                 // [0]: items
   int* many_rows = nullptr;
+  int* many_claim = nullptr;               // per transform its completed pass-A items, then the claim counter
   CUtensorMap* many_maps = nullptr;
   CUtensorMap* many_hmaps = nullptr;      // pinned
   void* many_maps_ptr = nullptr;
   void* many_scratch = nullptr;
   float2* many_wn_buf = nullptr;
+  unsigned char* many_fold8 = nullptr;     // R = 8 fold tables of both directions
+  float2* many_wn3 = nullptr;              // W_65536 in three levels, both directions
   tcfft::ManyWn many_wn[tcfft::kManyMaxWn] = {};
   // tcfftExecuteHost: sub-plans for the chunk batches (created on first use), copy-in,
   // compute and copy-out streams, per-chunk events
