@@ -189,7 +189,8 @@ tcfftStatus tcfftCheckDevice(tcfftPlan plan, void* stream);
 
 /* Limit, in nanoseconds, of every bounded device-side wait of this plan's
  * two-phase kernels (the cross-CTA completion counters and the shared-memory
- * ring barriers); 0 restores the default of 2 s.  A wait that runs out stops
+ * ring barriers, and those of the one-launch uneven-batch plans); 0 restores the
+ * default of 2 s.  A wait that runs out stops
  * its kernel early and raises the flag tcfftCheckDevice reports as
  * TCFFT_TIMEOUT.  Applies to the plan's sub-plans too.  No counterpart in the
  * reference, whose kernels never wait on one another. */
@@ -200,7 +201,8 @@ tcfftStatus tcfftSetWaitLimit(tcfftPlan plan, int64_t limit_ns);
  * that no number of completed tiles raises to its target, so the waits on it
  * run out after the wait limit and tcfftCheckDevice returns TCFFT_TIMEOUT.
  * Nothing faults; the output of that one execute is undefined, later executes
- * are unaffected.  Two-phase schedules only (others: TCFFT_NOT_SUPPORTED). */
+ * are unaffected.  Two-phase schedules and the one-launch uneven-batch plans of
+ * tcfftPlanMany with a transform of two passes (others: TCFFT_NOT_SUPPORTED). */
 tcfftStatus tcfftInjectWaitTimeout(tcfftPlan plan);
 
 tcfftStatus tcfftDestroy(tcfftPlan plan);

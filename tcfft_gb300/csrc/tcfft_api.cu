@@ -1415,6 +1415,8 @@ bool setup_many_pass(tcfftPlanImpl* p, int64_t count, const int32_t* ranks, cons
     if (cudaMemcpy(p->many_wn_buf, h.data(), wn_elems * sizeof(float2), cudaMemcpyHostToDevice) != cudaSuccess)
       return false;
   }
+  for (int64_t i = 0; i < count && p->many_xf_b < 0; ++i)
+    if (many_kind_b(xf[i].rank, xf[i].nx, xf[i].ny) >= 0) p->many_xf_b = (int)i;
   p->many_xf = std::move(xf);
   p->many_n[0] = (int)seq.size();
   p->many_n[1] = 0;
@@ -1524,6 +1526,11 @@ tcfftStatus exec_many_pass(tcfftPlanImpl* plan, void* data, cudaStream_t st, int
   const int64_t ntf = (int64_t)plan->many_xf.size();
   if (cuda_status(cudaMemsetAsync(plan->many_claim, 0, (size_t)(ntf + 1) * sizeof(int), st), "many counters"))
     return TCFFT_CUDA_ERROR;
+  if (plan->inject_timeout) {  // test hook: one transform's pass B waits for a count that never comes
+    plan->inject_timeout = false;
+    if (cuda_status(cudaMemsetAsync(plan->many_claim + plan->many_xf_b, 0x80, sizeof(int), st), "inject"))
+      return TCFFT_CUDA_ERROR;
+  }
   mp.items = plan->many_items;
   mp.n_items = plan->many_n[0];
   mp.claim = plan->many_claim + ntf;
@@ -2087,7 +2094,9 @@ tcfftStatus tcfftSetWaitLimit(tcfftPlan plan, int64_t limit_ns) {
 
 tcfftStatus tcfftInjectWaitTimeout(tcfftPlan plan) {
   if (!plan || plan->magic != tcfftPlanImpl::kMagic) return TCFFT_INVALID_PLAN;
-  if (plan->sched.kind != Schedule::kFused1d && plan->sched.kind != Schedule::kFused2d) return TCFFT_NOT_SUPPORTED;
+  const bool many = plan->kind == 3 && plan->many_ok && plan->many_xf_b >= 0;
+  if (plan->sched.kind != Schedule::kFused1d && plan->sched.kind != Schedule::kFused2d && !many)
+    return TCFFT_NOT_SUPPORTED;
   plan->inject_timeout = true;
   return TCFFT_SUCCESS;
 }

@@ -68,3 +68,45 @@ def test_noalloc_check_reports_clean_state(cuda_device):
     y = t.double().cpu().numpy()
     assert oracle.rel_l2(y[..., 0] + 1j * y[..., 1], oracle_1d(xq)) < tol_plain(n)
     assert np.isfinite(y).all()
+
+
+def test_many_plan_wait_timeout_and_recovery(cuda_device):
+    """The one-launch uneven-batch plan: one transform's completion counter is preset so
+    that its pass-B items never become ready; their bounded waits run out (1 ms), the
+    launch ends early with TCFFT_TIMEOUT, and the next execute is correct."""
+    import torch
+    from fftcheck import to_complex
+    shapes = [(1024,), (512, 256), (1 << 16,), (256, 256), (4096,), (2048,)]
+    rng = np.random.default_rng(4)
+    parts = [quantize(rng.uniform(-1, 1, tuple(s) + (2,)), "plain") for s in shapes]
+    flat = np.concatenate([p.reshape(-1, 2) for p in parts])
+    with tc.Plan.many(shapes) as p:
+        assert "persistent" in p.info["schedule"], p.info["schedule"]
+        p.set_wait_limit(1_000_000)
+        p.inject_wait_timeout()
+        buf = torch.from_numpy(flat).half().cuda()
+        t0 = time.perf_counter()
+        p.exec(buf)
+        with pytest.raises(tc.TcfftError) as e:
+            p.check_device()
+        assert e.value.status == 6, e.value
+        assert time.perf_counter() - t0 < 10.0
+        p.set_wait_limit(0)
+        buf = torch.from_numpy(flat).half().cuda()
+        p.exec(buf)
+        p.check_device()
+        got = buf.double().cpu().numpy()
+    off = 0
+    for x, s in zip(parts, shapes):
+        n = int(np.prod(s))
+        y = got[off:off + n].reshape(tuple(s) + (2,))
+        ref = oracle.fft_1d(to_complex(x)) if len(s) == 1 else oracle.fft_2d(to_complex(x))
+        assert oracle.rel_l2(to_complex(y), ref) < tol_plain(n), s
+        off += n
+
+
+def test_many_plan_without_pass_b_has_no_hook(cuda_device):
+    with tc.Plan.many([(256,), (1024,)]) as p:
+        with pytest.raises(tc.TcfftError) as e:
+            p.inject_wait_timeout()
+        assert e.value.status == 7
