@@ -309,9 +309,13 @@ __global__ void __launch_bounds__(384, 1) fft_many_kernel(const __grid_constant_
       int cnt = 0;
       bool failed = false;
       // the next item is claimed, read and its maps prefetched before the wait for a free
-      // stage, so that their latency overlaps the work already in flight
+      // stage, so that their latency overlaps the work already in flight; in the last two
+      // rounds of the grid the claim waits for the free stage instead, so that no CTA sits on
+      // items that an idle CTA could run
+      int last = -1;
       auto claim = [&](ManyItem& it) {
         const int idx = atomicAdd(p.claim, 1);
+        last = idx;
         if (idx >= p.n_items) {
           it.kind = -1;
           return;
@@ -323,13 +327,15 @@ __global__ void __launch_bounds__(384, 1) fft_many_kernel(const __grid_constant_
         }
       };
       ManyItem it;
-      claim(it);
+      bool have = false;
       while (true) {
         const int s = cnt % NST;
         if (!mbar_wait(&empty[s], ((cnt / NST) + 1) & 1, p.err, lim)) {
           failed = true;
           break;
         }
+        if (!have) claim(it);
+        have = false;
         if (it.kind < 0) {  // the end of the work: a descriptor of kind -1, no bytes
           s_meta[s].kind = -1;
           mbar_arrive(&full[s]);
@@ -347,7 +353,10 @@ __global__ void __launch_bounds__(384, 1) fft_many_kernel(const __grid_constant_
         mbar_arrive_expect_tx(&full[s], item_bytes(it));
         many_load(p, it, dst, &full[s]);
         ++cnt;
-        claim(it);
+        if (last + 2 * (int)gridDim.x < p.n_items) {
+          claim(it);
+          have = true;
+        }
       }
       // on an early exit let the loads still in flight land before the CTA ends (bounded); on the
       // normal exit the compute warps have waited for every load

@@ -1340,7 +1340,12 @@ bool setup_many_pass(tcfftPlanImpl* p, int64_t count, const int32_t* ranks, cons
       waiting.push_back({i, seq.size()});
       while (head < waiting.size() && waiting[head].second + lag <= seq.size()) emit_b(waiting[head++].first);
     }
+    // the pass-B items left after the last pass A run largest first: the smallest finish the launch
+    const size_t tail = seq.size();
     while (head < waiting.size()) emit_b(waiting[head++].first);
+    std::stable_sort(seq.begin() + tail, seq.end(), [](const ManyItem& a, const ManyItem& b) {
+      return a.nsub * many_item_elems(a.kind & 0xff) > b.nsub * many_item_elems(b.kind & 0xff);
+    });
   }
   // device arrays
   const size_t nit = seq.size();
