@@ -1999,7 +1999,9 @@ tcfftStatus tcfftExecuteHost(tcfftPlan plan, const void* host_in, void* host_out
   const int64_t es = plan->precision != TCFFT_PRECISION_PLAIN ? 8 : 4;
   const int64_t per = plan->kind == 2 ? plan->nx * plan->ny : plan->n;  // elements per transform
   const int64_t total = (plan->kind == 3 ? plan->span_elems : plan->total_elems) * es;
-  const int K = plan->kind == 3 ? 1 : (int)std::min<int64_t>(tcfftPlanImpl::kHostChunks, plan->batch);
+  static const int env_chunks = getenv("TCFFT_HOST_CHUNKS") ? atoi(getenv("TCFFT_HOST_CHUNKS")) : 0;
+  const int chunks = env_chunks >= 1 && env_chunks <= tcfftPlanImpl::kHostChunks ? env_chunks : 16;
+  const int K = plan->kind == 3 ? 1 : (int)std::min<int64_t>(chunks, plan->batch);
   if (K <= 1) {  // unchunked
     if (cuda_status(cudaMemcpyAsync(work, host_in, total, cudaMemcpyHostToDevice, st), "copy in"))
       return TCFFT_CUDA_ERROR;

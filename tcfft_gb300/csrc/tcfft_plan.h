@@ -108,7 +108,7 @@ struct tcfftPlanImpl {
   tcfft::ManyWn many_wn[tcfft::kManyMaxWn] = {};
   // tcfftExecuteHost: sub-plans for the chunk batches (created on first use), copy-in,
   // compute and copy-out streams, per-chunk events
-  static constexpr int kHostChunks = 16;
+  static constexpr int kHostChunks = 32;  // most chunks (events); 16 used unless TCFFT_HOST_CHUNKS says otherwise
   tcfftPlanImpl* host_sub[2] = {nullptr, nullptr};  // chunk batches b0 and b0 + 1
   int64_t host_b0 = 0;
   cudaStream_t host_st[3] = {};
