@@ -444,7 +444,7 @@ __global__ void __launch_bounds__(384, 1) fft_many_kernel(const __grid_constant_
         case kMkColWn1x16: case kMkColWn1x32: case kMkColWn2x32: {
           Wn3 wn;
           wn.tab = tab + kWn3;
-          wn.nmask = p.wn[it.wn].nmask;
+          wn.nmask = it.wn;  // N - 1
           wn.scale = 16 - (31 - __clz(wn.nmask + 1));
           if (kind == kMkColWn1x16)
             plain_col_tile<1, 16, true, MPI, MRHO, 2, Wn3>(jc, tab, base, warp, p.dsign, tile * 16, wn);

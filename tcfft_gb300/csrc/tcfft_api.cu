@@ -224,13 +224,11 @@ void free_tables(tcfftPlanImpl* p) {
   if (p->many_maps) cudaFree(p->many_maps);
   if (p->many_hmaps) cudaFreeHost(p->many_hmaps);
   if (p->many_scratch) cudaFree(p->many_scratch);
-  if (p->many_wn_buf) cudaFree(p->many_wn_buf);
   p->many_items = nullptr;
   p->many_rows = nullptr;
   p->many_maps = nullptr;
   p->many_hmaps = nullptr;
   p->many_scratch = nullptr;
-  p->many_wn_buf = nullptr;
   p->many_ok = false;
   for (int b = 0; b < tcfftPlanImpl::kBranches; ++b) {
     if (p->branch[b]) cudaStreamDestroy(p->branch[b]);
@@ -1259,7 +1257,6 @@ bool setup_many_pass(tcfftPlanImpl* p, int64_t count, const int32_t* ranks, cons
   if (p->precision != TCFFT_PRECISION_PLAIN || getenv("TCFFT_MANY_GRAPH")) return false;
   if (count > (int64_t)1 << 24) return false;
   std::vector<tcfftPlanImpl::ManyXf> xf((size_t)count);
-  std::vector<int64_t> wn_sizes;
   int64_t soff = 0;
   for (int64_t i = 0; i < count; ++i) {
     const int r = ranks[i];
@@ -1269,10 +1266,8 @@ bool setup_many_pass(tcfftPlanImpl* p, int64_t count, const int32_t* ranks, cons
     if (r == 1 && x >= 4096) {
       xf[i].soff = soff;
       soff += x;
-      if (std::find(wn_sizes.begin(), wn_sizes.end(), x) == wn_sizes.end()) wn_sizes.push_back(x);
     }
   }
-  if ((int)wn_sizes.size() > kManyMaxWn) return false;
   // Items: the listed 1D transforms (no pass B) first, then per transform its pass-A
   // items, with its pass-B items following lag items later (its intermediate is still in
   // L2 then and its pass A complete).  Transforms are taken in order of their kinds, so
@@ -1331,7 +1326,7 @@ bool setup_many_pass(tcfftPlanImpl* p, int64_t count, const int32_t* ranks, cons
       const auto k = kinds_of(i);
       int wn = 0;
       if (k.first == kMkColWn1x16 || k.first == kMkColWn1x32 || k.first == kMkColWn2x32)
-        wn = (int)(std::find(wn_sizes.begin(), wn_sizes.end(), t.nx) - wn_sizes.begin());
+        wn = (int)(t.nx - 1);
       const int64_t tiles = many_tiles(k.first, t.rank, t.nx, t.ny);
       for (int64_t tile = 0; tile < tiles; tile += sub_of(k.first)) {
         const int nsub = (int)std::min<int64_t>(sub_of(k.first), tiles - tile);
@@ -1386,40 +1381,6 @@ bool setup_many_pass(tcfftPlanImpl* p, int64_t count, const int32_t* ranks, cons
       (!rows.empty() &&
        cudaMemcpy(p->many_rows, rows.data(), rows.size() * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess))
     return false;
-  // W_N tables of each 1D size >= 4096, both directions: lo then hi
-  int64_t wn_elems = 0;
-  for (int64_t n : wn_sizes) {
-    const int lg = ilog2_exact(n), shift = (lg + 1) / 2;
-    wn_elems += 2 * ((int64_t(1) << shift) + (n >> shift));
-  }
-  if (wn_elems > 0) {
-    std::vector<float2> h((size_t)wn_elems);
-    if (cudaMalloc(&p->many_wn_buf, wn_elems * sizeof(float2)) != cudaSuccess) return false;
-    int64_t at = 0;
-    for (size_t w = 0; w < wn_sizes.size(); ++w) {
-      const int64_t n = wn_sizes[w];
-      const int lg = ilog2_exact(n), shift = (lg + 1) / 2;
-      const int64_t nlo = int64_t(1) << shift, nhi = n >> shift;
-      p->many_wn[w].shift = shift;
-      p->many_wn[w].nmask = (int)(n - 1);
-      for (int d = 0; d < 2; ++d) {
-        const long double sgn = d == 0 ? -1.0L : 1.0L;
-        const long double twopi = 2.0L * 3.141592653589793238462643383279502884L;
-        p->many_wn[w].lo[d] = p->many_wn_buf + at;
-        for (int64_t j = 0; j < nlo; ++j, ++at) {
-          const long double th = twopi * (long double)j / (long double)n;
-          h[at] = make_float2((float)cosl(th), (float)(sgn * sinl(th)));
-        }
-        p->many_wn[w].hi[d] = p->many_wn_buf + at;
-        for (int64_t j = 0; j < nhi; ++j, ++at) {
-          const long double th = twopi * (long double)(j << shift) / (long double)n;
-          h[at] = make_float2((float)cosl(th), (float)(sgn * sinl(th)));
-        }
-      }
-    }
-    if (cudaMemcpy(p->many_wn_buf, h.data(), wn_elems * sizeof(float2), cudaMemcpyHostToDevice) != cudaSuccess)
-      return false;
-  }
   for (int64_t i = 0; i < count && p->many_xf_b < 0; ++i)
     if (many_kind_b(xf[i].rank, xf[i].nx, xf[i].ny) >= 0) p->many_xf_b = (int)i;
   p->many_xf = std::move(xf);
@@ -1518,7 +1479,6 @@ tcfftStatus exec_many_pass(tcfftPlanImpl* plan, void* data, cudaStream_t st, int
   mp.row_list = plan->many_rows;
   mp.n_xf = (int)plan->many_xf.size();
   mp.tw2048 = plan->tables.tw2048[dir];
-  for (int w = 0; w < kManyMaxWn; ++w) mp.wn[w] = plan->many_wn[w];
   for (int d = 0; d < 2; ++d) {
     mp.fold8_t[d] = reinterpret_cast<const float2*>(plan->many_fold8 + d * many_fold8_bytes() + many_fold8_t_offset());
     mp.wn3[d] = plan->many_wn3 + 128 * d;

@@ -161,17 +161,9 @@ struct ManyItem {
   int tile;   // first tile of the transform's pass
   int count;  // listed rows: transforms in the item; kMkB: pass-A items of xf
   int nsub;   // consecutive tiles in the item (one stage holds them side by side)
-  int wn;     // kMkColWn*: W_N table index
+  int wn;     // kMkColWn*: N - 1 of the transform (its W_N factors come from W_65536)
   int pad[2];
 };
-// Two-level W_N tables of one 1D size (W_N^e = hi[e >> shift] lo[e & mask]), per direction.
-struct ManyWn {
-  const float2* lo[2];
-  const float2* hi[2];
-  int shift;
-  int nmask;
-};
-constexpr int kManyMaxWn = 8;
 struct ManyParams {
   const CUtensorMap* maps;  // [4 per transform], 64-byte aligned, global memory
   const ManyItem* items;
@@ -184,7 +176,6 @@ struct ManyParams {
   const float2* tw2048;     // W_2048^j of the direction
   const float2* fold8_t[2]; // T part of the R = 8 fold table, per direction (many_fold8_init)
   const float2* wn3[2];     // per direction: W_65536^(1024 i) (i < 64), W_65536^(32 i), W_65536^i (i < 32)
-  ManyWn wn[kManyMaxWn];
   int dir;
   float dsign;
   int* err;

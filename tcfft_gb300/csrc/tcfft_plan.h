@@ -86,7 +86,7 @@ struct tcfftPlanImpl {
   // executor (fft_many.cu) in place of the graph.  Per transform its element offset,
   // shape and scratch offset (1D N >= 4096); device item lists of both passes, the
   // row list, the transforms' tensor maps (re-encoded when the data pointer changes,
-  // through a pinned staging copy) and the W_N tables of the 1D sizes >= 4096.
+  // through a pinned staging copy).
   struct ManyXf {
     int rank;
     int64_t nx, ny, off, soff;
@@ -102,10 +102,8 @@ struct tcfftPlanImpl {
   CUtensorMap* many_hmaps = nullptr;      // pinned
   void* many_maps_ptr = nullptr;
   void* many_scratch = nullptr;
-  float2* many_wn_buf = nullptr;
   unsigned char* many_fold8 = nullptr;     // R = 8 fold tables of both directions
   float2* many_wn3 = nullptr;              // W_65536 in three levels, both directions
-  tcfft::ManyWn many_wn[tcfft::kManyMaxWn] = {};
   // tcfftExecuteHost: sub-plans for the chunk batches (created on first use), copy-in,
   // compute and copy-out streams, per-chunk events
   static constexpr int kHostChunks = 32;  // most chunks (events); 16 used unless TCFFT_HOST_CHUNKS says otherwise
