@@ -314,9 +314,9 @@ int item_kb_1d(int lg, bool split) {
   static const int env = getenv("TCFFT_ITEM_KB") ? atoi(getenv("TCFFT_ITEM_KB")) : 0;
   if (g_item_kb_override == 32 || g_item_kb_override == 64) return g_item_kb_override;
   if (env == 32 || env == 64) return env;
-  (void)lg;
-  (void)split;
-  return 64;
+  // 2^16 plain (256 x 256): 32 KiB items with a deeper ring, 948 us per 2^28 elements against
+  // 1032 us (the autotuner's choice); 64 KiB elsewhere (its choice from 2^17 to 2^22)
+  return lg == 16 && !split ? 32 : 64;
 }
 
 // Host-only schedule selection for a 1D size (no CUDA calls).
