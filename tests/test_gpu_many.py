@@ -226,3 +226,28 @@ def test_many_pass_agrees_with_graph(cuda_device, monkeypatch):
         n = int(np.prod(x.shape[:-1]))
         ref = (oracle.fft_1d(to_complex(x)) if x.ndim == 2 else oracle.fft_2d(to_complex(x))) / n
         assert oracle.rel_l2(to_complex(y), ref) < tol_plain(n)
+
+
+def test_many_pass_out_of_place_and_host(cuda_device):
+    """Out of place (the input copied into the output buffer, then the one launch) equals
+    in place, leaves the input untouched, and so does the host-buffer execute."""
+    shapes = [(2048,), (1 << 15,), (128, 512), (1024, 256), (4096,)]
+    parts, flat = pack(shapes, 13, "plain")
+    with tc.Plan.many(shapes) as p:
+        src = torch.from_numpy(flat).half().cuda()
+        keep = src.clone()
+        ref = src.clone()
+        p.exec(ref)
+        out = torch.zeros_like(src)
+        p.exec_out(src, out)
+        p.check_device()
+        assert torch.equal(src, keep)
+        assert torch.equal(out, ref)
+        h_in = torch.from_numpy(flat).half().pin_memory()
+        h_out = torch.empty_like(h_in).pin_memory()
+        work = torch.empty_like(src)
+        p.exec_host(h_in, h_out, work)
+        torch.cuda.synchronize()
+        p.check_device()
+        assert torch.equal(h_out, ref.cpu())
+    check(parts, unpack(out.double().cpu().numpy(), shapes), "plain")
