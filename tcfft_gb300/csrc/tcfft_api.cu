@@ -1256,6 +1256,8 @@ bool setup_many_pass(tcfftPlanImpl* p, int64_t count, const int32_t* ranks, cons
                      const int64_t* offsets) {
   if (p->precision != TCFFT_PRECISION_PLAIN || getenv("TCFFT_MANY_GRAPH")) return false;
   if (count > (int64_t)1 << 24) return false;
+  // tensor-map coordinates are 32-bit: the buffer-wide maps address the span in rows of 128 bytes
+  if (p->span_elems / 32 > (int64_t)INT32_MAX - 256) return false;
   std::vector<tcfftPlanImpl::ManyXf> xf((size_t)count);
   int64_t soff = 0;
   for (int64_t i = 0; i < count; ++i) {
