@@ -48,6 +48,8 @@ int small_tile_elems(int R, int mode) {
     case 17: return SmallCfg<4, kModeSplit>::kTE;
     case 18: return SmallCfg<4, kModeIo32>::kTE;
     case 32: return SmallCfg<8, kModePlain>::kTE;
+    case 33: return SmallCfg<8, kModeSplit>::kTE;
+    case 34: return SmallCfg<8, kModeIo32>::kTE;
     default: return 0;
   }
 }
@@ -69,6 +71,8 @@ cudaError_t launch_small(int R, int mode, const CUtensorMap& tmap, const CUtenso
     TCFFT_SMALL(4, kModeSplit)
     TCFFT_SMALL(4, kModeIo32)
     TCFFT_SMALL(8, kModePlain)
+    TCFFT_SMALL(8, kModeSplit)
+    TCFFT_SMALL(8, kModeIo32)
     default: return cudaErrorInvalidValue;
   }
 #undef TCFFT_SMALL

@@ -35,7 +35,12 @@ struct SmallCfg {
   static constexpr int kER = 128 / kES;                  // elements per 128-byte row
   static constexpr int kBoxElems = kER * 256;            // one TMA box: 256 rows
   static constexpr int kJPW = kWide ? (R >= 2 ? 1 : 2) : (R >= 4 ? 1 : 4 / R);  // jobs per warp
-  static constexpr int kTE = 8 * kJPW * kN;              // elements per tile
+  // 8-byte elements at N = 2048: two warps per transform, each computing four of the eight
+  // radix-8 sub-transforms, so that a tile of four transforms is one 64 KiB stage
+  static constexpr bool kPair = kWide && R == 8;
+  static constexpr int kQH = kPair ? R / 2 : R;           // sub-transforms q per warp
+  static constexpr int kJobs = kPair ? 4 : 8 * kJPW;      // transforms per tile
+  static constexpr int kTE = kJobs * kN;                  // elements per tile
   static constexpr int kBoxes = kTE / kBoxElems;
   static constexpr int kTileBytes = kTE * kES;
   static constexpr int kStages = 3;
@@ -157,7 +162,8 @@ __global__ void __launch_bounds__(256, SmallCfg<R, MODE>::kMinBlocks)
 
 #pragma unroll 1
     for (int jj = 0; jj < (ok ? C::kJPW : 0); ++jj) {
-      const uint32_t job = smem_addr(tile_base) + (uint32_t)((warp * C::kJPW + jj) * C::kN * C::kES);
+      const int job_idx = C::kPair ? (warp >> 1) : warp * C::kJPW + jj;
+      const uint32_t job = smem_addr(tile_base) + (uint32_t)(job_idx * C::kN * C::kES);
       if constexpr (C::kFold) {
         // plain R > 1: radix-R butterfly on packed half2, twiddles folded into the
         // per-q tensor-core stages; outputs k = q + R k' collected, then stored as R-runs
@@ -182,8 +188,11 @@ __global__ void __launch_bounds__(256, SmallCfg<R, MODE>::kMinBlocks)
         continue;
       }
       // ---------------- load + radix-R (DIF) + twiddle -> B operands per tile q
-      uint32_t bhi[R][2][2][2], blo[SPLIT ? R : 1][2][2][2];
-      float2 xs[SPLIT ? R : 1][2][2][2];  // split: fp32 operands until the job's scale is known
+      // (kPair: this warp keeps the sub-transforms q0 .. q0 + QH - 1)
+      constexpr int QH = C::kQH;
+      const int q0 = C::kPair ? (warp & 1) * QH : 0;
+      uint32_t bhi[QH][2][2][2], blo[SPLIT ? QH : 1][2][2][2];
+      float2 xs[SPLIT ? QH : 1][2][2][2];  // split: fp32 operands until the job's scale is known
       float inv = 1.f;
 #pragma unroll
       for (int kt = 0; kt < 2; ++kt)
@@ -201,23 +210,22 @@ __global__ void __launch_bounds__(256, SmallCfg<R, MODE>::kMinBlocks)
                 if constexpr (WIDE) x[a] = lds64f(addr);
                 else x[a] = unpack_h2(lds32(addr));
               }
-              if constexpr (R > 1) {
-                dft_small<R>(x, p.dsign);
+              if constexpr (R > 1) dft_small<R>(x, p.dsign);
 #pragma unroll
-                for (int q = 1; q < R; ++q)
-                  x[q] = cmul(x[q], lds64f(s_tw_addr + ((mval[kt][r][j] * q) & (C::kN - 1)) * 8));
-              }
-#pragma unroll
-              for (int q = 0; q < R; ++q) {
-                if constexpr (SPLIT) xs[q][kt][r][j] = x[q];
-                else bhi[q][kt][r][j] = pack_h2(x[q].x, x[q].y);
+              for (int qq = 0; qq < QH; ++qq) {
+                // this warp's half of the outputs (constant indices: x stays in registers)
+                float2 v = (C::kPair && q0 != 0) ? x[(QH + qq) % R] : x[qq];
+                const int q = q0 + qq;
+                if (R > 1 && q > 0) v = cmul(v, lds64f(s_tw_addr + ((mval[kt][r][j] * q) & (C::kN - 1)) * 8));
+                if constexpr (SPLIT) xs[qq][kt][r][j] = v;
+                else bhi[qq][kt][r][j] = pack_h2(v.x, v.y);
               }
             }
           }
       if constexpr (SPLIT) {
         float m = 0.f;
 #pragma unroll
-        for (int q = 0; q < R; ++q)
+        for (int q = 0; q < QH; ++q)
 #pragma unroll
           for (int kt = 0; kt < 2; ++kt)
 #pragma unroll
@@ -228,7 +236,7 @@ __global__ void __launch_bounds__(256, SmallCfg<R, MODE>::kMinBlocks)
         float sc;
         split_scale(warp_max(m), sc, inv);
 #pragma unroll
-        for (int q = 0; q < R; ++q)
+        for (int q = 0; q < QH; ++q)
 #pragma unroll
           for (int kt = 0; kt < 2; ++kt)
 #pragma unroll
@@ -239,12 +247,14 @@ __global__ void __launch_bounds__(256, SmallCfg<R, MODE>::kMinBlocks)
                 split_h2(make_float2(v.x * sc, v.y * sc), bhi[q][kt][r][j], blo[q][kt][r][j]);
               }
       }
-      __syncwarp();  // all lanes finished reading this job's region (in-place)
+      // all lanes (kPair: of both warps of the transform) finished reading its region (in place)
+      if constexpr (C::kPair) asm volatile("bar.sync %0, 64;" ::"r"(1 + (warp >> 1)) : "memory");
+      else __syncwarp();
 
       // ---------------- two radix-16 tensor-core stages per tile q
-      float2 res[R][2][2][2];  // wide: fp32 results; plain: packed half2 in .x bits
+      float2 res[QH][2][2][2];  // wide: fp32 results; plain: packed half2 in .x bits
 #pragma unroll
-      for (int q = 0; q < R; ++q) {
+      for (int q = 0; q < QH; ++q) {
         float acc[2][2][4];
         if constexpr (SPLIT) dft16_mma_split(afr, afr_lo, bhi[q], blo[q], acc);
         else dft16_mma(afr, bhi[q], acc);
@@ -298,8 +308,8 @@ __global__ void __launch_bounds__(256, SmallCfg<R, MODE>::kMinBlocks)
               if constexpr (R == 1) sts64f(base, res[0][h][e][hh]);
               else {
 #pragma unroll
-                for (int q2 = 0; q2 < R; q2 += 2) {
-                  const uint32_t addr = job + swz_w<8>(swz_w<8>(out_off[h][e][hh]) + q2) * 8;
+                for (int q2 = 0; q2 < QH; q2 += 2) {
+                  const uint32_t addr = job + swz_w<8>(swz_w<8>(out_off[h][e][hh]) + q0 + q2) * 8;
                   sts128f(addr, res[q2][h][e][hh], res[q2 + 1][h][e][hh]);
                 }
               }

@@ -339,7 +339,7 @@ tcfftStatus choose_1d(int64_t n, int64_t batch, int precision, Schedule& s, int 
     s.text = buf;
     return TCFFT_SUCCESS;
   }
-  if (n <= 2048 && !(split && n == 2048)) {
+  if (n <= 2048) {
     s.kind = Schedule::kSmall;
     s.R = (int)(n / 256);
     s.launches = 1;
@@ -348,18 +348,6 @@ tcfftStatus choose_1d(int64_t n, int64_t batch, int precision, Schedule& s, int 
     return TCFFT_SUCCESS;
   }
   const int lg = ilog2_exact(n);
-  if (split && n == 2048) {
-    // beyond the split range of the single-pass kernel (1024) and below the short-row phase
-    // (16 rows of 16 R): N = N1 x 64 from two sub-plans
-    s.kind = Schedule::kFourStep;
-    s.N1 = n / 64;
-    s.N2 = 64;
-    s.launches = 5;
-    snprintf(buf, sizeof buf, "fourstep(%s): N=%lld x 64, two sub-plans, 3 transposes (one with the twiddle)", pname,
-             (long long)s.N1);
-    s.text = buf;
-    return TCFFT_SUCCESS;
-  }
   if (resident_supported(n, split) && !getenv("TCFFT_NO_RESIDENT")) {
     s.kind = Schedule::kResident;
     s.N1 = 256;
@@ -687,24 +675,6 @@ tcfftStatus exec_plan(tcfftPlan plan, void* data, void* stream, int dir, int nor
     // [B][N1 rows k1][N2 cols k2] -> X[k1 + N1 k2] = [B][N2][N1]
     return cuda_status(launch_transpose(plan->big, data, plan->batch, s.N1, s.N2, es, plan->num_sms, st), "transpose");
   }
-  if (s.kind == Schedule::kFourStep) {
-    // x[n1 N2 + n2]: [B][N1][N2] -> [B][N2][N1]; rows of N1 -> Y[n2][k1]; times W_N^(n2 k1)
-    // and transposed -> [B][N1][N2]; rows of N2 -> Z[k1][k2]; X[k1 + N1 k2] = [B][N2][N1]
-    if (cuda_status(launch_transpose(data, plan->big, plan->batch, s.N1, s.N2, es, plan->num_sms, st), "transpose"))
-      return TCFFT_CUDA_ERROR;
-    tcfftStatus r = exec_plan(plan->subs[0], plan->big, stream, dir, norm);  // scaled by 1/N1
-    if (r != TCFFT_SUCCESS) return r;
-    if (cuda_status(launch_transpose_twiddle(plan->big, data, plan->batch, s.N2, s.N1, plan->n, dsign, split,
-                                             plan->num_sms, st),
-                    "transpose-twiddle"))
-      return TCFFT_CUDA_ERROR;
-    r = exec_plan(plan->subs[1], data, stream, dir, norm);  // scaled by 1/N2
-    if (r != TCFFT_SUCCESS) return r;
-    if (cuda_status(launch_transpose(data, plan->big, plan->batch, s.N1, s.N2, es, plan->num_sms, st), "transpose"))
-      return TCFFT_CUDA_ERROR;
-    return cuda_status(cudaMemcpyAsync(data, plan->big, plan->total_elems * es, cudaMemcpyDeviceToDevice, st),
-                       "copy back");
-  }
   if (s.kind == Schedule::kGeneric2d) {
     // an axis of 4096 runs as the resident kernel with transposed output, which
     // replaces that axis' transpose
@@ -922,27 +892,6 @@ tcfftStatus setup_large1d(tcfftPlanImpl* p) {
     p->sched.text += ", rows written transposed (no transpose pass)";
   }
   p->scratch_bytes += rows->scratch_bytes;
-  return TCFFT_SUCCESS;
-}
-
-// Four-step from two short sub-plans (rows of N1, rows of N2), one full-size
-// intermediate.
-tcfftStatus setup_fourstep(tcfftPlanImpl* p) {
-  const Schedule& s = p->sched;
-  const int es = p->precision != TCFFT_PRECISION_PLAIN ? 8 : 4;
-  p->scratch_bytes = p->n * p->batch * es;
-  if (cudaMalloc(&p->big, p->scratch_bytes) != cudaSuccess) return TCFFT_ALLOC_FAILED;
-  tcfftOptions o;
-  tcfftOptionsDefault(&o);
-  o.precision = p->precision;
-  tcfftPlan a = nullptr, b = nullptr;
-  tcfftStatus st = tcfftPlan1d(&a, s.N1, s.N2 * p->batch, &o);
-  if (st != TCFFT_SUCCESS) return st;
-  p->subs.push_back(a);
-  st = tcfftPlan1d(&b, s.N2, s.N1 * p->batch, &o);
-  if (st != TCFFT_SUCCESS) return st;
-  p->subs.push_back(b);
-  p->sched.launches = a->sched.launches + b->sched.launches + 4;
   return TCFFT_SUCCESS;
 }
 
@@ -1653,7 +1602,6 @@ tcfftStatus tcfftPlan1d(tcfftPlan* out, int64_t n, int64_t batch, const tcfftOpt
   if (st == TCFFT_SUCCESS && (p->sched.kind == Schedule::kFused1d || p->sched.kind == Schedule::kFused2d))
     st = alloc_fused(p);
   if (st == TCFFT_SUCCESS && s.kind == Schedule::kLarge1d) st = setup_large1d(p);
-  if (st == TCFFT_SUCCESS && s.kind == Schedule::kFourStep) st = setup_fourstep(p);
   if (st == TCFFT_SUCCESS && s.kind == Schedule::kResident) st = alloc_wn_tables(p, n);
   if (st == TCFFT_SUCCESS && o.autotune) st = autotune_plan(p, o);
   if (st == TCFFT_SUCCESS && o.input_order == TCFFT_ORDER_REFERENCE_DIGIT_REVERSED) st = setup_reference_order(p);

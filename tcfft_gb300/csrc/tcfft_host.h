@@ -60,10 +60,6 @@ cudaError_t launch_tiny(int64_t n, int mode, void* data, int64_t batch, const fl
 cudaError_t launch_transpose(const void* in, void* out, int64_t B, int64_t R, int64_t C, int es, int num_sms,
                              cudaStream_t st);
 
-// Transpose with the four-step twiddle: out[b][c][r] = in[b][r][c] * W_N^(r c).
-cudaError_t launch_transpose_twiddle(const void* in, void* out, int64_t B, int64_t R, int64_t C, int64_t N,
-                                     float dsign, bool split, int num_sms, cudaStream_t st);
-
 // Copies nblocks variable-size blocks (byte offsets, 16-byte aligned) in one launch (tcfft_gather.cu).
 cudaError_t launch_move_blocks(const void* src, void* dst, const long long* src_off, const long long* dst_off,
                                const long long* cum, int nblocks, long long total_chunks, int num_sms,

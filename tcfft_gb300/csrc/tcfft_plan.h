@@ -15,10 +15,8 @@ struct Schedule {
   //   full-size scratch, row FFTs of length N2 by a sub-plan, transpose back.
   // kGeneric2d: axes outside the fused 2D range: row FFTs (sub-plan), transpose, row FFTs of
   //   the other axis (sub-plan), transpose back.
-  // kFourStep: N = N1 N2 from two short sub-plans: transpose, rows of N1, transpose with the
-  //   W_N twiddle, rows of N2, transpose (the split precision at N = 2048).
   enum Kind {
-    kNone = 0, kSmall = 1, kFused1d = 2, kFused2d = 3, kTiny = 4, kLarge1d = 5, kGeneric2d = 6, kFourStep = 7,
+    kNone = 0, kSmall = 1, kFused1d = 2, kFused2d = 3, kTiny = 4, kLarge1d = 5, kGeneric2d = 6,
     kResident = 8,  // N = 4096..16384 plain: whole transforms in one CTA's shared memory (fft_resident.cu)
     kCluster = 9    // N = 2^15..2^18 plain: one transform per thread-block cluster (fft_cluster.cu)
   } kind = kNone;

@@ -78,60 +78,7 @@ __global__ void __launch_bounds__(256) transpose_vec_kernel(const uint4* __restr
   }
 }
 
-// out[b][c][r] = in[b][r][c] * W_N^(r c), W_N = exp(-2 pi i dsign / N): the
-// transpose of a four-step FFT with its twiddle (fp32 arithmetic).
-template <bool SPLIT>
-__global__ void __launch_bounds__(256) transpose_twiddle_kernel(const void* __restrict__ in_, void* __restrict__ out_,
-                                                                long long B, long long R, long long C, long long N,
-                                                                float dsign) {
-  using E = typename std::conditional<SPLIT, float2, uint32_t>::type;
-  const E* in = static_cast<const E*>(in_);
-  E* out = static_cast<E*>(out_);
-  __shared__ float2 tile[32][33];
-  const long long tr = (R + 31) / 32, tc = (C + 31) / 32, per = tr * tc, total = B * per;
-  for (long long t = blockIdx.x; t < total; t += gridDim.x) {
-    const long long b = t / per, rem = t - b * per;
-    const long long r0 = (rem / tc) * 32, c0 = (rem % tc) * 32;
-    const E* ib = in + b * R * C;
-    E* ob = out + b * R * C;
-    for (int i = threadIdx.y; i < 32; i += 8) {
-      const long long r = r0 + i, c = c0 + threadIdx.x;
-      if (r < R && c < C) {
-        float2 v;
-        if constexpr (SPLIT) v = ib[r * C + c];
-        else v = unpack_h2(ib[r * C + c]);
-        float sn, cs;
-        sincospif(2.0f * (float)((r * c) % N) / (float)N, &sn, &cs);
-        tile[i][threadIdx.x] = make_float2(v.x * cs + dsign * v.y * sn, v.y * cs - dsign * v.x * sn);
-      }
-    }
-    __syncthreads();
-    for (int i = threadIdx.y; i < 32; i += 8) {
-      const long long c = c0 + i, r = r0 + threadIdx.x;
-      if (r < R && c < C) {
-        const float2 v = tile[threadIdx.x][i];
-        if constexpr (SPLIT) ob[c * R + r] = v;
-        else ob[c * R + r] = pack_h2(v.x, v.y);
-      }
-    }
-    __syncthreads();
-  }
-}
-
 }  // namespace
-
-cudaError_t launch_transpose_twiddle(const void* in, void* out, int64_t B, int64_t R, int64_t C, int64_t N,
-                                     float dsign, bool split, int num_sms, cudaStream_t st) {
-  const long long tiles = B * ((R + 31) / 32) * ((C + 31) / 32);
-  long long blocks = tiles < (long long)num_sms * 16 ? tiles : (long long)num_sms * 16;
-  if (blocks < 1) blocks = 1;
-  const dim3 block(32, 8);
-  if (split)
-    transpose_twiddle_kernel<true><<<(unsigned)blocks, block, 0, st>>>(in, out, B, R, C, N, dsign);
-  else
-    transpose_twiddle_kernel<false><<<(unsigned)blocks, block, 0, st>>>(in, out, B, R, C, N, dsign);
-  return cudaGetLastError();
-}
 
 cudaError_t launch_transpose(const void* in, void* out, int64_t B, int64_t R, int64_t C, int es, int num_sms,
                              cudaStream_t st) {

@@ -129,13 +129,13 @@ def test_generic_2d_split(cuda_device, nx, ny):
 
 
 @pytest.mark.parametrize("n", [2048, 32768])
-def test_split_fourstep(cuda_device, n):
-    """Split precision at N = 2048 (beyond the split range of the single-pass
-    kernel, below the short-row phase: four-step from two sub-plans; also as a
-    2D axis) and 2^15 (512 x 64 two-phase kernel with radix-4 short rows)."""
+def test_split_2048_and_short_rows(cuda_device, n):
+    """Split precision at N = 2048 (single-pass kernel with two warps per transform,
+    each taking four of the eight radix-8 sub-transforms) and 2^15 (512 x 64
+    two-phase kernel with radix-4 short rows)."""
     xq = quantize(uniform_input((5, n), seed=21), "split")
     with tc.Plan(n=n, batch=5, precision="split") as p:
-        assert ("fourstep" if n == 2048 else "fused1d") in p.info["schedule"]
+        assert ("small(R=8" if n == 2048 else "fused1d") in p.info["schedule"]
         y = run_gpu(p, xq, "split")
         ya = run_gpu(p, xq, "split", adjoint=True)
     assert oracle.rel_l2(y, oracle_1d(xq)) < tol_split(n)
