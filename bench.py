@@ -653,8 +653,8 @@ def main():
                     torch, plan, x, args.precision, size, batch, kind)
         if not args.no_sweep and "n" in size_args:
             for key, fn in (("sweep", lambda: sweep(torch, tc, args.precision)),
-                            ("sweep_split", lambda: sweep(torch, tc, "split", lgs=(10, 12, 14, 16, 18, 20, 22))),
-                            ("sweep_fp32io", lambda: sweep(torch, tc, "fp32io", lgs=(10, 12, 14, 16, 18, 20, 22))),
+                            ("sweep_split", lambda: sweep(torch, tc, "split", lgs=(10, 11, 12, 14, 16, 18, 20, 22))),
+                            ("sweep_fp32io", lambda: sweep(torch, tc, "fp32io", lgs=(10, 11, 12, 14, 16, 18, 20, 22))),
                             ("sweep_2d", lambda: sweep_2d(torch, tc)),
                             ("uneven_batch", lambda: uneven_batch(torch, tc)),
                             ("uneven_batch_graph", lambda: uneven_batch(torch, tc, graph=True)),
