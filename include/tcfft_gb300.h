@@ -119,6 +119,21 @@ tcfftStatus tcfftPlan1d(tcfftPlan* plan, int64_t n, int64_t batch, const tcfftOp
  * composed from 1D plans and transposes. */
 tcfftStatus tcfftPlan2d(tcfftPlan* plan, int64_t nx, int64_t ny, int64_t batch, const tcfftOptions* opts);
 
+/* Strided layouts (cuFFT's "advanced layout" for one dimension): `batch`
+ * transforms of n points, point j of transform b at element
+ *   istride == 1:  b * idist + j            (batch stride; idist >= n, and
+ *                                            idist * element bytes a multiple of 128)
+ *   istride  > 1:  (b / istride) * n * istride + j * istride + b % istride
+ *                  (idist must be 1: istride transforms interleaved, i.e. the FFT
+ *                   along the middle axis of a [batch / istride][n][istride] array)
+ * The first form is an uneven-batch plan (tcfftPlanMany) with those offsets. The
+ * second is plain precision only, without normalisation, n = 128..2048, with
+ * istride a multiple of 128 / 32 / 32 / 16 / 8 for n = 128 / 256 / 512 / 1024 / 2048
+ * (TCFFT_NOT_SUPPORTED otherwise); it runs as one launch of column FFTs.  No
+ * counterpart in the reference (contiguous batches only). */
+tcfftStatus tcfftPlanStrided(tcfftPlan* plan, int64_t n, int64_t batch, int64_t istride, int64_t idist,
+                             const tcfftOptions* opts);
+
 /* Uneven batch in one launch: `count` independent transforms, transform i has
  * rank ranks[i] (1 or 2), shape (nx[i]) for 1D or (nx[i], ny[i]) for 2D, and
  * starts at element offset offsets[i] of the single device buffer passed to

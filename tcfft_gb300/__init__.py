@@ -82,6 +82,8 @@ _SIGNATURES = {
                     ctypes.c_int),
     "tcfftPlan2d": ([ctypes.POINTER(ctypes.c_void_p), ctypes.c_int64, ctypes.c_int64, ctypes.c_int64,
                      ctypes.POINTER(Options)], ctypes.c_int),
+    "tcfftPlanStrided": ([ctypes.POINTER(ctypes.c_void_p), ctypes.c_int64, ctypes.c_int64, ctypes.c_int64,
+                          ctypes.c_int64, ctypes.POINTER(Options)], ctypes.c_int),
     "tcfftPlanMany": ([ctypes.POINTER(ctypes.c_void_p), ctypes.c_int64, ctypes.POINTER(ctypes.c_int32),
                        ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64),
                        ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(Options)], ctypes.c_int),
@@ -246,6 +248,25 @@ class Plan:
         p = cls(precision=precision, _handle=h, _shapes=[tuple(s) for s in shapes])
         p.offsets = list(offsets)
         return p
+
+    @classmethod
+    def strided(cls, n, batch, istride=1, idist=None, precision="plain", direction=FORWARD, normalize=False):
+        """Strided 1D layout (tcfftPlanStrided): point j of transform b at element
+        ``b * idist + j`` (``istride == 1``), or, with ``istride > 1`` (``idist`` 1),
+        ``(b // istride) * n * istride + j * istride + b % istride``: the FFT along
+        the middle axis of a ``[batch // istride][n][istride]`` array."""
+        if idist is None:
+            idist = n if istride == 1 else 1
+        opts = Options()
+        lib().tcfftOptionsDefault(ctypes.byref(opts))
+        opts.precision = _precision_of(precision)
+        opts.direction = int(direction)
+        opts.normalization = NORM_BY_N if normalize else NORM_NONE
+        h = ctypes.c_void_p(None)
+        _check(lib().tcfftPlanStrided(ctypes.byref(h), int(n), int(batch), int(istride), int(idist),
+                                      ctypes.byref(opts)),
+               "tcfftPlanStrided(n=%d, batch=%d, istride=%d, idist=%d)" % (n, batch, istride, idist))
+        return cls(precision=precision, _handle=h)
 
     # -- execution -------------------------------------------------------
     def _ptr(self, data):

@@ -1140,7 +1140,10 @@ tcfftStatus check_errors(tcfftPlanImpl* p) {
 
 // ------------------------------------------------------------------ many-shape executor (plain)
 // Pass A / pass B kinds of a transform (kMkKinds: not supported by the executor).
+// Rank 3 is a "columns" transform: FFTs of nx points down the ny columns of an
+// [nx][ny] matrix (no pass A; tcfftPlanStrided with istride = ny).
 int many_kind_a(int rank, int64_t nx, int64_t ny) {
+  if (rank == 3) return -1;
   if (rank == 1) {
     switch (nx) {
       case 256: return kMkRow1 | kMkList;
@@ -1172,14 +1175,11 @@ int many_kind_b(int rank, int64_t nx, int64_t ny) {
       default: return nx <= 2048 ? -1 : kMkKinds;  // -1: no pass B
     }
   }
-  switch (nx) {
-    case 128: return kMkCol128;
-    case 256: return kMkCol1;
-    case 512: return kMkCol2;
-    case 1024: return kMkCol4;
-    case 2048: return kMkCol8;
-    default: return kMkKinds;
-  }
+  const int k = nx == 128 ? kMkCol128 : nx == 256 ? kMkCol1 : nx == 512 ? kMkCol2 : nx == 1024 ? kMkCol4
+              : nx == 2048 ? kMkCol8 : kMkKinds;
+  // whole tiles of columns (2D shapes have ny >= 128, a multiple of every tile width)
+  if (k != kMkKinds && ny % (k == kMkCol128 ? 128 : many_c(k)) != 0) return kMkKinds;
+  return k;
 }
 // 1D N >= 4096 = N1 x N2 in the executor (N1 = 256, 2^15: 512)
 int64_t many_n1(int64_t n) { return n == 32768 ? 512 : 256; }
@@ -1211,8 +1211,9 @@ bool setup_many_pass(tcfftPlanImpl* p, int64_t count, const int32_t* ranks, cons
   int64_t soff = 0;
   for (int64_t i = 0; i < count; ++i) {
     const int r = ranks[i];
-    const int64_t x = nx[i], y = r == 2 ? ny[i] : 1;
+    const int64_t x = nx[i], y = r >= 2 ? ny[i] : 1;
     if (many_kind_a(r, x, y) == kMkKinds || many_kind_b(r, x, y) == kMkKinds) return false;
+    if (r == 3 && many_kind_b(r, x, y) < 0) return false;
     xf[i] = {r, x, y, offsets[i], 0};
     if (r == 1 && x >= 4096) {
       xf[i].soff = soff;
@@ -1231,7 +1232,7 @@ bool setup_many_pass(tcfftPlanImpl* p, int64_t count, const int32_t* ranks, cons
     for (int64_t i = 0; i < count; ++i) {
       const auto& t = xf[i];
       const int k = many_kind_a(t.rank, t.nx, t.ny);
-      if (k & kMkList) listed[k & 0xff].push_back(i);
+      if (k >= 0 && (k & kMkList)) listed[k & 0xff].push_back(i);
       else order.push_back(i);
     }
     for (int kind = 0; kind < kMkKinds; ++kind) {
@@ -1265,7 +1266,7 @@ bool setup_many_pass(tcfftPlanImpl* p, int64_t count, const int32_t* ranks, cons
     auto emit_b = [&](int64_t i) {
       const auto& t = xf[i];
       const auto k = kinds_of(i);
-      const int na = (int)items_of(k.first, many_tiles(k.first, t.rank, t.nx, t.ny));
+      const int na = k.first < 0 ? 0 : (int)items_of(k.first, many_tiles(k.first, t.rank, t.nx, t.ny));
       const int64_t tiles = many_tiles(k.second, t.rank, t.nx, t.ny);
       for (int64_t tile = 0; tile < tiles; tile += sub_of(k.second)) {
         const int nsub = (int)std::min<int64_t>(sub_of(k.second), tiles - tile);
@@ -1275,6 +1276,10 @@ bool setup_many_pass(tcfftPlanImpl* p, int64_t count, const int32_t* ranks, cons
     for (int64_t i : order) {
       const auto& t = xf[i];
       const auto k = kinds_of(i);
+      if (k.first < 0) {  // columns only: no pass A, its pass-B items wait for nothing
+        emit_b(i);
+        continue;
+      }
       int wn = 0;
       if (k.first == kMkColWn1x16 || k.first == kMkColWn1x32 || k.first == kMkColWn2x32)
         wn = (int)(t.nx - 1);
@@ -1380,9 +1385,11 @@ CUresult encode_many_maps(tcfftPlanImpl* p, void* data) {
         if (r == CUDA_SUCCESS) r = encode_tmap(&m[3], dt, 4, base, dims, str, box, CU_TENSOR_MAP_SWIZZLE_128B);
       }
     } else {
-      const int ka = many_kind_a(2, t.nx, t.ny), kb = many_kind_b(2, t.nx, t.ny);
+      const int ka = many_kind_a(t.rank, t.nx, t.ny), kb = many_kind_b(t.rank, t.nx, t.ny);
       const int64_t elems = t.nx * t.ny;
-      if (ka == kMkRow128) {
+      if (ka < 0) {
+        // columns only: no pass-A map
+      } else if (ka == kMkRow128) {
         r = rows_map(&m[0], base, elems, 256);
       } else {
         const int64_t rows = (int64_t)many_c(ka) * t.ny / 32;
@@ -1457,6 +1464,7 @@ tcfftStatus exec_many_pass(tcfftPlanImpl* plan, void* data, cudaStream_t st, int
 
 tcfftStatus exec_many(tcfftPlanImpl* plan, void* data, cudaStream_t st, int dir, int norm) {
   if (plan->many_ok && !norm) return exec_many_pass(plan, data, st, dir);
+  if (plan->many_only) return TCFFT_NOT_SUPPORTED;  // no per-shape graph to normalise with
   const int es = plan->precision != TCFFT_PRECISION_PLAIN ? 8 : 4;
   const int g = 2 * dir + norm;  // one captured graph per direction and normalisation
   if (!plan->graph_exec[g] || plan->graph_ptr[g] != data) {
@@ -1670,6 +1678,72 @@ tcfftStatus tcfftPlan2d(tcfftPlan* out, int64_t nx, int64_t ny, int64_t batch, c
     delete p;
     return st;
   }
+  *out = p;
+  return TCFFT_SUCCESS;
+}
+
+tcfftStatus tcfftPlanStrided(tcfftPlan* out, int64_t n, int64_t batch, int64_t istride, int64_t idist,
+                             const tcfftOptions* opts) {
+  if (!out) return TCFFT_INVALID_VALUE;
+  *out = nullptr;
+  if (batch < 1 || istride < 1 || idist < 1) return TCFFT_INVALID_VALUE;
+  if (!is_pow2(n)) return TCFFT_INVALID_SIZE;
+  if (istride == 1) {  // batch stride: an uneven-batch plan with offsets b * idist
+    if (idist < n) return TCFFT_INVALID_VALUE;
+    if (batch > (int64_t)1 << 24) return TCFFT_INVALID_SIZE;
+    std::vector<int32_t> r((size_t)batch, 1);
+    std::vector<int64_t> x((size_t)batch, n), y((size_t)batch, 1), off((size_t)batch);
+    for (int64_t b = 0; b < batch; ++b) off[b] = b * idist;
+    tcfftStatus st = tcfftPlanMany(out, batch, r.data(), x.data(), y.data(), off.data(), opts);
+    if (st == TCFFT_SUCCESS) {
+      char buf[64];
+      snprintf(buf, sizeof buf, "strided(idist=%lld) ", (long long)idist);
+      (*out)->sched.text = buf + (*out)->sched.text;
+    }
+    return st;
+  }
+  // element stride: groups of istride interleaved transforms, each a columns transform
+  if (idist != 1 || batch % istride != 0) return TCFFT_NOT_SUPPORTED;
+  tcfftStatus st = validate_opts(opts);
+  if (st != TCFFT_SUCCESS) return st;
+  tcfftOptions o;
+  tcfftOptionsDefault(&o);
+  if (opts) o = *opts;
+  if (o.precision != TCFFT_PRECISION_PLAIN || o.input_order != TCFFT_ORDER_NATURAL ||
+      o.normalization != TCFFT_NORM_NONE)
+    return TCFFT_NOT_SUPPORTED;
+  const int64_t groups = batch / istride;
+  if (many_kind_b(3, n, istride) == kMkKinds || groups > (int64_t)1 << 24 ||
+      n * batch > (int64_t(1) << 40))
+    return TCFFT_NOT_SUPPORTED;
+  std::vector<int32_t> r((size_t)groups, 3);
+  std::vector<int64_t> x((size_t)groups, n), y((size_t)groups, istride), off((size_t)groups);
+  for (int64_t g = 0; g < groups; ++g) off[g] = g * n * istride;
+  tcfftPlanImpl* p = new (std::nothrow) tcfftPlanImpl();
+  if (!p) return TCFFT_ALLOC_FAILED;
+  p->kind = 3;
+  p->precision = o.precision;
+  p->direction = o.direction;
+  p->normalize = 0;
+  p->batch = groups;
+  p->total_elems = n * batch;
+  p->span_elems = n * batch;
+  p->many_only = true;
+  st = alloc_tables(p);
+  if (st == TCFFT_SUCCESS && !setup_many_pass(p, groups, r.data(), x.data(), y.data(), off.data()))
+    st = TCFFT_NOT_SUPPORTED;
+  if (st != TCFFT_SUCCESS) {
+    free_tables(p);
+    delete p;
+    return st;
+  }
+  p->sched.launches = 1;
+  char buf[200];
+  snprintf(buf, sizeof buf,
+           "strided(plain): %lld transforms of %lld points at stride %lld, one persistent launch of %d "
+           "column-FFT items",
+           (long long)batch, (long long)n, (long long)istride, p->many_n[0]);
+  p->sched.text = buf;
   *out = p;
   return TCFFT_SUCCESS;
 }

@@ -90,6 +90,7 @@ struct tcfftPlanImpl {
     int64_t nx, ny, off, soff;
   };
   bool many_ok = false;
+  bool many_only = false;                  // no per-shape graph (strided column plans)
   int many_xf_b = -1;                      // first transform with a pass B (timeout test hook)
   std::vector<ManyXf> many_xf;
   tcfft::ManyItem* many_items = nullptr;  // the item sequence of the one launch
