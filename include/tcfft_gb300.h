@@ -178,6 +178,14 @@ tcfftStatus tcfftExecuteOutOfPlace(tcfftPlan plan, const void* in, void* out, vo
  * it and C2R is unnormalised.  Options: precision, normalization, autotune;
  * direction must be TCFFT_FORWARD and input order natural. */
 tcfftStatus tcfftPlanReal1d(tcfftPlan* plan, int64_t n, int64_t batch, const tcfftOptions* opts);
+/* Real 2D transforms: `batch` real nx x ny arrays [batch][nx][ny] (powers of
+ * two, nx >= 16, ny >= 32; the split precision has no 128-point complex
+ * transform, so it takes neither nx = 128 nor ny = 256) and their halves
+ * [batch][nx][ny/2 + 1] (numpy's rfft2 / irfft2 layout), same precisions,
+ * options and normalisation rule as tcfftPlanReal1d (the 1/(nx ny) on C2R by
+ * default).  Rows as real 1D transforms, columns as complex 1D transforms of
+ * the transposed half spectrum; both calls use tcfftExecuteR2C / C2R. */
+tcfftStatus tcfftPlanReal2d(tcfftPlan* plan, int64_t nx, int64_t ny, int64_t batch, const tcfftOptions* opts);
 /* X = DFT(x) (sign -1; times 1/n with TCFFT_NORM_BY_N), the n/2 + 1
  * non-redundant values; `in` is not modified. */
 tcfftStatus tcfftExecuteR2C(tcfftPlan plan, const void* in, void* out, void* stream);

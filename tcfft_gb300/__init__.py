@@ -91,6 +91,8 @@ _SIGNATURES = {
     "tcfftExecuteAdjoint": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
     "tcfftExecuteInverse": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
     "tcfftExecuteOutOfPlace": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
+    "tcfftPlanReal2d": ([ctypes.POINTER(ctypes.c_void_p), ctypes.c_int64, ctypes.c_int64, ctypes.c_int64,
+                         ctypes.POINTER(Options)], ctypes.c_int),
     "tcfftPlanReal1d": ([ctypes.POINTER(ctypes.c_void_p), ctypes.c_int64, ctypes.c_int64, ctypes.POINTER(Options)],
                         ctypes.c_int),
     "tcfftExecuteR2C": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
@@ -360,23 +362,30 @@ class Plan:
 
 
 class RealPlan(Plan):
-    """Real 1D transforms of ``n`` points (tcfftPlanReal1d): ``r2c(x, out)`` maps
-    real ``[batch, n]`` (fp16 plain / fp32 split) to the Hermitian half
-    ``[batch, n // 2 + 1, 2]``; ``c2r(X, out)`` is its inverse (c2r(r2c(x)) = x:
-    the 1/n on c2r, or on r2c with ``normalize=True``)."""
+    """Real transforms (tcfftPlanReal1d / tcfftPlanReal2d).  1D, ``RealPlan(n, batch)``:
+    ``r2c(x, out)`` maps real ``[batch, n]`` (fp16 plain / fp32 split) to the
+    Hermitian half ``[batch, n // 2 + 1, 2]``.  2D, ``RealPlan(nx=, ny=, batch=)``:
+    real ``[batch, nx, ny]`` to ``[batch, nx, ny // 2 + 1, 2]`` (numpy's rfft2
+    layout).  ``c2r(X, out)`` is the inverse (c2r(r2c(x)) = x: the 1/N on c2r, or
+    on r2c with ``normalize=True``)."""
 
-    def __init__(self, n, batch=1, precision="plain", normalize=False, autotune=False):
+    def __init__(self, n=None, batch=1, precision="plain", normalize=False, autotune=False, nx=None, ny=None):
         self._handle = ctypes.c_void_p(None)
         self.precision = _precision_of(precision)
-        self.n, self.batch = int(n), int(batch)
-        self.nx = self.ny = None
+        self.n, self.batch = (int(n) if n else None), int(batch)
+        self.nx, self.ny = (int(nx) if nx else None), (int(ny) if ny else None)
         opts = Options()
         lib().tcfftOptionsDefault(ctypes.byref(opts))
         opts.precision = self.precision
         opts.normalization = NORM_BY_N if normalize else NORM_NONE
         opts.autotune = 1 if autotune else 0
-        _check(lib().tcfftPlanReal1d(ctypes.byref(self._handle), self.n, self.batch, ctypes.byref(opts)),
-               "tcfftPlanReal1d(n=%d, batch=%d)" % (self.n, self.batch))
+        if self.nx:
+            _check(lib().tcfftPlanReal2d(ctypes.byref(self._handle), self.nx, self.ny, self.batch,
+                                         ctypes.byref(opts)),
+                   "tcfftPlanReal2d(nx=%d, ny=%d, batch=%d)" % (self.nx, self.ny, self.batch))
+        else:
+            _check(lib().tcfftPlanReal1d(ctypes.byref(self._handle), self.n, self.batch, ctypes.byref(opts)),
+                   "tcfftPlanReal1d(n=%d, batch=%d)" % (self.n, self.batch))
 
     def _real_ptr(self, t):
         import torch

@@ -531,6 +531,32 @@ tcfftStatus exec_many(tcfftPlanImpl* plan, void* data, cudaStream_t st, int dir,
 // L2, so it is used up to 64 MiB per call (4096^2 x 1: 92 against 120 us with row
 // pass + transpose; 4096^2 x 16: 2.39 against 1.65 ms; 2^23 x 32: 1.56 against 1.40 ms).
 constexpr int64_t kToutMaxBytes = int64_t(64) << 20;
+tcfftStatus exec_plan(tcfftPlan plan, void* data, void* stream, int dir, int norm, const void* in);
+
+// Real 2D (kind 5).  R2C: real rows -> A [B][nx][h], transpose -> T [B][h][nx], complex
+// columns in place on T, transpose -> out [B][nx][h].  C2R: the same backwards (the
+// column inverse carries 1/nx unless R2C did, the row C2R 1/ny under the same rule).
+tcfftStatus exec_real2d(tcfftPlanImpl* p, const void* in, void* out, void* stream, bool forward) {
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  const int es = p->precision != TCFFT_PRECISION_PLAIN ? 8 : 4;
+  const int64_t h = p->ny / 2 + 1;
+  unsigned char* A = static_cast<unsigned char*>(p->big);
+  unsigned char* T = A + p->span_elems;
+  if (forward) {
+    tcfftStatus r = tcfftExecuteR2C(p->subs[0], in, A, stream);
+    if (r != TCFFT_SUCCESS) return r;
+    if (cuda_status(launch_transpose(A, T, p->batch, p->nx, h, es, p->num_sms, st), "transpose")) return TCFFT_CUDA_ERROR;
+    r = exec_plan(p->subs[1], T, stream, 0, p->normalize, nullptr);
+    if (r != TCFFT_SUCCESS) return r;
+    return cuda_status(launch_transpose(T, out, p->batch, h, p->nx, es, p->num_sms, st), "transpose");
+  }
+  if (cuda_status(launch_transpose(in, T, p->batch, p->nx, h, es, p->num_sms, st), "transpose")) return TCFFT_CUDA_ERROR;
+  tcfftStatus r = exec_plan(p->subs[1], T, stream, 1, p->normalize ? 0 : 1, nullptr);
+  if (r != TCFFT_SUCCESS) return r;
+  if (cuda_status(launch_transpose(T, A, p->batch, h, p->nx, es, p->num_sms, st), "transpose")) return TCFFT_CUDA_ERROR;
+  return tcfftExecuteC2R(p->subs[0], A, out, stream);
+}
+
 bool large1d_tout(const tcfftPlanImpl* p) {
   if (p->total_elems * 4 > kToutMaxBytes) return false;
   return p->precision == TCFFT_PRECISION_PLAIN && p->sched.N2 == 4096 &&
@@ -564,7 +590,7 @@ tcfftStatus exec_plan(tcfftPlan plan, void* data, void* stream, int dir, int nor
   if (!data) return TCFFT_INVALID_VALUE;
   if ((reinterpret_cast<uintptr_t>(data) & 127) != 0 || (reinterpret_cast<uintptr_t>(in) & 127) != 0)
     return TCFFT_MISALIGNED;
-  if (plan->kind == 4) return TCFFT_INVALID_VALUE;  // real plans run through tcfftExecuteR2C / C2R
+  if (plan->kind == 4 || plan->kind == 5) return TCFFT_INVALID_VALUE;  // real plans: tcfftExecuteR2C / C2R
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
   const bool split = plan->precision != TCFFT_PRECISION_PLAIN;  // 8-byte elements (split or fp32 I/O)
   const int mode = plan->precision;                             // kernel mode: kModePlain/Split/Io32
@@ -1893,6 +1919,63 @@ tcfftStatus tcfftExecuteOutOfPlace(tcfftPlan plan, const void* in, void* out, vo
   return exec_plan(plan, out, stream, plan->direction, plan->normalize, in);
 }
 
+tcfftStatus tcfftPlanReal2d(tcfftPlan* out, int64_t nx, int64_t ny, int64_t batch, const tcfftOptions* opts) {
+  if (!out) return TCFFT_INVALID_VALUE;
+  *out = nullptr;
+  tcfftStatus st = validate_opts(opts);
+  if (st != TCFFT_SUCCESS) return st;
+  tcfftOptions o;
+  tcfftOptionsDefault(&o);
+  if (opts) o = *opts;
+  if (o.input_order != TCFFT_ORDER_NATURAL || o.direction != TCFFT_FORWARD) return TCFFT_INVALID_VALUE;
+  if (!is_pow2(nx) || !is_pow2(ny) || nx < 16 || ny < 32 || batch < 1 || nx * ny > (int64_t(1) << 40) / batch)
+    return TCFFT_INVALID_SIZE;
+  const int64_t h = ny / 2 + 1;
+  const int es = o.precision != TCFFT_PRECISION_PLAIN ? 8 : 4;
+  tcfftPlanImpl* p = new (std::nothrow) tcfftPlanImpl();
+  if (!p) return TCFFT_ALLOC_FAILED;
+  p->kind = 5;
+  p->nx = nx;
+  p->ny = ny;
+  p->n = nx * ny;
+  p->batch = batch;
+  p->precision = o.precision;
+  p->normalize = o.normalization;
+  p->total_elems = nx * h * batch;  // complex elements of the half spectrum
+  p->sched.kind = Schedule::kNone;
+  st = alloc_tables(p);
+  // rows: real transforms of ny, carrying the plan's normalisation rule for 1/ny; columns:
+  // complex transforms of nx over the h columns of the half spectrum (1/nx on the normalised side)
+  tcfftOptions ro = o, co;
+  tcfftOptionsDefault(&co);
+  co.precision = o.precision;
+  co.autotune = o.autotune;
+  co.tune_cache_path = o.tune_cache_path;
+  tcfftPlan rows = nullptr, cols = nullptr;
+  if (st == TCFFT_SUCCESS) st = tcfftPlanReal1d(&rows, ny, nx * batch, &ro);
+  if (st == TCFFT_SUCCESS) p->subs.push_back(rows);
+  if (st == TCFFT_SUCCESS) st = tcfftPlan1d(&cols, nx, h * batch, &co);
+  if (st == TCFFT_SUCCESS) p->subs.push_back(cols);
+  // two half-spectrum buffers: [batch][nx][h] and its transpose [batch][h][nx]
+  const int64_t half_bytes = ((nx * h * batch * es + 255) / 256) * 256;
+  if (st == TCFFT_SUCCESS) {
+    p->scratch_bytes = 2 * half_bytes + rows->scratch_bytes + cols->scratch_bytes;
+    if (cudaMalloc(&p->big, 2 * half_bytes) != cudaSuccess) st = TCFFT_ALLOC_FAILED;
+    p->span_elems = half_bytes;  // byte offset of the second buffer
+  }
+  if (st != TCFFT_SUCCESS) {
+    free_tables(p);
+    delete p;
+    return st;
+  }
+  p->sched.launches = rows->sched.launches + cols->sched.launches + 2;
+  p->sched.text = "real2d(" + std::string(prec_name(o.precision)) + "): " + std::to_string(nx) + " x " +
+                  std::to_string(ny) + ", real rows, transpose, complex columns of " + std::to_string(nx) +
+                  ", transpose";
+  *out = p;
+  return TCFFT_SUCCESS;
+}
+
 tcfftStatus tcfftPlanReal1d(tcfftPlan* out, int64_t n, int64_t batch, const tcfftOptions* opts) {
   if (!out) return TCFFT_INVALID_VALUE;
   *out = nullptr;
@@ -1947,6 +2030,7 @@ tcfftStatus tcfftPlanReal1d(tcfftPlan* out, int64_t n, int64_t batch, const tcff
 
 tcfftStatus tcfftExecuteR2C(tcfftPlan plan, const void* in, void* out, void* stream) {
   if (!plan || plan->magic != tcfftPlanImpl::kMagic) return TCFFT_INVALID_PLAN;
+  if (plan->kind == 5 && in && out) return exec_real2d(plan, in, out, stream, true);
   if (plan->kind != 4 || !in || !out) return TCFFT_INVALID_VALUE;
   if ((reinterpret_cast<uintptr_t>(in) & 127) != 0) return TCFFT_MISALIGNED;
   const int64_t h = plan->n / 2;
@@ -1962,6 +2046,7 @@ tcfftStatus tcfftExecuteR2C(tcfftPlan plan, const void* in, void* out, void* str
 
 tcfftStatus tcfftExecuteC2R(tcfftPlan plan, const void* in, void* out, void* stream) {
   if (!plan || plan->magic != tcfftPlanImpl::kMagic) return TCFFT_INVALID_PLAN;
+  if (plan->kind == 5 && in && out) return exec_real2d(plan, in, out, stream, false);
   if (plan->kind != 4 || !in || !out) return TCFFT_INVALID_VALUE;
   if ((reinterpret_cast<uintptr_t>(out) & 127) != 0) return TCFFT_MISALIGNED;
   const int64_t h = plan->n / 2;
@@ -1978,6 +2063,7 @@ tcfftStatus tcfftExecuteC2R(tcfftPlan plan, const void* in, void* out, void* str
 tcfftStatus tcfftExecuteHost(tcfftPlan plan, const void* host_in, void* host_out, void* work, void* stream) {
   if (!plan || plan->magic != tcfftPlanImpl::kMagic) return TCFFT_INVALID_PLAN;
   if (!host_in || !host_out || !work) return TCFFT_INVALID_VALUE;
+  if (plan->kind == 4 || plan->kind == 5) return TCFFT_INVALID_VALUE;  // real plans: R2C / C2R
   if ((reinterpret_cast<uintptr_t>(work) & 127) != 0) return TCFFT_MISALIGNED;
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
   const int64_t es = plan->precision != TCFFT_PRECISION_PLAIN ? 8 : 4;

@@ -33,7 +33,8 @@ struct Schedule {
 struct tcfftPlanImpl {
   static constexpr uint32_t kMagic = 0x7cff7600u;
   uint32_t magic = kMagic;
-  int kind = 0;  // 1: 1D, 2: 2D, 3: many, 4: real 1D (R2C / C2R through subs[0], a complex plan of n / 2)
+  int kind = 0;  // 1: 1D, 2: 2D, 3: many, 4: real 1D (R2C / C2R through subs[0], a complex plan of n / 2),
+                 // 5: real 2D (subs[0] the real row plan, subs[1] the complex column plan)
   int64_t n = 0, nx = 0, ny = 0, batch = 0;
   int precision = 0, input_order = 0;
   int direction = 0, normalize = 0;  // of tcfftExecute (tcfftOptions)

@@ -13,7 +13,7 @@ import pytest
 
 import oracle
 import tcfft_gb300 as tc
-from fftcheck import quantize, to_complex, tol, uniform_input
+from fftcheck import quantize, to_complex, tol, tol_plain, uniform_input
 
 pytestmark = pytest.mark.gpu
 
@@ -131,3 +131,46 @@ def test_real_plan_rejects_bad_use(cuda_device):
         t = torch.zeros((1, 1024), dtype=torch.float16, device="cuda")
         with pytest.raises(tc.TcfftError):
             p.exec(t)               # a real plan has no complex execute
+
+
+REAL2D = [(64, 128, 3, "plain"), (256, 256, 2, "plain"), (1024, 512, 2, "plain"), (16, 64, 5, "plain"),
+          (256, 2048, 1, "split"), (512, 64, 2, "split"), (64, 512, 3, "split"), (256, 1024, 2, "fp32io")]
+
+
+@pytest.mark.parametrize("nx,ny,batch,precision", REAL2D)
+def test_real_2d(cuda_device, nx, ny, batch, precision):
+    """R2C 2D against the FP64 2D DFT's first ny/2 + 1 columns; C2R 2D against
+    numpy's FP64 irfft2 of the same half spectrum; the round trip returns x."""
+    import torch
+    h = ny // 2 + 1
+    bound = tol_plain(nx * ny) if precision == "fp32io" else tol(precision, nx * ny)  # fp16 arithmetic
+    rng = np.random.default_rng(nx + ny + batch)
+    dt_np = np.float16 if precision == "plain" else np.float32
+    dt = torch.float16 if precision == "plain" else torch.float32
+    x = rng.uniform(-1, 1, (batch, nx, ny)).astype(dt_np)
+    xt = torch.from_numpy(x).to(cuda_device)
+    spec = torch.empty((batch, nx, h, 2), dtype=dt, device=cuda_device)
+    y = torch.empty_like(xt)
+    with tc.RealPlan(nx=nx, ny=ny, batch=batch, precision=precision) as p:
+        assert "real2d" in p.info["schedule"], p.info["schedule"]
+        p.r2c(xt, spec)
+        p.check_device()
+        X = to_complex(spec.double().cpu().numpy())
+        ref = oracle.fft_2d(x.astype(np.float64) + 0j)[..., :h]
+        err = oracle.rel_l2(X, ref)
+        assert np.isfinite(X).all() and err < bound, "R2C %dx%d: rel-L2 %.3e" % (nx, ny, err)
+        p.c2r(spec, y)
+        p.check_device()
+        back = y.double().cpu().numpy()
+        assert oracle.rel_l2(back, x.astype(np.float64)) < 2 * bound
+        # C2R of a spectrum with arbitrary values (numpy's irfft2 semantics)
+        Xin = quantize(uniform_input((batch, nx, h), seed=nx % 37) * np.sqrt(nx * ny) / 2, precision)
+        st = torch.from_numpy(Xin).to(dt).to(cuda_device)
+        keep = st.clone()
+        p.c2r(st, y)
+        p.check_device()
+        assert torch.equal(st, keep), "C2R modified its input"
+    want = np.fft.irfft2(to_complex(Xin), s=(nx, ny))
+    got = y.double().cpu().numpy()
+    err = oracle.rel_l2(got, want)
+    assert np.isfinite(got).all() and err < bound, "C2R %dx%d: rel-L2 %.3e" % (nx, ny, err)
