@@ -364,7 +364,9 @@ tcfftStatus choose_1d(int64_t n, int64_t batch, int precision, Schedule& s, int 
     // 2^15: 512 x 64 (plain: 1.24 ms for 2^28 elements against 1.48 ms for 256 x 128 and
     // 1.38 ms for 1024 x 32: 64 KiB column tiles and a radix-4 short-row phase; split: the
     // short-row phase's R <= 4 limit)
-    const int64_t n1 = lg == 15 ? 512 : 256;
+    int64_t n1 = lg == 15 ? 512 : 256;
+    if (getenv("TCFFT_N1")) n1 = atoll(getenv("TCFFT_N1"));  // decomposition override (measurements)
+    if (n1 < 256 || n1 > 2048 || n / n1 < 16 || n / n1 > 128) return TCFFT_NOT_SUPPORTED;
     k.role0 = kRoleCol;
     k.R0 = (int)(n1 / 256);
     k.C0 = n1 == 512 ? (split ? 16 : 32) : 16;
@@ -374,6 +376,7 @@ tcfftStatus choose_1d(int64_t n, int64_t batch, int precision, Schedule& s, int 
     k.split = split;
     k.io32 = io32;
     if (split && k.R1 > 4) return TCFFT_NOT_SUPPORTED;
+    if (!fused_shape(k, nullptr)) return TCFFT_NOT_SUPPORTED;  // e.g. an override naming no compiled kernel
     s.kind = Schedule::kFused1d;
     s.N1 = n1;
     s.N2 = n / n1;
