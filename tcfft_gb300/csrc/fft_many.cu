@@ -9,10 +9,14 @@
 //           region of the transform), 2D rows;
 //   pass B: 1D N >= 4096 phase 1 (rows of N2 from the scratch, written
 //           transposed into the transform), 2D columns.
-// Every transform has its own tensor maps (four per transform, in global
-// memory), so no transform is moved to a batch of its shape first; each item
-// names its kind, transform and tile, and the job bodies are those of the
-// two-phase executor (fft_fused.cuh) and of the 16R-point jobs (fft_job.cuh).
+// Columns-only transforms (the element strides of tcfftPlanStrided) have a pass B
+// and no pass A.  Every transform has its own tensor maps (four per transform, in
+// global memory), so no transform is moved to a batch of its shape first.  An
+// item holds up to one 64 KiB stage: consecutive tiles of one transform side by
+// side, or up to C whole 1D transforms of 256R points loaded through four
+// buffer-wide maps (one per R).  The job bodies are those of the two-phase
+// executor (fft_fused.cuh) and of the 16R-point jobs (fft_job.cuh); the four-step
+// twiddles of every 1D size come from W_65536 in three shared-memory levels.
 //
 // CTA = 8 compute warps + 1 TMA-load warp + 1 TMA-store warp (the two-phase
 // executor's structure).  The items form one sequence in which a transform's
