@@ -251,3 +251,40 @@ def test_many_pass_out_of_place_and_host(cuda_device):
         p.check_device()
         assert torch.equal(h_out, ref.cpu())
     check(parts, unpack(out.double().cpu().numpy(), shapes), "plain")
+
+
+@pytest.mark.parametrize("seed", [31, 32, 33])
+def test_many_pass_random_batches(cuda_device, seed):
+    """Random uneven batches over every shape the one-launch executor takes (1D 2^8..2^16,
+    2D axes 2^7..2^11), random 128-byte-aligned gaps, both directions, each transform
+    against FP64 and every gap untouched."""
+    rng = np.random.default_rng(seed)
+    count = int(rng.integers(20, 60))
+    shapes = []
+    for _ in range(count):
+        if rng.random() < 0.6:
+            shapes.append((1 << int(rng.integers(8, 17)),))
+        else:
+            shapes.append((1 << int(rng.integers(7, 12)), 1 << int(rng.integers(7, 12))))
+    shapes = [s for s in shapes if int(np.prod(s)) <= 1 << 20]
+    parts, _ = pack(shapes, seed, "plain")
+    offsets, at = [], 0
+    for s in shapes:
+        at += 32 * int(rng.integers(0, 4))  # 0..3 gaps of 128 bytes
+        offsets.append(at)
+        at += int(np.prod(s))
+    buf = torch.full((at + 64, 2), 3.0, dtype=torch.float16, device="cuda")
+    for x, o in zip(parts, offsets):
+        buf[o:o + x.reshape(-1, 2).shape[0]] = torch.from_numpy(x.reshape(-1, 2)).half()
+    adjoint = bool(seed % 2)
+    with tc.Plan.many(shapes, offsets=offsets) as p:
+        assert "persistent" in p.info["schedule"], p.info["schedule"]
+        p.exec(buf, adjoint=adjoint)
+        p.check_device()
+    got = buf.double().cpu().numpy()
+    ys = [got[o:o + int(np.prod(s))].reshape(tuple(s) + (2,)) for s, o in zip(shapes, offsets)]
+    check(parts, ys, "plain", adjoint=adjoint)
+    covered = np.zeros(got.shape[0], dtype=bool)
+    for s, o in zip(shapes, offsets):
+        covered[o:o + int(np.prod(s))] = True
+    assert (got[~covered] == 3.0).all(), "a gap was written"
