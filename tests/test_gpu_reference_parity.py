@@ -69,7 +69,8 @@ def _require_reference():
 
 
 @pytest.mark.parametrize("kind", ["uniform", "reference_generator"])
-@pytest.mark.parametrize("n,batch", [(256, 32), (512, 32), (1024, 32), (131072, 1), (262144, 1), (524288, 1)])
+@pytest.mark.parametrize("n,batch", [(256, 32), (512, 32), (1024, 32), (131072, 1), (262144, 1), (524288, 1),
+                                     (1 << 24, 1)])
 def test_no_worse_than_reference_1d(cuda_device, n, batch, kind):
     x = _inputs((batch, n), kind, seed=42)
     xq = quantize(x, "plain")
