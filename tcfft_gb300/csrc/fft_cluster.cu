@@ -11,14 +11,35 @@
 //   [256 rows n1][N2 cols n2] view (two 32-column tiles, 64 KiB, loaded with
 //   the digit-ordered 5D boxes of the column role);
 //   phase 0: 256-point column FFTs in place, times W_N^(n2 k1);
-//   cluster barrier (remote mbarrier arrivals, release/acquire at cluster scope);
-//   phase 1: CTA r transforms rows k1 in [r 256/CL, (r+1) 256/CL) of length N2,
-//            reading each row's elements from the CTA that holds them
-//            (ld.shared::cluster); results stay in registers;
-//   cluster barrier (every CTA has read every slice);
+//   exchange: CTA r pushes to every CTA q of the cluster, itself included, the rows
+//            k1 in [q RPC, (q+1) RPC) of its two tiles (RPC = 256 / CL).  In the
+//            column role's row order those rows are 4 runs of 64 / CL consecutive
+//            tile rows per tile, so the exchange is 8 CL bulk shared::cluster copies
+//            per CTA, each completing on the receiver's mbarrier for that sender.
+//            The receive buffer keeps the bytes as they were (the swizzle phase of
+//            each row is that of its original row), so the row phase reads them
+//            with the bank pattern of a local tile;
+//   phase 1: CTA r transforms its RPC rows k1 of length N2 from its receive buffer
+//            (local shared-memory loads only); results stay in registers;
 //   output: X[k1 + 256 k2] of its rows written into its own stage and stored
 //            with 2D TMA boxes (rows k2 of 256/CL contiguous k1).
 // One HBM read and one write per element, no scratch, no global counters.
+//
+// Per transform c (every CTA of a cluster runs the same sequence of transforms),
+// three kinds of mbarrier, every wait on them bounded:
+//   recv[y]  (one per sender y, this CTA included: 1 arrival, this CTA arming it at
+//            the start of c, plus the 64 KiB / CL bytes of y's pieces): y's pieces of
+//            c have landed;
+//   pfree    (8 (CL - 1) arrivals, every compute warp of every peer after its row
+//            phase of c): the peers' receive buffers may take the pieces of c + 1;
+//   sent     (CL - 1 arrivals, each peer once it has all its pieces of c): this
+//            CTA's stage may be overwritten by the output of c (its own pieces have
+//            landed before its row phase).  The pieces of c + 1 into its own receive
+//            buffer follow its row phase of c in program order.
+// At exit every CTA passes a cluster barrier (no piece is pushed after it), waits
+// until the pieces its peers pushed to it (their counts, read remotely) have
+// landed, and passes a second barrier, so no CTA leaves while a copy into it is
+// in flight.
 #include <mutex>
 
 #include "fft_fused.cuh"
@@ -77,12 +98,20 @@ __device__ __forceinline__ bool wait_cluster(uint64_t* bar, uint32_t parity, int
   }
   return true;
 }
+// bulk copy of `bytes` (a multiple of 16) from this CTA's shared memory to a peer's,
+// completing `bytes` transactions on the peer's mbarrier `bar` (shared::cluster addresses)
+__device__ __forceinline__ void bulk_push(uint32_t dst, uint32_t src, uint32_t bytes, uint32_t bar) {
+  asm volatile("cp.async.bulk.shared::cluster.shared::cta.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+               ::"r"(dst), "r"(src), "r"(bytes), "r"(bar)
+               : "memory");
+}
 __device__ __forceinline__ void cluster_sync_all() {
   asm volatile("barrier.cluster.arrive.release.aligned;\nbarrier.cluster.wait.acquire.aligned;" ::: "memory");
 }
 
 template <int CL>
 struct ClCfg {
+  static constexpr int kLgCL = CL == 2 ? 1 : CL == 4 ? 2 : CL == 8 ? 3 : 4;
   static constexpr int kN2 = 64 * CL;
   static constexpr int kN = 256 * kN2;
   static constexpr int kRPC = 256 / CL;                  // phase-1 rows per CTA
@@ -92,20 +121,31 @@ struct ClCfg {
   static constexpr int kBH = kN2 < 256 ? kN2 : 256;      // output box height (rows k2)
   static constexpr int kTileBytes = 256 * 32 * 4;        // one 32-column tile
   static constexpr int kStageBytes = 65536;
-  static constexpr int kStages = 3;
-  static constexpr int kLog2N = 14 + (CL == 2 ? 1 : CL == 4 ? 2 : CL == 8 ? 3 : 4);
+  static constexpr int kStages = 2;
+  // receive buffer: per sender q and tile t a block of the RPC tile rows of this CTA's k1
+  // range (4 pieces of kPieceRows consecutive rows), at (2 q + t) kBlockBytes
+  static constexpr int kRecvBytes = 65536;
+  static constexpr int kPieceRows = 64 / CL;
+  static constexpr int kPieceBytes = kPieceRows * 128;
+  static constexpr int kBlockBytes = kRPC * 128;
+  static constexpr int kPieces = 8 * CL;                          // pushed per transform
+  static constexpr uint32_t kSenderTx = 8u * kPieceBytes;         // bytes from one sender
+  static constexpr int kLog2N = 14 + kLgCL;
   static constexpr int kTwShift = (kLog2N + 1) / 2;
   static constexpr int kTwLo = 1 << kTwShift, kTwHi = kN >> kTwShift;
   static constexpr int kFold1 = (CL >= 4) ? FoldTab<kR1>::kBytes : 0;
   static constexpr int kTabBytes = (kTwLo + kTwHi + 128) * 8 + FoldTab<1>::kBytes + kFold1;
-  static constexpr int kBars = 5 * kStages;
-  static constexpr int kSmem = kStages * kStageBytes + kTabBytes + 1024 + kBars * 8 + 64;
+  static constexpr int kBars = 3 * kStages + CL + 2;
+  static constexpr int kCtl = 2 + CL;  // ints: transforms pushed, transforms armed, received per sender
+  static constexpr int kSmem = kStages * kStageBytes + kRecvBytes + kTabBytes + 1024 + kBars * 8 + kCtl * 4 + 64;
   using PI = BitPerm<0, 1, 3, 2>;
   // row phase: lane digit t in bits 0-1 of m1, so that one load instruction (fixed r, kt, j, a)
-  // reads a single 64-column slice, i.e. a single peer CTA
+  // reads a single 64-column slice, i.e. a single sender's block
   using PI1 = BitPerm<2, 0, 1, 3>;
   using RHO = BitPerm<0, 2, 3, 1>;
   static_assert(kRPC * kN2 * 4 == kStageBytes, "a CTA's output slice is one stage");
+  static_assert(2 * CL * kBlockBytes == kRecvBytes && 4 * kPieceBytes == kBlockBytes, "receive buffer layout");
+  static_assert(kPieceBytes % 16 == 0, "bulk copies move multiples of 16 bytes");
 };
 
 struct ClParams {
@@ -119,10 +159,25 @@ struct ClParams {
 };
 
 template <int CL>
-__device__ __forceinline__ void compute_warps(unsigned char* smem, uint64_t* full, uint64_t* computed, uint64_t* p0,
-                                              uint64_t* p1, unsigned char* s_fold0, unsigned char* s_fold1,
-                                              float2* s_tw128, float2* s_twlo, float2* s_twhi, const ClParams& p,
-                                              uint32_t rank, long long first, long long step);
+__device__ __forceinline__ void compute_warps(unsigned char* smem, uint64_t* full, uint64_t* computed, uint64_t* recv,
+                                              uint64_t* pfree, uint64_t* sent, int* ctl, unsigned char* s_fold0,
+                                              unsigned char* s_fold1, float2* s_tw128, float2* s_twlo,
+                                              float2* s_twhi, const ClParams& p, uint32_t rank, long long first,
+                                              long long step);
+
+// Exit: wait until every piece a peer pushed to this CTA has landed (the peers' push counts are
+// read after a cluster barrier, so no further piece follows).  One thread.
+template <int CL>
+__device__ __forceinline__ void drain_pieces(uint64_t* recv, int* ctl, uint32_t rank, int* err) {
+  using Cfg = ClCfg<CL>;
+  for (int y = 0; y < CL; ++y) {
+    const int pushed = (int)ld_cluster(mapa(smem_addr(&ctl[0]), (uint32_t)y));
+    for (int c = ctl[2 + y]; c < pushed; ++c) {
+      if (c >= ctl[1]) mbar_arrive_expect_tx(&recv[y], Cfg::kSenderTx);  // a phase not armed yet
+      if (!mbar_wait(&recv[y], (uint32_t)c & 1, err)) break;
+    }
+  }
+}
 
 template <int CL>
 __global__ void __launch_bounds__(384, 1) fft_cluster_kernel(const __grid_constant__ CUtensorMap load_map,
@@ -137,7 +192,7 @@ __global__ void __launch_bounds__(384, 1) fft_cluster_kernel(const __grid_consta
   // aligning it the same way keeps local and remote offsets equal
   unsigned char* smem =
       reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-  unsigned char* tab = smem + NST * Cfg::kStageBytes;
+  unsigned char* tab = smem + NST * Cfg::kStageBytes + Cfg::kRecvBytes;
   float2* s_twlo = reinterpret_cast<float2*>(tab);
   float2* s_twhi = s_twlo + Cfg::kTwLo;
   float2* s_tw128 = s_twhi + Cfg::kTwHi;  // W_128^j (CL = 2 rows)
@@ -146,8 +201,10 @@ __global__ void __launch_bounds__(384, 1) fft_cluster_kernel(const __grid_consta
   uint64_t* full = reinterpret_cast<uint64_t*>(tab + Cfg::kTabBytes);
   uint64_t* computed = full + NST;
   uint64_t* empty = computed + NST;
-  uint64_t* p0 = empty + NST;  // column phase done, all CTAs (8 CL arrivals)
-  uint64_t* p1 = p0 + NST;     // row phase has read every slice (8 CL arrivals)
+  uint64_t* recv = empty + NST;  // [CL] by sender rank
+  uint64_t* pfree = recv + CL;
+  uint64_t* sent = pfree + 1;
+  int* ctl = reinterpret_cast<int*>(sent + 1);  // [0] transforms pushed, [1] armed, [2 + y] received from y
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const uint32_t rank = cluster_rank();
@@ -157,9 +214,11 @@ __global__ void __launch_bounds__(384, 1) fft_cluster_kernel(const __grid_consta
       mbar_init(&full[s], 1);
       mbar_init(&computed[s], 8);
       mbar_init(&empty[s], 1);
-      mbar_init(&p0[s], 8 * CL);
-      mbar_init(&p1[s], 8 * CL);
     }
+    for (int y = 0; y < CL; ++y) mbar_init(&recv[y], 1);
+    mbar_init(pfree, 8 * (CL - 1));
+    mbar_init(sent, CL - 1);
+    for (int i = 0; i < Cfg::kCtl; ++i) ctl[i] = 0;
     fence_barrier_init();
   }
   for (int j = tid; j < Cfg::kTwLo; j += blockDim.x) s_twlo[j] = p.twlo[j];
@@ -171,7 +230,7 @@ __global__ void __launch_bounds__(384, 1) fft_cluster_kernel(const __grid_consta
   cluster_sync_all();  // every CTA's barriers are initialised before any remote arrival
 
   if (warp >= 8) asm volatile("setmaxnreg.dec.sync.aligned.u32 %0;" ::"n"(56));
-  // every warp, the auxiliary ones included, ends at the closing cluster barrier
+  // every warp, the auxiliary ones included, ends at the closing cluster barriers
   if (warp >= 10) {
     // idle
   } else if (warp == 8) {  // ------------------------------------------------ TMA producer
@@ -211,16 +270,22 @@ __global__ void __launch_bounds__(384, 1) fft_cluster_kernel(const __grid_consta
     }
     __syncwarp();
   } else {
-    compute_warps<CL>(smem, full, computed, p0, p1, s_fold0, s_fold1, s_tw128, s_twlo, s_twhi, p, rank, first, step);
+    compute_warps<CL>(smem, full, computed, recv, pfree, sent, ctl, s_fold0, s_fold1, s_tw128, s_twlo, s_twhi, p,
+                      rank, first, step);
   }
-  cluster_sync_all();  // no CTA leaves while another may still read its shared memory
+  __syncwarp();
+  cluster_sync_all();  // no piece is pushed after this barrier
+  if (tid == 0) drain_pieces<CL>(recv, ctl, rank, p.err);
+  __syncwarp();
+  cluster_sync_all();  // no CTA leaves while a piece may land in it or a peer reads its count
 }
 
 template <int CL>
-__device__ __forceinline__ void compute_warps(unsigned char* smem, uint64_t* full, uint64_t* computed, uint64_t* p0,
-                                              uint64_t* p1, unsigned char* s_fold0, unsigned char* s_fold1,
-                                              float2* s_tw128, float2* s_twlo, float2* s_twhi, const ClParams& p,
-                                              uint32_t rank, long long first, long long step) {
+__device__ __forceinline__ void compute_warps(unsigned char* smem, uint64_t* full, uint64_t* computed, uint64_t* recv,
+                                              uint64_t* pfree, uint64_t* sent, int* ctl, unsigned char* s_fold0,
+                                              unsigned char* s_fold1, float2* s_tw128, float2* s_twlo,
+                                              float2* s_twhi, const ClParams& p, uint32_t rank, long long first,
+                                              long long step) {
   using Cfg = ClCfg<CL>;
   using PI = typename Cfg::PI;
   using RHO = typename Cfg::RHO;
@@ -232,6 +297,7 @@ __device__ __forceinline__ void compute_warps(unsigned char* smem, uint64_t* ful
   init_job_consts<false, PI, RHO>(jc, p.tw2048);
   if constexpr (CL >= 4) init_job_consts<false, PI1, RHO>(jc1, p.tw2048);
   const uint32_t fold0 = smem_addr(s_fold0), fold1 = smem_addr(s_fold1), tw128 = smem_addr(s_tw128);
+  const uint32_t rbuf = smem_addr(smem + NST * Cfg::kStageBytes);
   WnTable wn;
   wn.hi = smem_addr(s_twhi);
   wn.lo = smem_addr(s_twlo);
@@ -240,38 +306,72 @@ __device__ __forceinline__ void compute_warps(unsigned char* smem, uint64_t* ful
   wn.global = false;
   wn.shift = Cfg::kTwShift;
   wn.nmask = Cfg::kN - 1;
-  uint32_t remote_p0[CL], remote_p1[CL];
   const int g = lane >> 2, tq = lane & 3;
+  const bool leader = warp == 0 && lane == 0;
   int cnt = 0;
   for (long long it = first; it < p.batch; it += step, ++cnt) {
     const int s = cnt % NST;
-    const uint32_t par = (cnt / NST) & 1;
-    bool ok = named_bar_and(2, 256, mbar_wait(&full[s], par, p.err));
+    const uint32_t par = (cnt / NST) & 1, tpar = (uint32_t)cnt & 1;
     const uint32_t base = smem_addr(smem + s * Cfg::kStageBytes);
+    if (leader) {  // arm the receive barriers of this transform (pieces may already be landing)
+      for (int y = 0; y < CL; ++y) mbar_arrive_expect_tx(&recv[y], Cfg::kSenderTx);
+      ctl[1] = cnt + 1;
+    }
+    bool ok = named_bar_and(2, 256, mbar_wait(&full[s], par, p.err));
     if (ok) {
-#pragma unroll
-      for (int q = 0; q < CL; ++q) {
-        remote_p0[q] = mapa(smem_addr(&p0[s]), q);
-        remote_p1[q] = mapa(smem_addr(&p1[s]), q);
-      }
       // phase 0: the two 32-column tiles of this CTA's slice
 #pragma unroll 1
       for (int t = 0; t < 2; ++t)
         plain_col_tile<1, 32, true, PI, RHO>(jc, fold0, base + t * Cfg::kTileBytes, warp, p.dsign,
                                              (int)(64 * rank + 32 * t), wn, p.oscale);
-      __syncwarp();
-      if (lane == 0)
-        for (int q = 0; q < CL; ++q) arrive_remote(remote_p0[q]);
-      ok = named_bar_and(2, 256, wait_cluster(&p0[s], par, p.err));
+      fence_proxy_async_smem();  // the pieces are read by bulk copies
     }
+    ok = named_bar_and(2, 256, ok);
+    if (warp == 0) {
+      // push: once every peer's receive buffer is free (their row phase of the previous
+      // transform is done), piece i = (receiver q, tile t, run hi) goes to q's block (rank, t)
+      bool go = ok;
+      if (lane == 0 && go) go = wait_cluster(pfree, (uint32_t)(cnt + 1) & 1, p.err);
+      go = __shfl_sync(0xffffffffu, go, 0);
+      if (go) {
+        for (int i = lane; i < Cfg::kPieces; i += 32) {
+          const int t = (i >> 2) & 1, hi = i & 3;
+          const uint32_t q = (uint32_t)(i >> 3);
+          const uint32_t src =
+              base + (uint32_t)(t * Cfg::kTileBytes + ((hi << 6) | ((int)q << (6 - Cfg::kLgCL))) * 128);
+          const uint32_t dst =
+              mapa(rbuf + (uint32_t)((2 * (int)rank + t) * Cfg::kBlockBytes + hi * Cfg::kPieceBytes), q);
+          bulk_push(dst, src, (uint32_t)Cfg::kPieceBytes, mapa(smem_addr(&recv[rank]), q));
+        }
+      }
+      __syncwarp();
+      if (lane == 0 && go) ctl[0] = cnt + 1;
+      ok = go;
+    }
+    // every sender's pieces of this transform
+    bool got = ok;
+#pragma unroll 1
+    for (int y = 0; y < CL; ++y)
+      if (got) {
+        got = mbar_wait(&recv[y], tpar, p.err);
+        if (got && leader) ctl[2 + y] = cnt + 1;
+      }
+    ok = named_bar_and(2, 256, got);
+    if (ok && leader)
+      for (int y = 0; y < CL; ++y)
+        if (y != (int)rank) arrive_remote(mapa(smem_addr(sent), (uint32_t)y));
     constexpr int OUTN = 64;  // output values held per lane
     uint32_t out[OUTN];
     if (ok) {
-      // phase 1: rows k1 = rank RPC + ...; element (k1, n2) lives in CTA n2 / 64
+      // phase 1: rows k1 = rank RPC + ...; element (k1, n2) was computed by CTA n2 / 64 and sits in
+      // that sender's block of the receive buffer, at its tile row's rank among the rows of this
+      // k1 range, with the swizzle of the original row
       auto elem = [&](int k1, int n2) {
-        const uint32_t local = base + (uint32_t)(((n2 & 63) >> 5) * Cfg::kTileBytes) +
-                               ctile_off<32, 4>(col_out_row(k1, 0), n2 & 31);
-        return ld_cluster(mapa(local, (uint32_t)(n2 >> 6)));
+        const int q = n2 >> 6, t = (n2 >> 5) & 1;
+        const int row = col_out_row(k1, 0);
+        const uint32_t off = ctile_off<32, 4>(row, n2 & 31);
+        const int crow = (row & (Cfg::kPieceRows - 1)) | ((row >> 6) * Cfg::kPieceRows);
+        return lds32(rbuf + (uint32_t)((2 * q + t) * Cfg::kBlockBytes + crow * 128) + (off & 127u));
       };
       if constexpr (CL == 2) {
         // 128 rows per CTA: one job of 16 rows (length 128 = 16 x 8) per warp
@@ -294,10 +394,12 @@ __device__ __forceinline__ void compute_warps(unsigned char* smem, uint64_t* ful
         }
       }
       __syncwarp();
-      if (lane == 0)
-        for (int q = 0; q < CL; ++q) arrive_remote(remote_p1[q]);
-      ok = named_bar_and(2, 256, wait_cluster(&p1[s], par, p.err));
+      if (lane == 0)  // this warp has read its part of the receive buffer
+        for (int y = 0; y < CL; ++y)
+          if (y != (int)rank) arrive_remote(mapa(smem_addr(pfree), (uint32_t)y));
     }
+    // the stage is overwritten only once every peer holds its pieces of this transform
+    ok = named_bar_and(2, 256, ok && wait_cluster(sent, tpar, p.err));
     if (ok) {
       // output rows k2 of this CTA's RPC consecutive k1, chunks of W columns
       auto put = [&](int k1l, int k2, uint32_t v) {
@@ -391,14 +493,17 @@ cudaError_t dispatch_cluster(int64_t n, const CUtensorMap& lm, const CUtensorMap
 }  // namespace
 
 // Whether this GPU can run the cluster kernel for n (plain): it needs CL co-resident CTAs of
-// ~215 KiB shared memory each in one GPU processing cluster.
-bool cluster_supported(int64_t n, bool split, int num_sms) {
+// ~215 KiB shared memory each in one GPU processing cluster.  *active_clusters: how many such
+// clusters the device holds at once.
+bool cluster_supported(int64_t n, bool split, int num_sms, int* active_clusters) {
   if (split || n < (1 << 15) || n > (1 << 18)) return false;
   CUtensorMap dummy;
   memset(&dummy, 0, sizeof dummy);
   ClParams p = {};
   int active = 0;
-  return dispatch_cluster(n, dummy, dummy, p, num_sms, nullptr, &active) == cudaSuccess && active > 0;
+  const bool ok = dispatch_cluster(n, dummy, dummy, p, num_sms, nullptr, &active) == cudaSuccess && active > 0;
+  if (active_clusters) *active_clusters = active;
+  return ok;
 }
 
 cudaError_t launch_cluster(int64_t n, void* data, int64_t batch, const float2* tw2048, const float2* twlo,

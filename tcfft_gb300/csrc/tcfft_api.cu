@@ -1620,19 +1620,21 @@ tcfftStatus tcfftPlan1d(tcfftPlan* out, int64_t n, int64_t batch, const tcfftOpt
   p->radices_x = chain;
   st = alloc_tables(p);
   const char* cl_env = getenv("TCFFT_CLUSTER");
+  int active_clusters = 0;
   if (st == TCFFT_SUCCESS && s.kind == Schedule::kFused1d && cl_env && atoi(cl_env) != 0 &&
-      cluster_supported(n, o.precision != TCFFT_PRECISION_PLAIN, p->num_sms)) {
+      cluster_supported(n, o.precision != TCFFT_PRECISION_PLAIN, p->num_sms, &active_clusters)) {
     // opt-in: clusters of N / 2^14 CTAs, one transform per cluster, no L2 round trip.  Correct at
-    // N = 2^15..2^18 but slower than the two-phase kernel above 2^15 (remote shared-memory loads
-    // and the cluster-wide barrier between the phases), so the planner does not pick it by itself.
+    // N = 2^15..2^18 but slower than the two-phase kernel (warps waiting at the exchange barriers,
+    // bank conflicts of its write-back and row phase: 1.32 against 1.13 ms at 2^15 for 2^28
+    // elements, 4.3 against 0.9 ms at 2^18), so the planner does not pick it by itself.
     p->sched = Schedule();
     p->sched.kind = Schedule::kCluster;
     p->sched.N1 = 256;
     p->sched.N2 = n / 256;
     p->sched.launches = 1;
     char buf[160];
-    snprintf(buf, sizeof buf, "cluster(plain): N=256 x %lld on %lld CTAs sharing shared memory, one HBM pass",
-             (long long)(n / 256), (long long)(n >> 14));
+    snprintf(buf, sizeof buf, "cluster(plain): N=256 x %lld on %lld CTAs sharing shared memory, %d clusters, one HBM pass",
+             (long long)(n / 256), (long long)(n >> 14), active_clusters);
     p->sched.text = buf;
     st = alloc_wn_tables(p, n);
   }

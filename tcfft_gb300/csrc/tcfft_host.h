@@ -88,7 +88,7 @@ cudaError_t launch_resident_tout(int64_t n, const void* in, void* out, int64_t b
                                  float oscale = 1.f);
 
 // One transform per thread-block cluster, N = 2^15..2^18 plain (fft_cluster.cu).
-bool cluster_supported(int64_t n, bool split, int num_sms);
+bool cluster_supported(int64_t n, bool split, int num_sms, int* active_clusters = nullptr);
 cudaError_t launch_cluster(int64_t n, void* data, int64_t batch, const float2* tw2048, const float2* twlo,
                            const float2* twhi, float dsign, int* err, int num_sms, cudaStream_t st, CUtensorMap* lm,
                            CUtensorMap* sm, bool encode, float oscale = 1.f, const void* in = nullptr);

@@ -148,14 +148,18 @@ def test_split_2048_and_short_rows(cuda_device, n):
     assert oracle.rel_l2(y2, oracle_2d(x2)) < tol_split(256 * 2048)
 
 
+@pytest.mark.parametrize("many", [False, True])
 @pytest.mark.parametrize("n", [1 << 15, 1 << 16, 1 << 17, 1 << 18])
-def test_cluster_opt_in(cuda_device, monkeypatch, n):
+def test_cluster_opt_in(cuda_device, monkeypatch, n, many):
     """The thread-block-cluster kernel (one transform per cluster of N / 2^14
     CTAs, phases exchanged through distributed shared memory), selected with
-    TCFFT_CLUSTER=1 where the device can co-schedule the cluster."""
+    TCFFT_CLUSTER=1 where the device can co-schedule the cluster.  `many`: at
+    least four transforms per cluster, so that both stages, the receive buffer
+    and every per-transform barrier are reused (parities 0 and 1)."""
     monkeypatch.setenv("TCFFT_CLUSTER", "1")
-    batch = 5
-    xq = quantize(uniform_input((batch, n), seed=n % 97), "plain")
+    cl = n >> 14
+    batch = 4 * (152 // cl) + 3 if many else 5
+    xq = quantize(uniform_input((batch, n), seed=n % 97 + batch), "plain")
     with tc.Plan(n=n, batch=batch) as p:
         sched = p.info["schedule"]
         y = run_gpu(p, xq, "plain")
