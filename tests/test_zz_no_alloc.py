@@ -59,6 +59,43 @@ def test_noalloc_matches_plan_two_calls(cuda_device, n, batch, precision):
             assert err < bound, "n=%d call %d direction %d: rel-L2 %.3e vs FP64" % (n, call, direction, err)
 
 
+@pytest.mark.parametrize("n,batch,precision", [(1 << 16, 3, "plain"), (1 << 14, 2, "split")])
+def test_noalloc_stream_capture(cuda_device, tmp_path, n, batch, precision):
+    """A call captured into a CUDA graph, after one warm-up call has set up the
+    static arrays, replays correctly.  The capture runs in the global capture
+    mode, which fails any allocation call made during it; the graph holds the
+    table kernel, the counter memset and the transform, and no allocation node."""
+    import torch
+    dt = torch.float16 if precision == "plain" else torch.float32
+    prec = 0 if precision == "plain" else 1
+    x = quantize(uniform_input((batch, n), seed=n % 37 + 5), precision)
+    xt = torch.from_numpy(x).to(dt).to(cuda_device)
+    t = xt.clone()
+    assert _noalloc(t.clone(), n, batch, precision, 0) == 0  # warm-up: set-up outside the capture
+    g = torch.cuda.CUDAGraph()
+    dump = hasattr(g, "enable_debug_mode") and hasattr(g, "debug_dump")
+    if dump:
+        g.enable_debug_mode()
+    with torch.cuda.graph(g, capture_error_mode="global"):
+        st = tc.lib().tcfftExecute1dNoAlloc(ctypes.c_void_p(t.data_ptr()), n, batch, prec, 0,
+                                            ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+    assert st == 0
+    exact = oracle_1d(x)
+    for rep in range(2):
+        t.copy_(xt)
+        g.replay()
+        torch.cuda.synchronize()
+        assert tc.lib().tcfftCheckDeviceNoAlloc(None) == 0
+        y = to_complex(t.double().cpu().numpy())
+        err = np.linalg.norm(y - exact) / np.linalg.norm(exact)
+        assert err < tol(precision, n), "replay %d: rel-L2 %.3e" % (rep, err)
+    if dump:
+        path = tmp_path / "noalloc_graph.dot"
+        g.debug_dump(str(path))
+        text = path.read_text().lower()
+        assert "mem_alloc" not in text and "memalloc" not in text, "allocation node in the captured graph"
+
+
 def test_noalloc_rejects_sizes_beyond_limit(cuda_device):
     import torch
     t = torch.zeros((1, 1 << 22, 2), dtype=torch.float16, device=cuda_device)
