@@ -1,5 +1,6 @@
-// fft_resident.cu -- 1D FFTs of N = 256 x 16 R1 (R1 = 1, 2, 4: N = 4096, 8192,
-// 16384) held entirely in one CTA's shared memory.
+// fft_resident.cu -- 1D FFTs of N = 256 x 16 R1 (R1 = 1, 2, 4, 8: N = 4096, 8192,
+// 16384, 32768) held entirely in one CTA's shared memory (32768: a variant with one
+// transform in two stages, after the first kernel below).
 //
 // Same four-step factorisation as the two-phase kernel (fft_fused.cuh), but a
 // whole transform (16-64 KiB) fits in one 64 KiB stage, so both phases run on
@@ -489,10 +490,207 @@ cudaError_t launch_resident_t(const CUtensorMap& lm, const CUtensorMap& sm, cons
   return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------------------
+// N = 32768 = 256 x 128 plain.  A transform (128 KiB) fills two of the three 64 KiB
+// stages (A, B: its four 32-column tiles); the third (C) takes half of the output.
+//   phase 0: 256-point column FFTs of the four tiles in place, times W_N^(n2 k1);
+//   phase 1, round 1: the 8 jobs of rows k1 < 128 (one 16-row job of 128 points per
+//            warp), outputs written straight into C; C is stored;
+//   round 2: the 8 jobs of rows k1 >= 128, outputs written into the tile rows round 1
+//            consumed (in the column role's row order, k1 < 128 are the tile rows with
+//            bit 5 clear: 4 runs of 32 rows per tile, 4 KiB each), stored the same way;
+//   the next transform is loaded once the second half has been read out (one
+//   transform in flight per CTA; its load is not overlapped with compute).
+// Output box (one TMA store, 4 KiB): 32 consecutive k1 x k2 bits 3-5 x k2 bits 0-1,
+// at fixed k1 bits 5-7, k2 bit 2 and k2 bit 6.  The row jobs run with the identity
+// output digit order (k2 = q + 8 (g + 8 h)), so the 8 lanes g of one store
+// instruction write 8 box rows of different swizzle phases and the 4 lanes t write
+// k1 bits 0-1 of one chunk: one wavefront per instruction.
+struct Res32kCfg {
+  static constexpr int kN = 32768, kC = 32, kCG = 4;  // N2 = 128 = 16 x 8
+  static constexpr int kTileBytes = 256 * kC * 4;  // 32 KiB
+  static constexpr int kStageBytes = 65536;
+  static constexpr int kInBytes = 2 * kStageBytes;  // A + B
+  static constexpr int kBoxBytes = 4096;
+  static constexpr int kTwShift = 8, kTwLo = 256, kTwHi = 128;
+  static constexpr int kTabBytes = (kTwLo + kTwHi) * 8 + FoldTab<8>::kABytes;
+  static constexpr int kSmem = 3 * kStageBytes + kTabBytes + 1024 + 256;
+  static constexpr int kThreads = 384;
+  using PI = BitPerm<0, 1, 3, 2>;    // phase 0 (column jobs)
+  using PI1 = BitPerm<0, 2, 3, 1>;   // phase 1: lane t reads points 4t .. 4t + 3
+  using RHO = BitPerm<0, 2, 3, 1>;   // phase 0
+  using RHO1 = BitPerm<0, 1, 2, 3>;  // phase 1: output digit k0 = g + 8 h
+  static_assert(kTileBytes * kCG == kInBytes, "a transform fills stages A and B");
+  static_assert(16 * kBoxBytes == kStageBytes, "half an output is 16 boxes");
+};
+
+// Byte address of output X[k1 + 256 k2] (k1 in the given round's half): box u = 4 c + k2
+// bit 2 + 2 k2 bit 6 (c = k1 bits 5-6) in C (round 0) or in run u & 3 of tile u >> 2 (round
+// 1), box row k2 bits 3-5 | k2 bits 0-1 << 3, 128-byte swizzle.
+__device__ __forceinline__ uint32_t res32k_out(uint32_t abase, uint32_t cbase, int round, int k1, int k2) {
+  const int u = 4 * ((k1 >> 5) & 3) + ((k2 >> 2) & 1) + 2 * (k2 >> 6);
+  const int row = ((k2 >> 3) & 7) | ((k2 & 3) << 3);
+  const uint32_t box = round == 0 ? cbase + (uint32_t)(u * Res32kCfg::kBoxBytes)
+                                  : abase + (uint32_t)((u >> 2) * Res32kCfg::kTileBytes + (u & 3) * 8192);
+  return box + ctile_off<32, 4>(row, k1 & 31);
+}
+
+__global__ void __launch_bounds__(384, 1) fft_resident32k_kernel(const __grid_constant__ CUtensorMap load_map,
+                                                                  const __grid_constant__ CUtensorMap store_map,
+                                                                  const ResParams p) {
+  using Cfg = Res32kCfg;
+  using PI = Cfg::PI;
+  using PI1 = Cfg::PI1;
+  using RHO = Cfg::RHO;
+  using RHO1 = Cfg::RHO1;
+  constexpr int C = Cfg::kC, CG = Cfg::kCG;
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  unsigned char* smem =
+      reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  unsigned char* cbuf = smem + Cfg::kInBytes;
+  unsigned char* tab = cbuf + Cfg::kStageBytes;
+  float2* s_twlo = reinterpret_cast<float2*>(tab);
+  float2* s_twhi = s_twlo + Cfg::kTwLo;
+  unsigned char* s_fold = reinterpret_cast<unsigned char*>(s_twhi + Cfg::kTwHi);
+  uint64_t* full = reinterpret_cast<uint64_t*>(tab + Cfg::kTabBytes);  // the transform is loaded
+  uint64_t* infree = full + 1;  // stages A and B read out (second half stored)
+  uint64_t* cfree = full + 2;   // stage C read out (first half stored)
+  uint64_t* half = full + 3;    // [2]: a half of the output written (8 compute warps)
+
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  if (tid == 0) {
+    mbar_init(full, 1);
+    mbar_init(infree, 1);
+    mbar_init(cfree, 1);
+    mbar_init(&half[0], 8);
+    mbar_init(&half[1], 8);
+    fence_barrier_init();
+  }
+  for (int j = tid; j < Cfg::kTwLo; j += blockDim.x) s_twlo[j] = p.twlo[j];
+  for (int j = tid; j < Cfg::kTwHi; j += blockDim.x) s_twhi[j] = p.twhi[j];
+  build_fold_table<8, PI1, RHO1, false>(s_fold, p.tw2048, tid, blockDim.x);  // phase-1 radix-8 fold (A part)
+  __syncthreads();
+
+  if (warp >= 8) asm volatile("setmaxnreg.dec.sync.aligned.u32 %0;" ::"n"(56));
+  if (warp >= 10) return;
+  if (warp == 8) {  // ------------------------------------------------ TMA producer
+    if (lane == 0) {
+      prefetch_tmap(&load_map);
+      int cnt = 0;
+      for (long long it = blockIdx.x; it < p.batch; it += gridDim.x, ++cnt) {
+        if (!mbar_wait(infree, (uint32_t)(cnt + 1) & 1, p.err)) break;
+        mbar_arrive_expect_tx(full, Cfg::kInBytes);
+#pragma unroll 1
+        for (int cg = 0; cg < CG; ++cg)
+          tma_load_5d(smem + cg * Cfg::kTileBytes, &load_map, cg * C, 0, 0, 0, (int)it, full);
+      }
+      if (cnt > 0) mbar_wait(full, (uint32_t)(cnt - 1) & 1, nullptr);  // the last load has landed
+    }
+    return;
+  }
+  if (warp == 9) {  // ------------------------------------------------ TMA storer
+    if (lane == 0) {
+      prefetch_tmap(&store_map);
+      int cnt = 0;
+      for (long long it = blockIdx.x; it < p.batch; it += gridDim.x, ++cnt) {
+#pragma unroll 1
+        for (int round = 0; round < 2; ++round) {
+          if (!mbar_wait(&half[round], (uint32_t)cnt & 1, p.err)) {
+            cnt = -1;
+            break;
+          }
+#pragma unroll 1
+          for (int u = 0; u < 16; ++u) {
+            const unsigned char* src = round == 0 ? cbuf + u * Cfg::kBoxBytes
+                                                  : smem + (u >> 2) * Cfg::kTileBytes + (u & 3) * 8192;
+            tma_store_5d(&store_map, 128 * round + 32 * (u >> 2), 0, 0, u & 1, ((u >> 1) & 1) + 2 * (int)it, src);
+          }
+          bulk_commit();
+          bulk_wait_read<0>();
+          mbar_arrive(round == 0 ? cfree : infree);
+        }
+        if (cnt < 0) break;
+      }
+      bulk_wait<0>();
+    }
+    return;
+  }
+
+  // ------------------------------------------------------------------ compute warps
+  asm volatile("setmaxnreg.inc.sync.aligned.u32 %0;" ::"n"(224));
+  JobConsts<false> jc, jc1;
+  init_job_consts<false, PI, RHO>(jc, p.tw2048);
+  init_job_consts<false, PI1, RHO1>(jc1, p.tw2048);
+  const uint32_t fold = smem_addr(s_fold);
+  const uint32_t abase = smem_addr(smem), cbase = smem_addr(cbuf);
+  WnTable wn;
+  wn.hi = smem_addr(s_twhi);
+  wn.lo = smem_addr(s_twlo);
+  wn.ghi = p.twhi;
+  wn.glo = p.twlo;
+  wn.global = false;
+  wn.shift = Cfg::kTwShift;
+  wn.nmask = Cfg::kN - 1;
+  const int tq = lane & 3;
+  int cnt = 0;
+  for (long long it = blockIdx.x; it < p.batch; it += gridDim.x, ++cnt) {
+    bool ok = named_bar_and(2, 256, mbar_wait(full, (uint32_t)cnt & 1, p.err));
+    if (ok) {
+      // phase 0: columns of 256 (in place, digit-ordered rows), twiddle W_N^(n2 k1); two passes of
+      // two columns per warp, as for the one-transform stages of 16384
+#pragma unroll 1
+      for (int tile = 0; tile < CG; ++tile)
+#pragma unroll 1
+        for (int h = 0; h < 2; ++h)
+          plain_col_tile<1, C, true, PI, RHO, 2>(jc, fold, abase + tile * Cfg::kTileBytes, warp + 8 * h, p.dsign,
+                                                 tile * C, wn, p.oscale);
+    }
+    // round 1 writes into C once its previous contents have been stored
+    ok = named_bar_and(2, 256, ok && mbar_wait(cfree, (uint32_t)(cnt + 1) & 1, p.err));
+#pragma unroll 1
+    for (int round = 0; round < 2; ++round) {
+      if (ok) {
+        // 16 rows k1 per job, FFT over n2 (length 128); job jl = warp + 8 round
+        const int jl = warp + 8 * round;
+        auto ld4 = [&](int v, int a, uint32_t(&w)[4]) {
+          const int n = 4 * tq + 16 * a;
+          lds128(abase + (uint32_t)((n >> 5) * Cfg::kTileBytes) +
+                     ctile_off<C, 4>(col_out_row(kap_of<C>(v, jl), 0), n & (C - 1)),
+                 w);
+        };
+        auto st = [&](int v, int k2, int, int, float2 val) {
+          sts32(res32k_out(abase, cbase, round, kap_of<C>(v, jl), k2), pack_h2(val.x, val.y));
+        };
+        fft16r_job_q_fold<8, PI1, RHO1>(jc1, fold, p.dsign, ld4, st);
+      }
+      fence_proxy_async_smem();  // the half is read by TMA stores
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&half[round]);
+      // round 2 overwrites the rows round 1 read: every warp has finished round 1
+      if (round == 0) ok = named_bar_and(2, 256, ok);
+    }
+    if (!ok) break;
+  }
+}
+
+cudaError_t launch_resident32k(const CUtensorMap& lm, const CUtensorMap& sm, const ResParams& p, int num_sms,
+                               cudaStream_t st) {
+  using Cfg = Res32kCfg;
+  static std::once_flag once;
+  static cudaError_t init_err = cudaSuccess;
+  std::call_once(once, [&] {
+    init_err = cudaFuncSetAttribute(fft_resident32k_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg::kSmem);
+  });
+  if (init_err != cudaSuccess) return init_err;
+  const long long grid = p.batch < num_sms ? p.batch : num_sms;
+  fft_resident32k_kernel<<<(int)grid, Cfg::kThreads, Cfg::kSmem, st>>>(lm, sm, p);
+  return cudaGetLastError();
+}
+
 }  // namespace
 
 bool resident_supported(int64_t n, bool split) {
-  return split ? (n == 4096 || n == 8192) : (n == 4096 || n == 8192 || n == 16384);
+  return split ? (n == 4096 || n == 8192) : (n == 4096 || n == 8192 || n == 16384 || n == 32768);
 }
 
 // Tensor maps: column-tile loads of the [B*256 rows][N2 cols] view; stores of
@@ -538,7 +736,19 @@ cudaError_t launch_resident(int64_t n, void* data, int64_t batch, const float2* 
                             CUtensorMap* lm, CUtensorMap* sm, bool encode, float oscale, const void* in) {
   const int64_t n2 = n / 256;
   const int C = n2 < 32 ? (int)n2 : 32;
-  if (encode) {
+  if (encode && n == 32768) {
+    // stores: 4 KiB boxes of X[k1 + 256 k2] with dims (k1, k2 bits 3-5, k2 bits 0-1, k2 bit 2,
+    // k2 bit 6 together with the transform index), the layout of res32k_out
+    void* src = const_cast<void*>(in ? in : data);
+    if (encode_col_load(lm, CU_TENSOR_MAP_DATA_TYPE_UINT32, src, n2, batch, 4, C, 1) != CUDA_SUCCESS)
+      return cudaErrorInvalidValue;
+    uint64_t dims[5] = {256, 8, 4, 2, (uint64_t)(2 * batch)};
+    uint64_t str[4] = {8 * 1024, 1024, 4 * 1024, 64 * 1024};
+    uint32_t box[5] = {32, 8, 4, 1, 1};
+    if (encode_tmap(sm, CU_TENSOR_MAP_DATA_TYPE_UINT32, 5, data, dims, str, box, CU_TENSOR_MAP_SWIZZLE_128B) !=
+        CUDA_SUCCESS)
+      return cudaErrorInvalidValue;
+  } else if (encode) {
     void* src = const_cast<void*>(in ? in : data);  // loads from the input, stores to data
     if (encode_col_load(lm, CU_TENSOR_MAP_DATA_TYPE_UINT32, src, n2, batch, 4, C, 1) != CUDA_SUCCESS)
       return cudaErrorInvalidValue;
@@ -564,6 +774,7 @@ cudaError_t launch_resident(int64_t n, void* data, int64_t batch, const float2* 
     case 4096: return launch_resident_t<1>(*lm, *sm, p, num_sms, st);
     case 8192: return launch_resident_t<2>(*lm, *sm, p, num_sms, st);
     case 16384: return launch_resident_t<4>(*lm, *sm, p, num_sms, st);
+    case 32768: return launch_resident32k(*lm, *sm, p, num_sms, st);
     default: return cudaErrorInvalidValue;
   }
 }

@@ -361,9 +361,9 @@ tcfftStatus choose_1d(int64_t n, int64_t batch, int precision, Schedule& s, int 
   if (lg >= 12 && lg <= 15) {
     // N = 256 x N2 with short rows N2 = 16 R1: phase 0 columns of 256, phase 1 16 rows per warp
     FusedKey k;
-    // 2^15: 512 x 64 (plain: 1.24 ms for 2^28 elements against 1.48 ms for 256 x 128 and
-    // 1.38 ms for 1024 x 32: 64 KiB column tiles and a radix-4 short-row phase; split: the
-    // short-row phase's R <= 4 limit)
+    // 2^15 (split, or plain with the resident kernel turned off): 512 x 64 (plain: 1.24 ms for
+    // 2^28 elements against 1.48 ms for 256 x 128 and 1.38 ms for 1024 x 32: 64 KiB column tiles
+    // and a radix-4 short-row phase; split: the short-row phase's R <= 4 limit)
     int64_t n1 = lg == 15 ? 512 : 256;
     if (getenv("TCFFT_N1")) n1 = atoll(getenv("TCFFT_N1"));  // decomposition override (measurements)
     if (n1 < 256 || n1 > 2048 || n / n1 < 16 || n / n1 > 128) return TCFFT_NOT_SUPPORTED;

@@ -55,12 +55,12 @@ def test_describe_small(n):
 
 @pytest.mark.parametrize("n", [4096, 1 << 15, 1 << 16, 1 << 20, 1 << 22])
 def test_describe_fused(n):
-    assert ("resident" if n == 4096 else "fused1d") in tc.describe_1d(n, 4)
+    assert ("resident" if n in (4096, 1 << 15) else "fused1d") in tc.describe_1d(n, 4)
 
 
 @pytest.mark.parametrize("n,precision,expect", [
     (4096, 1, "resident(split)"), (8192, 1, "resident(split)"), (16384, 0, "resident(plain)"),
-    (1 << 15, 0, "N=512 x 64"), (1 << 15, 1, "N=512 x 64"), (2048, 1, "small(R=8,split)"),
+    (1 << 15, 0, "resident(plain): N=256 x 128"), (1 << 15, 1, "N=512 x 64"), (2048, 1, "small(R=8,split)"),
     (1 << 21, 0, "N=1024 x 2048"), (1 << 21, 1, "large1d(split): N=512 x 4096"),
     (1 << 23, 0, "large1d(plain): N=2048 x 4096"), (1 << 20, 0, "N=1024 x 1024")])
 def test_describe_schedule_choice(n, precision, expect):

@@ -97,7 +97,7 @@ def test_plain_large(cuda_device, n, batch):
     xq = quantize(x, "plain")
     with tc.Plan(n=n, batch=batch) as p:
         sched = p.info["schedule"]
-        assert sched.startswith("resident" if 4096 <= n <= 16384 else "fused1d"), sched
+        assert sched.startswith("resident" if 4096 <= n <= 32768 else "fused1d"), sched
         y = run_gpu(p, xq, "plain")
     ref = oracle_1d(xq)
     assert np.isfinite(y).all()

@@ -148,6 +148,21 @@ def test_split_2048_and_short_rows(cuda_device, n):
     assert oracle.rel_l2(y2, oracle_2d(x2)) < tol_split(256 * 2048)
 
 
+@pytest.mark.parametrize("batch", [3, 400])
+def test_resident_32768(cuda_device, batch):
+    """N = 2^15 plain held whole in one CTA's shared memory (a transform in two
+    stages, the output written and stored in two halves): forward and adjoint
+    against FP64, with up to three transforms per CTA at batch 400."""
+    n = 1 << 15
+    xq = quantize(uniform_input((batch, n), seed=batch + 15), "plain")
+    with tc.Plan(n=n, batch=batch) as p:
+        assert p.info["schedule"].startswith("resident(plain)"), p.info["schedule"]
+        y = run_gpu(p, xq, "plain")
+        ya = run_gpu(p, xq, "plain", adjoint=True)
+    assert oracle.rel_l2(y, oracle_1d(xq)) < tol_plain(n)
+    assert oracle.rel_l2(ya, oracle_1d(xq, adjoint=True)) < tol_plain(n)
+
+
 @pytest.mark.parametrize("many", [False, True])
 @pytest.mark.parametrize("n", [1 << 15, 1 << 16, 1 << 17, 1 << 18])
 def test_cluster_opt_in(cuda_device, monkeypatch, n, many):
