@@ -491,16 +491,20 @@ cudaError_t launch_resident_t(const CUtensorMap& lm, const CUtensorMap& sm, cons
 }
 
 // ---------------------------------------------------------------------------
-// N = 32768 = 256 x 128 plain.  A transform (128 KiB) fills two of the three 64 KiB
-// stages (A, B: its four 32-column tiles); the third (C) takes half of the output.
-//   phase 0: 256-point column FFTs of the four tiles in place, times W_N^(n2 k1);
+// N = 32768 = 256 x 128 plain.  Shared memory holds three 64 KiB regions.  Transform c
+// takes its four 32-column tiles in regions in0 = -c mod 3 (tiles 0, 1) and in1 = in0 + 1
+// (tiles 2, 3), and half of its output in out = in0 + 2:
+//   phase 0: 256-point column FFTs of the four tiles in place, times W_N^(n2 k1)
+//            (tiles 0, 1 as soon as they have landed, then tiles 2, 3);
 //   phase 1, round 1: the 8 jobs of rows k1 < 128 (one 16-row job of 128 points per
-//            warp), outputs written straight into C; C is stored;
+//            warp), outputs written straight into region out, which is then stored;
 //   round 2: the 8 jobs of rows k1 >= 128, outputs written into the tile rows round 1
 //            consumed (in the column role's row order, k1 < 128 are the tile rows with
-//            bit 5 clear: 4 runs of 32 rows per tile, 4 KiB each), stored the same way;
-//   the next transform is loaded once the second half has been read out (one
-//   transform in flight per CTA; its load is not overlapped with compute).
+//            bit 5 clear: 4 runs of 32 rows per tile, 4 KiB each), stored the same way.
+// Transform c + 1 loads its tiles 0, 1 into region out(c) as soon as round 1's store has
+// read it (during round 2), and its tiles 2, 3 into in0(c) once round 2's store has read
+// the runs; its round-1 output goes to in1(c).  So the loads overlap round 2 and the
+// next transform's first column tiles.
 // Output box (one TMA store, 4 KiB): 32 consecutive k1 x k2 bits 3-5 x k2 bits 0-1,
 // at fixed k1 bits 5-7, k2 bit 2 and k2 bit 6.  The row jobs run with the identity
 // output digit order (k2 = q + 8 (g + 8 h)), so the 8 lanes g of one store
@@ -508,31 +512,47 @@ cudaError_t launch_resident_t(const CUtensorMap& lm, const CUtensorMap& sm, cons
 // k1 bits 0-1 of one chunk: one wavefront per instruction.
 struct Res32kCfg {
   static constexpr int kN = 32768, kC = 32, kCG = 4;  // N2 = 128 = 16 x 8
-  static constexpr int kTileBytes = 256 * kC * 4;  // 32 KiB
-  static constexpr int kStageBytes = 65536;
-  static constexpr int kInBytes = 2 * kStageBytes;  // A + B
+  static constexpr int kTileBytes = 256 * kC * 4;     // 32 KiB
+  static constexpr int kRegionBytes = 65536;          // two tiles, or half of the output
+  static constexpr int kHalfBytes = 2 * kTileBytes;
   static constexpr int kBoxBytes = 4096;
   static constexpr int kTwShift = 8, kTwLo = 256, kTwHi = 128;
   static constexpr int kTabBytes = (kTwLo + kTwHi) * 8 + FoldTab<8>::kABytes;
-  static constexpr int kSmem = 3 * kStageBytes + kTabBytes + 1024 + 256;
+  static constexpr int kSmem = 3 * kRegionBytes + kTabBytes + 1024 + 256;
   static constexpr int kThreads = 384;
   using PI = BitPerm<0, 1, 3, 2>;    // phase 0 (column jobs)
   using PI1 = BitPerm<0, 2, 3, 1>;   // phase 1: lane t reads points 4t .. 4t + 3
   using RHO = BitPerm<0, 2, 3, 1>;   // phase 0
   using RHO1 = BitPerm<0, 1, 2, 3>;  // phase 1: output digit k0 = g + 8 h
-  static_assert(kTileBytes * kCG == kInBytes, "a transform fills stages A and B");
-  static_assert(16 * kBoxBytes == kStageBytes, "half an output is 16 boxes");
+  static_assert(kHalfBytes == kRegionBytes, "two tiles fill a region");
+  static_assert(16 * kBoxBytes == kRegionBytes, "half an output is 16 boxes");
+};
+
+// Regions of transform c (shared-memory addresses): tiles 0-1, tiles 2-3, round-1 output.
+struct Res32kRegions {
+  uint32_t t01, t23, out;
+  __device__ __forceinline__ Res32kRegions(uint32_t base, int cnt) {
+    const int r0 = (3 - cnt % 3) % 3;
+    t01 = base + (uint32_t)(r0 * Res32kCfg::kRegionBytes);
+    t23 = base + (uint32_t)(((r0 + 1) % 3) * Res32kCfg::kRegionBytes);
+    out = base + (uint32_t)(((r0 + 2) % 3) * Res32kCfg::kRegionBytes);
+  }
+  __device__ __forceinline__ uint32_t tile(int t) const {
+    return (t < 2 ? t01 : t23) + (uint32_t)((t & 1) * Res32kCfg::kTileBytes);
+  }
+  // box u of a round: in region out (round 0) or run u & 3 of tile u >> 2 (round 1)
+  __device__ __forceinline__ uint32_t box(int round, int u) const {
+    return round == 0 ? out + (uint32_t)(u * Res32kCfg::kBoxBytes) : tile(u >> 2) + (uint32_t)((u & 3) * 8192);
+  }
 };
 
 // Byte address of output X[k1 + 256 k2] (k1 in the given round's half): box u = 4 c + k2
-// bit 2 + 2 k2 bit 6 (c = k1 bits 5-6) in C (round 0) or in run u & 3 of tile u >> 2 (round
-// 1), box row k2 bits 3-5 | k2 bits 0-1 << 3, 128-byte swizzle.
-__device__ __forceinline__ uint32_t res32k_out(uint32_t abase, uint32_t cbase, int round, int k1, int k2) {
+// bit 2 + 2 k2 bit 6 (c = k1 bits 5-6), box row k2 bits 3-5 | k2 bits 0-1 << 3, 128-byte
+// swizzle.
+__device__ __forceinline__ uint32_t res32k_out(const Res32kRegions& rg, int round, int k1, int k2) {
   const int u = 4 * ((k1 >> 5) & 3) + ((k2 >> 2) & 1) + 2 * (k2 >> 6);
   const int row = ((k2 >> 3) & 7) | ((k2 & 3) << 3);
-  const uint32_t box = round == 0 ? cbase + (uint32_t)(u * Res32kCfg::kBoxBytes)
-                                  : abase + (uint32_t)((u >> 2) * Res32kCfg::kTileBytes + (u & 3) * 8192);
-  return box + ctile_off<32, 4>(row, k1 & 31);
+  return rg.box(round, u) + ctile_off<32, 4>(row, k1 & 31);
 }
 
 __global__ void __launch_bounds__(384, 1) fft_resident32k_kernel(const __grid_constant__ CUtensorMap load_map,
@@ -543,25 +563,26 @@ __global__ void __launch_bounds__(384, 1) fft_resident32k_kernel(const __grid_co
   using PI1 = Cfg::PI1;
   using RHO = Cfg::RHO;
   using RHO1 = Cfg::RHO1;
-  constexpr int C = Cfg::kC, CG = Cfg::kCG;
+  constexpr int C = Cfg::kC;
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* smem =
       reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-  unsigned char* cbuf = smem + Cfg::kInBytes;
-  unsigned char* tab = cbuf + Cfg::kStageBytes;
+  unsigned char* tab = smem + 3 * Cfg::kRegionBytes;
   float2* s_twlo = reinterpret_cast<float2*>(tab);
   float2* s_twhi = s_twlo + Cfg::kTwLo;
   unsigned char* s_fold = reinterpret_cast<unsigned char*>(s_twhi + Cfg::kTwHi);
-  uint64_t* full = reinterpret_cast<uint64_t*>(tab + Cfg::kTabBytes);  // the transform is loaded
-  uint64_t* infree = full + 1;  // stages A and B read out (second half stored)
-  uint64_t* cfree = full + 2;   // stage C read out (first half stored)
-  uint64_t* half = full + 3;    // [2]: a half of the output written (8 compute warps)
+  uint64_t* full = reinterpret_cast<uint64_t*>(tab + Cfg::kTabBytes);  // [2]: tiles 0-1, tiles 2-3 landed
+  uint64_t* outfree = full + 2;  // round 1's output region read out by its store
+  uint64_t* runsfree = full + 3; // round 2's runs read out by their store
+  uint64_t* half = full + 4;     // [2]: a half of the output written (8 compute warps)
+  const uint32_t base = smem_addr(smem);
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   if (tid == 0) {
-    mbar_init(full, 1);
-    mbar_init(infree, 1);
-    mbar_init(cfree, 1);
+    mbar_init(&full[0], 1);
+    mbar_init(&full[1], 1);
+    mbar_init(outfree, 1);
+    mbar_init(runsfree, 1);
     mbar_init(&half[0], 8);
     mbar_init(&half[1], 8);
     fence_barrier_init();
@@ -576,15 +597,27 @@ __global__ void __launch_bounds__(384, 1) fft_resident32k_kernel(const __grid_co
   if (warp == 8) {  // ------------------------------------------------ TMA producer
     if (lane == 0) {
       prefetch_tmap(&load_map);
+      int issued[2] = {0, 0};
       int cnt = 0;
       for (long long it = blockIdx.x; it < p.batch; it += gridDim.x, ++cnt) {
-        if (!mbar_wait(infree, (uint32_t)(cnt + 1) & 1, p.err)) break;
-        mbar_arrive_expect_tx(full, Cfg::kInBytes);
+        const Res32kRegions rg(base, cnt);
+        bool ok = true;
 #pragma unroll 1
-        for (int cg = 0; cg < CG; ++cg)
-          tma_load_5d(smem + cg * Cfg::kTileBytes, &load_map, cg * C, 0, 0, 0, (int)it, full);
+        for (int h = 0; h < 2 && ok; ++h) {
+          // tiles 0-1 go to the previous transform's round-1 output region, tiles 2-3 to its
+          // tiles 0-1 region (which held its round-2 runs)
+          ok = mbar_wait(h == 0 ? outfree : runsfree, (uint32_t)(cnt + 1) & 1, p.err);
+          if (!ok) break;
+          mbar_arrive_expect_tx(&full[h], Cfg::kHalfBytes);
+#pragma unroll 1
+          for (int t = 2 * h; t < 2 * h + 2; ++t)
+            tma_load_5d(smem + (rg.tile(t) - base), &load_map, t * C, 0, 0, 0, (int)it, &full[h]);
+          ++issued[h];
+        }
+        if (!ok) break;
       }
-      if (cnt > 0) mbar_wait(full, (uint32_t)(cnt - 1) & 1, nullptr);  // the last load has landed
+      for (int h = 0; h < 2; ++h)  // the last loads have landed
+        if (issued[h] > 0) mbar_wait(&full[h], (uint32_t)(issued[h] - 1) & 1, nullptr);
     }
     return;
   }
@@ -592,24 +625,21 @@ __global__ void __launch_bounds__(384, 1) fft_resident32k_kernel(const __grid_co
     if (lane == 0) {
       prefetch_tmap(&store_map);
       int cnt = 0;
-      for (long long it = blockIdx.x; it < p.batch; it += gridDim.x, ++cnt) {
+      bool ok = true;
+      for (long long it = blockIdx.x; it < p.batch && ok; it += gridDim.x, ++cnt) {
+        const Res32kRegions rg(base, cnt);
 #pragma unroll 1
         for (int round = 0; round < 2; ++round) {
-          if (!mbar_wait(&half[round], (uint32_t)cnt & 1, p.err)) {
-            cnt = -1;
-            break;
-          }
+          ok = mbar_wait(&half[round], (uint32_t)cnt & 1, p.err);
+          if (!ok) break;
 #pragma unroll 1
-          for (int u = 0; u < 16; ++u) {
-            const unsigned char* src = round == 0 ? cbuf + u * Cfg::kBoxBytes
-                                                  : smem + (u >> 2) * Cfg::kTileBytes + (u & 3) * 8192;
-            tma_store_5d(&store_map, 128 * round + 32 * (u >> 2), 0, 0, u & 1, ((u >> 1) & 1) + 2 * (int)it, src);
-          }
+          for (int u = 0; u < 16; ++u)
+            tma_store_5d(&store_map, 128 * round + 32 * (u >> 2), 0, 0, u & 1, ((u >> 1) & 1) + 2 * (int)it,
+                         smem + (rg.box(round, u) - base));
           bulk_commit();
           bulk_wait_read<0>();
-          mbar_arrive(round == 0 ? cfree : infree);
+          mbar_arrive(round == 0 ? outfree : runsfree);
         }
-        if (cnt < 0) break;
       }
       bulk_wait<0>();
     }
@@ -622,7 +652,6 @@ __global__ void __launch_bounds__(384, 1) fft_resident32k_kernel(const __grid_co
   init_job_consts<false, PI, RHO>(jc, p.tw2048);
   init_job_consts<false, PI1, RHO1>(jc1, p.tw2048);
   const uint32_t fold = smem_addr(s_fold);
-  const uint32_t abase = smem_addr(smem), cbase = smem_addr(cbuf);
   WnTable wn;
   wn.hi = smem_addr(s_twhi);
   wn.lo = smem_addr(s_twlo);
@@ -634,19 +663,26 @@ __global__ void __launch_bounds__(384, 1) fft_resident32k_kernel(const __grid_co
   const int tq = lane & 3;
   int cnt = 0;
   for (long long it = blockIdx.x; it < p.batch; it += gridDim.x, ++cnt) {
-    bool ok = named_bar_and(2, 256, mbar_wait(full, (uint32_t)cnt & 1, p.err));
-    if (ok) {
-      // phase 0: columns of 256 (in place, digit-ordered rows), twiddle W_N^(n2 k1); two passes of
-      // two columns per warp, as for the one-transform stages of 16384
+    const Res32kRegions rg(base, cnt);
+    bool ok = true;
+    // phase 0: columns of 256 (in place, digit-ordered rows), twiddle W_N^(n2 k1); two passes of
+    // two columns per warp, as for the one-transform stages of 16384.  Tiles 0-1 start before
+    // tiles 2-3 have landed.
 #pragma unroll 1
-      for (int tile = 0; tile < CG; ++tile)
+    for (int hh = 0; hh < 2; ++hh) {
+      ok = named_bar_and(2, 256, ok && mbar_wait(&full[hh], (uint32_t)cnt & 1, p.err));
+      if (ok) {
 #pragma unroll 1
-        for (int h = 0; h < 2; ++h)
-          plain_col_tile<1, C, true, PI, RHO, 2>(jc, fold, abase + tile * Cfg::kTileBytes, warp + 8 * h, p.dsign,
-                                                 tile * C, wn, p.oscale);
+        for (int tile = 2 * hh; tile < 2 * hh + 2; ++tile)
+#pragma unroll 1
+          for (int h = 0; h < 2; ++h)
+            plain_col_tile<1, C, true, PI, RHO, 2>(jc, fold, rg.tile(tile), warp + 8 * h, p.dsign, tile * C, wn,
+                                                   p.oscale);
+      }
     }
-    // round 1 writes into C once its previous contents have been stored
-    ok = named_bar_and(2, 256, ok && mbar_wait(cfree, (uint32_t)(cnt + 1) & 1, p.err));
+    // every column tile is complete; round 1's output region was freed before tiles 2-3 were
+    // loaded (it held the previous transform's round-2 runs)
+    ok = named_bar_and(2, 256, ok);
 #pragma unroll 1
     for (int round = 0; round < 2; ++round) {
       if (ok) {
@@ -654,12 +690,10 @@ __global__ void __launch_bounds__(384, 1) fft_resident32k_kernel(const __grid_co
         const int jl = warp + 8 * round;
         auto ld4 = [&](int v, int a, uint32_t(&w)[4]) {
           const int n = 4 * tq + 16 * a;
-          lds128(abase + (uint32_t)((n >> 5) * Cfg::kTileBytes) +
-                     ctile_off<C, 4>(col_out_row(kap_of<C>(v, jl), 0), n & (C - 1)),
-                 w);
+          lds128(rg.tile(n >> 5) + ctile_off<C, 4>(col_out_row(kap_of<C>(v, jl), 0), n & (C - 1)), w);
         };
         auto st = [&](int v, int k2, int, int, float2 val) {
-          sts32(res32k_out(abase, cbase, round, kap_of<C>(v, jl), k2), pack_h2(val.x, val.y));
+          sts32(res32k_out(rg, round, kap_of<C>(v, jl), k2), pack_h2(val.x, val.y));
         };
         fft16r_job_q_fold<8, PI1, RHO1>(jc1, fold, p.dsign, ld4, st);
       }
