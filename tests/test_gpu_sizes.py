@@ -172,6 +172,7 @@ def test_cluster_opt_in(cuda_device, monkeypatch, n, many):
     least four transforms per cluster, so that both stages, the receive buffer
     and every per-transform barrier are reused (parities 0 and 1)."""
     monkeypatch.setenv("TCFFT_CLUSTER", "1")
+    monkeypatch.setenv("TCFFT_NO_RESIDENT", "1")  # 2^15 plain is resident by default
     cl = n >> 14
     batch = 4 * (152 // cl) + 3 if many else 5
     xq = quantize(uniform_input((batch, n), seed=n % 97 + batch), "plain")
