@@ -254,6 +254,10 @@ tcfftStatus tcfftGetPlanInfo(tcfftPlan plan, tcfftPlanInfo* info);
  * planner; used by CPU tests). Writes a short text into buf. */
 tcfftStatus tcfftDescribe1d(int64_t n, int64_t batch, int32_t precision, char* buf, size_t buf_len);
 
+/* The same for a 2D shape [batch][nx][ny]: the fused 2D kernel for axes of 256..2048 (split and
+ * fp32 I/O: up to 1024), else rows, transpose, rows, transpose through 1D plans. */
+tcfftStatus tcfftDescribe2d(int64_t nx, int64_t ny, int64_t batch, int32_t precision, char* buf, size_t buf_len);
+
 /* Library version string. */
 const char* tcfftVersion(void);
 

@@ -105,6 +105,8 @@ _SIGNATURES = {
     "tcfftGetPlanInfo": ([ctypes.c_void_p, ctypes.POINTER(PlanInfo)], ctypes.c_int),
     "tcfftDescribe1d": ([ctypes.c_int64, ctypes.c_int64, ctypes.c_int32, ctypes.c_char_p, ctypes.c_size_t],
                         ctypes.c_int),
+    "tcfftDescribe2d": ([ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, ctypes.c_int32, ctypes.c_char_p,
+                         ctypes.c_size_t], ctypes.c_int),
     "tcfftVersion": ([], ctypes.c_char_p),
     "tcfftExecute1dNoAlloc": ([ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_int32, ctypes.c_int32,
                                ctypes.c_void_p], ctypes.c_int),
@@ -144,6 +146,14 @@ def describe_1d(n, batch=1, precision=PRECISION_PLAIN):
     """Host-only schedule description for a 1D size (no GPU needed)."""
     buf = ctypes.create_string_buffer(256)
     _check(lib().tcfftDescribe1d(int(n), int(batch), int(precision), buf, 256), "tcfftDescribe1d")
+    return buf.value.decode()
+
+
+def describe_2d(nx, ny, batch=1, precision=PRECISION_PLAIN):
+    """Host-only schedule description for a 2D shape [batch][nx][ny] (no GPU needed)."""
+    buf = ctypes.create_string_buffer(256)
+    _check(lib().tcfftDescribe2d(int(nx), int(ny), int(batch), _precision_of(precision), buf, 256),
+           "tcfftDescribe2d")
     return buf.value.decode()
 
 

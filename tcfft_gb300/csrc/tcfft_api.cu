@@ -494,6 +494,26 @@ tcfftStatus choose_2d(int64_t nx, int64_t ny, int64_t batch, int precision, Sche
   return TCFFT_SUCCESS;
 }
 
+// The 2D schedule: the fused 2D kernel where choose_2d takes the shape, otherwise rows of ny,
+// transpose, rows of nx, transpose, from 1D plans (both axes must be valid 1D sizes).
+tcfftStatus choose_2d_any(int64_t nx, int64_t ny, int64_t batch, int precision, Schedule& s, int num_sms = 152) {
+  if (choose_2d(nx, ny, batch, precision, s, num_sms) == TCFFT_SUCCESS) return TCFFT_SUCCESS;
+  Schedule sx, sy;
+  if (!is_pow2(nx) || !is_pow2(ny) || batch < 1 || nx * ny > (int64_t(1) << 40) / batch) return TCFFT_INVALID_SIZE;
+  tcfftStatus ex = choose_1d(nx, ny * batch, precision, sx), ey = choose_1d(ny, nx * batch, precision, sy);
+  if (ex != TCFFT_SUCCESS) return ex;
+  if (ey != TCFFT_SUCCESS) return ey;
+  s = Schedule();
+  s.kind = Schedule::kGeneric2d;
+  s.N1 = nx;
+  s.N2 = ny;
+  char buf[160];
+  snprintf(buf, sizeof buf, "generic2d(%s): rows of %lld, transpose, rows of %lld, transpose", prec_name(precision),
+           (long long)ny, (long long)nx);
+  s.text = buf;
+  return TCFFT_SUCCESS;
+}
+
 // Device tables for the reference input order; chains must be supported by the reference.
 tcfftStatus setup_reference_order(tcfftPlanImpl* p) {
   const int es = p->precision != TCFFT_PRECISION_PLAIN ? 8 : 4;
@@ -1588,6 +1608,18 @@ tcfftStatus tcfftDescribe1d(int64_t n, int64_t batch, int32_t precision, char* b
   return TCFFT_SUCCESS;
 }
 
+tcfftStatus tcfftDescribe2d(int64_t nx, int64_t ny, int64_t batch, int32_t precision, char* buf, size_t len) {
+  if (!buf || len == 0) return TCFFT_INVALID_VALUE;
+  if (precision != TCFFT_PRECISION_PLAIN && precision != TCFFT_PRECISION_SPLIT &&
+      precision != TCFFT_PRECISION_FP32_IO)
+    return TCFFT_INVALID_VALUE;
+  Schedule s;
+  tcfftStatus st = choose_2d_any(nx, ny, batch, precision, s);
+  if (st != TCFFT_SUCCESS) return st;
+  snprintf(buf, len, "%s", s.text.c_str());
+  return TCFFT_SUCCESS;
+}
+
 tcfftStatus tcfftPlan1d(tcfftPlan* out, int64_t n, int64_t batch, const tcfftOptions* opts) {
   if (!out) return TCFFT_INVALID_VALUE;
   *out = nullptr;
@@ -1662,23 +1694,8 @@ tcfftStatus tcfftPlan2d(tcfftPlan* out, int64_t nx, int64_t ny, int64_t batch, c
   tcfftOptionsDefault(&o);
   if (opts) o = *opts;
   Schedule s;
-  st = choose_2d(nx, ny, batch, o.precision, s, current_num_sms());
-  if (st != TCFFT_SUCCESS) {
-    // shapes outside the fused 2D range: compose from 1D plans (both axes must be valid 1D sizes)
-    Schedule sx, sy;
-    if (!is_pow2(nx) || !is_pow2(ny) || batch < 1 || nx * ny > (int64_t(1) << 40) / batch) return TCFFT_INVALID_SIZE;
-    tcfftStatus ex = choose_1d(nx, ny * batch, o.precision, sx), ey = choose_1d(ny, nx * batch, o.precision, sy);
-    if (ex != TCFFT_SUCCESS) return ex;
-    if (ey != TCFFT_SUCCESS) return ey;
-    s = Schedule();
-    s.kind = Schedule::kGeneric2d;
-    s.N1 = nx;
-    s.N2 = ny;
-    char buf[160];
-    snprintf(buf, sizeof buf, "generic2d(%s): rows of %lld, transpose, rows of %lld, transpose",
-             prec_name(o.precision), (long long)ny, (long long)nx);
-    s.text = buf;
-  }
+  st = choose_2d_any(nx, ny, batch, o.precision, s, current_num_sms());
+  if (st != TCFFT_SUCCESS) return st;
   std::vector<int> cx = {(int)nx}, cy = {(int)ny};
   if (o.input_order == TCFFT_ORDER_REFERENCE_DIGIT_REVERSED) {
     cx = reference_radices_2d_axis(nx);

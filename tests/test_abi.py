@@ -68,6 +68,25 @@ def test_describe_schedule_choice(n, precision, expect):
     assert expect in tc.describe_1d(n, 4, precision=precision)
 
 
+@pytest.mark.parametrize("nx,ny,precision,expect", [
+    (1024, 1024, 0, "fused2d(plain): 1024 x 1024"), (256, 2048, 0, "fused2d(plain): 256 x 2048"),
+    (2048, 2048, 0, "fused2d(plain)"), (512, 512, 1, "fused2d(split)"), (1024, 1024, 2, "fused2d(fp32io)"),
+    (2048, 256, 1, "generic2d(split): rows of 256, transpose, rows of 2048"),
+    (128, 128, 0, "generic2d(plain): rows of 128"), (4096, 4096, 0, "generic2d(plain): rows of 4096"),
+    (64, 4096, 0, "generic2d(plain): rows of 4096, transpose, rows of 64")])
+def test_describe_2d_schedule_choice(nx, ny, precision, expect):
+    """The 2D planner (host logic only): the fused kernel for axes of 256..2048 (8-byte
+    elements: up to 1024), 1D plans and transposes otherwise."""
+    assert expect in tc.describe_2d(nx, ny, 4, precision=precision)
+
+
+@pytest.mark.parametrize("nx,ny,batch", [(100, 256, 1), (256, 3000, 1), (256, 256, 0), (1 << 28, 2, 1)])
+def test_describe_2d_rejects_bad_shapes(nx, ny, batch):
+    with pytest.raises(tc.TcfftError) as e:
+        tc.describe_2d(nx, ny, batch)
+    assert e.value.status == 2
+
+
 @pytest.mark.parametrize("n,batch", [(100, 1), (8, 1), (0, 1), (256, 0), (1 << 28, 1)])
 def test_describe_rejects_bad_sizes(n, batch):
     with pytest.raises(tc.TcfftError) as e:
