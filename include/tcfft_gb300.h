@@ -258,6 +258,22 @@ tcfftStatus tcfftDescribe1d(int64_t n, int64_t batch, int32_t precision, char* b
  * fp32 I/O: up to 1024), else rows, transpose, rows, transpose through 1D plans. */
 tcfftStatus tcfftDescribe2d(int64_t nx, int64_t ny, int64_t batch, int32_t precision, char* buf, size_t buf_len);
 
+/* Diagnostics, host only (no GPU): the work items of the one-launch many-shape executor for the
+ * transforms of a tcfftPlanMany call (plain precision) on a GPU with num_sms SMs, in launch
+ * order.  Writes min(capacity, *n_items) items, six int32 each, into `items`:
+ *   kind      bits 0-7 the work kind; 0x100 a group of listed 1D transforms (N <= 2048, one pass);
+ *             0x200 a pass-B item; 0x400 a pass-A item (it releases its transform's pass B)
+ *   xf        the transform (pass A / B), or the group's first entry in the listed transforms
+ *   tile      the first tile of the transform's pass
+ *   count     listed: transforms in the group; pass B: pass-A items of the transform
+ *   tiles     consecutive tiles in the item
+ *   elements  complex elements the item covers
+ * TCFFT_NOT_SUPPORTED when a shape is not one the executor runs (the plan then replays its
+ * per-shape graph). */
+tcfftStatus tcfftDescribeManyItems(int64_t count, const int32_t* ranks, const int64_t* nx, const int64_t* ny,
+                                   const int64_t* offsets, int32_t num_sms, int32_t* items, int64_t capacity,
+                                   int64_t* n_items);
+
 /* Library version string. */
 const char* tcfftVersion(void);
 

@@ -107,6 +107,10 @@ _SIGNATURES = {
                         ctypes.c_int),
     "tcfftDescribe2d": ([ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, ctypes.c_int32, ctypes.c_char_p,
                          ctypes.c_size_t], ctypes.c_int),
+    "tcfftDescribeManyItems": ([ctypes.c_int64, ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int64),
+                                ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64), ctypes.c_int32,
+                                ctypes.POINTER(ctypes.c_int32), ctypes.c_int64, ctypes.POINTER(ctypes.c_int64)],
+                               ctypes.c_int),
     "tcfftVersion": ([], ctypes.c_char_p),
     "tcfftExecute1dNoAlloc": ([ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_int32, ctypes.c_int32,
                                ctypes.c_void_p], ctypes.c_int),
@@ -147,6 +151,29 @@ def describe_1d(n, batch=1, precision=PRECISION_PLAIN):
     buf = ctypes.create_string_buffer(256)
     _check(lib().tcfftDescribe1d(int(n), int(batch), int(precision), buf, 256), "tcfftDescribe1d")
     return buf.value.decode()
+
+
+def describe_many_items(shapes, num_sms=152, offsets=None):
+    """Host-only diagnostics: the one-launch many-shape executor's work items for ``shapes``
+    (as in ``Plan.many``), in launch order, as a list of (kind, xf, tile, count, tiles, elements) tuples
+    (tcfftDescribeManyItems); raises TcfftError (status 7) when the executor does not run them."""
+    count = len(shapes)
+    ranks = (ctypes.c_int32 * count)(*[len(s) for s in shapes])
+    nxs = (ctypes.c_int64 * count)(*[int(s[0]) for s in shapes])
+    nys = (ctypes.c_int64 * count)(*[int(s[1]) if len(s) > 1 else 1 for s in shapes])
+    if offsets is None:
+        offsets, acc = [], 0
+        for s in shapes:
+            offsets.append(acc)
+            acc += int(s[0]) * (int(s[1]) if len(s) > 1 else 1)
+    offa = (ctypes.c_int64 * count)(*[int(o) for o in offsets])
+    n = ctypes.c_int64(0)
+    _check(lib().tcfftDescribeManyItems(count, ranks, nxs, nys, offa, int(num_sms), None, 0, ctypes.byref(n)),
+           "tcfftDescribeManyItems")
+    buf = (ctypes.c_int32 * (6 * max(n.value, 1)))()
+    _check(lib().tcfftDescribeManyItems(count, ranks, nxs, nys, offa, int(num_sms), buf, n.value, ctypes.byref(n)),
+           "tcfftDescribeManyItems")
+    return [tuple(buf[6 * i:6 * i + 6]) for i in range(n.value)]
 
 
 def describe_2d(nx, ny, batch=1, precision=PRECISION_PLAIN):

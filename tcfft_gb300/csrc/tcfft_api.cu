@@ -1248,16 +1248,16 @@ int64_t many_tiles(int kind, int rank, int64_t nx, int64_t ny) {
   }
 }
 
-// Builds the executor's items, row list, scratch and W_N tables; false (nothing
-// allocated that the plan does not free) when a shape is not supported.
-bool setup_many_pass(tcfftPlanImpl* p, int64_t count, const int32_t* ranks, const int64_t* nx, const int64_t* ny,
-                     const int64_t* offsets) {
-  if (p->precision != TCFFT_PRECISION_PLAIN || getenv("TCFFT_MANY_GRAPH")) return false;
-  if (count > (int64_t)1 << 24) return false;
-  // tensor-map coordinates are 32-bit: the buffer-wide maps address the span in rows of 128 bytes
-  if (p->span_elems / 32 > (int64_t)INT32_MAX - 256) return false;
-  std::vector<tcfftPlanImpl::ManyXf> xf((size_t)count);
-  int64_t soff = 0;
+// The executor's work (host logic only): per transform its shape and scratch offset, the item
+// sequence of the one launch and the row list of the listed 1D transforms.  False when a shape is
+// not one the executor runs.
+bool build_many_items(int64_t count, const int32_t* ranks, const int64_t* nx, const int64_t* ny,
+                      const int64_t* offsets, int num_sms, std::vector<tcfftPlanImpl::ManyXf>& xf,
+                      std::vector<ManyItem>& seq, std::vector<int>& rows, int64_t& soff) {
+  xf.assign((size_t)count, tcfftPlanImpl::ManyXf{});
+  seq.clear();
+  rows.clear();
+  soff = 0;
   for (int64_t i = 0; i < count; ++i) {
     const int r = ranks[i];
     const int64_t x = nx[i], y = r >= 2 ? ny[i] : 1;
@@ -1273,8 +1273,6 @@ bool setup_many_pass(tcfftPlanImpl* p, int64_t count, const int32_t* ranks, cons
   // items, with its pass-B items following lag items later (its intermediate is still in
   // L2 then and its pass A complete).  Transforms are taken in order of their kinds, so
   // that the CTAs run at most a few kinds at a time.
-  std::vector<ManyItem> seq;
-  std::vector<int> rows;
   {
     std::vector<int64_t> listed[kMkKinds];
     std::vector<int64_t> order;
@@ -1303,7 +1301,7 @@ bool setup_many_pass(tcfftPlanImpl* p, int64_t count, const int32_t* ranks, cons
     // 8 x 134 and 12 x 123 (a pass-B item that waits stalls its CTA's producer)
     static const double lag_env = getenv("TCFFT_MANY_LAG") ? atof(getenv("TCFFT_MANY_LAG")) : 0.0;
     const double lag_mult = lag_env > 0.0 ? lag_env : 10.0;
-    const size_t lag = (size_t)(lag_mult * (double)p->num_sms);
+    const size_t lag = (size_t)(lag_mult * (double)num_sms);
     std::vector<std::pair<int64_t, size_t>> waiting;  // (transform, sequence length after its pass A)
     size_t head = 0;
     // consecutive tiles of a transform share an item up to one 64 KiB stage
@@ -1347,6 +1345,22 @@ bool setup_many_pass(tcfftPlanImpl* p, int64_t count, const int32_t* ranks, cons
       return a.nsub * many_item_elems(a.kind & 0xff) > b.nsub * many_item_elems(b.kind & 0xff);
     });
   }
+  return true;
+}
+
+// Builds the executor's items, row list, scratch and W_N tables; false (nothing
+// allocated that the plan does not free) when a shape is not supported.
+bool setup_many_pass(tcfftPlanImpl* p, int64_t count, const int32_t* ranks, const int64_t* nx, const int64_t* ny,
+                     const int64_t* offsets) {
+  if (p->precision != TCFFT_PRECISION_PLAIN || getenv("TCFFT_MANY_GRAPH")) return false;
+  if (count > (int64_t)1 << 24) return false;
+  // tensor-map coordinates are 32-bit: the buffer-wide maps address the span in rows of 128 bytes
+  if (p->span_elems / 32 > (int64_t)INT32_MAX - 256) return false;
+  std::vector<tcfftPlanImpl::ManyXf> xf;
+  std::vector<ManyItem> seq;
+  std::vector<int> rows;
+  int64_t soff = 0;
+  if (!build_many_items(count, ranks, nx, ny, offsets, p->num_sms, xf, seq, rows, soff)) return false;
   // device arrays
   const size_t nit = seq.size();
   if (cudaMalloc(&p->many_items, std::max<size_t>(nit, 1) * sizeof(ManyItem)) != cudaSuccess ||
@@ -1617,6 +1631,35 @@ tcfftStatus tcfftDescribe2d(int64_t nx, int64_t ny, int64_t batch, int32_t preci
   tcfftStatus st = choose_2d_any(nx, ny, batch, precision, s);
   if (st != TCFFT_SUCCESS) return st;
   snprintf(buf, len, "%s", s.text.c_str());
+  return TCFFT_SUCCESS;
+}
+
+tcfftStatus tcfftDescribeManyItems(int64_t count, const int32_t* ranks, const int64_t* nx, const int64_t* ny,
+                                   const int64_t* offsets, int32_t num_sms, int32_t* items, int64_t capacity,
+                                   int64_t* n_items) {
+  if (count < 1 || !ranks || !nx || !offsets || !n_items || num_sms < 1 || (capacity > 0 && !items))
+    return TCFFT_INVALID_VALUE;
+  for (int64_t i = 0; i < count; ++i)
+    if ((ranks[i] != 1 && !ny) || ranks[i] < 1 || ranks[i] > 3 || nx[i] < 1 || (ranks[i] >= 2 && ny[i] < 1))
+      return TCFFT_INVALID_VALUE;
+  std::vector<tcfftPlanImpl::ManyXf> xf;
+  std::vector<ManyItem> seq;
+  std::vector<int> rows;
+  int64_t soff = 0;
+  if (!build_many_items(count, ranks, nx, ny ? ny : nx, offsets, num_sms, xf, seq, rows, soff))
+    return TCFFT_NOT_SUPPORTED;
+  *n_items = (int64_t)seq.size();
+  for (int64_t i = 0; i < capacity && i < (int64_t)seq.size(); ++i) {
+    const ManyItem& it = seq[(size_t)i];
+    int32_t* o = items + 6 * i;
+    const int k = it.kind & 0xff;
+    o[0] = it.kind;
+    o[1] = it.xf;
+    o[2] = it.tile;
+    o[3] = it.count;
+    o[4] = it.nsub;
+    o[5] = (it.kind & kMkList) ? it.count * 256 * many_r(k) : it.nsub * many_item_elems(k);
+  }
   return TCFFT_SUCCESS;
 }
 
