@@ -147,3 +147,20 @@ def test_plan_rejects_bad_options_before_touching_the_gpu(field, value):
 def test_options_struct_layout_matches_header():
     """The ctypes mirror of tcfftOptions has the header's size (pointer-aligned)."""
     assert ctypes.sizeof(tc.Options) == 32
+
+
+@pytest.mark.parametrize("n,batch,istride,idist,kw,status", [
+    (256, 48, 48, 1, {}, 7),                        # not whole 32-column tiles
+    (4096, 32, 32, 1, {}, 7),                       # columns longer than 2048
+    (512, 64, 32, 1, {"precision": "split"}, 7),   # element strides: plain precision only
+    (512, 64, 32, 1, {"normalize": True}, 7),      # normalised inverse needs the per-shape graph
+    (512, 65, 32, 1, {}, 7),                        # batch not a multiple of the stride
+    (512, 64, 32, 2, {}, 7),                        # both strides
+    (1024, 4, 1, 512, {}, 1),                       # transforms would overlap
+    (1000, 4, 1, 1000, {}, 2),                      # not a power of two
+    (1024, 0, 1, 1024, {}, 1)])                     # empty batch
+def test_strided_layouts_refused_before_touching_the_gpu(n, batch, istride, idist, kw, status):
+    """tcfftPlanStrided's layout checks are host logic: they run before any device call."""
+    with pytest.raises(tc.TcfftError) as e:
+        tc.Plan.strided(n, batch, istride=istride, idist=idist, **kw)
+    assert e.value.status == status
