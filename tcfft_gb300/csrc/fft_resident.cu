@@ -496,15 +496,15 @@ cudaError_t launch_resident_t(const CUtensorMap& lm, const CUtensorMap& sm, cons
 // (tiles 2, 3), and half of its output in out = in0 + 2:
 //   phase 0: 256-point column FFTs of the four tiles in place, times W_N^(n2 k1)
 //            (tiles 0, 1 as soon as they have landed, then tiles 2, 3);
-//   phase 1, round 1: the 8 jobs of rows k1 < 128 (one 16-row job of 128 points per
+//   phase 1, first half: the 8 jobs of rows k1 < 128 (one 16-row job of 128 points per
 //            warp), outputs written straight into region out, which is then stored;
-//   round 2: the 8 jobs of rows k1 >= 128, outputs written into the tile rows round 1
-//            consumed (in the column role's row order, k1 < 128 are the tile rows with
+//   second half: the 8 jobs of rows k1 >= 128, outputs written into the tile rows the
+//            first half consumed (in the column role's row order, k1 < 128 are the tile rows with
 //            bit 5 clear: 4 runs of 32 rows per tile, 4 KiB each), stored the same way.
-// Transform c + 1 loads its tiles 0, 1 into region out(c) as soon as round 1's store has
-// read it (during round 2), and its tiles 2, 3 into in0(c) once round 2's store has read
-// the runs; its round-1 output goes to in1(c).  So the loads overlap round 2 and the
-// next transform's first column tiles.
+// Transform c + 1 loads its tiles 0, 1 into region out(c) as soon as the first half's store
+// has read it (during the second half), and its tiles 2, 3 into in0(c) once the second
+// half's store has read the runs; its first-half output goes to in1(c).  So the loads
+// overlap the second half and the next transform's first column tiles.
 // Output box (one TMA store, 4 KiB): 32 consecutive k1 x k2 bits 3-5 x k2 bits 0-1,
 // at fixed k1 bits 5-7, k2 bit 2 and k2 bit 6.  The row jobs run with the identity
 // output digit order (k2 = q + 8 (g + 8 h)), so the 8 lanes g of one store
@@ -528,7 +528,7 @@ struct Res32kCfg {
   static_assert(16 * kBoxBytes == kRegionBytes, "half an output is 16 boxes");
 };
 
-// Regions of transform c (shared-memory addresses): tiles 0-1, tiles 2-3, round-1 output.
+// Regions of transform c (shared-memory addresses): tiles 0-1, tiles 2-3, first-half output.
 struct Res32kRegions {
   uint32_t t01, t23, out;
   __device__ __forceinline__ Res32kRegions(uint32_t base, int cnt) {
@@ -540,19 +540,19 @@ struct Res32kRegions {
   __device__ __forceinline__ uint32_t tile(int t) const {
     return (t < 2 ? t01 : t23) + (uint32_t)((t & 1) * Res32kCfg::kTileBytes);
   }
-  // box u of a round: in region out (round 0) or run u & 3 of tile u >> 2 (round 1)
-  __device__ __forceinline__ uint32_t box(int round, int u) const {
-    return round == 0 ? out + (uint32_t)(u * Res32kCfg::kBoxBytes) : tile(u >> 2) + (uint32_t)((u & 3) * 8192);
+  // box u of a row half: in region out (first half, rh 0) or run u & 3 of tile u >> 2 (rh 1)
+  __device__ __forceinline__ uint32_t box(int rh, int u) const {
+    return rh == 0 ? out + (uint32_t)(u * Res32kCfg::kBoxBytes) : tile(u >> 2) + (uint32_t)((u & 3) * 8192);
   }
 };
 
-// Byte address of output X[k1 + 256 k2] (k1 in the given round's half): box u = 4 c + k2
+// Byte address of output X[k1 + 256 k2] (k1 in row half rh): box u = 4 c + k2
 // bit 2 + 2 k2 bit 6 (c = k1 bits 5-6), box row k2 bits 3-5 | k2 bits 0-1 << 3, 128-byte
 // swizzle.
-__device__ __forceinline__ uint32_t res32k_out(const Res32kRegions& rg, int round, int k1, int k2) {
+__device__ __forceinline__ uint32_t res32k_out(const Res32kRegions& rg, int rh, int k1, int k2) {
   const int u = 4 * ((k1 >> 5) & 3) + ((k2 >> 2) & 1) + 2 * (k2 >> 6);
   const int row = ((k2 >> 3) & 7) | ((k2 & 3) << 3);
-  return rg.box(round, u) + ctile_off<32, 4>(row, k1 & 31);
+  return rg.box(rh, u) + ctile_off<32, 4>(row, k1 & 31);
 }
 
 __global__ void __launch_bounds__(384, 1) fft_resident32k_kernel(const __grid_constant__ CUtensorMap load_map,
@@ -572,8 +572,8 @@ __global__ void __launch_bounds__(384, 1) fft_resident32k_kernel(const __grid_co
   float2* s_twhi = s_twlo + Cfg::kTwLo;
   unsigned char* s_fold = reinterpret_cast<unsigned char*>(s_twhi + Cfg::kTwHi);
   uint64_t* full = reinterpret_cast<uint64_t*>(tab + Cfg::kTabBytes);  // [2]: tiles 0-1, tiles 2-3 landed
-  uint64_t* outfree = full + 2;  // round 1's output region read out by its store
-  uint64_t* runsfree = full + 3; // round 2's runs read out by their store
+  uint64_t* outfree = full + 2;  // the first half's output region read out by its store
+  uint64_t* runsfree = full + 3; // the second half's runs read out by their store
   uint64_t* half = full + 4;     // [2]: a half of the output written (8 compute warps)
   const uint32_t base = smem_addr(smem);
 
@@ -604,8 +604,8 @@ __global__ void __launch_bounds__(384, 1) fft_resident32k_kernel(const __grid_co
         bool ok = true;
 #pragma unroll 1
         for (int h = 0; h < 2 && ok; ++h) {
-          // tiles 0-1 go to the previous transform's round-1 output region, tiles 2-3 to its
-          // tiles 0-1 region (which held its round-2 runs)
+          // tiles 0-1 go to the previous transform's first-half output region, tiles 2-3 to its
+          // tiles 0-1 region (which held its second-half runs)
           ok = mbar_wait(h == 0 ? outfree : runsfree, (uint32_t)(cnt + 1) & 1, p.err);
           if (!ok) break;
           mbar_arrive_expect_tx(&full[h], Cfg::kHalfBytes);
@@ -629,16 +629,16 @@ __global__ void __launch_bounds__(384, 1) fft_resident32k_kernel(const __grid_co
       for (long long it = blockIdx.x; it < p.batch && ok; it += gridDim.x, ++cnt) {
         const Res32kRegions rg(base, cnt);
 #pragma unroll 1
-        for (int round = 0; round < 2; ++round) {
-          ok = mbar_wait(&half[round], (uint32_t)cnt & 1, p.err);
+        for (int rh = 0; rh < 2; ++rh) {
+          ok = mbar_wait(&half[rh], (uint32_t)cnt & 1, p.err);
           if (!ok) break;
 #pragma unroll 1
           for (int u = 0; u < 16; ++u)
-            tma_store_5d(&store_map, 128 * round + 32 * (u >> 2), 0, 0, u & 1, ((u >> 1) & 1) + 2 * (int)it,
-                         smem + (rg.box(round, u) - base));
+            tma_store_5d(&store_map, 128 * rh + 32 * (u >> 2), 0, 0, u & 1, ((u >> 1) & 1) + 2 * (int)it,
+                         smem + (rg.box(rh, u) - base));
           bulk_commit();
           bulk_wait_read<0>();
-          mbar_arrive(round == 0 ? outfree : runsfree);
+          mbar_arrive(rh == 0 ? outfree : runsfree);
         }
       }
       bulk_wait<0>();
@@ -680,28 +680,28 @@ __global__ void __launch_bounds__(384, 1) fft_resident32k_kernel(const __grid_co
                                                    p.oscale);
       }
     }
-    // every column tile is complete; round 1's output region was freed before tiles 2-3 were
-    // loaded (it held the previous transform's round-2 runs)
+    // every column tile is complete; the first half's output region was freed before tiles 2-3
+    // were loaded (it held the previous transform's second-half runs)
     ok = named_bar_and(2, 256, ok);
 #pragma unroll 1
-    for (int round = 0; round < 2; ++round) {
+    for (int rh = 0; rh < 2; ++rh) {
       if (ok) {
-        // 16 rows k1 per job, FFT over n2 (length 128); job jl = warp + 8 round
-        const int jl = warp + 8 * round;
+        // 16 rows k1 per job, FFT over n2 (length 128); job jl = warp + 8 rh
+        const int jl = warp + 8 * rh;
         auto ld4 = [&](int v, int a, uint32_t(&w)[4]) {
           const int n = 4 * tq + 16 * a;
           lds128(rg.tile(n >> 5) + ctile_off<C, 4>(col_out_row(kap_of<C>(v, jl), 0), n & (C - 1)), w);
         };
         auto st = [&](int v, int k2, int, int, float2 val) {
-          sts32(res32k_out(rg, round, kap_of<C>(v, jl), k2), pack_h2(val.x, val.y));
+          sts32(res32k_out(rg, rh, kap_of<C>(v, jl), k2), pack_h2(val.x, val.y));
         };
         fft16r_job_q_fold<8, PI1, RHO1>(jc1, fold, p.dsign, ld4, st);
       }
       fence_proxy_async_smem();  // the half is read by TMA stores
       __syncwarp();
-      if (lane == 0) mbar_arrive(&half[round]);
-      // round 2 overwrites the rows round 1 read: every warp has finished round 1
-      if (round == 0) ok = named_bar_and(2, 256, ok);
+      if (lane == 0) mbar_arrive(&half[rh]);
+      // the second half overwrites the rows the first half read: every warp has finished it
+      if (rh == 0) ok = named_bar_and(2, 256, ok);
     }
     if (!ok) break;
   }
