@@ -352,15 +352,22 @@ def sweep_2d(torch, tc):
     return out
 
 
-def uneven_batch(torch, tc, graph=False):
-    """The uneven-batch workload: 512 1D transforms of 2^8..2^16 and 64 2D transforms
-    of 2^7..2^10 per axis (seed 2), back to back in one buffer, one plan: the persistent
-    many-shape passes, or (graph=True) the per-shape sub-plans replayed as one CUDA graph."""
+def uneven_shapes():
+    """The uneven-batch workload's shapes: 512 1D transforms of 2^8..2^16 and 64 2D transforms
+    of 2^7..2^10 per axis (seed 2), shuffled."""
     import numpy as np
     rng = np.random.default_rng(2)
     shapes = [(1 << int(e),) for e in rng.integers(8, 17, size=512)]
     shapes += [(1 << int(a), 1 << int(b)) for a, b in rng.integers(7, 11, size=(64, 2))]
-    shapes = [shapes[i] for i in rng.permutation(len(shapes))]
+    return [shapes[i] for i in rng.permutation(len(shapes))]
+
+
+def uneven_batch(torch, tc, graph=False):
+    """The uneven-batch workload (uneven_shapes), back to back in one buffer, one plan: the
+    persistent many-shape passes, or (graph=True) the per-shape sub-plans replayed as one CUDA
+    graph."""
+    import numpy as np
+    shapes = uneven_shapes()
     elems = sum(int(np.prod(sh)) for sh in shapes)
     flops = sum(5.0 * int(np.prod(sh)) * math.log2(int(np.prod(sh))) for sh in shapes)
     x = torch.empty((elems, 2), dtype=torch.float16, device="cuda").uniform_(-1, 1)
@@ -526,6 +533,8 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=10.0)
     ap.add_argument("--profile", action="store_true",
                     help="only the warm-up and timed calls (for ncu captures); prints the time per call")
+    ap.add_argument("--uneven", action="store_true",
+                    help="with --profile: the uneven-batch plan (tcfftPlanMany of the bench's 576 shapes)")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
 
@@ -571,6 +580,16 @@ def main():
     else:
         torch.cuda.set_device(0)
     dev_index = torch.cuda.current_device()
+
+    if args.profile and args.uneven:
+        import numpy as np
+        shapes = uneven_shapes()
+        elems = sum(int(np.prod(sh)) for sh in shapes)
+        xu = torch.empty((elems, 2), dtype=torch.float16, device="cuda").uniform_(-1, 1)
+        with tc.Plan.many(shapes) as p:
+            secs = time_device(torch, p, xu, args.steps, args.warmup)
+            print(json.dumps({"profile_run": p.info["schedule"], "ms_per_call": secs / args.steps * 1e3}), flush=True)
+        return
 
     dt = torch.float16 if args.precision == "plain" else torch.float32
     gen = torch.Generator(device="cuda")
