@@ -164,3 +164,25 @@ def test_strided_layouts_refused_before_touching_the_gpu(n, batch, istride, idis
     with pytest.raises(tc.TcfftError) as e:
         tc.Plan.strided(n, batch, istride=istride, idist=idist, **kw)
     assert e.value.status == status
+
+
+@pytest.mark.parametrize("n", [1 << 12, 1 << 15, 1 << 16, 1 << 18, 1 << 20, 1 << 22])
+@pytest.mark.parametrize("precision", [0, 1, 2])
+def test_two_phase_ring_sizing(n, precision):
+    """Two-phase schedules keep a scratch ring of S = 2 D + 2 slots for a lag of D transforms
+    between a transform's phase 0 and phase 1, 1 <= D <= batch, D not shrinking as the batch
+    grows (host logic; the kernels' cross-CTA waits rely on it)."""
+    import re
+    last = 0
+    for batch in [1, 2, 3, 5, 8, 64, 256, 4096]:
+        if n * batch > 1 << 31:
+            break
+        text = tc.describe_1d(n, batch, precision=precision)
+        m = re.search(r"lag (\d+), (\d+) slots", text)
+        if not m:  # resident, composite or single-pass schedules have no ring
+            assert "fused1d" not in text, text
+            continue
+        d, slots = int(m.group(1)), int(m.group(2))
+        assert slots == 2 * d + 2 and 1 <= d <= batch, text
+        assert d >= last, "lag shrank with a larger batch: " + text
+        last = d
