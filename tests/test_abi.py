@@ -186,3 +186,29 @@ def test_two_phase_ring_sizing(n, precision):
         assert slots == 2 * d + 2 and 1 <= d <= batch, text
         assert d >= last, "lag shrank with a larger batch: " + text
         last = d
+
+
+# The planner's 1D schedule by log2 N, plain and 8-byte-element precisions (split and fp32 I/O
+# share their schedules); "-" is TCFFT_NOT_SUPPORTED (no 128-point split / fp32-I/O path).
+SUPPORT_1D = {
+    "plain": ["tiny"] * 4 + ["small"] * 4 + ["resident"] * 4 + ["fused1d"] * 7 + ["large1d"] * 5,
+    "8-byte": ["tiny"] * 3 + ["-"] + ["small"] * 4 + ["resident"] * 2 + ["fused1d"] * 7 + ["large1d"] * 7,
+}
+
+
+@pytest.mark.parametrize("precision", [0, 1, 2])
+def test_1d_support_matrix(precision):
+    """Every power of two 16..2^27 in plain precision, and all but 128 in split / fp32 I/O."""
+    expect = SUPPORT_1D["plain" if precision == 0 else "8-byte"]
+    for lg in range(4, 28):
+        want = expect[lg - 4]
+        if want == "-":
+            with pytest.raises(tc.TcfftError) as e:
+                tc.describe_1d(1 << lg, 1, precision=precision)
+            assert e.value.status == 7
+        else:
+            assert tc.describe_1d(1 << lg, 1, precision=precision).startswith(want), (lg, want)
+    for bad in (8, 1 << 28, 3 << 10):
+        with pytest.raises(tc.TcfftError) as e:
+            tc.describe_1d(bad, 1, precision=precision)
+        assert e.value.status == 2
