@@ -212,3 +212,29 @@ def test_1d_support_matrix(precision):
         with pytest.raises(tc.TcfftError) as e:
             tc.describe_1d(bad, 1, precision=precision)
         assert e.value.status == 2
+
+
+def test_reference_order_sizes_match_the_oracle_table():
+    """Plans in the reference's digit-reversed input order exist exactly for the sizes the
+    reference's planner defines (the oracle's table, pinned against the reference's host code):
+    other sizes are refused with TCFFT_INVALID_SIZE before any device work."""
+    import oracle
+    lib = tc.lib()
+    opts = tc.Options()
+    assert lib.tcfftOptionsDefault(ctypes.byref(opts)) == 0
+    opts.input_order = 1  # TCFFT_ORDER_REFERENCE_DIGIT_REVERSED
+    for lg in range(4, 28):
+        h = ctypes.c_void_p(None)
+        st = lib.tcfftPlan1d(ctypes.byref(h), 1 << lg, 1, ctypes.byref(opts))
+        if st == 0:
+            lib.tcfftDestroy(h)
+        assert (st == 2) == (oracle.reference_radices(1 << lg) is None), (lg, st)
+    for ax in range(7, 12):
+        for ay in range(7, 12):
+            h = ctypes.c_void_p(None)
+            st = lib.tcfftPlan2d(ctypes.byref(h), 1 << ax, 1 << ay, 1, ctypes.byref(opts))
+            if st == 0:
+                lib.tcfftDestroy(h)
+            ok = oracle.reference_radices_2d_axis(1 << ax) is not None and \
+                oracle.reference_radices_2d_axis(1 << ay) is not None
+            assert (st == 2) == (not ok), (ax, ay, st)
